@@ -1,0 +1,226 @@
+/*
+ * rmg.h -- C ABI of the GB300 range-sensor ray-casting library.
+ *
+ * Every entry point is plain C: POD structs, raw pointers, sizes, an int
+ * status.  No exception crosses this boundary and no torch type appears in it.
+ * Device pointers are CUDA device (or managed) addresses; host pointers are
+ * ordinary process memory.  `stream` is a cudaStream_t passed as void*
+ * (NULL = the legacy default stream).  All GPU work is enqueued
+ * asynchronously on that stream unless a function says it synchronises.
+ *
+ * Each declaration names the rmagine (uos/rmagine v2.4.2) interface it
+ * replaces, as path:line inside that project.
+ */
+#ifndef RMG_H
+#define RMG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RMG_ABI_VERSION 1
+
+/* ---------------------------------------------------------------------------
+ * Status codes.  The C++ wrapper turns a non-zero status into an exception,
+ * mirroring RM_THROW / CudaException (src/rmagine_core/include/rmagine/util/
+ * exceptions.h:48,78-85).
+ * ------------------------------------------------------------------------- */
+typedef enum rmg_status {
+  RMG_OK = 0,
+  RMG_ERR_INVALID_ARG = 1,       /* NULL handle, size out of range, bad model */
+  RMG_ERR_CUDA = 2,              /* a CUDA runtime call failed */
+  RMG_ERR_OOM = 3,               /* device allocation failed */
+  RMG_ERR_TIMEOUT = 4,           /* rmg_stream_wait ran out of time */
+  RMG_ERR_TRAVERSAL_BUDGET = 5,  /* a ray exceeded its node-visit budget (corrupt BVH) */
+  RMG_ERR_NO_DEVICE = 6,         /* no CUDA device, or not an sm_103 part */
+  RMG_ERR_UNSUPPORTED = 7        /* option value outside the compiled variants */
+} rmg_status;
+
+/* ---------------------------------------------------------------------------
+ * Plain data types, byte-compatible with rmagine's.
+ * ------------------------------------------------------------------------- */
+
+/* rmagine::Vector3 (math/types/Vector3.hpp:52-56): 12 B. */
+typedef struct rmg_vec3 { float x, y, z; } rmg_vec3;
+
+/* rmagine::Quaternion (math/types/Quaternion.hpp:58-64): x, y, z, w. */
+typedef struct rmg_quat { float x, y, z, w; } rmg_quat;
+
+/* rmagine::Transform (math/types/Transform.hpp:63-68): 32 B, same field order. */
+typedef struct rmg_transform { rmg_quat R; rmg_vec3 t; uint32_t stamp; } rmg_transform;
+
+/* rmagine::Face (types/mesh_types.h:54-73): three vertex indices. */
+typedef struct rmg_face { uint32_t v0, v1, v2; } rmg_face;
+
+/* rmagine::Matrix3x3 storage is column-major: data[col*3 + row]
+ * (math/types/Matrix.tcc:81-84). */
+typedef struct rmg_mat3 { float data[9]; } rmg_mat3;
+
+/* rmagine::CrossStatistics (math/types/CrossStatistics.hpp:51-57): 64 B. */
+typedef struct rmg_cross_stats {
+  rmg_vec3 dataset_mean;
+  rmg_vec3 model_mean;
+  rmg_mat3 covariance;   /* (1/n) sum (m_i - m_mean)(d_i - d_mean)^T, column-major */
+  uint32_t n_meas;
+} rmg_cross_stats;
+
+/* rmagine::Interval / DiscreteInterval (types/sensor_models.h:54-105). */
+typedef struct rmg_interval { float min, max; } rmg_interval;
+typedef struct rmg_discrete_interval { float min, inc; uint32_t size; } rmg_discrete_interval;
+
+typedef enum rmg_model_kind {
+  RMG_MODEL_SPHERICAL = 0,  /* SphericalModel  sensor_models.h:118-215 */
+  RMG_MODEL_PINHOLE = 1,    /* PinholeModel    sensor_models.h:217-315 */
+  RMG_MODEL_O1DN = 2,       /* O1DnModel_      sensor_models.h:338-417 */
+  RMG_MODEL_ONDN = 3        /* OnDnModel_      sensor_models.h:422-502 */
+} rmg_model_kind;
+
+/* One sensor model.  Fields a kind does not use are ignored.
+ *  spherical: phi (vertical, rows), theta (horizontal, cols), range
+ *  pinhole:   width, height, range, f[2] = (fx, fy), c[2] = (cx, cy)
+ *  O1Dn:      width, height, range, orig, dirs[width*height]
+ *  OnDn:      width, height, range, origs[width*height], dirs[width*height]
+ * dirs / origs are HOST pointers; rmg_sensor_create copies them. */
+typedef struct rmg_model {
+  uint32_t kind;
+  uint32_t width;
+  uint32_t height;
+  rmg_interval range;
+  rmg_discrete_interval phi;
+  rmg_discrete_interval theta;
+  float f[2];
+  float c[2];
+  rmg_vec3 orig;
+  const rmg_vec3* dirs;
+  const rmg_vec3* origs;
+} rmg_model;
+
+/* Result buffers of one simulate call: the attribute set of rmagine's
+ * IntAttrAll bundle (simulation/SimulationResults.hpp:56-159).  DEVICE
+ * pointers, each sized n_poses*width*height, indexed
+ * pose*width*height + row*width + col (SphereSimulatorEmbree.tcc:75-82).
+ * A NULL pointer means "not requested", like a zero-sized Memory in the
+ * reference's set_simulation_flags_ (embree_common.h:79-139). */
+typedef struct rmg_outputs {
+  uint8_t* hits;
+  float* ranges;
+  rmg_vec3* points;
+  rmg_vec3* normals;
+  uint32_t* face_ids;
+  uint32_t* geom_ids;
+  uint32_t* object_ids;
+} rmg_outputs;
+
+/* Traversal launch options (the knobs the autotuner searches). */
+typedef struct rmg_launch_config {
+  uint32_t stack_depth;   /* short-stack entries per ray; 0 = stackless (parent pointers) */
+  uint32_t block_warps;   /* warps per CTA */
+  uint32_t tile_w;        /* a warp covers tile_h x tile_w rays of one pose */
+  uint32_t tile_h;        /* tile_w * tile_h must be 32 */
+} rmg_launch_config;
+
+typedef struct rmg_map_info {
+  uint32_t n_vertices;
+  uint32_t n_faces;
+  uint32_t n_nodes;       /* internal BVH nodes */
+  uint32_t depth;         /* longest root-to-leaf path (edges) */
+  uint64_t device_bytes;  /* BVH nodes + packed triangles + vertices + faces */
+  float bounds_lo[3];
+  float bounds_hi[3];
+} rmg_map_info;
+
+typedef struct rmg_map rmg_map;        /* opaque: triangle mesh + LBVH on one GPU */
+typedef struct rmg_sensor rmg_sensor;  /* opaque: model + its device ray-direction table */
+
+/* ---------------------------------------------------------------------------
+ * Library / device.
+ * ------------------------------------------------------------------------- */
+const char* rmg_status_string(int status);
+/* Last error message of the calling thread ("" when none). */
+const char* rmg_last_error(void);
+int rmg_abi_version(void);
+/* Number of SMs and compute capability of the current device. */
+int rmg_device_info(int* sm_count, int* cc_major, int* cc_minor);
+/* Polls the stream until its work is done or timeout_ms elapses
+ * (RMG_ERR_TIMEOUT).  Never blocks longer than the timeout. */
+int rmg_stream_wait(void* stream, uint32_t timeout_ms);
+
+/* ---------------------------------------------------------------------------
+ * Map: triangle mesh + LBVH.
+ * Replaces EmbreeMesh::init/computeFaceNormals/apply + EmbreeScene::commit
+ * (src/rmagine_embree/src/map/embree/EmbreeMesh.cpp:162-335,
+ *  EmbreeScene.cpp:187-191) and OptixScene::commit (OptixScene.cpp:242-481).
+ * vertices / faces are HOST arrays, copied before the call returns.  The
+ * build runs on `stream` and the call synchronises with it.  n_faces == 0 is
+ * allowed: every ray of such a map misses.
+ * ------------------------------------------------------------------------- */
+int rmg_map_build(const rmg_vec3* vertices, uint32_t n_vertices,
+                  const rmg_face* faces, uint32_t n_faces,
+                  void* stream, rmg_map** out);
+/* Moves the vertices (same count, same faces) and refits every box of the
+ * existing tree bottom-up without re-sorting.  Needs exclusive use of the
+ * map (no simulate in flight).  Synchronises with `stream`. */
+int rmg_map_refit(rmg_map* map, const rmg_vec3* vertices, uint32_t n_vertices, void* stream);
+int rmg_map_destroy(rmg_map* map);
+int rmg_map_info_get(const rmg_map* map, rmg_map_info* out);
+/* Copies the tree to host memory (tests): nodes = n_nodes*16 floats/ints
+ * (the 64-byte node records), tris = n_faces*12 floats (48-byte records),
+ * leaf_order = n_faces sorted face ids.  Any pointer may be NULL. */
+int rmg_map_export(const rmg_map* map, void* nodes, void* tris, uint32_t* leaf_order);
+/* Reads the map's device error word (synchronous).  Returns RMG_OK or the
+ * recorded error (e.g. RMG_ERR_TRAVERSAL_BUDGET); `clear` != 0 resets it. */
+int rmg_map_status(rmg_map* map, int clear);
+/* Test hook: overwrite one child link of one BVH node (synchronous).  Used
+ * to check that a corrupt tree ends in RMG_ERR_TRAVERSAL_BUDGET, not a
+ * fault; values are range-checked so every link stays inside the arrays. */
+int rmg_map_debug_set_child(rmg_map* map, uint32_t node, uint32_t which, int32_t child);
+
+/* ---------------------------------------------------------------------------
+ * Sensor model.
+ * Replaces XSimulator::setModel (SphereSimulatorEmbree.hpp:115-116,
+ * SphereSimulatorOptix.hpp:130-131).  The model's per-ray sensor-frame
+ * directions (and OnDn origins) are materialised once in device memory:
+ * SphericalModel::getDirection (sensor_models.h:169-174) and
+ * PinholeModel::getDirection (:256-276) are evaluated on the GPU; O1Dn/OnDn
+ * tables (:375-384, :460-468) are copied from the host arrays.
+ * ------------------------------------------------------------------------- */
+int rmg_sensor_create(const rmg_model* model, void* stream, rmg_sensor** out);
+int rmg_sensor_destroy(rmg_sensor* sensor);
+/* Copies the sensor-frame direction table (width*height) to host memory. */
+int rmg_sensor_directions(const rmg_sensor* sensor, rmg_vec3* host_out);
+int rmg_sensor_size(const rmg_sensor* sensor, uint32_t* width, uint32_t* height);
+
+/* ---------------------------------------------------------------------------
+ * Simulate.
+ * Replaces {Sphere,Pinhole,O1Dn,OnDn}Simulator{Embree,Optix}::simulate
+ * (SphereSimulatorEmbree.tcc:51-254, PinholeSimulatorEmbree.tcc:51-254,
+ *  O1DnSimulatorEmbree.tcc:50-254, OnDnSimulatorEmbree.tcc:51-257;
+ *  SphereSimulatorOptix.tcc:44-90 for the device-buffer form).
+ * Tsb: HOST pointer to one sensor-to-base transform (setTsb,
+ *      SimulatorEmbree.hpp:60-61).
+ * Tbm: DEVICE array of n_poses base-to-map transforms.
+ * Semantics follow the Embree path: closest hit in (0, range.max]; hits =
+ * (t >= range.min); ranges = t; points = dir_s*t (+ orig_s); normals =
+ * geometric normal in the sensor frame facing the ray; face_ids = primitive
+ * id; geom_ids = object_ids = 0 (single mesh).  Misses: hits 0, ranges =
+ * range.max + 1, points/normals NaN, ids UINT32_MAX.
+ * Asynchronous on `stream`.
+ * ------------------------------------------------------------------------- */
+int rmg_simulate(const rmg_map* map, const rmg_sensor* sensor,
+                 const rmg_transform* Tsb, const rmg_transform* Tbm, uint32_t n_poses,
+                 const rmg_outputs* out, void* stream);
+/* Same with explicit launch options (NULL = library default). */
+int rmg_simulate_ex(const rmg_map* map, const rmg_sensor* sensor,
+                    const rmg_transform* Tsb, const rmg_transform* Tbm, uint32_t n_poses,
+                    const rmg_outputs* out, const rmg_launch_config* cfg, void* stream);
+/* Fills *cfg with the library default for this sensor/map. */
+int rmg_default_launch_config(const rmg_map* map, const rmg_sensor* sensor, rmg_launch_config* cfg);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RMG_H */

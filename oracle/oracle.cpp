@@ -1,0 +1,781 @@
+// ORACLE -- test infrastructure only.  CPU restatement of rmagine's Embree
+// simulation path, used by tests/, __graft_entry__.smoke() and the CPU
+// baseline leg of bench.py as the checker.  Nothing in the product links,
+// imports or executes this file.
+//
+// What it restates (uos/rmagine v2.4.2, paths inside that project):
+//   * ray generation    src/rmagine_core/include/rmagine/types/sensor_models.h:169-174 (spherical),
+//                       :256-276 (pinhole), :375-384 (O1Dn), :460-468 (OnDn)
+//   * pose math         src/rmagine_core/include/rmagine/math/types/Transform.tcc:24-42,
+//                       Quaternion.tcc:35-75
+//   * ray setup         src/rmagine_embree/include/rmagine/simulation/SphereSimulatorEmbree.tcc:69-99,
+//                       O1DnSimulatorEmbree.tcc:84-99, OnDnSimulatorEmbree.tcc:86-101
+//   * attributes        SphereSimulatorEmbree.tcc:104-249, O1DnSimulatorEmbree.tcc:132
+//   * closest hit       rtcIntersect1 (Embree v4.4.0, third party, not vendored): restated as
+//                       the watertight binary32 test of Woop, Benthin and Wald (JCGT 2013) over
+//                       every triangle, closest t in (0, range.max], ties to the smaller face id.
+// The arithmetic is written operation by operation (build with
+// -ffp-contract=off; fmaf() only where the published method fuses) so that a
+// ray and a triangle test give the same binary32 results on any IEEE host.
+//
+// Acceleration: a binned-SAH BVH with a conservative binary64 box test, so the
+// tree never changes which triangle is found.  A second, canonical LBVH
+// (Morton codes, Karras radix tree) mirrors the GPU library's tree for the
+// tree-equality test and for counting node visits and triangle tests.
+// FP64 re-intersection (Moeller-Trumbore in binary64) certifies rays whose
+// results disagree.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+struct V3 { float x, y, z; };
+struct Qt { float x, y, z, w; };
+struct Tf { Qt R; V3 t; };
+
+// Quaternion.tcc:35-42, terms summed left to right.
+Qt qmul(const Qt& a, const Qt& b) {
+  Qt r;
+  r.x = a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y;
+  r.y = a.w * b.y - a.x * b.z + a.y * b.w + a.z * b.x;
+  r.z = a.w * b.z + a.x * b.y - a.y * b.x + a.z * b.w;
+  r.w = a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z;
+  return r;
+}
+Qt qinv(const Qt& q) { return Qt{-q.x, -q.y, -q.z, q.w}; }
+// Quaternion.tcc:68-75: q * (p, 0) * q^-1.
+V3 qrot(const Qt& q, const V3& p) {
+  const Qt P{p.x, p.y, p.z, 0.0f};
+  const Qt r = qmul(qmul(q, P), qinv(q));
+  return V3{r.x, r.y, r.z};
+}
+// Transform.tcc:34-42.
+Tf tmul(const Tf& a, const Tf& b) {
+  Tf r;
+  const V3 rt = qrot(a.R, b.t);
+  r.R = qmul(a.R, b.R);
+  r.t = V3{rt.x + a.t.x, rt.y + a.t.y, rt.z + a.t.z};
+  return r;
+}
+Tf load_tf(const float* p) { return Tf{Qt{p[0], p[1], p[2], p[3]}, V3{p[4], p[5], p[6]}}; }
+
+// ---------------------------------------------------------------------------
+// Watertight binary32 ray/triangle test.
+// ---------------------------------------------------------------------------
+struct RayW { float ox, oy, oz; int kx, ky, kz; float Sx, Sy, Sz; };
+
+inline float cmp(const V3& v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : v.z); }
+
+RayW make_rayw(const V3& o, const V3& d) {
+  RayW r;
+  r.ox = o.x; r.oy = o.y; r.oz = o.z;
+  const float ax = std::fabs(d.x), ay = std::fabs(d.y), az = std::fabs(d.z);
+  int kz = 0;
+  if (ay > ax) kz = 1;
+  if (az > std::max(ax, ay)) kz = 2;
+  int kx = (kz + 1) % 3, ky = (kx + 1) % 3;
+  if (cmp(d, kz) < 0.0f) std::swap(kx, ky);
+  r.kx = kx; r.ky = ky; r.kz = kz;
+  r.Sx = cmp(d, kx) / cmp(d, kz);
+  r.Sy = cmp(d, ky) / cmp(d, kz);
+  r.Sz = 1.0f / cmp(d, kz);
+  return r;
+}
+
+bool tri_hit(const RayW& r, const V3& p0, const V3& p1, const V3& p2, float tfar, float& t_out) {
+  const V3 A{p0.x - r.ox, p0.y - r.oy, p0.z - r.oz};
+  const V3 B{p1.x - r.ox, p1.y - r.oy, p1.z - r.oz};
+  const V3 C{p2.x - r.ox, p2.y - r.oy, p2.z - r.oz};
+  const float Akz = cmp(A, r.kz), Bkz = cmp(B, r.kz), Ckz = cmp(C, r.kz);
+  const float Ax = std::fmaf(-r.Sx, Akz, cmp(A, r.kx));
+  const float Ay = std::fmaf(-r.Sy, Akz, cmp(A, r.ky));
+  const float Bx = std::fmaf(-r.Sx, Bkz, cmp(B, r.kx));
+  const float By = std::fmaf(-r.Sy, Bkz, cmp(B, r.ky));
+  const float Cx = std::fmaf(-r.Sx, Ckz, cmp(C, r.kx));
+  const float Cy = std::fmaf(-r.Sy, Ckz, cmp(C, r.ky));
+  const float CxBy = Cx * By, CyBx = Cy * Bx;
+  const float AxCy = Ax * Cy, AyCx = Ay * Cx;
+  const float BxAy = Bx * Ay, ByAx = By * Ax;
+  float U = CxBy - CyBx, Vv = AxCy - AyCx, W = BxAy - ByAx;
+  if (U == 0.0f || Vv == 0.0f || W == 0.0f) {
+    U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+    Vv = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+    W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+  }
+  if ((U < 0.0f || Vv < 0.0f || W < 0.0f) && (U > 0.0f || Vv > 0.0f || W > 0.0f)) return false;
+  const float det = (U + Vv) + W;
+  if (det == 0.0f) return false;
+  const float Az = r.Sz * Akz, Bz = r.Sz * Bkz, Cz = r.Sz * Ckz;
+  const float T = std::fmaf(U, Az, std::fmaf(Vv, Bz, W * Cz));
+  const float t = T / det;
+  if (!(t > 0.0f) || !(t <= tfar)) return false;
+  t_out = t;
+  return true;
+}
+
+struct Mesh {
+  std::vector<V3> v;       // vertices
+  std::vector<uint32_t> f; // 3 per face
+  V3 vert(uint32_t face, int k) const { return v[f[3 * face + k]]; }
+};
+
+// ---------------------------------------------------------------------------
+// Binned-SAH BVH with conservative binary64 box tests.
+// ---------------------------------------------------------------------------
+struct BoxD { double lo[3], hi[3]; };
+
+struct SahNode {
+  BoxD box;
+  int left, right;   // children for internal nodes
+  int first, count;  // primitive range for leaves (count > 0)
+};
+
+struct SahBvh {
+  Mesh mesh;
+  std::vector<SahNode> nodes;
+  std::vector<uint32_t> prims;
+  double pad;  // absolute box padding
+};
+
+BoxD empty_box() {
+  BoxD b;
+  for (int k = 0; k < 3; ++k) { b.lo[k] = INFINITY; b.hi[k] = -INFINITY; }
+  return b;
+}
+void grow(BoxD& b, const V3& p) {
+  const double c[3] = {p.x, p.y, p.z};
+  for (int k = 0; k < 3; ++k) { b.lo[k] = std::min(b.lo[k], c[k]); b.hi[k] = std::max(b.hi[k], c[k]); }
+}
+void grow(BoxD& b, const BoxD& o) {
+  for (int k = 0; k < 3; ++k) { b.lo[k] = std::min(b.lo[k], o.lo[k]); b.hi[k] = std::max(b.hi[k], o.hi[k]); }
+}
+double area(const BoxD& b) {
+  double e[3];
+  for (int k = 0; k < 3; ++k) e[k] = std::max(0.0, b.hi[k] - b.lo[k]);
+  return 2.0 * (e[0] * e[1] + e[1] * e[2] + e[2] * e[0]);
+}
+
+struct BuildCtx {
+  const Mesh* mesh;
+  std::vector<BoxD> tb;
+  std::vector<double> cen;  // 3 per tri
+  std::vector<uint32_t>* prims;
+  std::vector<SahNode>* nodes;
+};
+
+int build_sah(BuildCtx& c, int first, int count) {
+  const int idx = (int)c.nodes->size();
+  c.nodes->push_back(SahNode{});
+  BoxD b = empty_box(), cb = empty_box();
+  for (int i = first; i < first + count; ++i) {
+    const uint32_t p = (*c.prims)[i];
+    grow(b, c.tb[p]);
+    const double* q = &c.cen[3 * p];
+    for (int k = 0; k < 3; ++k) { cb.lo[k] = std::min(cb.lo[k], q[k]); cb.hi[k] = std::max(cb.hi[k], q[k]); }
+  }
+  (*c.nodes)[idx].box = b;
+  if (count <= 4) {
+    (*c.nodes)[idx].first = first; (*c.nodes)[idx].count = count;
+    (*c.nodes)[idx].left = (*c.nodes)[idx].right = -1;
+    return idx;
+  }
+  const int NB = 16;
+  double best_cost = INFINITY;
+  int best_axis = -1, best_split = -1;
+  for (int ax = 0; ax < 3; ++ax) {
+    const double ext = cb.hi[ax] - cb.lo[ax];
+    if (!(ext > 0.0)) continue;
+    BoxD bins[NB];
+    int cnt[NB] = {0};
+    for (int k = 0; k < NB; ++k) bins[k] = empty_box();
+    for (int i = first; i < first + count; ++i) {
+      const uint32_t p = (*c.prims)[i];
+      int bi = (int)((c.cen[3 * p + ax] - cb.lo[ax]) / ext * NB);
+      bi = std::min(std::max(bi, 0), NB - 1);
+      cnt[bi]++;
+      grow(bins[bi], c.tb[p]);
+    }
+    double ra[NB];
+    int rc[NB];
+    BoxD acc = empty_box();
+    int n = 0;
+    for (int k = NB - 1; k > 0; --k) { grow(acc, bins[k]); n += cnt[k]; ra[k] = area(acc); rc[k] = n; }
+    acc = empty_box(); n = 0;
+    for (int k = 0; k < NB - 1; ++k) {
+      grow(acc, bins[k]); n += cnt[k];
+      if (n == 0 || rc[k + 1] == 0) continue;
+      const double cost = area(acc) * n + ra[k + 1] * rc[k + 1];
+      if (cost < best_cost) { best_cost = cost; best_axis = ax; best_split = k; }
+    }
+  }
+  int mid;
+  if (best_axis < 0) {
+    mid = first + count / 2;
+  } else {
+    const double ext = cb.hi[best_axis] - cb.lo[best_axis];
+    auto it = std::partition(c.prims->begin() + first, c.prims->begin() + first + count, [&](uint32_t p) {
+      int bi = (int)((c.cen[3 * p + best_axis] - cb.lo[best_axis]) / ext * NB);
+      bi = std::min(std::max(bi, 0), NB - 1);
+      return bi <= best_split;
+    });
+    mid = (int)(it - c.prims->begin());
+    if (mid == first || mid == first + count) mid = first + count / 2;
+  }
+  const int l = build_sah(c, first, mid - first);
+  const int r = build_sah(c, mid, first + count - mid);
+  (*c.nodes)[idx].left = l; (*c.nodes)[idx].right = r;
+  (*c.nodes)[idx].count = 0;
+  return idx;
+}
+
+struct RayD { double o[3], inv[3]; };
+
+bool box_hit(const RayD& r, const BoxD& b, double pad, double tfar, double& tmin_out) {
+  double tmin = 0.0, tmax = tfar;
+  for (int k = 0; k < 3; ++k) {
+    double t0 = (b.lo[k] - pad - r.o[k]) * r.inv[k];
+    double t1 = (b.hi[k] + pad - r.o[k]) * r.inv[k];
+    if (std::isnan(t0) || std::isnan(t1)) { t0 = -INFINITY; t1 = INFINITY; }
+    if (t0 > t1) std::swap(t0, t1);
+    tmin = std::max(tmin, t0);
+    tmax = std::min(tmax, t1);
+  }
+  tmin_out = tmin;
+  return tmin <= tmax * (1.0 + 1e-9) + 1e-12;
+}
+
+struct HitF { float t; uint32_t face; bool hit; };
+
+HitF closest_hit(const SahBvh& bvh, const V3& o, const V3& d, float tfar, uint64_t* tri_tests) {
+  HitF h{tfar, 0xffffffffu, false};
+  if (bvh.nodes.empty()) return h;
+  const RayW rw = make_rayw(o, d);
+  RayD rd;
+  const double dd[3] = {d.x, d.y, d.z}, oo[3] = {o.x, o.y, o.z};
+  for (int k = 0; k < 3; ++k) { rd.o[k] = oo[k]; rd.inv[k] = 1.0 / dd[k]; }
+  int stack[128];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp) {
+    const SahNode& n = bvh.nodes[stack[--sp]];
+    double tmin;
+    if (!box_hit(rd, n.box, bvh.pad, (double)h.t, tmin)) continue;
+    if (n.count > 0) {
+      for (int i = n.first; i < n.first + n.count; ++i) {
+        const uint32_t f = bvh.prims[i];
+        float t;
+        if (tri_hit(rw, bvh.mesh.vert(f, 0), bvh.mesh.vert(f, 1), bvh.mesh.vert(f, 2), h.t, t)) {
+          if (t < h.t || f < h.face) { h.t = t; h.face = f; h.hit = true; }
+        }
+        if (tri_tests) ++*tri_tests;
+      }
+    } else {
+      double tl, tr;
+      const bool hl = box_hit(rd, bvh.nodes[n.left].box, bvh.pad, (double)h.t, tl);
+      const bool hr = box_hit(rd, bvh.nodes[n.right].box, bvh.pad, (double)h.t, tr);
+      if (hl && hr) {
+        if (tl <= tr) { stack[sp++] = n.right; stack[sp++] = n.left; }
+        else { stack[sp++] = n.left; stack[sp++] = n.right; }
+      } else if (hl) stack[sp++] = n.left;
+      else if (hr) stack[sp++] = n.right;
+    }
+  }
+  return h;
+}
+
+// ---------------------------------------------------------------------------
+// Canonical LBVH (same construction as the GPU library's map builder).
+// ---------------------------------------------------------------------------
+struct LNode { float a[4], b[4], c[4]; int32_t d[4]; };  // 64 B, same field meaning
+
+struct Lbvh {
+  std::vector<LNode> nodes;
+  std::vector<float> tris;        // 12 floats per leaf
+  std::vector<uint32_t> order;    // face id per leaf
+  std::vector<int> leaf_parent;
+};
+
+uint64_t spread3(uint64_t x) {
+  x &= 0x1fffffull;
+  x = (x | (x << 32)) & 0x001f00000000ffffull;
+  x = (x | (x << 16)) & 0x001f0000ff0000ffull;
+  x = (x | (x << 8)) & 0x100f00f00f00f00full;
+  x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+  x = (x | (x << 2)) & 0x1249249249249249ull;
+  return x;
+}
+
+int clz64(uint64_t x) { return x ? __builtin_clzll(x) : 64; }
+int clz32(uint32_t x) { return x ? __builtin_clz(x) : 32; }
+
+int ldelta(const std::vector<uint64_t>& k, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  if (k[i] == k[j]) return 64 + clz32((uint32_t)(i ^ j));
+  return clz64(k[i] ^ k[j]);
+}
+
+void lbvh_build(const Mesh& m, Lbvh& L) {
+  const int n = (int)(m.f.size() / 3);
+  L.nodes.clear(); L.tris.clear(); L.order.clear(); L.leaf_parent.clear();
+  if (n == 0) return;
+  std::vector<V3> cen(n);
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  const float third = 0.333333343f;
+  for (int i = 0; i < n; ++i) {
+    const V3 a = m.vert(i, 0), b = m.vert(i, 1), c = m.vert(i, 2);
+    cen[i] = V3{((a.x + b.x) + c.x) * third, ((a.y + b.y) + c.y) * third, ((a.z + b.z) + c.z) * third};
+    const float q[3] = {cen[i].x, cen[i].y, cen[i].z};
+    for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], q[k]); hi[k] = std::max(hi[k], q[k]); }
+  }
+  float scale[3];
+  for (int k = 0; k < 3; ++k) {
+    const float ext = hi[k] - lo[k];
+    scale[k] = ext > 0.0f ? 2097152.0f / ext : 0.0f;
+  }
+  std::vector<uint64_t> key(n);
+  for (int i = 0; i < n; ++i) {
+    const float q[3] = {cen[i].x, cen[i].y, cen[i].z};
+    uint64_t qq[3];
+    for (int k = 0; k < 3; ++k) {
+      float v = (q[k] - lo[k]) * scale[k];
+      v = std::min(std::max(v, 0.0f), 2097151.0f);
+      qq[k] = (uint64_t)(uint32_t)v;
+    }
+    key[i] = (spread3(qq[0]) << 2) | (spread3(qq[1]) << 1) | spread3(qq[2]);
+  }
+  std::vector<uint32_t> idx(n);
+  std::iota(idx.begin(), idx.end(), 0u);
+  std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
+  std::vector<uint64_t> sk(n);
+  for (int i = 0; i < n; ++i) sk[i] = key[idx[i]];
+  L.order = idx;
+  L.tris.resize(12 * (size_t)n);
+  for (int k = 0; k < n; ++k) {
+    const uint32_t f = idx[k];
+    for (int j = 0; j < 3; ++j) {
+      const V3 p = m.vert(f, j);
+      L.tris[12 * k + 4 * j + 0] = p.x; L.tris[12 * k + 4 * j + 1] = p.y; L.tris[12 * k + 4 * j + 2] = p.z;
+      float w = 0.0f;
+      if (j == 0) std::memcpy(&w, &f, 4);
+      L.tris[12 * k + 4 * j + 3] = w;
+    }
+  }
+  L.leaf_parent.assign(n, -1);
+  if (n == 1) {
+    LNode nd;
+    const float* t = &L.tris[0];
+    const float far = 1e30f;
+    const float lx = std::min(std::min(t[0], t[4]), t[8]), hx = std::max(std::max(t[0], t[4]), t[8]);
+    const float ly = std::min(std::min(t[1], t[5]), t[9]), hy = std::max(std::max(t[1], t[5]), t[9]);
+    const float lz = std::min(std::min(t[2], t[6]), t[10]), hz = std::max(std::max(t[2], t[6]), t[10]);
+    const float a[4] = {lx, hx, ly, hy}, b[4] = {far, far, far, far}, c[4] = {lz, hz, far, far};
+    std::memcpy(nd.a, a, 16); std::memcpy(nd.b, b, 16); std::memcpy(nd.c, c, 16);
+    nd.d[0] = -1; nd.d[1] = -1; nd.d[2] = -1; nd.d[3] = 0;
+    L.nodes.assign(1, nd);
+    return;
+  }
+  L.nodes.assign(n - 1, LNode{});
+  L.nodes[0].d[2] = -1;
+  for (int i = 0; i < n - 1; ++i) {
+    const int d = (ldelta(sk, n, i, i + 1) - ldelta(sk, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = ldelta(sk, n, i, i - d);
+    int lmax = 2;
+    while (ldelta(sk, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+      if (ldelta(sk, n, i, i + (l + t) * d) > dmin) l += t;
+    const int j = i + l * d;
+    const int dnode = ldelta(sk, n, i, j);
+    int s = 0;
+    for (int div = 2;; div <<= 1) {
+      const int t = (l + div - 1) / div;
+      if (ldelta(sk, n, i, i + (s + t) * d) > dnode) s += t;
+      if (t <= 1) break;
+    }
+    const int gamma = i + s * d + std::min(d, 0);
+    const int first = std::min(i, j), last = std::max(i, j);
+    int left, right;
+    if (first == gamma) { left = ~gamma; L.leaf_parent[gamma] = i; }
+    else { left = gamma; L.nodes[gamma].d[2] = i; }
+    if (last == gamma + 1) { right = ~(gamma + 1); L.leaf_parent[gamma + 1] = i; }
+    else { right = gamma + 1; L.nodes[gamma + 1].d[2] = i; }
+    L.nodes[i].d[0] = left; L.nodes[i].d[1] = right; L.nodes[i].d[3] = dnode;
+  }
+  // boxes: post-order (children have larger or smaller indices; recurse iteratively)
+  struct FB { float lo[3], hi[3]; };
+  std::vector<FB> nb(n - 1);
+  std::vector<char> done(n - 1, 0);
+  auto tri_box = [&](int k) {
+    FB b;
+    const float* t = &L.tris[12 * (size_t)k];
+    for (int a = 0; a < 3; ++a) {
+      b.lo[a] = std::min(std::min(t[a], t[4 + a]), t[8 + a]);
+      b.hi[a] = std::max(std::max(t[a], t[4 + a]), t[8 + a]);
+    }
+    return b;
+  };
+  std::vector<int> st;
+  st.push_back(0);
+  while (!st.empty()) {
+    const int i = st.back();
+    const int l = L.nodes[i].d[0], r = L.nodes[i].d[1];
+    bool ready = true;
+    if (l >= 0 && !done[l]) { st.push_back(l); ready = false; }
+    if (r >= 0 && !done[r]) { st.push_back(r); ready = false; }
+    if (!ready) continue;
+    st.pop_back();
+    const FB bl = l < 0 ? tri_box(~l) : nb[l];
+    const FB br = r < 0 ? tri_box(~r) : nb[r];
+    LNode& nd = L.nodes[i];
+    nd.a[0] = bl.lo[0]; nd.a[1] = bl.hi[0]; nd.a[2] = bl.lo[1]; nd.a[3] = bl.hi[1];
+    nd.b[0] = br.lo[0]; nd.b[1] = br.hi[0]; nd.b[2] = br.lo[1]; nd.b[3] = br.hi[1];
+    nd.c[0] = bl.lo[2]; nd.c[1] = bl.hi[2]; nd.c[2] = br.lo[2]; nd.c[3] = br.hi[2];
+    for (int a = 0; a < 3; ++a) {
+      nb[i].lo[a] = std::min(bl.lo[a], br.lo[a]);
+      nb[i].hi[a] = std::max(bl.hi[a], br.hi[a]);
+    }
+    done[i] = 1;
+  }
+}
+
+// The GPU traversal order on the canonical LBVH (binary32 slab tests in the
+// same form), instrumented: counts internal-node visits and triangle tests.
+const float kWiden = 1.00000024f;
+
+void slab(const float inv[3], const float oi[3], const float lo[3], const float hi[3], float& tmin, float& tmax) {
+  float t0[3], t1[3];
+  for (int k = 0; k < 3; ++k) {
+    t0[k] = std::fmaf(lo[k], inv[k], -oi[k]);
+    t1[k] = std::fmaf(hi[k], inv[k], -oi[k]);
+  }
+  tmin = std::max(std::max(std::min(t0[0], t1[0]), std::min(t0[1], t1[1])), std::max(std::min(t0[2], t1[2]), 0.0f));
+  tmax = std::min(std::min(std::max(t0[0], t1[0]), std::max(t0[1], t1[1])), std::max(t0[2], t1[2]));
+}
+
+HitF lbvh_trace(const Lbvh& L, const V3& o, const V3& d, float tfar, uint64_t& visits, uint64_t& tests) {
+  HitF h{tfar, 0xffffffffu, false};
+  if (L.nodes.empty()) return h;
+  const RayW rw = make_rayw(o, d);
+  const float dd[3] = {d.x, d.y, d.z}, oo[3] = {o.x, o.y, o.z};
+  float inv[3], oi[3];
+  for (int k = 0; k < 3; ++k) {
+    inv[k] = std::fabs(dd[k]) > 1e-20f ? 1.0f / dd[k] : std::copysign(1e20f, dd[k]);
+    oi[k] = oo[k] * inv[k];
+  }
+  auto test = [&](int k) {
+    const float* t = &L.tris[12 * (size_t)k];
+    float tt;
+    ++tests;
+    if (tri_hit(rw, V3{t[0], t[1], t[2]}, V3{t[4], t[5], t[6]}, V3{t[8], t[9], t[10]}, h.t, tt)) {
+      uint32_t f;
+      std::memcpy(&f, &t[3], 4);
+      if (tt < h.t || f < h.face) { h.t = tt; h.face = f; h.hit = true; }
+    }
+  };
+  std::vector<std::pair<int, float>> stack;
+  int node = 0;
+  for (;;) {
+    ++visits;
+    const LNode& n = L.nodes[node];
+    const float llo[3] = {n.a[0], n.a[2], n.c[0]}, lhi[3] = {n.a[1], n.a[3], n.c[1]};
+    const float rlo[3] = {n.b[0], n.b[2], n.c[2]}, rhi[3] = {n.b[1], n.b[3], n.c[3]};
+    float tl, tL, tr, tR;
+    slab(inv, oi, llo, lhi, tl, tL);
+    slab(inv, oi, rlo, rhi, tr, tR);
+    bool hl = tl <= std::min(tL, h.t) * kWiden;
+    bool hr = tr <= std::min(tR, h.t) * kWiden;
+    if (hl && n.d[0] < 0) { test(~n.d[0]); hl = false; }
+    if (hr && n.d[1] < 0) { test(~n.d[1]); hr = false; }
+    hl = hl && tl <= h.t * kWiden;
+    hr = hr && tr <= h.t * kWiden;
+    if (hl && hr) {
+      const bool lf = tl <= tr;
+      stack.push_back({lf ? n.d[1] : n.d[0], lf ? tr : tl});
+      node = lf ? n.d[0] : n.d[1];
+      continue;
+    }
+    if (hl || hr) { node = hl ? n.d[0] : n.d[1]; continue; }
+    bool found = false;
+    while (!stack.empty()) {
+      const auto e = stack.back();
+      stack.pop_back();
+      if (e.second <= h.t * kWiden) { node = e.first; found = true; break; }
+    }
+    if (!found) break;
+  }
+  return h;
+}
+
+// ---------------------------------------------------------------------------
+// Sensor-model rays.
+// ---------------------------------------------------------------------------
+struct Model {
+  int kind;
+  uint32_t W, H;
+  float rmin, rmax;
+  const float* dirs;   // W*H*3 sensor-frame directions
+  const float* origs;  // OnDn: W*H*3
+  V3 orig;             // O1Dn
+};
+
+void make_ray(const Model& m, const Tf& Tsm, uint32_t loc, V3& dir_s, V3& orig_s, V3& o, V3& d) {
+  dir_s = V3{m.dirs[3 * loc], m.dirs[3 * loc + 1], m.dirs[3 * loc + 2]};
+  d = qrot(Tsm.R, dir_s);
+  if (m.kind == 0 || m.kind == 1) {
+    orig_s = V3{0.0f, 0.0f, 0.0f};
+    o = Tsm.t;
+  } else {
+    orig_s = m.kind == 2 ? m.orig : V3{m.origs[3 * loc], m.origs[3 * loc + 1], m.origs[3 * loc + 2]};
+    const V3 r = qrot(Tsm.R, orig_s);  // Transform::mult(Vector3): R*v + t
+    o = V3{r.x + Tsm.t.x, r.y + Tsm.t.y, r.z + Tsm.t.z};
+  }
+}
+
+int nthreads_or_default(int n) {
+#ifdef _OPENMP
+  return n > 0 ? n : omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_max_threads(void) { return nthreads_or_default(0); }
+
+// SphericalModel::getDirection: phi/theta from DiscreteInterval::getValue in
+// binary32, then the C library's cosf/sinf as in sensor_models.h:169-174.
+void orc_dirs_spherical(float phi_min, float phi_inc, uint32_t phi_size, float theta_min, float theta_inc,
+                        uint32_t theta_size, float* out) {
+  for (uint32_t v = 0; v < phi_size; ++v) {
+    const float phi = phi_min + (float)v * phi_inc;
+    const float cp = cosf(phi), sp = sinf(phi);
+    for (uint32_t h = 0; h < theta_size; ++h) {
+      const float th = theta_min + (float)h * theta_inc;
+      const float ct = cosf(th), st = sinf(th);
+      float* o = out + 3 * ((size_t)v * theta_size + h);
+      o[0] = cp * ct; o[1] = cp * st; o[2] = sp;
+    }
+  }
+}
+
+// PinholeModel::getDirection.
+void orc_dirs_pinhole(uint32_t W, uint32_t H, float fx, float fy, float cx, float cy, float* out) {
+  for (uint32_t v = 0; v < H; ++v) {
+    for (uint32_t h = 0; h < W; ++h) {
+      const float px = ((float)h - cx) / fx, py = ((float)v - cy) / fy, pz = 1.0f;
+      const float n = std::sqrt((px * px + py * py) + pz * pz);
+      const float x = px / n, y = py / n, z = pz / n;
+      float* o = out + 3 * ((size_t)v * W + h);
+      o[0] = z; o[1] = -x; o[2] = -y;
+    }
+  }
+}
+
+void* orc_bvh_build(const float* verts, uint32_t nv, const uint32_t* faces, uint32_t nf) {
+  SahBvh* b = new SahBvh;
+  b->mesh.v.resize(nv);
+  for (uint32_t i = 0; i < nv; ++i) b->mesh.v[i] = V3{verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]};
+  b->mesh.f.assign(faces, faces + 3 * (size_t)nf);
+  b->prims.resize(nf);
+  std::iota(b->prims.begin(), b->prims.end(), 0u);
+  double maxabs = 1.0;
+  for (const V3& p : b->mesh.v) maxabs = std::max({maxabs, (double)std::fabs(p.x), (double)std::fabs(p.y), (double)std::fabs(p.z)});
+  b->pad = maxabs * 1e-6;
+  if (nf == 0) return b;
+  BuildCtx c;
+  c.mesh = &b->mesh;
+  c.tb.resize(nf);
+  c.cen.resize(3 * (size_t)nf);
+  for (uint32_t i = 0; i < nf; ++i) {
+    BoxD bb = empty_box();
+    for (int k = 0; k < 3; ++k) grow(bb, b->mesh.vert(i, k));
+    c.tb[i] = bb;
+    for (int k = 0; k < 3; ++k) c.cen[3 * i + k] = 0.5 * (bb.lo[k] + bb.hi[k]);
+  }
+  c.prims = &b->prims;
+  c.nodes = &b->nodes;
+  b->nodes.reserve(2 * (size_t)nf);
+  build_sah(c, 0, (int)nf);
+  return b;
+}
+
+void orc_bvh_free(void* p) { delete static_cast<SahBvh*>(p); }
+
+// Simulate n_poses x H x W rays with Embree-path semantics.  kind: 0 spherical,
+// 1 pinhole, 2 O1Dn, 3 OnDn.  dirs (and origs for OnDn) are the model's
+// sensor-frame tables; Tsb is one 8-float transform record, Tbm n_poses of them.
+// Any output pointer may be NULL.  Counts triangle tests when `tri_tests` != NULL.
+int orc_simulate(void* bvhp, int kind, uint32_t W, uint32_t H, float rmin, float rmax, const float* dirs,
+                 const float* origs, const float* orig, const float* Tsb, const float* Tbm, uint32_t n_poses,
+                 uint8_t* hits, float* ranges, float* points, float* normals, uint32_t* face_ids,
+                 uint32_t* geom_ids, uint32_t* object_ids, int nthreads, uint64_t* tri_tests) {
+  const SahBvh& bvh = *static_cast<SahBvh*>(bvhp);
+  Model m{kind, W, H, rmin, rmax, dirs, origs, orig ? V3{orig[0], orig[1], orig[2]} : V3{0, 0, 0}};
+  const Tf tsb = load_tf(Tsb);
+  const int64_t total = (int64_t)n_poses * W * H;
+  const float nanf_ = std::numeric_limits<float>::quiet_NaN();
+  uint64_t tests_total = 0;
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads_or_default(nthreads)) reduction(+ : tests_total)
+  for (int64_t gid = 0; gid < total; ++gid) {
+    const uint32_t pid = (uint32_t)(gid / ((int64_t)W * H));
+    const uint32_t loc = (uint32_t)(gid - (int64_t)pid * W * H);
+    const Tf Tsm = tmul(load_tf(Tbm + 8 * (size_t)pid), tsb);
+    V3 dir_s, orig_s, o, d;
+    make_ray(m, Tsm, loc, dir_s, orig_s, o, d);
+    uint64_t tt = 0;
+    const HitF h = closest_hit(bvh, o, d, rmax, tri_tests ? &tt : nullptr);
+    tests_total += tt;
+    if (h.hit) {
+      const float t = h.t;
+      if (hits) hits[gid] = t >= rmin ? 1 : 0;
+      if (ranges) ranges[gid] = t;
+      if (points) {
+        float p[3] = {dir_s.x * t, dir_s.y * t, dir_s.z * t};
+        if (kind >= 2) { p[0] = p[0] + orig_s.x; p[1] = p[1] + orig_s.y; p[2] = p[2] + orig_s.z; }
+        std::memcpy(points + 3 * gid, p, 12);
+      }
+      if (normals) {
+        const V3 p0 = bvh.mesh.vert(h.face, 0), p1 = bvh.mesh.vert(h.face, 1), p2 = bvh.mesh.vert(h.face, 2);
+        const V3 e1{p1.x - p0.x, p1.y - p0.y, p1.z - p0.z}, e2{p2.x - p0.x, p2.y - p0.y, p2.z - p0.z};
+        V3 n{e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
+        float len = std::sqrt((n.x * n.x + n.y * n.y) + n.z * n.z);
+        n = V3{n.x / len, n.y / len, n.z / len};
+        n = qrot(qinv(Tsm.R), n);
+        const float dp = (dir_s.x * n.x + dir_s.y * n.y) + dir_s.z * n.z;
+        if (dp > 0.0f) n = V3{-n.x, -n.y, -n.z};
+        len = std::sqrt((n.x * n.x + n.y * n.y) + n.z * n.z);
+        const float q[3] = {n.x / len, n.y / len, n.z / len};
+        std::memcpy(normals + 3 * gid, q, 12);
+      }
+      if (face_ids) face_ids[gid] = h.face;
+      if (geom_ids) geom_ids[gid] = 0;
+      if (object_ids) object_ids[gid] = 0;
+    } else {
+      if (hits) hits[gid] = 0;
+      if (ranges) ranges[gid] = rmax + 1.0f;
+      if (points) { points[3 * gid] = nanf_; points[3 * gid + 1] = nanf_; points[3 * gid + 2] = nanf_; }
+      if (normals) { normals[3 * gid] = nanf_; normals[3 * gid + 1] = nanf_; normals[3 * gid + 2] = nanf_; }
+      if (face_ids) face_ids[gid] = 0xffffffffu;
+      if (geom_ids) geom_ids[gid] = 0xffffffffu;
+      if (object_ids) object_ids[gid] = 0xffffffffu;
+    }
+  }
+  if (tri_tests) *tri_tests = tests_total;
+  return 0;
+}
+
+// Rays of the same workload (origins and map-frame directions), for
+// re-intersection by the certifier.  out_o / out_d: 3 floats per requested ray.
+int orc_rays(int kind, uint32_t W, uint32_t H, const float* dirs, const float* origs, const float* orig,
+             const float* Tsb, const float* Tbm, const uint64_t* gids, uint64_t n, float* out_o, float* out_d) {
+  Model m{kind, W, H, 0, 0, dirs, origs, orig ? V3{orig[0], orig[1], orig[2]} : V3{0, 0, 0}};
+  const Tf tsb = load_tf(Tsb);
+  for (uint64_t i = 0; i < n; ++i) {
+    const uint64_t gid = gids[i];
+    const uint32_t pid = (uint32_t)(gid / ((uint64_t)W * H));
+    const uint32_t loc = (uint32_t)(gid - (uint64_t)pid * W * H);
+    const Tf Tsm = tmul(load_tf(Tbm + 8 * (size_t)pid), tsb);
+    V3 dir_s, orig_s, o, d;
+    make_ray(m, Tsm, loc, dir_s, orig_s, o, d);
+    out_o[3 * i] = o.x; out_o[3 * i + 1] = o.y; out_o[3 * i + 2] = o.z;
+    out_d[3 * i] = d.x; out_d[3 * i + 1] = d.y; out_d[3 * i + 2] = d.z;
+  }
+  return 0;
+}
+
+// Binary64 Moeller-Trumbore of one ray against one face.  Writes t and the
+// smallest barycentric coordinate (negative = outside).  Returns 1 when the
+// plane is hit in front of the origin (t > 0).
+int orc_intersect_f64(void* bvhp, const float* o, const float* d, uint32_t face, double* t_out,
+                      double* minbary_out) {
+  const SahBvh& bvh = *static_cast<SahBvh*>(bvhp);
+  const V3 a = bvh.mesh.vert(face, 0), b = bvh.mesh.vert(face, 1), c = bvh.mesh.vert(face, 2);
+  const double p0[3] = {a.x, a.y, a.z}, p1[3] = {b.x, b.y, b.z}, p2[3] = {c.x, c.y, c.z};
+  const double O[3] = {o[0], o[1], o[2]}, D[3] = {d[0], d[1], d[2]};
+  double e1[3], e2[3], s[3];
+  for (int k = 0; k < 3; ++k) { e1[k] = p1[k] - p0[k]; e2[k] = p2[k] - p0[k]; s[k] = O[k] - p0[k]; }
+  const double pv[3] = {D[1] * e2[2] - D[2] * e2[1], D[2] * e2[0] - D[0] * e2[2], D[0] * e2[1] - D[1] * e2[0]};
+  const double det = e1[0] * pv[0] + e1[1] * pv[1] + e1[2] * pv[2];
+  if (det == 0.0) { *t_out = INFINITY; *minbary_out = -INFINITY; return 0; }
+  const double u = (s[0] * pv[0] + s[1] * pv[1] + s[2] * pv[2]) / det;
+  const double qv[3] = {s[1] * e1[2] - s[2] * e1[1], s[2] * e1[0] - s[0] * e1[2], s[0] * e1[1] - s[1] * e1[0]};
+  const double v = (D[0] * qv[0] + D[1] * qv[1] + D[2] * qv[2]) / det;
+  const double t = (e2[0] * qv[0] + e2[1] * qv[1] + e2[2] * qv[2]) / det;
+  *t_out = t;
+  *minbary_out = std::min(std::min(u, v), 1.0 - u - v);
+  return t > 0.0 ? 1 : 0;
+}
+
+// Closest binary32 hit of explicit rays (origins/directions), any tree.
+int orc_trace_rays(void* bvhp, const float* o, const float* d, uint64_t n, float tfar, float* t_out,
+                   uint32_t* face_out, int nthreads) {
+  const SahBvh& bvh = *static_cast<SahBvh*>(bvhp);
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads_or_default(nthreads))
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const HitF h = closest_hit(bvh, V3{o[3 * i], o[3 * i + 1], o[3 * i + 2]},
+                               V3{d[3 * i], d[3 * i + 1], d[3 * i + 2]}, tfar, nullptr);
+    t_out[i] = h.hit ? h.t : INFINITY;
+    face_out[i] = h.face;
+  }
+  return 0;
+}
+
+// ---- canonical LBVH ----------------------------------------------------------
+void* orc_lbvh_build(const float* verts, uint32_t nv, const uint32_t* faces, uint32_t nf) {
+  Mesh m;
+  m.v.resize(nv);
+  for (uint32_t i = 0; i < nv; ++i) m.v[i] = V3{verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]};
+  m.f.assign(faces, faces + 3 * (size_t)nf);
+  Lbvh* L = new Lbvh;
+  lbvh_build(m, *L);
+  return L;
+}
+
+void orc_lbvh_free(void* p) { delete static_cast<Lbvh*>(p); }
+
+uint32_t orc_lbvh_num_nodes(void* p) { return (uint32_t)static_cast<Lbvh*>(p)->nodes.size(); }
+
+// nodes: n_nodes * 16 words (64-byte records), tris: n_faces * 12 floats, order: n_faces.
+void orc_lbvh_export(void* p, void* nodes, float* tris, uint32_t* order) {
+  const Lbvh& L = *static_cast<Lbvh*>(p);
+  if (nodes && !L.nodes.empty()) std::memcpy(nodes, L.nodes.data(), L.nodes.size() * sizeof(LNode));
+  if (tris && !L.tris.empty()) std::memcpy(tris, L.tris.data(), L.tris.size() * 4);
+  if (order && !L.order.empty()) std::memcpy(order, L.order.data(), L.order.size() * 4);
+}
+
+// Traverses explicit rays through the canonical LBVH in the GPU kernel's
+// order and returns per-ray node visits and triangle tests plus the hit.
+int orc_lbvh_count(void* p, const float* o, const float* d, uint64_t n, float tfar, uint32_t* visits,
+                   uint32_t* tests, float* t_out, uint32_t* face_out, int nthreads) {
+  const Lbvh& L = *static_cast<Lbvh*>(p);
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads_or_default(nthreads))
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    uint64_t v = 0, t = 0;
+    const HitF h = lbvh_trace(L, V3{o[3 * i], o[3 * i + 1], o[3 * i + 2]}, V3{d[3 * i], d[3 * i + 1], d[3 * i + 2]},
+                              tfar, v, t);
+    visits[i] = (uint32_t)v;
+    tests[i] = (uint32_t)t;
+    if (t_out) t_out[i] = h.hit ? h.t : INFINITY;
+    if (face_out) face_out[i] = h.face;
+  }
+  return 0;
+}
+
+// SAH-tree node count (the tree-quality yardstick).
+uint32_t orc_bvh_num_nodes(void* p) { return (uint32_t)static_cast<SahBvh*>(p)->nodes.size(); }
+
+}  // extern "C"

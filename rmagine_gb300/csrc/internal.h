@@ -1,0 +1,73 @@
+// Host-side internals shared by the translation units: handle structs, error
+// reporting, allocation helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+struct rmg_map {
+  int device;
+  uint32_t n_vertices;
+  uint32_t n_faces;
+  uint32_t n_nodes;
+  uint32_t depth;
+  float lo[3], hi[3];
+  // device arrays
+  float* d_vertices;          // 3*n_vertices
+  uint32_t* d_faces;          // 3*n_faces
+  rmg::Node* d_nodes;         // n_nodes
+  rmg::Tri* d_tris;           // n_faces (leaf order)
+  uint32_t* d_leaf_order;     // n_faces: face id of each leaf
+  int* d_leaf_parent;         // n_faces: parent node of each leaf
+  unsigned int* d_flags;      // n_nodes refit visit counters
+  unsigned int* d_status;     // 1 word: device error status
+};
+
+struct rmg_sensor {
+  int device;
+  rmg_model model;            // copy; dirs/origs pointers cleared
+  uint32_t width, height;
+  float* d_dirs;              // 3*width*height
+  float* d_origs;             // 3*width*height (OnDn only)
+};
+
+namespace rmg {
+
+void set_error(const std::string& msg);
+int fail(int status, const std::string& msg);
+// Maps a CUDA error to a status, recording the message.  Returns RMG_OK for
+// cudaSuccess.
+int cuda_status(cudaError_t e, const char* what);
+
+#define RMG_CUDA_TRY(expr)                                     \
+  do {                                                         \
+    cudaError_t _e = (expr);                                   \
+    if (_e != cudaSuccess) return ::rmg::cuda_status(_e, #expr); \
+  } while (0)
+
+template <typename T>
+int dev_alloc(T** p, size_t count, const char* what) {
+  *p = nullptr;
+  if (count == 0) return RMG_OK;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(e == cudaErrorMemoryAllocation ? RMG_ERR_OOM : RMG_ERR_CUDA,
+                std::string("cudaMalloc failed for ") + what);
+  }
+  return RMG_OK;
+}
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+DeviceMap device_view(const rmg_map* m);
+SensorDev device_view(const rmg_sensor* s);
+
+int device_sm_count();
+
+}  // namespace rmg

@@ -1,0 +1,21 @@
+// Kernel launchers shared between translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace rmg {
+
+struct TraceParams;
+
+cudaError_t launch_trace_pose(const TraceParams& P, int stack_depth, unsigned grid, unsigned block,
+                              cudaStream_t st);
+cudaError_t launch_trace_single(const TraceParams& P, int stack_depth, unsigned grid,
+                                unsigned block, cudaStream_t st);
+cudaError_t launch_trace_table(const TraceParams& P, int stack_depth, unsigned grid, unsigned block,
+                               cudaStream_t st);
+
+inline bool valid_stack_depth(uint32_t s) { return s == 0 || s == 4 || s == 8 || s == 16 || s == 32; }
+
+}  // namespace rmg

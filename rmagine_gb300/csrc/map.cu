@@ -1,0 +1,535 @@
+// Map construction: triangle mesh -> linear BVH on the GPU.
+//
+// Replaces the BVH build that rmagine delegates to Embree
+// (src/rmagine_embree/src/map/embree/EmbreeScene.cpp:187-191, quality MEDIUM)
+// and OptiX (src/rmagine_optix/src/map/optix/OptixScene.cpp:242-481).
+//
+// Build (Karras, "Maximizing Parallelism in the Construction of BVHs,
+// Octrees, and k-d Trees", HPG 2012):
+//   1. centroid bounds of all triangles (two-level reduction)
+//   2. 63-bit Morton code of each centroid (21 bits per axis)
+//   3. stable radix sort of (code, face index): ties ordered by index
+//   4. radix tree over the sorted codes, one thread per internal node; equal
+//      codes are disambiguated by the index (the paper's augmentation)
+//   5. triangles packed in leaf order as 48-byte records
+//   6. bottom-up refit of the child boxes with per-node arrival counters
+// Leaves hold exactly one triangle.  The result is a pure function of the
+// input arrays (no atomics influence the topology), so the same mesh always
+// yields the same tree.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+
+#include "internal.h"
+
+namespace rmg {
+namespace {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ float3 load_v(const float* v, uint32_t i) {
+  return make_float3(v[3 * i + 0], v[3 * i + 1], v[3 * i + 2]);
+}
+
+// Centroid in a fixed operation order: ((v0 + v1) + v2) * 0.333333343f.
+__device__ __forceinline__ float3 centroid(const float* v, const uint32_t* f, uint32_t i) {
+  const float3 a = load_v(v, f[3 * i + 0]);
+  const float3 b = load_v(v, f[3 * i + 1]);
+  const float3 c = load_v(v, f[3 * i + 2]);
+  const float third = 0.333333343f;
+  return make_float3(__fmul_rn(__fadd_rn(__fadd_rn(a.x, b.x), c.x), third),
+                     __fmul_rn(__fadd_rn(__fadd_rn(a.y, b.y), c.y), third),
+                     __fmul_rn(__fadd_rn(__fadd_rn(a.z, b.z), c.z), third));
+}
+
+__global__ void k_centroid_bounds(const float* v, const uint32_t* f, uint32_t n, float* partial) {
+  float lo[3] = {INFINITY, INFINITY, INFINITY};
+  float hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float3 c = centroid(v, f, i);
+    lo[0] = fminf(lo[0], c.x); lo[1] = fminf(lo[1], c.y); lo[2] = fminf(lo[2], c.z);
+    hi[0] = fmaxf(hi[0], c.x); hi[1] = fmaxf(hi[1], c.y); hi[2] = fmaxf(hi[2], c.z);
+  }
+  __shared__ float s[6][kBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = 0; k < 3; ++k) {
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+      hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+    }
+  }
+  if (lane == 0) {
+    for (int k = 0; k < 3; ++k) { s[k][warp] = lo[k]; s[3 + k][warp] = hi[k]; }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < kBlock / 32; ++w) {
+      for (int k = 0; k < 3; ++k) {
+        s[k][0] = fminf(s[k][0], s[k][w]);
+        s[3 + k][0] = fmaxf(s[3 + k][0], s[3 + k][w]);
+      }
+    }
+    for (int k = 0; k < 6; ++k) partial[6 * blockIdx.x + k] = s[k][0];
+  }
+}
+
+__global__ void k_bounds_final(const float* partial, int nblocks, float* out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  float r[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  for (int b = 0; b < nblocks; ++b) {
+    for (int k = 0; k < 3; ++k) {
+      r[k] = fminf(r[k], partial[6 * b + k]);
+      r[3 + k] = fmaxf(r[3 + k], partial[6 * b + 3 + k]);
+    }
+  }
+  for (int k = 0; k < 6; ++k) out[k] = r[k];
+}
+
+// Spreads the low 21 bits of x so that bit i lands on bit 3i.
+__device__ __forceinline__ uint64_t spread3(uint64_t x) {
+  x &= 0x1fffffull;
+  x = (x | (x << 32)) & 0x001f00000000ffffull;
+  x = (x | (x << 16)) & 0x001f0000ff0000ffull;
+  x = (x | (x << 8)) & 0x100f00f00f00f00full;
+  x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+  x = (x | (x << 2)) & 0x1249249249249249ull;
+  return x;
+}
+
+__device__ __forceinline__ uint32_t quantize(float c, float lo, float scale) {
+  float q = __fmul_rn(__fsub_rn(c, lo), scale);
+  q = fminf(fmaxf(q, 0.0f), 2097151.0f);
+  return (uint32_t)q;
+}
+
+// code = sum_i x_i << (3i+2) | y_i << (3i+1) | z_i << 3i
+__global__ void k_morton(const float* v, const uint32_t* f, uint32_t n, const float* bounds,
+                         uint64_t* keys, uint32_t* vals) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float3 c = centroid(v, f, i);
+  float scale[3];
+  for (int k = 0; k < 3; ++k) {
+    const float ext = __fsub_rn(bounds[3 + k], bounds[k]);
+    scale[k] = ext > 0.0f ? __fdiv_rn(2097152.0f, ext) : 0.0f;
+  }
+  const uint64_t qx = quantize(c.x, bounds[0], scale[0]);
+  const uint64_t qy = quantize(c.y, bounds[1], scale[1]);
+  const uint64_t qz = quantize(c.z, bounds[2], scale[2]);
+  keys[i] = (spread3(qx) << 2) | (spread3(qy) << 1) | spread3(qz);
+  vals[i] = i;
+}
+
+__device__ __forceinline__ int delta(const uint64_t* k, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  const uint64_t a = k[i], b = k[j];
+  if (a == b) return 64 + __clz(i ^ j);
+  return __clzll((long long)(a ^ b));
+}
+
+__global__ void k_karras(const uint64_t* keys, int n, Node* nodes, int* leaf_parent) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+  const int dmin = delta(keys, n, i, i - d);
+  int lmax = 2;
+  while (delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t >= 1; t >>= 1)
+    if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+  const int j = i + l * d;
+  const int dnode = delta(keys, n, i, j);
+  int s = 0;
+  for (int div = 2;; div <<= 1) {
+    const int t = (l + div - 1) / div;
+    if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    if (t <= 1) break;
+  }
+  const int gamma = i + s * d + min(d, 0);
+  const int first = min(i, j), last = max(i, j);
+  int left, right;
+  if (first == gamma) { left = ~gamma; leaf_parent[gamma] = i; }
+  else { left = gamma; nodes[gamma].d.z = i; }
+  if (last == gamma + 1) { right = ~(gamma + 1); leaf_parent[gamma + 1] = i; }
+  else { right = gamma + 1; nodes[gamma + 1].d.z = i; }
+  nodes[i].d.x = left;
+  nodes[i].d.y = right;
+  nodes[i].d.w = dnode;
+  if (i == 0) nodes[0].d.z = -1;
+}
+
+__global__ void k_pack(const float* v, const uint32_t* f, const uint32_t* order, uint32_t n,
+                       Tri* tris, uint32_t* leaf_order) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t fid = order[k];
+  const float3 a = load_v(v, f[3 * fid + 0]);
+  const float3 b = load_v(v, f[3 * fid + 1]);
+  const float3 c = load_v(v, f[3 * fid + 2]);
+  Tri t;
+  t.v0 = make_float4(a.x, a.y, a.z, __int_as_float((int)fid));
+  t.v1 = make_float4(b.x, b.y, b.z, 0.0f);
+  t.v2 = make_float4(c.x, c.y, c.z, 0.0f);
+  tris[k] = t;
+  if (leaf_order) leaf_order[k] = fid;
+}
+
+struct Box { float lo[3], hi[3]; };
+
+__device__ __forceinline__ Box tri_box(const Tri* tris, int k) {
+  const float4 a = __ldcg(&tris[k].v0), b = __ldcg(&tris[k].v1), c = __ldcg(&tris[k].v2);
+  Box r;
+  r.lo[0] = fminf(fminf(a.x, b.x), c.x); r.hi[0] = fmaxf(fmaxf(a.x, b.x), c.x);
+  r.lo[1] = fminf(fminf(a.y, b.y), c.y); r.hi[1] = fmaxf(fmaxf(a.y, b.y), c.y);
+  r.lo[2] = fminf(fminf(a.z, b.z), c.z); r.hi[2] = fmaxf(fmaxf(a.z, b.z), c.z);
+  return r;
+}
+
+__device__ __forceinline__ Box node_box(const Node* nodes, int i) {
+  const float4 a = __ldcg(&nodes[i].a), b = __ldcg(&nodes[i].b), c = __ldcg(&nodes[i].c);
+  Box r;
+  r.lo[0] = fminf(a.x, b.x); r.hi[0] = fmaxf(a.y, b.y);
+  r.lo[1] = fminf(a.z, b.z); r.hi[1] = fmaxf(a.w, b.w);
+  r.lo[2] = fminf(c.x, c.z); r.hi[2] = fmaxf(c.y, c.w);
+  return r;
+}
+
+__device__ __forceinline__ Box child_box(const Node* nodes, const Tri* tris, int c) {
+  return c < 0 ? tri_box(tris, ~c) : node_box(nodes, c);
+}
+
+// One thread per leaf walks towards the root; the second thread to reach a
+// node writes that node's two child boxes and continues.
+__global__ void k_refit(Node* nodes, const Tri* tris, const int* leaf_parent, unsigned int* flags,
+                        uint32_t n) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  int node = leaf_parent[k];
+  while (node >= 0) {
+    __threadfence();
+    const unsigned int old = atomicAdd(&flags[node], 1u);
+    if (old == 0) return;
+    __threadfence();
+    const int4 link = __ldcg(&nodes[node].d);
+    const Box L = child_box(nodes, tris, link.x);
+    const Box R = child_box(nodes, tris, link.y);
+    __stcg(&nodes[node].a, make_float4(L.lo[0], L.hi[0], L.lo[1], L.hi[1]));
+    __stcg(&nodes[node].b, make_float4(R.lo[0], R.hi[0], R.lo[1], R.hi[1]));
+    __stcg(&nodes[node].c, make_float4(L.lo[2], L.hi[2], R.lo[2], R.hi[2]));
+    node = link.z;
+  }
+}
+
+__global__ void k_depth(const Node* nodes, const int* leaf_parent, uint32_t n, unsigned int* out) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  unsigned int d = 1;
+  int node = leaf_parent[k];
+  int guard = 0;
+  while (node >= 0 && nodes[node].d.z >= 0 && guard < (1 << 20)) {
+    node = nodes[node].d.z;
+    ++d;
+    ++guard;
+  }
+  atomicMax(out, d);
+}
+
+inline unsigned grid_for(size_t n, int block = kBlock) {
+  return (unsigned)((n + block - 1) / block);
+}
+
+// Single-triangle map: one node whose right child is a phantom box far
+// outside any ray's reach (t ~ 1e30 > range.max), so traversal never takes it.
+void single_node(const float* v, const uint32_t* f, Node* out) {
+  float lo[3], hi[3];
+  for (int k = 0; k < 3; ++k) {
+    const float a = v[3 * f[0] + k], b = v[3 * f[1] + k], c = v[3 * f[2] + k];
+    lo[k] = std::min(std::min(a, b), c);
+    hi[k] = std::max(std::max(a, b), c);
+  }
+  const float far = 1e30f;
+  out->a = make_float4(lo[0], hi[0], lo[1], hi[1]);
+  out->b = make_float4(far, far, far, far);
+  out->c = make_float4(lo[2], hi[2], far, far);
+  out->d = make_int4(-1, -1, -1, 0);
+}
+
+void free_map(rmg_map* m) {
+  if (!m) return;
+  cudaFree(m->d_vertices);
+  cudaFree(m->d_faces);
+  cudaFree(m->d_nodes);
+  cudaFree(m->d_tris);
+  cudaFree(m->d_leaf_order);
+  cudaFree(m->d_leaf_parent);
+  cudaFree(m->d_flags);
+  cudaFree(m->d_status);
+  delete m;
+}
+
+// Packs the triangles and refits all boxes of an existing topology.
+int repack_and_refit(rmg_map* m, cudaStream_t st, const uint32_t* d_order) {
+  const uint32_t n = m->n_faces;
+  if (n == 0) return RMG_OK;
+  k_pack<<<grid_for(n), kBlock, 0, st>>>(m->d_vertices, m->d_faces, d_order, n, m->d_tris,
+                                        nullptr);
+  RMG_CUDA_TRY(cudaGetLastError());
+  if (n == 1) {
+    // recompute the single node's box on the host from the new vertices
+    float v[9];
+    uint32_t f[3];
+    RMG_CUDA_TRY(cudaMemcpyAsync(f, m->d_faces, sizeof(f), cudaMemcpyDeviceToHost, st));
+    RMG_CUDA_TRY(cudaStreamSynchronize(st));
+    const uint32_t local[3] = {0, 1, 2};
+    for (int k = 0; k < 3; ++k)
+      RMG_CUDA_TRY(cudaMemcpyAsync(v + 3 * k, m->d_vertices + 3 * f[k], 3 * sizeof(float),
+                                   cudaMemcpyDeviceToHost, st));
+    RMG_CUDA_TRY(cudaStreamSynchronize(st));
+    Node node;
+    single_node(v, local, &node);
+    RMG_CUDA_TRY(cudaMemcpyAsync(m->d_nodes, &node, sizeof(Node), cudaMemcpyHostToDevice, st));
+    return RMG_OK;
+  }
+  RMG_CUDA_TRY(cudaMemsetAsync(m->d_flags, 0, m->n_nodes * sizeof(unsigned int), st));
+  k_refit<<<grid_for(n), kBlock, 0, st>>>(m->d_nodes, m->d_tris, m->d_leaf_parent, m->d_flags, n);
+  RMG_CUDA_TRY(cudaGetLastError());
+  return RMG_OK;
+}
+
+void update_info(rmg_map* m, cudaStream_t st) {
+  for (int k = 0; k < 3; ++k) { m->lo[k] = INFINITY; m->hi[k] = -INFINITY; }
+  if (m->n_faces == 0) return;
+  Node root;
+  if (cudaMemcpyAsync(&root, m->d_nodes, sizeof(Node), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    return;
+  if (cudaStreamSynchronize(st) != cudaSuccess) return;
+  if (m->n_faces == 1) {
+    m->lo[0] = root.a.x; m->hi[0] = root.a.y; m->lo[1] = root.a.z; m->hi[1] = root.a.w;
+    m->lo[2] = root.c.x; m->hi[2] = root.c.y;
+    return;
+  }
+  m->lo[0] = std::min(root.a.x, root.b.x); m->hi[0] = std::max(root.a.y, root.b.y);
+  m->lo[1] = std::min(root.a.z, root.b.z); m->hi[1] = std::max(root.a.w, root.b.w);
+  m->lo[2] = std::min(root.c.x, root.c.z); m->hi[2] = std::max(root.c.y, root.c.w);
+}
+
+}  // namespace
+
+DeviceMap device_view(const rmg_map* m) {
+  DeviceMap d;
+  d.nodes = m->d_nodes;
+  d.tris = m->d_tris;
+  d.n_nodes = (int)m->n_nodes;
+  d.n_tris = (int)m->n_faces;
+  d.root = m->n_faces > 0 ? 0 : -1;
+  d.status = m->d_status;
+  return d;
+}
+
+}  // namespace rmg
+
+using namespace rmg;
+
+extern "C" int rmg_map_build(const rmg_vec3* vertices, uint32_t n_vertices, const rmg_face* faces,
+                             uint32_t n_faces, void* stream, rmg_map** out) {
+  if (!out) return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: out is NULL");
+  *out = nullptr;
+  if (n_faces > 0 && (!vertices || !faces))
+    return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: vertices/faces are NULL");
+  if (n_faces > (1u << 30)) return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: too many faces");
+  for (uint32_t i = 0; i < n_faces; ++i) {
+    if (faces[i].v0 >= n_vertices || faces[i].v1 >= n_vertices || faces[i].v2 >= n_vertices)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: face index out of range");
+  }
+  cudaStream_t st = as_stream(stream);
+  rmg_map* m = new (std::nothrow) rmg_map;
+  if (!m) return fail(RMG_ERR_OOM, "rmg_map_build: host allocation");
+  std::memset(m, 0, sizeof(*m));
+  cudaGetDevice(&m->device);
+  m->n_vertices = n_vertices;
+  m->n_faces = n_faces;
+  m->n_nodes = n_faces >= 2 ? n_faces - 1 : (n_faces == 1 ? 1 : 0);
+
+  int s = RMG_OK;
+  auto check = [&](int r) { if (s == RMG_OK) s = r; return s == RMG_OK; };
+
+  check(dev_alloc(&m->d_status, 1, "status"));
+  if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(m->d_status, 0, sizeof(unsigned int), st), "memset");
+  if (s == RMG_OK && n_faces == 0) {
+    s = cuda_status(cudaStreamSynchronize(st), "sync");
+    if (s != RMG_OK) { free_map(m); return s; }
+    update_info(m, st);
+    *out = m;
+    return RMG_OK;
+  }
+  check(dev_alloc(&m->d_vertices, 3 * (size_t)n_vertices, "vertices"));
+  check(dev_alloc(&m->d_faces, 3 * (size_t)n_faces, "faces"));
+  check(dev_alloc(&m->d_nodes, m->n_nodes, "nodes"));
+  check(dev_alloc(&m->d_tris, n_faces, "tris"));
+  check(dev_alloc(&m->d_leaf_order, n_faces, "leaf order"));
+  check(dev_alloc(&m->d_leaf_parent, n_faces, "leaf parent"));
+  check(dev_alloc(&m->d_flags, m->n_nodes, "flags"));
+  if (s != RMG_OK) { free_map(m); return s; }
+  s = cuda_status(cudaMemcpyAsync(m->d_vertices, vertices, 12 * (size_t)n_vertices,
+                                  cudaMemcpyHostToDevice, st), "copy vertices");
+  if (s == RMG_OK)
+    s = cuda_status(cudaMemcpyAsync(m->d_faces, faces, 12 * (size_t)n_faces,
+                                    cudaMemcpyHostToDevice, st), "copy faces");
+  if (s != RMG_OK) { free_map(m); return s; }
+
+  if (n_faces == 1) {
+    Node node;
+    const uint32_t local[3] = {0, 1, 2};
+    float v[9];
+    for (int k = 0; k < 3; ++k) {
+      const uint32_t vi = k == 0 ? faces[0].v0 : (k == 1 ? faces[0].v1 : faces[0].v2);
+      v[3 * k + 0] = vertices[vi].x; v[3 * k + 1] = vertices[vi].y; v[3 * k + 2] = vertices[vi].z;
+    }
+    single_node(v, local, &node);
+    const uint32_t zero = 0;
+    const int minus1 = -1;
+    s = cuda_status(cudaMemcpyAsync(m->d_nodes, &node, sizeof(Node), cudaMemcpyHostToDevice, st), "node");
+    if (s == RMG_OK) s = cuda_status(cudaMemcpyAsync(m->d_leaf_order, &zero, 4, cudaMemcpyHostToDevice, st), "order");
+    if (s == RMG_OK) s = cuda_status(cudaMemcpyAsync(m->d_leaf_parent, &minus1, 4, cudaMemcpyHostToDevice, st), "parent");
+    if (s == RMG_OK) {
+      k_pack<<<1, 32, 0, st>>>(m->d_vertices, m->d_faces, m->d_leaf_order, 1, m->d_tris, nullptr);
+      s = cuda_status(cudaGetLastError(), "k_pack");
+    }
+    if (s == RMG_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
+    if (s != RMG_OK) { free_map(m); return s; }
+    m->depth = 1;
+    update_info(m, st);
+    *out = m;
+    return RMG_OK;
+  }
+
+  // ---- scratch ----------------------------------------------------------
+  const uint32_t n = n_faces;
+  const int nb = std::min<int>((int)grid_for(n), 4 * device_sm_count());
+  float* d_partial = nullptr;
+  float* d_bounds = nullptr;
+  uint64_t *d_keys = nullptr, *d_keys2 = nullptr;
+  uint32_t *d_vals = nullptr, *d_vals2 = nullptr;
+  unsigned int* d_depth = nullptr;
+  void* d_temp = nullptr;
+  size_t temp_bytes = 0;
+  check(dev_alloc(&d_partial, 6 * (size_t)nb, "partial bounds"));
+  check(dev_alloc(&d_bounds, 6, "bounds"));
+  check(dev_alloc(&d_keys, n, "keys"));
+  check(dev_alloc(&d_keys2, n, "keys2"));
+  check(dev_alloc(&d_vals, n, "vals"));
+  check(dev_alloc(&d_vals2, n, "vals2"));
+  check(dev_alloc(&d_depth, 1, "depth"));
+  if (s == RMG_OK) {
+    s = cuda_status(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, d_keys, d_keys2, d_vals,
+                                                     d_vals2, (int)n, 0, 63, st), "sort size");
+  }
+  if (s == RMG_OK) {
+    char* tmp = nullptr;
+    s = dev_alloc(&tmp, temp_bytes, "sort temp");
+    d_temp = tmp;
+  }
+  if (s == RMG_OK) {
+    k_centroid_bounds<<<nb, kBlock, 0, st>>>(m->d_vertices, m->d_faces, n, d_partial);
+    k_bounds_final<<<1, 32, 0, st>>>(d_partial, nb, d_bounds);
+    k_morton<<<grid_for(n), kBlock, 0, st>>>(m->d_vertices, m->d_faces, n, d_bounds, d_keys, d_vals);
+    s = cuda_status(cudaGetLastError(), "morton");
+  }
+  if (s == RMG_OK)
+    s = cuda_status(cub::DeviceRadixSort::SortPairs(d_temp, temp_bytes, d_keys, d_keys2, d_vals,
+                                                     d_vals2, (int)n, 0, 63, st), "sort");
+  if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(m->d_nodes, 0, sizeof(Node) * m->n_nodes, st), "memset");
+  if (s == RMG_OK) {
+    k_karras<<<grid_for(n - 1), kBlock, 0, st>>>(d_keys2, (int)n, m->d_nodes, m->d_leaf_parent);
+    k_pack<<<grid_for(n), kBlock, 0, st>>>(m->d_vertices, m->d_faces, d_vals2, n, m->d_tris,
+                                          m->d_leaf_order);
+    s = cuda_status(cudaGetLastError(), "karras");
+  }
+  if (s == RMG_OK) s = repack_and_refit(m, st, m->d_leaf_order);
+  if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(d_depth, 0, 4, st), "memset");
+  if (s == RMG_OK) {
+    k_depth<<<grid_for(n), kBlock, 0, st>>>(m->d_nodes, m->d_leaf_parent, n, d_depth);
+    s = cuda_status(cudaGetLastError(), "depth");
+  }
+  unsigned int depth = 0;
+  if (s == RMG_OK) s = cuda_status(cudaMemcpyAsync(&depth, d_depth, 4, cudaMemcpyDeviceToHost, st), "depth copy");
+  if (s == RMG_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
+  cudaFree(d_partial); cudaFree(d_bounds); cudaFree(d_keys); cudaFree(d_keys2);
+  cudaFree(d_vals); cudaFree(d_vals2); cudaFree(d_depth); cudaFree(d_temp);
+  if (s != RMG_OK) { free_map(m); return s; }
+  m->depth = depth;
+  update_info(m, st);
+  *out = m;
+  return RMG_OK;
+}
+
+extern "C" int rmg_map_refit(rmg_map* m, const rmg_vec3* vertices, uint32_t n_vertices, void* stream) {
+  if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_refit: map is NULL");
+  if (n_vertices != m->n_vertices)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_map_refit: vertex count differs from the build");
+  if (m->n_faces == 0) return RMG_OK;
+  if (!vertices) return fail(RMG_ERR_INVALID_ARG, "rmg_map_refit: vertices is NULL");
+  cudaStream_t st = as_stream(stream);
+  RMG_CUDA_TRY(cudaMemcpyAsync(m->d_vertices, vertices, 12 * (size_t)n_vertices,
+                               cudaMemcpyHostToDevice, st));
+  int s = repack_and_refit(m, st, m->d_leaf_order);
+  if (s != RMG_OK) return s;
+  RMG_CUDA_TRY(cudaStreamSynchronize(st));
+  update_info(m, st);
+  return RMG_OK;
+}
+
+extern "C" int rmg_map_destroy(rmg_map* m) {
+  if (!m) return RMG_OK;
+  free_map(m);
+  return RMG_OK;
+}
+
+extern "C" int rmg_map_info_get(const rmg_map* m, rmg_map_info* out) {
+  if (!m || !out) return fail(RMG_ERR_INVALID_ARG, "rmg_map_info_get: NULL argument");
+  out->n_vertices = m->n_vertices;
+  out->n_faces = m->n_faces;
+  out->n_nodes = m->n_nodes;
+  out->depth = m->depth;
+  out->device_bytes = (uint64_t)m->n_nodes * sizeof(Node) + (uint64_t)m->n_faces * sizeof(Tri) +
+                      12ull * m->n_vertices + 12ull * m->n_faces;
+  for (int k = 0; k < 3; ++k) { out->bounds_lo[k] = m->lo[k]; out->bounds_hi[k] = m->hi[k]; }
+  return RMG_OK;
+}
+
+extern "C" int rmg_map_export(const rmg_map* m, void* nodes, void* tris, uint32_t* leaf_order) {
+  if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_export: map is NULL");
+  if (nodes && m->n_nodes)
+    RMG_CUDA_TRY(cudaMemcpy(nodes, m->d_nodes, sizeof(Node) * m->n_nodes, cudaMemcpyDeviceToHost));
+  if (tris && m->n_faces)
+    RMG_CUDA_TRY(cudaMemcpy(tris, m->d_tris, sizeof(Tri) * m->n_faces, cudaMemcpyDeviceToHost));
+  if (leaf_order && m->n_faces)
+    RMG_CUDA_TRY(cudaMemcpy(leaf_order, m->d_leaf_order, 4ull * m->n_faces, cudaMemcpyDeviceToHost));
+  return RMG_OK;
+}
+
+extern "C" int rmg_map_status(rmg_map* m, int clear) {
+  if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_status: map is NULL");
+  unsigned int word = 0;
+  RMG_CUDA_TRY(cudaMemcpy(&word, m->d_status, 4, cudaMemcpyDeviceToHost));
+  if (clear) RMG_CUDA_TRY(cudaMemset(m->d_status, 0, 4));
+  if (word != 0) {
+    set_error("a kernel recorded a device error on this map");
+    return (int)word;
+  }
+  return RMG_OK;
+}
+
+extern "C" int rmg_map_debug_set_child(rmg_map* m, uint32_t node, uint32_t which, int32_t child) {
+  if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: map is NULL");
+  if (node >= m->n_nodes || which > 1)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: node/which out of range");
+  if (child >= 0 ? (uint32_t)child >= m->n_nodes : (uint32_t)(~child) >= m->n_faces)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: child out of range");
+  const size_t off = offsetof(Node, d) + (which ? sizeof(int) : 0);
+  RMG_CUDA_TRY(cudaMemcpy(reinterpret_cast<char*>(m->d_nodes + node) + off, &child, sizeof(int),
+                          cudaMemcpyHostToDevice));
+  return RMG_OK;
+}

@@ -1,0 +1,105 @@
+// rmg_simulate: the C entry point of the plain (one sensor, many poses) path.
+#include <string>
+
+#include "internal.h"
+#include "launch.h"
+#include "trace.cuh"
+
+namespace rmg {
+
+int default_config(const rmg_sensor* s, rmg_launch_config* cfg) {
+  cfg->stack_depth = 8;
+  cfg->block_warps = 4;
+  if (s && s->width >= 8 && s->height >= 4) { cfg->tile_w = 8; cfg->tile_h = 4; }
+  else if (s && s->height < 4 && s->height > 1) { cfg->tile_w = 16; cfg->tile_h = 2; }
+  else { cfg->tile_w = 32; cfg->tile_h = 1; }
+  return RMG_OK;
+}
+
+int check_config(const rmg_launch_config& c) {
+  if (!valid_stack_depth(c.stack_depth))
+    return fail(RMG_ERR_UNSUPPORTED, "launch config: stack_depth must be 0, 4, 8, 16 or 32");
+  if (c.block_warps < 1 || c.block_warps > 8)
+    return fail(RMG_ERR_UNSUPPORTED, "launch config: block_warps must be 1..8");
+  if (c.tile_w == 0 || (c.tile_w & (c.tile_w - 1)) != 0 || c.tile_w > 32 || c.tile_w * c.tile_h != 32)
+    return fail(RMG_ERR_UNSUPPORTED, "launch config: tile_w must be a power of two with tile_w*tile_h == 32");
+  return RMG_OK;
+}
+
+int log2u(uint32_t v) {
+  int l = 0;
+  while ((1u << l) < v) ++l;
+  return l;
+}
+
+// Fills the parameter block of one sensor's launch; returns the tile count.
+int make_trace_params(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                      const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
+                      const rmg_launch_config& cfg, TraceParams& P) {
+  P.map = device_view(map);
+  P.sen = device_view(sensor);
+  const rmg_transform Tsb_ = *Tsb;
+  P.Tsb = Tf{Q{Tsb_.R.x, Tsb_.R.y, Tsb_.R.z, Tsb_.R.w}, V{Tsb_.t.x, Tsb_.t.y, Tsb_.t.z}};
+  P.Tbm = Tbm;
+  P.n_poses = n_poses;
+  P.out = *out;
+  P.tile_w_log2 = (uint32_t)log2u(cfg.tile_w);
+  P.tile_h = cfg.tile_h;
+  P.tiles_x = (sensor->width + cfg.tile_w - 1) / cfg.tile_w;
+  const uint32_t tiles_y = (sensor->height + cfg.tile_h - 1) / cfg.tile_h;
+  P.tiles_per_pose = P.tiles_x * tiles_y;
+  P.n_tiles = (uint64_t)P.tiles_per_pose * n_poses;
+  P.budget = 2u * map->n_nodes + 64u;
+  return RMG_OK;
+}
+
+int launch_plain(const TraceParams& P, const rmg_sensor* sensor, const rmg_launch_config& cfg,
+                 cudaStream_t st) {
+  const uint64_t blocks = (P.n_tiles + cfg.block_warps - 1) / cfg.block_warps;
+  if (blocks > 0x7fffffffull) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate: too many rays for one launch");
+  const unsigned block = 32u * cfg.block_warps;
+  cudaError_t e;
+  switch (sensor->model.kind) {
+    case RMG_MODEL_SPHERICAL:
+    case RMG_MODEL_PINHOLE: e = launch_trace_pose(P, (int)cfg.stack_depth, (unsigned)blocks, block, st); break;
+    case RMG_MODEL_O1DN: e = launch_trace_single(P, (int)cfg.stack_depth, (unsigned)blocks, block, st); break;
+    default: e = launch_trace_table(P, (int)cfg.stack_depth, (unsigned)blocks, block, st); break;
+  }
+  return cuda_status(e, "trace launch");
+}
+
+}  // namespace rmg
+
+using namespace rmg;
+
+extern "C" int rmg_default_launch_config(const rmg_map* map, const rmg_sensor* sensor,
+                                         rmg_launch_config* cfg) {
+  (void)map;
+  if (!cfg) return fail(RMG_ERR_INVALID_ARG, "rmg_default_launch_config: cfg is NULL");
+  return default_config(sensor, cfg);
+}
+
+extern "C" int rmg_simulate_ex(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                               const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
+                               const rmg_launch_config* cfg_in, void* stream) {
+  if (!map || !sensor || !Tsb || !out)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_simulate: NULL map, sensor, Tsb or outputs");
+  if (n_poses == 0) return RMG_OK;
+  if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate: Tbm is NULL");
+  rmg_launch_config cfg;
+  if (cfg_in) cfg = *cfg_in; else default_config(sensor, &cfg);
+  int s = check_config(cfg);
+  if (s != RMG_OK) return s;
+  if (!out->hits && !out->ranges && !out->points && !out->normals && !out->face_ids &&
+      !out->geom_ids && !out->object_ids)
+    return RMG_OK;  // nothing requested: the reference writes nothing either
+  TraceParams P;
+  make_trace_params(map, sensor, Tsb, Tbm, n_poses, out, cfg, P);
+  return launch_plain(P, sensor, cfg, as_stream(stream));
+}
+
+extern "C" int rmg_simulate(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                            const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
+                            void* stream) {
+  return rmg_simulate_ex(map, sensor, Tsb, Tbm, n_poses, out, nullptr, stream);
+}

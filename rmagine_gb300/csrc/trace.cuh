@@ -1,0 +1,303 @@
+// Per-ray closest-hit traversal of the LBVH and the attribute epilogue.
+//
+// This is the GPU restatement of the per-ray body of rmagine's simulators:
+//   SphereSimulatorEmbree.tcc:69-249 (ray setup, rtcIntersect1, attributes)
+//   O1DnSimulatorEmbree.tcc:84-132, OnDnSimulatorEmbree.tcc:86-134 (origins)
+// with the BVH query done by this file instead of Embree/OptiX.
+//
+// Traversal ("short stack + parent pointers"):
+//   * Every internal node carries both child boxes; a visit tests the two
+//     boxes, intersects leaf children (one triangle each) on the spot and
+//     descends into the nearer hit internal child.
+//   * A 128-bit trail records, one bit per level, whether the other child of
+//     that level is still pending.  The pending children themselves are kept
+//     in a circular short stack of SS entries (SS = 0: none).  When the stack
+//     has run dry but the trail still has pending levels, the ray climbs the
+//     parent links to the pending level and takes the sibling: stackless
+//     backtracking in the manner of Hapala et al. 2011 / Afra and
+//     Szirmay-Kalos 2014, so any SS gives the same visits and results.
+//   * Box tests widen the interval by 2^-22 relative; triangle tests are the
+//     watertight test of common.cuh.  Closest-hit ties are broken by the
+//     smaller face id, so the result does not depend on traversal order.
+//   * Every ray has a step budget (2 * internal nodes + 64 node visits and
+//     parent climbs, more than any valid tree needs).  Exceeding it records
+//     RMG_ERR_TRAVERSAL_BUDGET in the map's device status word and ends the
+//     ray as a miss: a corrupt tree cannot hang the kernel.
+#pragma once
+
+#include "common.cuh"
+
+namespace rmg {
+
+constexpr float kWiden = 1.00000024f;  // 1 + 2^-22
+
+enum OriginKind { ORIGIN_POSE = 0, ORIGIN_SINGLE = 1, ORIGIN_TABLE = 2 };
+
+struct Hit {
+  float t;
+  int tri;          // packed (leaf-order) triangle index, -1 = none
+  uint32_t face;    // original face id
+};
+
+struct RayBox {
+  float ix, iy, iz;     // 1/d (zero components replaced by +-1e20)
+  float oix, oiy, oiz;  // o/d
+};
+
+__device__ __forceinline__ RayBox make_raybox(const V& o, const V& d) {
+  RayBox r;
+  r.ix = fabsf(d.x) > 1e-20f ? __frcp_rn(d.x) : copysignf(1e20f, d.x);
+  r.iy = fabsf(d.y) > 1e-20f ? __frcp_rn(d.y) : copysignf(1e20f, d.y);
+  r.iz = fabsf(d.z) > 1e-20f ? __frcp_rn(d.z) : copysignf(1e20f, d.z);
+  r.oix = o.x * r.ix;
+  r.oiy = o.y * r.iy;
+  r.oiz = o.z * r.iz;
+  return r;
+}
+
+// Slab test of one box; tmin includes the ray's tnear = 0.
+__device__ __forceinline__ void slab(const RayBox& r, float lox, float hix, float loy, float hiy,
+                                     float loz, float hiz, float& tmin, float& tmax) {
+  const float x0 = fmaf(lox, r.ix, -r.oix), x1 = fmaf(hix, r.ix, -r.oix);
+  const float y0 = fmaf(loy, r.iy, -r.oiy), y1 = fmaf(hiy, r.iy, -r.oiy);
+  const float z0 = fmaf(loz, r.iz, -r.oiz), z1 = fmaf(hiz, r.iz, -r.oiz);
+  tmin = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), 0.0f));
+  tmax = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
+}
+
+__device__ __forceinline__ bool visit(float tmin, float tmax, float best) {
+  return tmin <= fminf(tmax, best) * kWiden;
+}
+
+__device__ __forceinline__ void test_tri(const DeviceMap& map, const RayW& rw, int k, Hit& h) {
+  const Tri* tp = map.tris + k;
+  const float4 p0 = __ldg(&tp->v0), p1 = __ldg(&tp->v1), p2 = __ldg(&tp->v2);
+  float t;
+  if (tri_hit(rw, p0, p1, p2, h.t, t)) {
+    const uint32_t f = __float_as_uint(p0.w);
+    if (t < h.t || f < h.face) { h.t = t; h.tri = k; h.face = f; }
+  }
+}
+
+// 128-bit trail helpers.
+__device__ __forceinline__ void trail_push(uint64_t& lo, uint64_t& hi, uint64_t bit) {
+  hi = (hi << 1) | (lo >> 63);
+  lo = (lo << 1) | bit;
+}
+__device__ __forceinline__ int trail_ctz(uint64_t lo, uint64_t hi) {
+  return lo ? (__ffsll((long long)lo) - 1) : (64 + __ffsll((long long)hi) - 1);
+}
+__device__ __forceinline__ void trail_shr(uint64_t& lo, uint64_t& hi, int k) {
+  if (k >= 64) { lo = hi >> (k - 64); hi = 0; }
+  else if (k > 0) { lo = (lo >> k) | (hi << (64 - k)); hi >>= k; }
+}
+
+template <int SS>
+__device__ __forceinline__ void trace_ray(const DeviceMap& map, const V& o, const V& d, float tfar,
+                                          unsigned budget, Hit& h, bool& over_budget) {
+  h.t = tfar;
+  h.tri = -1;
+  h.face = 0xffffffffu;
+  if (map.root < 0) return;
+  const RayW rw = make_rayw(o, d);
+  const RayBox rb = make_raybox(o, d);
+
+  int node = map.root;
+  uint64_t tlo = 0, thi = 0;
+  int stk[SS > 0 ? SS : 1];
+  float stkt[SS > 0 ? SS : 1];
+  int sp = 0, top = 0;
+  unsigned steps = 0;
+
+  for (;;) {
+    if (++steps > budget) { over_budget = true; h.tri = -1; h.t = tfar; h.face = 0xffffffffu; return; }
+    const Node* np = map.nodes + node;
+    const float4 a = __ldg(&np->a);
+    const float4 b = __ldg(&np->b);
+    const float4 c = __ldg(&np->c);
+    const int4 ln = __ldg(&np->d);
+    float tminL, tmaxL, tminR, tmaxR;
+    slab(rb, a.x, a.y, a.z, a.w, c.x, c.y, tminL, tmaxL);
+    slab(rb, b.x, b.y, b.z, b.w, c.z, c.w, tminR, tmaxR);
+    bool hitL = visit(tminL, tmaxL, h.t);
+    bool hitR = visit(tminR, tmaxR, h.t);
+    if (hitL && ln.x < 0) { test_tri(map, rw, ~ln.x, h); hitL = false; }
+    if (hitR && ln.y < 0) { test_tri(map, rw, ~ln.y, h); hitR = false; }
+    hitL = hitL && tminL <= h.t * kWiden;
+    hitR = hitR && tminR <= h.t * kWiden;
+    if (hitL && hitR) {
+      const bool lf = tminL <= tminR;
+      const int nearc = lf ? ln.x : ln.y;
+      if (SS > 0) {
+        top = (top + 1) & (SS - 1);
+        stk[top] = lf ? ln.y : ln.x;
+        stkt[top] = lf ? tminR : tminL;
+        sp = sp < SS ? sp + 1 : SS;
+      }
+      trail_push(tlo, thi, 1);
+      node = nearc;
+      continue;
+    }
+    if (hitL || hitR) {
+      trail_push(tlo, thi, 0);
+      node = hitL ? ln.x : ln.y;
+      continue;
+    }
+    // ---- backtrack to the nearest pending level ----
+    bool found = false;
+    while (tlo | thi) {
+      const int k = trail_ctz(tlo, thi);
+      trail_shr(tlo, thi, k);
+      tlo ^= 1ull;
+      if (SS > 0 && sp > 0) {
+        const int cand = stk[top];
+        const float ct = stkt[top];
+        top = (top - 1) & (SS > 0 ? SS - 1 : 0);
+        --sp;
+        node = cand;
+        if (ct <= h.t * kWiden) { found = true; break; }
+      } else {
+        // The trail never holds more levels than the path below the root, so
+        // a climb that reaches the root's parent (-1) means a corrupt tree.
+        for (int j = 0; j < k && node >= 0; ++j) node = __ldg(&map.nodes[node].d.z);
+        steps += (unsigned)k;
+        const int p = node >= 0 ? __ldg(&map.nodes[node].d.z) : -1;
+        if (steps > budget || p < 0) {
+          over_budget = true; h.tri = -1; h.t = tfar; h.face = 0xffffffffu; return;
+        }
+        const Node* pp = map.nodes + p;
+        const int4 pl = __ldg(&pp->d);
+        float tmin, tmax;
+        int sib;
+        if (pl.x == node) {
+          sib = pl.y;
+          const float4 bb = __ldg(&pp->b);
+          const float4 cc = __ldg(&pp->c);
+          slab(rb, bb.x, bb.y, bb.z, bb.w, cc.z, cc.w, tmin, tmax);
+        } else {
+          sib = pl.x;
+          const float4 aa = __ldg(&pp->a);
+          const float4 cc = __ldg(&pp->c);
+          slab(rb, aa.x, aa.y, aa.z, aa.w, cc.x, cc.y, tmin, tmax);
+        }
+        node = sib;
+        if (visit(tmin, tmax, h.t)) { found = true; break; }
+      }
+    }
+    if (!found) return;
+  }
+}
+
+struct TraceParams {
+  DeviceMap map;
+  SensorDev sen;
+  Tf Tsb;
+  const rmg_transform* Tbm;
+  uint32_t n_poses;
+  rmg_outputs out;
+  uint32_t tile_w_log2;
+  uint32_t tile_h;
+  uint32_t tiles_x;
+  uint32_t tiles_per_pose;
+  uint64_t n_tiles;
+  unsigned budget;
+};
+
+// Writes all requested attributes of one ray (SphereSimulatorEmbree.tcc:104-249).
+template <int OK>
+__device__ __forceinline__ void write_attributes(const TraceParams& P, uint64_t gid, const Hit& h,
+                                                 const V& dir_s, const V& orig_s, const Tf& Tsm) {
+  const rmg_outputs& out = P.out;
+  const float rmin = P.sen.range_min, rmax = P.sen.range_max;
+  if (h.tri >= 0) {
+    const float t = h.t;
+    if (out.hits) out.hits[gid] = t >= rmin ? 1 : 0;
+    if (out.ranges) out.ranges[gid] = t;
+    if (out.points) {
+      V p{mul(dir_s.x, t), mul(dir_s.y, t), mul(dir_s.z, t)};
+      if (OK != ORIGIN_POSE) { p.x = add(p.x, orig_s.x); p.y = add(p.y, orig_s.y); p.z = add(p.z, orig_s.z); }
+      float* po = reinterpret_cast<float*>(out.points) + 3 * gid;
+      po[0] = p.x; po[1] = p.y; po[2] = p.z;
+    }
+    if (out.normals) {
+      const Tri* tp = P.map.tris + h.tri;
+      const float4 p0 = __ldg(&tp->v0), p1 = __ldg(&tp->v1), p2 = __ldg(&tp->v2);
+      const V e1{sub(p1.x, p0.x), sub(p1.y, p0.y), sub(p1.z, p0.z)};
+      const V e2{sub(p2.x, p0.x), sub(p2.y, p0.y), sub(p2.z, p0.z)};
+      V n{sub(mul(e1.y, e2.z), mul(e1.z, e2.y)), sub(mul(e1.z, e2.x), mul(e1.x, e2.z)),
+          sub(mul(e1.x, e2.y), mul(e1.y, e2.x))};
+      float len = __fsqrt_rn(add(add(mul(n.x, n.x), mul(n.y, n.y)), mul(n.z, n.z)));
+      n = V{__fdiv_rn(n.x, len), __fdiv_rn(n.y, len), __fdiv_rn(n.z, len)};
+      n = qrot(qconj(Tsm.R), n);
+      const float dp = add(add(mul(dir_s.x, n.x), mul(dir_s.y, n.y)), mul(dir_s.z, n.z));
+      if (dp > 0.0f) n = V{-n.x, -n.y, -n.z};
+      len = __fsqrt_rn(add(add(mul(n.x, n.x), mul(n.y, n.y)), mul(n.z, n.z)));
+      float* no = reinterpret_cast<float*>(out.normals) + 3 * gid;
+      no[0] = __fdiv_rn(n.x, len); no[1] = __fdiv_rn(n.y, len); no[2] = __fdiv_rn(n.z, len);
+    }
+    if (out.face_ids) out.face_ids[gid] = h.face;
+    if (out.geom_ids) out.geom_ids[gid] = 0u;
+    if (out.object_ids) out.object_ids[gid] = 0u;
+  } else {
+    const float nanf_ = __int_as_float(0x7fc00000);
+    if (out.hits) out.hits[gid] = 0;
+    if (out.ranges) out.ranges[gid] = add(rmax, 1.0f);
+    if (out.points) {
+      float* po = reinterpret_cast<float*>(out.points) + 3 * gid;
+      po[0] = nanf_; po[1] = nanf_; po[2] = nanf_;
+    }
+    if (out.normals) {
+      float* no = reinterpret_cast<float*>(out.normals) + 3 * gid;
+      no[0] = nanf_; no[1] = nanf_; no[2] = nanf_;
+    }
+    if (out.face_ids) out.face_ids[gid] = 0xffffffffu;
+    if (out.geom_ids) out.geom_ids[gid] = 0xffffffffu;
+    if (out.object_ids) out.object_ids[gid] = 0xffffffffu;
+  }
+}
+
+// Ray setup of one (pose, row, col): SphereSimulatorEmbree.tcc:69-99.
+template <int OK>
+__device__ __forceinline__ void setup_ray(const SensorDev& sen, const Tf& Tsm, uint32_t loc, V& dir_s,
+                                          V& orig_s, V& o, V& d) {
+  dir_s = V{__ldg(sen.dirs + 3 * loc), __ldg(sen.dirs + 3 * loc + 1), __ldg(sen.dirs + 3 * loc + 2)};
+  d = qrot(Tsm.R, dir_s);
+  if (OK == ORIGIN_POSE) {
+    orig_s = V{0.0f, 0.0f, 0.0f};
+    o = Tsm.t;
+  } else {
+    if (OK == ORIGIN_SINGLE) orig_s = V{sen.orig.x, sen.orig.y, sen.orig.z};
+    else orig_s = V{__ldg(sen.origs + 3 * loc), __ldg(sen.origs + 3 * loc + 1), __ldg(sen.origs + 3 * loc + 2)};
+    const V r = qrot(Tsm.R, orig_s);
+    o = V{add(r.x, Tsm.t.x), add(r.y, Tsm.t.y), add(r.z, Tsm.t.z)};
+  }
+}
+
+// One warp = one tile of tile_h x tile_w rays of one pose.
+template <int OK, int SS>
+__global__ void __launch_bounds__(256) k_trace(const TraceParams P) {
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= P.n_tiles) return;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t pose = (uint32_t)(warp / P.tiles_per_pose);
+  const uint32_t r = (uint32_t)(warp - (uint64_t)pose * P.tiles_per_pose);
+  const uint32_t ty = r / P.tiles_x, tx = r - ty * P.tiles_x;
+  const uint32_t tile_w = 1u << P.tile_w_log2;
+  const uint32_t vid = ty * P.tile_h + (lane >> P.tile_w_log2);
+  const uint32_t hid = tx * tile_w + (lane & (tile_w - 1));
+  const uint32_t W = P.sen.width, H = P.sen.height;
+  if (vid >= H || hid >= W) return;
+  const uint32_t loc = vid * W + hid;
+  const uint64_t gid = (uint64_t)pose * W * H + loc;
+
+  const Tf Tsm = tmul(load_tf(P.Tbm[pose]), P.Tsb);
+  V dir_s, orig_s, o, d;
+  setup_ray<OK>(P.sen, Tsm, loc, dir_s, orig_s, o, d);
+  Hit h;
+  bool over = false;
+  trace_ray<SS>(P.map, o, d, P.sen.range_max, P.budget, h, over);
+  if (over) atomicExch(P.map.status, (unsigned)RMG_ERR_TRAVERSAL_BUDGET);
+  write_attributes<OK>(P, gid, h, dir_s, orig_s, Tsm);
+}
+
+}  // namespace rmg

@@ -1,0 +1,20 @@
+// Instantiates the traversal kernel for ORIGIN_POSE rays (see trace.cuh).
+#include "trace.cuh"
+#include "launch.h"
+
+namespace rmg {
+
+cudaError_t launch_trace_pose(const TraceParams& P, int stack_depth, unsigned grid, unsigned block,
+                               cudaStream_t st) {
+  switch (stack_depth) {
+    case 0: k_trace<ORIGIN_POSE, 0><<<grid, block, 0, st>>>(P); break;
+    case 4: k_trace<ORIGIN_POSE, 4><<<grid, block, 0, st>>>(P); break;
+    case 8: k_trace<ORIGIN_POSE, 8><<<grid, block, 0, st>>>(P); break;
+    case 16: k_trace<ORIGIN_POSE, 16><<<grid, block, 0, st>>>(P); break;
+    case 32: k_trace<ORIGIN_POSE, 32><<<grid, block, 0, st>>>(P); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace rmg

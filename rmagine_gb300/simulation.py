@@ -1,0 +1,350 @@
+"""Map and simulators with rmagine's interface, computing on the GB300 through librmg_gb300.
+
+Mirrors, for the GPU:
+  * SimulatorEmbree::setMap / setTsb            (SimulatorEmbree.hpp:58-61)
+  * XSimulator::setModel                         (SphereSimulatorEmbree.hpp:115-116)
+  * XSimulator::simulate(Tbm, bundle) / simulate<BundleT>(Tbm)
+                                                 (SphereSimulatorEmbree.hpp:130-155,
+                                                  SphereSimulatorOptix.hpp:141-160)
+  * Bundle / IntAttrAll / resize_memory_bundle   (SimulationResults.hpp:56-215)
+
+Device memory is torch CUDA tensors (torch is used for allocation and
+streams only).  Bundles whose tensors live on the device are filled
+asynchronously on the current stream, like the OptiX simulators; bundles in
+host memory go through a device staging buffer and the call synchronises,
+like the reference's RAM overloads.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Iterable
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .sensors import O1DnModel, OnDnModel, PinholeModel, SphericalModel
+
+ATTRIBUTES = ("hits", "ranges", "points", "normals", "face_ids", "geom_ids", "object_ids")
+_DTYPES = {
+    "hits": (torch.uint8, ()),
+    "ranges": (torch.float32, ()),
+    "points": (torch.float32, (3,)),
+    "normals": (torch.float32, (3,)),
+    "face_ids": (torch.int32, ()),    # uint32 bit patterns (torch has no uint32 arithmetic)
+    "geom_ids": (torch.int32, ()),
+    "object_ids": (torch.int32, ()),
+}
+
+
+def _stream_ptr(device: torch.device | None = None) -> C.c_void_p:
+    return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def _ptr(t: torch.Tensor | None) -> C.c_void_p | None:
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+# ---- transforms ----------------------------------------------------------------
+def make_transforms(q_xyzw, t, device=None) -> torch.Tensor:
+    """Packs rotations (x, y, z, w) and translations into rmagine Transform records.
+
+    Returns a float32 tensor [N, 8] whose rows are byte-identical to
+    rmagine::Transform (Quaternion R; Vector3 t; uint32 stamp = 0).
+    """
+    q = np.asarray(q_xyzw, dtype=np.float32).reshape(-1, 4)
+    tt = np.asarray(t, dtype=np.float32).reshape(-1, 3)
+    out = np.zeros((q.shape[0], 8), np.float32)
+    out[:, :4] = q
+    out[:, 4:7] = tt
+    ten = torch.from_numpy(out)
+    return ten.to(device) if device is not None else ten
+
+
+def identity_transforms(n: int, device=None) -> torch.Tensor:
+    q = np.tile(np.array([[0.0, 0.0, 0.0, 1.0]], np.float32), (n, 1))
+    return make_transforms(q, np.zeros((n, 3), np.float32), device)
+
+
+def transform_c(T) -> L.TransformC:
+    a = np.asarray(T, dtype=np.float32).reshape(-1)
+    if a.size == 7:
+        a = np.concatenate([a, np.zeros(1, np.float32)])
+    tc = L.TransformC()
+    tc.R = L.Quat(float(a[0]), float(a[1]), float(a[2]), float(a[3]))
+    tc.t = L.Vec3(float(a[4]), float(a[5]), float(a[6]))
+    tc.stamp = 0
+    return tc
+
+
+# ---- map ------------------------------------------------------------------------
+class Map:
+    """A triangle mesh with its LBVH on the current CUDA device (rmg_map)."""
+
+    def __init__(self, vertices, faces, stream=None):
+        self._h = None
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        f = np.ascontiguousarray(faces, dtype=np.uint32).reshape(-1, 3)
+        self.n_vertices, self.n_faces = v.shape[0], f.shape[0]
+        h = C.c_void_p()
+        L.call("rmg_map_build", v.ctypes.data_as(C.c_void_p), v.shape[0], f.ctypes.data_as(C.c_void_p),
+               f.shape[0], stream if stream is not None else _stream_ptr(), C.byref(h))
+        self._h = h
+
+    @property
+    def handle(self) -> C.c_void_p:
+        if self._h is None:
+            raise L.RmgError(L.RMG_ERR_INVALID_ARG, "Map", "map was destroyed")
+        return self._h
+
+    def refit(self, vertices, stream=None) -> None:
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        L.call("rmg_map_refit", self.handle, v.ctypes.data_as(C.c_void_p), v.shape[0],
+               stream if stream is not None else _stream_ptr())
+
+    def info(self) -> dict:
+        inf = L.MapInfoC()
+        L.call("rmg_map_info_get", self.handle, C.byref(inf))
+        return {"n_vertices": inf.n_vertices, "n_faces": inf.n_faces, "n_nodes": inf.n_nodes,
+                "depth": inf.depth, "device_bytes": inf.device_bytes,
+                "bounds_lo": list(inf.bounds_lo), "bounds_hi": list(inf.bounds_hi)}
+
+    def export(self) -> dict:
+        """Downloads the tree: nodes [n_nodes, 16] (12 float + 4 int32 views), tris [n_faces, 12]."""
+        inf = self.info()
+        nodes = np.zeros((inf["n_nodes"], 16), np.float32)
+        tris = np.zeros((inf["n_faces"], 12), np.float32)
+        order = np.zeros(inf["n_faces"], np.uint32)
+        L.call("rmg_map_export", self.handle, nodes.ctypes.data_as(C.c_void_p),
+               tris.ctypes.data_as(C.c_void_p), order.ctypes.data_as(C.c_void_p))
+        return {"boxes": nodes[:, :12].copy(), "links": nodes.view(np.int32)[:, 12:].copy(),
+                "tris": tris, "leaf_order": order}
+
+    def status(self, clear: bool = True) -> int:
+        return int(L.load().rmg_map_status(self.handle, 1 if clear else 0))
+
+    def destroy(self) -> None:
+        if self._h is not None:
+            L.load().rmg_map_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Sensor:
+    """A sensor model with its device direction table (rmg_sensor)."""
+
+    def __init__(self, model, stream=None):
+        self._h = None
+        self.model = model
+        mc = model.to_c()
+        h = C.c_void_p()
+        L.call("rmg_sensor_create", C.byref(mc), stream if stream is not None else _stream_ptr(), C.byref(h))
+        self._h = h
+        w, hh = C.c_uint32(), C.c_uint32()
+        L.call("rmg_sensor_size", h, C.byref(w), C.byref(hh))
+        self.width, self.height = w.value, hh.value
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def directions(self) -> np.ndarray:
+        out = np.zeros((self.width * self.height, 3), np.float32)
+        L.call("rmg_sensor_directions", self._h, out.ctypes.data_as(C.c_void_p))
+        return out
+
+    def destroy(self) -> None:
+        if self._h is not None:
+            L.load().rmg_sensor_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+# ---- result bundles ----------------------------------------------------------------
+class Bundle:
+    """A set of result attributes (rmagine Bundle<Hits, Ranges, ...>).
+
+    Attributes not in the bundle stay None and are not computed, like a
+    Bundle type without that attribute in the reference."""
+
+    def __init__(self, *attrs: str):
+        for a in attrs:
+            if a not in ATTRIBUTES:
+                raise ValueError(f"unknown attribute {a!r}")
+        self.attrs = tuple(a for a in ATTRIBUTES if a in attrs)
+        for a in ATTRIBUTES:
+            setattr(self, a, None)
+
+    def has(self, attr: str) -> bool:
+        return attr in self.attrs
+
+    def tensors(self) -> dict:
+        return {a: getattr(self, a) for a in self.attrs if getattr(self, a) is not None}
+
+
+def IntAttrAll() -> Bundle:
+    """SimulationResults.hpp:152-159."""
+    return Bundle(*ATTRIBUTES)
+
+
+def resize_memory_bundle(bundle: Bundle, W: int, H: int, N: int = 1, device="cuda",
+                         pin_memory: bool = False) -> Bundle:
+    """SimulationResults.hpp:176-215: sizes every attribute buffer to W*H*N."""
+    n = int(W) * int(H) * int(N)
+    for a in bundle.attrs:
+        dt, tail = _DTYPES[a]
+        if str(device) == "cpu":
+            t = torch.empty((n, *tail), dtype=dt, pin_memory=pin_memory)
+        else:
+            t = torch.empty((n, *tail), dtype=dt, device=device)
+        setattr(bundle, a, t)
+    return bundle
+
+
+def outputs_c(bundle: Bundle) -> L.OutputsC:
+    o = L.OutputsC()
+    for a in ATTRIBUTES:
+        t = getattr(bundle, a, None)
+        setattr(o, a, None if t is None or t.numel() == 0 else t.data_ptr())
+    return o
+
+
+def launch_config(stack_depth=8, block_warps=4, tile_w=8, tile_h=4) -> L.LaunchConfigC:
+    return L.LaunchConfigC(stack_depth, block_warps, tile_w, tile_h)
+
+
+# ---- simulators -------------------------------------------------------------------
+class _Simulator:
+    model_type: type = object
+
+    def __init__(self, map: Map | None = None):
+        self._map = map
+        self._sensor: Sensor | None = None
+        self._model = None
+        self._Tsb = transform_c([0, 0, 0, 1, 0, 0, 0])
+        self.launch_config: L.LaunchConfigC | None = None
+        self._staging: dict = {}
+
+    # SimulatorEmbree::setMap
+    def setMap(self, map: Map) -> None:
+        self._map = map
+
+    def map(self) -> Map | None:
+        return self._map
+
+    # SimulatorEmbree::setTsb
+    def setTsb(self, T) -> None:
+        if isinstance(T, torch.Tensor):
+            T = T.detach().cpu().numpy()
+        self._Tsb = transform_c(np.asarray(T).reshape(-1)[:8])
+
+    def setModel(self, model) -> None:
+        if not isinstance(model, self.model_type):
+            raise TypeError(f"{type(self).__name__}.setModel expects {self.model_type.__name__}")
+        self._model = model
+        if self._sensor is not None:
+            self._sensor.destroy()
+        self._sensor = Sensor(model)
+
+    def model(self):
+        return self._model
+
+    @property
+    def sensor(self) -> Sensor:
+        if self._sensor is None:
+            raise L.RmgError(L.RMG_ERR_INVALID_ARG, "simulate", "no model set")
+        return self._sensor
+
+    def _check_ready(self) -> None:
+        if self._map is None:
+            raise L.RmgError(L.RMG_ERR_INVALID_ARG, "simulate", "no map set")
+        self.sensor  # noqa: B018
+
+    def simulate(self, Tbm, bundle: Bundle | None = None, attrs: Iterable[str] | None = None) -> Bundle:
+        """simulate(Tbm, bundle) fills `bundle`; simulate(Tbm) allocates an IntAttrAll-like
+        bundle (or `attrs`) on the device, like simulate<BundleT>(Tbm)."""
+        self._check_ready()
+        if not isinstance(Tbm, torch.Tensor):
+            Tbm = torch.as_tensor(np.asarray(Tbm, np.float32).reshape(-1, 8))
+        Tbm = Tbm.reshape(-1, 8)
+        n = Tbm.shape[0]
+        W, H = self.sensor.width, self.sensor.height
+        if bundle is None:
+            bundle = Bundle(*(attrs if attrs is not None else ATTRIBUTES))
+            resize_memory_bundle(bundle, W, H, n, device="cuda")
+        for a, t in bundle.tensors().items():
+            if t.shape[0] != W * H * n:
+                raise L.RmgError(L.RMG_ERR_INVALID_ARG, "simulate",
+                                 f"{a} holds {t.shape[0]} elements, expected {W * H * n}")
+        on_host = any(not t.is_cuda for t in bundle.tensors().values())
+        if on_host:
+            return self._simulate_host(Tbm, bundle, n)
+        Tbm_d = Tbm if Tbm.is_cuda else Tbm.to("cuda", non_blocking=True)
+        Tbm_d = Tbm_d.contiguous()
+        self._launch(Tbm_d, n, bundle, _stream_ptr())
+        return bundle
+
+    def _launch(self, Tbm_d: torch.Tensor, n: int, bundle: Bundle, stream) -> None:
+        out = outputs_c(bundle)
+        lib = L.load()
+        if self.launch_config is None:
+            st = lib.rmg_simulate(self._map.handle, self.sensor.handle, C.byref(self._Tsb),
+                                  C.c_void_p(Tbm_d.data_ptr()), n, C.byref(out), stream)
+        else:
+            st = lib.rmg_simulate_ex(self._map.handle, self.sensor.handle, C.byref(self._Tsb),
+                                     C.c_void_p(Tbm_d.data_ptr()), n, C.byref(out),
+                                     C.byref(self.launch_config), stream)
+        L.check(st, "rmg_simulate")
+
+    def _simulate_host(self, Tbm: torch.Tensor, bundle: Bundle, n: int) -> Bundle:
+        dev = Bundle(*bundle.attrs)
+        for a, t in bundle.tensors().items():
+            key = (a, tuple(t.shape), t.dtype)
+            buf = self._staging.get(key)
+            if buf is None:
+                buf = torch.empty(t.shape, dtype=t.dtype, device="cuda")
+                self._staging[key] = buf
+            setattr(dev, a, buf)
+        Tbm_d = Tbm.to("cuda", non_blocking=True).contiguous()
+        self._launch(Tbm_d, n, dev, _stream_ptr())
+        for a, t in bundle.tensors().items():
+            t.copy_(getattr(dev, a), non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return bundle
+
+
+class SphereSimulator(_Simulator):
+    """SphereSimulatorEmbree / SphereSimulatorOptix on the GB300."""
+    model_type = SphericalModel
+
+
+class PinholeSimulator(_Simulator):
+    model_type = PinholeModel
+
+
+class O1DnSimulator(_Simulator):
+    model_type = O1DnModel
+
+
+class OnDnSimulator(_Simulator):
+    model_type = OnDnModel
+
+
+def make_simulator(model, map: Map | None = None) -> _Simulator:
+    """Simulator.hpp:52-78 (SimulatorType<ModelT, CompT>) for this backend."""
+    for cls in (SphereSimulator, PinholeSimulator, O1DnSimulator, OnDnSimulator):
+        if isinstance(model, cls.model_type):
+            sim = cls(map)
+            sim.setModel(model)
+            return sim
+    raise TypeError(f"no simulator for model {type(model).__name__}")
