@@ -270,11 +270,14 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="terrain1m_spherical")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--poses", type=int, default=0, help="use only the first N poses (small profiling case)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     sc, model, poses, attrs, desc = workload(args.workload)
+    if args.poses:
+        poses = poses[:args.poses]
     W, H = model_size(model)
     config = dict(desc)
     config.update({"poses": int(poses.shape[0]), "rays_per_step": int(poses.shape[0] * W * H),
