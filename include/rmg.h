@@ -219,6 +219,36 @@ int rmg_simulate_ex(const rmg_map* map, const rmg_sensor* sensor,
 /* Fills *cfg with the library default for this sensor/map. */
 int rmg_default_launch_config(const rmg_map* map, const rmg_sensor* sensor, rmg_launch_config* cfg);
 
+/* ---------------------------------------------------------------------------
+ * LBVH build without device allocation.
+ * No counterpart in the reference: rmagine's maps always allocate their own
+ * memory.  This is for callers that cannot call cudaMalloc -- code running
+ * while a CUDA graph is being captured (an allocation would break the
+ * capture), real-time loops that forbid allocator calls, hosts that give the
+ * library one fixed device arena.  The caller passes the mesh in DEVICE
+ * memory and receives the tree in its own DEVICE buffers, in the same record
+ * layouts rmg_map_export returns; the build's temporary data (Morton keys,
+ * sort buffers, bounds) lives in a fixed 4 MiB device array inside the
+ * library, which limits the mesh to RMG_NOALLOC_MAX_FACES faces (larger
+ * meshes return RMG_ERR_INVALID_ARG).  The first call on a device looks up
+ * that array's address; make it before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU race.  Synchronises with `stream` once
+ * (face-index check).
+ * ------------------------------------------------------------------------- */
+#define RMG_NOALLOC_MAX_FACES 65536u
+
+typedef struct rmg_lbvh_buffers {
+  void* nodes;            /* max(n_faces - 1, 1) 64-byte node records, 16-byte aligned */
+  void* tris;             /* n_faces 48-byte triangle records, 16-byte aligned */
+  uint32_t* leaf_order;   /* n_faces: face id of each leaf */
+  int32_t* leaf_parent;   /* n_faces: parent node of each leaf */
+  uint32_t* flags;        /* max(n_faces - 1, 1) refit counters (cleared by the call) */
+} rmg_lbvh_buffers;
+
+int rmg_lbvh_build_noalloc(const rmg_vec3* vertices, uint32_t n_vertices,
+                           const rmg_face* faces, uint32_t n_faces,
+                           const rmg_lbvh_buffers* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -102,6 +102,13 @@ class MapInfoC(C.Structure):
     ]
 
 
+class LbvhBuffersC(C.Structure):
+    _fields_ = [("nodes", C.c_void_p), ("tris", C.c_void_p), ("leaf_order", C.c_void_p),
+                ("leaf_parent", C.c_void_p), ("flags", C.c_void_p)]
+
+
+RMG_NOALLOC_MAX_FACES = 65536
+
 # name -> (restype, argtypes); every symbol include/rmg.h declares
 _P = C.c_void_p
 _U32 = C.c_uint32
@@ -126,6 +133,7 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_simulate_ex": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(OutputsC),
                                   C.POINTER(LaunchConfigC), _P]),
     "rmg_default_launch_config": (C.c_int, [_P, _P, C.POINTER(LaunchConfigC)]),
+    "rmg_lbvh_build_noalloc": (C.c_int, [_P, _U32, _P, _U32, C.POINTER(LbvhBuffersC), _P]),
 }
 
 _lib: C.CDLL | None = None

@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "internal.h"
@@ -531,5 +532,160 @@ extern "C" int rmg_map_debug_set_child(rmg_map* m, uint32_t node, uint32_t which
   const size_t off = offsetof(Node, d) + (which ? sizeof(int) : 0);
   RMG_CUDA_TRY(cudaMemcpy(reinterpret_cast<char*>(m->d_nodes + node) + off, &child, sizeof(int),
                           cudaMemcpyHostToDevice));
+  return RMG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// rmg_lbvh_build_noalloc: the LBVH build into caller-owned device memory,
+// with no device allocation.  No counterpart in the reference.
+//
+// Callers that cannot allocate device memory (code running while a CUDA graph
+// is being captured, real-time loops whose allocator calls are forbidden,
+// hosts that give the library one fixed device arena) still need temporary
+// space for the Morton keys, their sorted copy, the sort's own temporary
+// storage and the partial bounds.  That space is the file-scope array below:
+// kNoAllocScratchBytes bytes that every GPU which loads this library holds
+// until the process exits.  It bounds the mesh to RMG_NOALLOC_MAX_FACES.
+//
+// The first call on a device resolves the array's device address with
+// cudaGetSymbolAddress (the host-side name is only a stand-in and must never
+// be handed to a kernel); make that first call before any stream capture.
+// All calls share the one array and it keeps the previous call's contents:
+// the words that must start at zero are cleared by each call, and calls whose
+// work overlaps on the GPU (different streams, no ordering between them) race
+// on the array and produce garbage.  The call synchronises with `stream` once,
+// after checking the face indices on the device.
+// ---------------------------------------------------------------------------
+namespace rmg {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 4u << 20;  // 4 MiB
+static __device__ __align__(256) unsigned char g_lbvh_scratch[kNoAllocScratchBytes];
+
+struct NoAllocSetup {
+  bool ready = false;
+  unsigned char* base = nullptr;
+  size_t sort_temp_bytes = 0;  // CUB temporary storage needed for RMG_NOALLOC_MAX_FACES pairs
+};
+
+constexpr int kMaxDevices = 64;
+NoAllocSetup g_noalloc[kMaxDevices];
+std::mutex g_noalloc_mutex;
+
+__global__ void k_check_faces(const uint32_t* f, uint32_t n_faces, uint32_t n_vertices, unsigned int* bad) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * n_faces) return;
+  if (f[i] >= n_vertices) atomicExch(bad, 1u);
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+int noalloc_setup(int dev, NoAllocSetup** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (dev < 0 || dev >= kMaxDevices) return fail(RMG_ERR_NO_DEVICE, "rmg_lbvh_build_noalloc: device id");
+  NoAllocSetup& s = g_noalloc[dev];
+  if (!s.ready) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_lbvh_scratch);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_lbvh_scratch)");
+    size_t bytes = 0;
+    const cudaError_t e2 = cub::DeviceRadixSort::SortPairs(
+        nullptr, bytes, (const uint64_t*)nullptr, (uint64_t*)nullptr, (const uint32_t*)nullptr,
+        (uint32_t*)nullptr, (int)RMG_NOALLOC_MAX_FACES, 0, 63);
+    if (e2 != cudaSuccess) return cuda_status(e2, "sort temp size");
+    s.base = static_cast<unsigned char*>(p);
+    s.sort_temp_bytes = bytes;
+    s.ready = true;
+  }
+  *out = &s;
+  return RMG_OK;
+}
+
+}  // namespace
+}  // namespace rmg
+
+extern "C" int rmg_lbvh_build_noalloc(const rmg_vec3* vertices, uint32_t n_vertices, const rmg_face* faces,
+                                      uint32_t n_faces, const rmg_lbvh_buffers* out, void* stream) {
+  if (!out) return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: out is NULL");
+  if (n_faces > RMG_NOALLOC_MAX_FACES)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: n_faces exceeds RMG_NOALLOC_MAX_FACES (65536)");
+  if (n_faces == 0) return RMG_OK;
+  if (!vertices || !faces || !out->nodes || !out->tris || !out->leaf_order || !out->leaf_parent || !out->flags)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: NULL input or output buffer");
+  if ((reinterpret_cast<uintptr_t>(out->nodes) | reinterpret_cast<uintptr_t>(out->tris)) & 15u)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: nodes/tris must be 16-byte aligned");
+  int dev = 0;
+  RMG_CUDA_TRY(cudaGetDevice(&dev));
+  NoAllocSetup* su = nullptr;
+  int s = noalloc_setup(dev, &su);
+  if (s != RMG_OK) return s;
+
+  cudaStream_t st = as_stream(stream);
+  const uint32_t n = n_faces;
+  const int nb = std::min<int>((int)grid_for(n), 4 * device_sm_count());
+  // carve the scratch array
+  unsigned char* p = su->base;
+  size_t off = 0;
+  auto take = [&](size_t bytes) { unsigned char* q = p + off; off = align256(off + bytes); return q; };
+  uint64_t* keys = reinterpret_cast<uint64_t*>(take(8ull * n));
+  uint64_t* keys2 = reinterpret_cast<uint64_t*>(take(8ull * n));
+  uint32_t* vals = reinterpret_cast<uint32_t*>(take(4ull * n));
+  uint32_t* vals2 = reinterpret_cast<uint32_t*>(take(4ull * n));
+  float* partial = reinterpret_cast<float*>(take(24ull * nb));
+  float* bounds = reinterpret_cast<float*>(take(24));
+  unsigned int* bad = reinterpret_cast<unsigned int*>(take(4));
+  void* temp = take(su->sort_temp_bytes);
+  size_t temp_bytes = 0;
+  RMG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, keys, keys2, vals, vals2, (int)n, 0, 63, st));
+  if (off > kNoAllocScratchBytes || temp_bytes > su->sort_temp_bytes)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: scratch array too small for this mesh");
+
+  const float* v = reinterpret_cast<const float*>(vertices);
+  const uint32_t* f = reinterpret_cast<const uint32_t*>(faces);
+  Node* nodes = static_cast<Node*>(out->nodes);
+  Tri* tris = static_cast<Tri*>(out->tris);
+
+  // face indices are checked on the device before any kernel dereferences them
+  RMG_CUDA_TRY(cudaMemsetAsync(bad, 0, 4, st));
+  k_check_faces<<<grid_for(3ull * n), kBlock, 0, st>>>(f, n, n_vertices, bad);
+  RMG_CUDA_TRY(cudaGetLastError());
+  unsigned int bad_h = 0;
+  RMG_CUDA_TRY(cudaMemcpyAsync(&bad_h, bad, 4, cudaMemcpyDeviceToHost, st));
+  RMG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (bad_h) return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: face index out of range");
+
+  if (n == 1) {
+    uint32_t fi[3];
+    RMG_CUDA_TRY(cudaMemcpy(fi, f, sizeof(fi), cudaMemcpyDeviceToHost));
+    float vv[9];
+    for (int k = 0; k < 3; ++k)
+      RMG_CUDA_TRY(cudaMemcpy(vv + 3 * k, v + 3ull * fi[k], 12, cudaMemcpyDeviceToHost));
+    const uint32_t local[3] = {0, 1, 2};
+    Node node;
+    single_node(vv, local, &node);
+    const uint32_t zero = 0;
+    const int minus1 = -1;
+    RMG_CUDA_TRY(cudaMemcpyAsync(nodes, &node, sizeof(Node), cudaMemcpyHostToDevice, st));
+    RMG_CUDA_TRY(cudaMemcpyAsync(out->leaf_order, &zero, 4, cudaMemcpyHostToDevice, st));
+    RMG_CUDA_TRY(cudaMemcpyAsync(out->leaf_parent, &minus1, 4, cudaMemcpyHostToDevice, st));
+    RMG_CUDA_TRY(cudaMemsetAsync(out->flags, 0, 4, st));
+    k_pack<<<1, 32, 0, st>>>(v, f, out->leaf_order, 1, tris, nullptr);
+    RMG_CUDA_TRY(cudaGetLastError());
+    RMG_CUDA_TRY(cudaStreamSynchronize(st));
+    return RMG_OK;
+  }
+
+  k_centroid_bounds<<<nb, kBlock, 0, st>>>(v, f, n, partial);
+  k_bounds_final<<<1, 32, 0, st>>>(partial, nb, bounds);
+  k_morton<<<grid_for(n), kBlock, 0, st>>>(v, f, n, bounds, keys, vals);
+  RMG_CUDA_TRY(cudaGetLastError());
+  RMG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(temp, temp_bytes, keys, keys2, vals, vals2, (int)n, 0, 63, st));
+  RMG_CUDA_TRY(cudaMemsetAsync(nodes, 0, sizeof(Node) * (n - 1), st));
+  k_karras<<<grid_for(n - 1), kBlock, 0, st>>>(keys2, (int)n, nodes, out->leaf_parent);
+  k_pack<<<grid_for(n), kBlock, 0, st>>>(v, f, vals2, n, tris, out->leaf_order);
+  RMG_CUDA_TRY(cudaGetLastError());
+  RMG_CUDA_TRY(cudaMemsetAsync(out->flags, 0, 4ull * (n - 1), st));
+  k_refit<<<grid_for(n), kBlock, 0, st>>>(nodes, tris, out->leaf_parent, out->flags, n);
+  RMG_CUDA_TRY(cudaGetLastError());
   return RMG_OK;
 }
