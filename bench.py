@@ -1,21 +1,24 @@
 #!/usr/bin/env python
-"""Throughput of the range-sensor ray-casting path on the GB300.
+"""Throughput of the range-sensor ray-casting path (and its companions) on the GB300.
 
-A step = one rmg_simulate call over all poses of the workload (one launch of
-the traversal kernel), inputs (map, sensor table, poses) resident in HBM.
-Default workload: the ~1M-triangle terrain (708 x 708 heightfield, 999,698
-triangles, plus 2,000 boxes = 1,023,698 triangles), an Ouster-like spherical
-sensor 128 x 1024 (+-22.5 deg), 1,000 poses 1.5 m above the ground, all five
-attributes (Hits, Ranges, Points, Normals, FaceIds): 131,072,000 rays.
+Default workload (`--workload terrain1m_spherical`): a step = one rmg_simulate call over all
+poses (one launch of the traversal kernel), map / sensor table / poses resident in HBM.  The
+~1M-triangle terrain (708 x 708 heightfield = 999,698 triangles + 2,000 boxes = 1,023,698),
+an Ouster-like spherical sensor 128 x 1024 (+-22.5 deg), 1,000 poses 1.5 m above the ground,
+all five attributes (Hits, Ranges, Points, Normals, FaceIds): 131,072,000 rays per step.
 
-Prints one JSON line (rank 0).  `--impl reference` times the CPU path of the
-reference's semantics on the host cores instead (see cpu_leg()).
+Other workloads: terrain1m_pinhole, terrain2m_spherical (2,117,058 triangles), room_vlp16;
+icp_stats (8192 batches x 32768 correspondences: statistics_p2p + Umeyama forward and the
+backward, correspondences/s); pose_grad (2.1M-triangle terrain, spherical 64 x 1024, 4096
+poses: fused ray cast + range adjoint, pose-gradient evaluations/s).
+
+Prints one JSON line (rank 0).  `--impl reference` times the CPU restatement of the reference's
+semantics on the host cores instead (see the cpu_* functions).
 """
 from __future__ import annotations
 
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess
@@ -33,46 +36,50 @@ IDENT = np.array([0, 0, 0, 1, 0, 0, 0, 0], np.float32)
 ALL = ("hits", "ranges", "points", "normals", "face_ids")
 OUT_BYTES = {"hits": 1, "ranges": 4, "points": 12, "normals": 12, "face_ids": 4, "geom_ids": 4, "object_ids": 4}
 
-# Mean internal-node visits and triangle tests per ray of the canonical LBVH
-# in the kernel's traversal order, measured by the oracle's instrumented
-# traversal (oracle.CanonicalLbvh.count) on a fixed 0.1% ray sample
-# (rng seed 0) of each workload; tests/test_work_constants.py re-derives them.
+# Mean internal-node visits and triangle tests per ray of the canonical LBVH in the kernel's
+# traversal order, measured by the oracle's instrumented traversal (oracle.CanonicalLbvh.count)
+# on a fixed 0.1% ray sample (rng seed 0) of each workload; tests/test_work_constants.py
+# re-derives them on smaller samples.
 WORK_PER_RAY = {
-    "terrain1m_spherical": {"nodes": 39.94, "tris": 1.886},
+    "terrain1m_spherical": {"nodes": 39.942, "tris": 1.886},
+    "terrain1m_pinhole": {"nodes": 36.787, "tris": 1.711},
+    "terrain2m_spherical": {"nodes": 40.516, "tris": 1.860},
+    "room_vlp16": {"nodes": 68.997, "tris": 4.149},
+    "pose_grad": {"nodes": 40.046, "tris": 1.855},
 }
 
+# Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel,
+# from one ncu capture of the workload (profiles/).
+TRAFFIC: dict = {}
 
-def workload(name: str):
+RAYCAST = ("terrain1m_spherical", "terrain1m_pinhole", "terrain2m_spherical", "room_vlp16")
+
+
+def raycast_workload(name: str):
     from rmagine_gb300 import scenes, sensors
 
-    if name == "terrain1m_spherical":
+    if name in ("terrain1m_spherical", "terrain1m_pinhole"):
         sc = scenes.million_triangle_terrain(seed=0)
-        model = sensors.ouster_like(128, 1024, 45.0, 0.5, 130.0)
-        poses = scenes.terrain_poses(sc, 1000, seed=2)
-        desc = {"workload": "terrain 708x708 + 2000 boxes (1,023,698 tris), spherical 128x1024, 1000 poses, "
-                            "Hits+Ranges+Points+Normals+FaceIds"}
-        return sc, model, poses, ALL, desc
-    if name == "terrain1m_pinhole":
-        sc = scenes.million_triangle_terrain(seed=0)
-        model = sensors.depth_camera(640, 480, 90.0, 0.3, 130.0)
-        poses = scenes.terrain_poses(sc, 1000, seed=2)
-        desc = {"workload": "terrain 708x708 + 2000 boxes (1,023,698 tris), pinhole 640x480, 1000 poses, "
-                            "Hits+Ranges+Points+Normals+FaceIds"}
-        return sc, model, poses, ALL, desc
-    if name == "terrain2m_spherical":
+        tri = "terrain 708x708 + 2000 boxes (1,023,698 tris)"
+    elif name == "terrain2m_spherical":
         sc = scenes.terrain(grid=1024, n_boxes=2000, seed=0)
-        model = sensors.ouster_like(128, 1024, 45.0, 0.5, 130.0)
-        poses = scenes.terrain_poses(sc, 1000, seed=2)
-        desc = {"workload": "terrain 1024x1024 + 2000 boxes (2,117,058 tris), spherical 128x1024, 1000 poses, "
-                            "Hits+Ranges+Points+Normals+FaceIds"}
-        return sc, model, poses, ALL, desc
-    if name == "room_vlp16":
+        tri = "terrain 1024x1024 + 2000 boxes (2,117,058 tris)"
+    elif name == "room_vlp16":
         sc = scenes.box_room(seed=0, n_boxes=200)
         model = sensors.vlp16_900()
         poses = scenes.room_poses(100, seed=1)
-        desc = {"workload": "box room + 200 boxes (2,412 tris), VLP-16 16x900, 100 poses, Hits+Ranges"}
-        return sc, model, poses, ("hits", "ranges"), desc
-    raise SystemExit(f"unknown workload {name}")
+        return sc, model, poses, ("hits", "ranges"), {
+            "workload": "box room + 200 boxes (2,412 tris), VLP-16 16x900, 100 poses, Hits+Ranges"}
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    if name.endswith("pinhole"):
+        model = sensors.depth_camera(640, 480, 90.0, 0.3, 130.0)
+        mdesc = "pinhole 640x480 (90 deg hfov)"
+    else:
+        model = sensors.ouster_like(128, 1024, 45.0, 0.5, 130.0)
+        mdesc = "spherical 128x1024 (+-22.5 deg)"
+    poses = scenes.terrain_poses(sc, 1000, seed=2)
+    return sc, model, poses, ALL, {"workload": f"{tri}, {mdesc}, 1000 poses, Hits+Ranges+Points+Normals+FaceIds"}
 
 
 def model_size(model):
@@ -81,7 +88,7 @@ def model_size(model):
     return oracle.model_size(model)
 
 
-# ---- clocks --------------------------------------------------------------------------------
+# ---- clocks ------------------------------------------------------------------------------
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -133,30 +140,78 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def measured_peaks():
+def measured_hbm():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
-        d = json.loads(p.read_text())
-        return float(d["hbm_gbs"]), "measured"
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
 
 
-# ---- CPU leg (oracle port of the reference semantics) -------------------------------------------
-def cpu_leg(sc, model, poses, attrs, target_s: float = 15.0, max_poses: int | None = None):
-    """Times the oracle's OpenMP restatement of rmagine's Embree path on all host cores over a
-    bounded pose sample (map build excluded, as in the reference's benchmark loop)."""
+def roofline(bytes_per_unit, units_per_launch, launch_s, note, traffic=None):
+    peak, kind = measured_hbm()
+    achieved = bytes_per_unit * units_per_launch / launch_s / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": kind,
+            "algorithmic_bytes_per_unit": round(bytes_per_unit, 2), "units_per_launch": int(units_per_launch),
+            "note": note}
+
+
+class Timer:
+    """Per-step CUDA events on the launching stream with an L2 flush between steps."""
+
+    def __init__(self, dev, steps):
+        import torch
+
+        self.torch = torch
+        self.dev = dev
+        self.flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+        self.ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(steps)]
+
+    def run(self, fn, world):
+        torch = self.torch
+        stream = torch.cuda.current_stream(self.dev)
+        barrier(world)
+        torch.cuda.synchronize(self.dev)
+        with ClockSampler(self.dev.index) as clk:
+            for s, e in self.ev:
+                self.flush.zero_()  # evict L2 between timed steps (outside the events)
+                s.record(stream)
+                fn()
+                e.record(stream)
+            torch.cuda.synchronize(self.dev)
+        barrier(world)
+        ms = [s.elapsed_time(e) for s, e in self.ev]
+        total = sum(ms)
+        if world > 1:
+            import torch.distributed as dist
+
+            t = torch.tensor([total], device=self.dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total = float(t.item())
+        return total, ms, clk.summary()
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ---- ray casting -------------------------------------------------------------------------
+def cpu_raycast(sc, model, poses, attrs, target_s=15.0):
+    """The oracle's OpenMP restatement of rmagine's Embree path on all host cores over a bounded
+    pose sample (map build excluded, as in the reference's benchmark loop)."""
     import oracle
 
     ocs = oracle.Scene(sc.vertices, sc.faces)
     threads = oracle.lib().orc_max_threads()
     W, H = model_size(model)
-    # probe with one pose to size the sample
     t0 = time.perf_counter()
     ocs.simulate(model, IDENT, poses[:1], attrs=attrs, nthreads=threads)
     per_pose = max(time.perf_counter() - t0, 1e-4)
     n = int(max(1, min(len(poses), target_s / per_pose)))
-    if max_poses:
-        n = min(n, max_poses)
     t0 = time.perf_counter()
     ocs.simulate(model, IDENT, poses[:n], attrs=attrs, nthreads=threads)
     dt = time.perf_counter() - t0
@@ -166,12 +221,14 @@ def cpu_leg(sc, model, poses, attrs, target_s: float = 15.0, max_poses: int | No
                       f"of the Embree path (Embree itself is not buildable here)", "seconds": dt}
 
 
-# ---- GPU leg ---------------------------------------------------------------------------------------
-def gpu_leg(args, sc, model, poses, attrs, desc, rank, world):
+def gpu_raycast(args, world):
     import torch
 
     import rmagine_gb300 as rm
 
+    sc, model, poses, attrs, desc = raycast_workload(args.workload)
+    if args.poses:
+        poses = poses[:args.poses]
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     W, H = model_size(model)
@@ -181,85 +238,271 @@ def gpu_leg(args, sc, model, poses, attrs, desc, rank, world):
     sim = rm.make_simulator(model, m)
     Tbm = torch.from_numpy(poses).to(dev)
     bundle = rm.resize_memory_bundle(rm.Bundle(*attrs), W, H, n, device=dev)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > L2
-    stream = torch.cuda.current_stream(dev)
-
-    def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
-
     for _ in range(args.warmup):
         sim.simulate(Tbm, bundle)
     torch.cuda.synchronize(dev)
     if m.status() != 0:
         raise RuntimeError("device status error during warm-up")
-
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    barrier()
-    torch.cuda.synchronize(dev)
-    with ClockSampler(dev.index) as clk:
-        for i in range(args.steps):
-            flush.zero_()  # evict L2 between timed steps (outside the events)
-            starts[i].record(stream)
-            sim.simulate(Tbm, bundle)
-            ends[i].record(stream)
-        torch.cuda.synchronize(dev)
-    barrier()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(step_ms)
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms, step_ms, clocks = Timer(dev, args.steps).run(lambda: sim.simulate(Tbm, bundle), world)
     if m.status() != 0:
         raise RuntimeError("device status error in the timed region")
     value = world * rays * args.steps / (total_ms / 1e3) / 1e6
 
-    # e2e through the public API: host (pinned) poses in, host (pinned) bundle out, synchronous
+    # e2e through the public API: pinned host poses in, pinned host bundle out, synchronous
     host_poses = torch.from_numpy(poses).pin_memory()
     hb = rm.resize_memory_bundle(rm.Bundle(*attrs), W, H, n, device="cpu", pin_memory=True)
-    sim.simulate(host_poses, hb)  # warm the staging buffers
+    sim.simulate(host_poses, hb)
     e2e_t = []
     for _ in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         sim.simulate(host_poses, hb)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_value = rays / (sum(e2e_t) / len(e2e_t)) / 1e6
-    d2h = rays * sum(OUT_BYTES[a] for a in attrs)
-
-    bytes_per_ray = None
+    e2e = rays / (sum(e2e_t) / len(e2e_t)) / 1e6
+    out_b = sum(OUT_BYTES[a] for a in attrs)
     wk = WORK_PER_RAY.get(args.workload)
-    peak, peak_kind = measured_peaks()
-    roofline = None
+    rl = None
     if wk:
-        bytes_per_ray = sum(OUT_BYTES[a] for a in attrs) + 64 * wk["nodes"] + 48 * wk["tris"]
-        per_launch_s = total_ms / args.steps / 1e3
-        achieved = bytes_per_ray * rays / per_launch_s / 1e9
-        roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                    "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
-                    "algorithmic_bytes_per_ray": round(bytes_per_ray, 1),
-                    "note": "algorithmic bytes = outputs + 64 B per node visit + 48 B per triangle test; "
-                            "node and triangle fetches are served mostly from L2"}
-        tr = TRAFFIC.get(args.workload)
-        if tr:
-            roofline["traffic"] = tr
-    return {
-        "value": value, "ms_per_step": total_ms / args.steps, "step_ms": step_ms, "rays_per_step": rays,
-        "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": int(poses.nbytes),
-                "d2h_bytes_per_step": int(d2h)},
-        "roofline": roofline, "clocks": clk.summary(), "map": m.info(),
-    }
+        rl = roofline(out_b + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
+                      "algorithmic bytes per ray = outputs + 64 B per node visit + 48 B per triangle test; "
+                      "node and triangle fetches are served mostly from L1/L2, so this exceeds the HBM roof",
+                      TRAFFIC.get(args.workload))
+    config = dict(desc)
+    config.update({"poses": int(n), "rays_per_step": int(rays), "triangles": int(sc.n_faces),
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": f"replicas{world}" if world > 1 else "single"})
+    line = {"metric": "Mrays/s", "unit": "Mrays/s", "value": round(value, 2), "ms_per_step": round(total_ms / args.steps, 3),
+            "dtype": "f32", "config": config, "gpu_launches": args.steps,
+            "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": int(poses.nbytes),
+                    "d2h_bytes_per_step": int(rays * out_b)},
+            "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms],
+            "map": {k: m.info()[k] for k in ("n_faces", "n_nodes", "depth", "device_bytes")}}
+    return line, lambda: cpu_raycast(sc, model, poses, attrs), config
 
 
-# Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# traversal kernel from one ncu capture of the workload; see profiles/.
-TRAFFIC: dict = {}
+# ---- ICP statistics + Umeyama (forward and backward) -----------------------------------------
+def icp_data(B, N, dev, seed=0):
+    """Source points U([-25,25]^3); targets = R src + t + N(0, 0.01) with 5% outliers + U(-5,5)^3;
+    per-batch uniform random R and t ~ U(-5,5)^3.  Generated on the device (seeded)."""
+    import torch
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    src = torch.rand((B, N, 3), generator=g, device=dev) * 50 - 25
+    q = torch.randn((B, 4), generator=g, device=dev)
+    q = q / q.norm(dim=1, keepdim=True)
+    x, y, z, w = q.unbind(1)
+    R = torch.stack([torch.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], 1),
+                     torch.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], 1),
+                     torch.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], 1)], 1)
+    t = torch.rand((B, 3), generator=g, device=dev) * 10 - 5
+    tgt = torch.empty_like(src)
+    for b0 in range(0, B, 512):
+        b1 = min(B, b0 + 512)
+        tgt[b0:b1] = torch.bmm(src[b0:b1], R[b0:b1].transpose(1, 2)) + t[b0:b1, None, :]
+    tgt += torch.randn(tgt.shape, generator=g, device=dev) * 0.01
+    out = torch.rand((B, N), generator=g, device=dev) < 0.05
+    tgt += out[..., None] * (torch.rand(tgt.shape, generator=g, device=dev) * 10 - 5)
+    return src.contiguous(), tgt.contiguous()
+
+
+def cpu_icp(src_h, tgt_h, target_s=10.0):
+    from oracle import stats as ost
+
+    B = src_h.shape[0]
+    t0 = time.perf_counter()
+    ost.umeyama(ost.stats(*ost.correspondences(src_h[:1], tgt_h[:1])))
+    per = max(time.perf_counter() - t0, 1e-4)
+    n = int(max(1, min(B, target_s / per)))
+    t0 = time.perf_counter()
+    ost.umeyama(ost.stats(*ost.correspondences(src_h[:n], tgt_h[:n])))
+    dt = time.perf_counter() - t0
+    corr = n * src_h.shape[1]
+    return {"value": corr / dt / 1e9, "unit": "Gcorr/s", "cores": 1, "kind": "port",
+            "sample": f"{n} of {B} batches ({corr} correspondences), forward statistics + Umeyama only, "
+                      f"numpy binary64 restatement (single thread)", "seconds": dt}
+
+
+def gpu_icp(args, world):
+    import ctypes as C
+
+    import torch
+
+    from rmagine_gb300 import _lib
+    from rmagine_gb300 import statistics as rs
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    B, N = (args.poses or 8192), 32768
+    src, tgt = icp_data(B, N, dev)
+    corr = B * N
+    stats = torch.empty((B, 16), dtype=torch.float32, device=dev)
+    T = torch.empty((B, 8), dtype=torch.float32, device=dev)
+    gR = torch.randn((B, 9), device=dev)
+    gt = torch.randn((B, 3), device=dev)
+    gd = torch.empty_like(src)
+    gm = torch.empty_like(tgt)
+    pc = rs.UmeyamaReductionConstraints().to_c()
+    lib = _lib.load()
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+
+    def fwd():
+        st = torch.cuda.current_stream(dev).cuda_stream
+        _lib.check(lib.rmg_statistics_p2p(None, 0, p(src), None, None, p(tgt), None, None, C.byref(pc), B, N,
+                                          p(stats), p(T), C.c_void_p(st)), "rmg_statistics_p2p")
+
+    def bwd():
+        st = torch.cuda.current_stream(dev).cuda_stream
+        _lib.check(lib.rmg_umeyama_backward(None, 0, p(src), None, None, p(tgt), None, None, C.byref(pc), B, N,
+                                            p(stats), p(gR), p(gt), p(gd), p(gm), C.c_void_p(st)),
+                   "rmg_umeyama_backward")
+
+    def step():
+        fwd()
+        bwd()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    total_ms, step_ms, clocks = Timer(dev, args.steps).run(step, world)
+    f_ms, _, _ = Timer(dev, args.steps).run(fwd, world)
+    b_ms, _, _ = Timer(dev, args.steps).run(bwd, world)
+    value = world * corr * args.steps / (total_ms / 1e3) / 1e9
+    # e2e: host (pinned) clouds in, stats + transforms + gradients back
+    hs, ht = src.cpu().pin_memory(), tgt.cpu().pin_memory()
+    hgd = torch.empty(hs.shape, dtype=torch.float32, pin_memory=True)
+    hgm = torch.empty(hs.shape, dtype=torch.float32, pin_memory=True)
+    e2e_t = []
+    for _ in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        ds, dt_ = hs.to(dev, non_blocking=True), ht.to(dev, non_blocking=True)
+        s_, T_ = rs.statistics(ds, dt_)
+        a, b = rs.umeyama_backward(ds, dt_, s_, grad_R=gR, grad_t=gt)
+        hgd.copy_(a, non_blocking=True)
+        hgm.copy_(b, non_blocking=True)
+        T_.cpu()
+        torch.cuda.synchronize(dev)
+        e2e_t.append(time.perf_counter() - t0)
+        del ds, dt_, a, b
+    e2e = corr / (sum(e2e_t) / len(e2e_t)) / 1e9
+    fwd_s, bwd_s = f_ms / args.steps / 1e3, b_ms / args.steps / 1e3
+    rl_f = roofline(24, corr, fwd_s, "k_stats: 24 B per correspondence read (dataset + model points)",
+                    TRAFFIC.get("icp_stats_fwd"))
+    rl_b = roofline(48, corr, bwd_s, "k_umeyama_bwd_stream: 24 B read + 24 B gradients written per correspondence",
+                    TRAFFIC.get("icp_stats_bwd"))
+    dominant, other = (rl_b, rl_f) if bwd_s >= fwd_s else (rl_f, rl_b)
+    config = {"workload": f"ICP statistics_p2p + Umeyama forward and backward, {B} batches x {N} correspondences "
+                          f"(src U[-25,25]^3, tgt = R src + t + N(0,0.01), 5% outliers)",
+              "batches": B, "correspondences_per_step": corr, "l2": "flushed between timed steps (256 MB write)",
+              "parallelism": f"replicas{world}" if world > 1 else "single"}
+    line = {"metric": "Gcorr/s", "unit": "Gcorr/s", "value": round(value, 3),
+            "ms_per_step": round(total_ms / args.steps, 3), "dtype": "f32 (f64 accumulation)", "config": config,
+            "gpu_launches": 5 * args.steps,
+            "forward_ms": round(f_ms / args.steps, 3), "backward_ms": round(b_ms / args.steps, 3),
+            "e2e": {"value": round(e2e, 3), "unit": "Gcorr/s", "h2d_bytes_per_step": int(2 * 12 * corr),
+                    "d2h_bytes_per_step": int(2 * 12 * corr + 32 * B)},
+            "roofline": dominant, "roofline_other_kernel": other, "clocks": clocks,
+            "step_ms": [round(x, 3) for x in step_ms]}
+    src_h = src[:min(B, 64)].cpu().numpy()
+    tgt_h = tgt[:min(B, 64)].cpu().numpy()
+    return line, lambda: cpu_icp(src_h, tgt_h), config
+
+
+# ---- pose gradient -----------------------------------------------------------------------------
+def posegrad_workload(n_poses):
+    from rmagine_gb300 import scenes, sensors
+
+    sc = scenes.terrain(grid=1024, n_boxes=2000, seed=0)
+    model = sensors.ouster_like(64, 1024, 45.0, 0.5, 130.0)
+    true = scenes.terrain_poses(sc, n_poses, seed=3)
+    est = scenes.perturb_poses(true, 4, 0.1, 2.0)
+    return sc, model, true, est
+
+
+def cpu_posegrad(sc, model, true, est, obs_h, target_s=10.0):
+    import oracle
+    from oracle import grad as og
+
+    ocs = oracle.Scene(sc.vertices, sc.faces)
+    threads = oracle.lib().orc_max_threads()
+    W, H = model_size(model)
+    dirs = oracle.directions(model)
+
+    def run(n):
+        sim = ocs.simulate(model, IDENT, est[:n], attrs=("ranges", "face_ids"), nthreads=threads)
+        obs = obs_h[:n * W * H]
+        f, r = sim["face_ids"], sim["ranges"]
+        valid = (f != 0xFFFFFFFF) & (r >= model.range.min) & (obs >= model.range.min) & (obs <= model.range.max)
+        gid = np.nonzero(valid)[0]
+        rset = og.RayFaceSet(sc.vertices, sc.faces, IDENT, est[:n], dirs[gid % (W * H)], np.zeros((gid.size, 3)),
+                             gid // (W * H), f[gid], obs[gid])
+        return rset.analytic(n, 0.2)
+
+    t0 = time.perf_counter()
+    run(1)
+    per = max(time.perf_counter() - t0, 1e-4)
+    n = int(max(1, min(len(est), obs_h.size // (W * H), target_s / per)))
+    t0 = time.perf_counter()
+    run(n)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "pose-grad evals/s", "cores": int(threads), "kind": "port",
+            "sample": f"{n} of {len(est)} poses: oracle OpenMP ray cast + numpy binary64 adjoint", "seconds": dt}
+
+
+def gpu_posegrad(args, world):
+    import torch
+
+    import rmagine_gb300 as rm
+    from rmagine_gb300 import grad as rg
+
+    n_poses = args.poses or 4096
+    sc, model, true, est = posegrad_workload(n_poses)
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    W, H = model_size(model)
+    rays = n_poses * W * H
+    m = rm.Map(sc.vertices, sc.faces)
+    sim = rm.SphereSimulator(m)
+    sim.setModel(model)
+    obs = sim.simulate(torch.from_numpy(true).to(dev), attrs=("ranges",)).ranges
+    Test = torch.from_numpy(est).to(dev)
+    for _ in range(args.warmup):
+        rg.range_pose_grad(sim, Test, obs, 0.2)
+    torch.cuda.synchronize(dev)
+    total_ms, step_ms, clocks = Timer(dev, args.steps).run(lambda: rg.range_pose_grad(sim, Test, obs, 0.2), world)
+    if m.status() != 0:
+        raise RuntimeError("device status error in the timed region")
+    value = world * n_poses * args.steps / (total_ms / 1e3)
+    host_est = torch.from_numpy(est).pin_memory()
+    host_obs = obs.cpu().pin_memory()
+    e2e_t = []
+    for _ in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        g, l_ = rg.range_pose_grad(sim, host_est, host_obs, 0.2)
+        g.cpu()
+        l_.cpu()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e = n_poses / (sum(e2e_t) / len(e2e_t))
+    wk = WORK_PER_RAY["pose_grad"]
+    rl = roofline(4 + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
+                  "per ray: observed range 4 B + 64 B per node visit + 48 B per triangle test (the adjoint re-reads "
+                  "the hit triangle from L1); node/triangle fetches are served mostly from L1/L2",
+                  TRAFFIC.get("pose_grad"))
+    config = {"workload": f"pose gradient: terrain 1024x1024 + 2000 boxes (2,117,058 tris), spherical 64x1024, "
+                          f"{n_poses} poses perturbed N(0,0.1 m) / N(0,2 deg), Huber 0.2 m",
+              "poses": n_poses, "rays_per_step": rays, "l2": "flushed between timed steps (256 MB write)",
+              "parallelism": f"replicas{world}" if world > 1 else "single"}
+    line = {"metric": "pose-grad evals/s", "unit": "poses/s", "value": round(value, 1),
+            "mrays_per_s": round(world * rays * args.steps / (total_ms / 1e3) / 1e6, 1),
+            "ms_per_step": round(total_ms / args.steps, 3), "dtype": "f32", "config": config,
+            "gpu_launches": 2 * args.steps,
+            "e2e": {"value": round(e2e, 1), "unit": "poses/s", "h2d_bytes_per_step": int(est.nbytes + 4 * rays),
+                    "d2h_bytes_per_step": int(28 * n_poses)},
+            "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
+    obs_h = obs[:8 * W * H].cpu().numpy()
+    return line, lambda: cpu_posegrad(sc, model, true, est, obs_h), config
 
 
 def main():
@@ -270,65 +513,82 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="terrain1m_spherical")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--poses", type=int, default=0, help="use only the first N poses (small profiling case)")
+    ap.add_argument("--poses", type=int, default=0, help="use only the first N poses / batches (profiling case)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
-    sc, model, poses, attrs, desc = workload(args.workload)
-    if args.poses:
-        poses = poses[:args.poses]
-    W, H = model_size(model)
-    config = dict(desc)
-    config.update({"poses": int(poses.shape[0]), "rays_per_step": int(poses.shape[0] * W * H),
-                   "triangles": int(sc.n_faces), "l2": "flushed between timed steps (256 MB write)",
-                   "parallelism": f"replicas{world}" if world > 1 else "single"})
-    base = {"metric": "Mrays/s", "unit": "Mrays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded procedural terrain and poses)", "config": config}
+    base = {"n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "data": "synthetic (seeded procedural inputs)"}
 
     if args.impl == "reference":
         if rank != 0:
             return
-        from oracle import build as ob
-
-        ob.build()
-        vals = []
-        leg = None
-        for _ in range(args.warmup + args.steps):
-            leg = cpu_leg(sc, model, poses, attrs, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))
-            vals.append(leg["value"])
-        v = statistics.mean(vals[args.warmup:]) if len(vals) > args.warmup else vals[-1]
-        out = dict(base)
-        out.update({"impl": "reference", "value": round(v, 3), "ms_per_step": round(1e3 * leg["seconds"], 1),
-                    "gpu_launches": 0,
-                    "cpu_baseline": {"value": round(v, 3), "unit": "Mrays/s", "cores": leg["cores"],
-                                     "kind": "port", "sample": leg["sample"]},
-                    "e2e": {"value": round(v, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
-                            "d2h_bytes_per_step": 0}})
-        print(json.dumps(out))
+        print(json.dumps(reference_arm(args, base)))
         return
 
     if world > 1:
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    res = gpu_leg(args, sc, model, poses, attrs, desc, rank, world)
+    if args.workload in RAYCAST:
+        line, cpu, _ = gpu_raycast(args, world)
+    elif args.workload == "icp_stats":
+        line, cpu, _ = gpu_icp(args, world)
+    elif args.workload == "pose_grad":
+        line, cpu, _ = gpu_posegrad(args, world)
+    else:
+        raise SystemExit(f"unknown workload {args.workload}")
     if rank != 0:
         return
     out = dict(base)
-    out.update({"value": round(res["value"], 2), "ms_per_step": round(res["ms_per_step"], 3),
-                "e2e": res["e2e"], "roofline": res["roofline"], "clocks": res["clocks"],
-                "gpu_launches": args.steps, "step_ms": [round(x, 3) for x in res["step_ms"]],
-                "map": {k: res["map"][k] for k in ("n_faces", "n_nodes", "depth", "device_bytes")}})
+    out.update(line)
     if not args.no_cpu_baseline:
         from oracle import build as ob
 
         ob.build()
-        cpu = cpu_leg(sc, model, poses, attrs)
-        out["cpu_baseline"] = {k: (round(v, 3) if isinstance(v, float) else v) for k, v in cpu.items()
-                               if k != "seconds"}
+        c = cpu()
+        out["cpu_baseline"] = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in c.items() if k != "seconds"}
     print(json.dumps(out))
+
+
+def reference_arm(args, base):
+    """CPU leg on the host cores for the same workload and metric (the reference's Embree path is not
+    buildable; the oracle's restatement of it stands in)."""
+    from oracle import build as ob
+
+    ob.build()
+    if args.workload in RAYCAST:
+        sc, model, poses, attrs, desc = raycast_workload(args.workload)
+        run = lambda: cpu_raycast(sc, model, poses, attrs, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
+        metric, unit, config = "Mrays/s", "Mrays/s", desc
+    elif args.workload == "icp_stats":
+        rng = np.random.default_rng(0)
+        src = rng.uniform(-25, 25, (64, 32768, 3)).astype(np.float32)
+        tgt = (src + rng.normal(0, 0.01, src.shape)).astype(np.float32)
+        run = lambda: cpu_icp(src, tgt, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
+        metric, unit, config = "Gcorr/s", "Gcorr/s", {"workload": "ICP statistics_p2p + Umeyama (CPU sample)"}
+    elif args.workload == "pose_grad":
+        sc, model, true, est = posegrad_workload(16)
+        import oracle
+
+        obs = oracle.Scene(sc.vertices, sc.faces).simulate(model, IDENT, true, attrs=("ranges",))["ranges"]
+        run = lambda: cpu_posegrad(sc, model, true, est, obs, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
+        metric, unit, config = "pose-grad evals/s", "poses/s", {"workload": "pose gradient (CPU sample)"}
+    else:
+        raise SystemExit(f"unknown workload {args.workload}")
+    vals, leg = [], None
+    for _ in range(args.warmup + args.steps):
+        leg = run()
+        vals.append(leg["value"])
+    v = statistics.mean(vals[args.warmup:]) if len(vals) > args.warmup else vals[-1]
+    out = dict(base)
+    out.update({"impl": "reference", "metric": metric, "unit": unit, "value": round(v, 4), "dtype": "f32",
+                "ms_per_step": round(1e3 * leg["seconds"], 1), "config": config, "gpu_launches": 0,
+                "cpu_baseline": {"value": round(v, 4), "unit": unit, "cores": leg["cores"], "kind": leg["kind"],
+                                 "sample": leg["sample"]},
+                "e2e": {"value": round(v, 4), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+    return out
 
 
 if __name__ == "__main__":

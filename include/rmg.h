@@ -220,6 +220,76 @@ int rmg_simulate_ex(const rmg_map* map, const rmg_sensor* sensor,
 int rmg_default_launch_config(const rmg_map* map, const rmg_sensor* sensor, rmg_launch_config* cfg);
 
 /* ---------------------------------------------------------------------------
+ * Range adjoint (no counterpart in the reference: rmagine has no
+ * differentiable simulator).  Casts the rays of every pose exactly as
+ * rmg_simulate does and, in the same kernel, accumulates per pose
+ *   loss = sum Huber_delta(r_sim - r_obs),  grad = dloss/dxi (6 floats)
+ * over rays with a simulated hit (range.min <= t) and an observation in
+ * [range.min, range.max].  xi = (rho, omega) is the right perturbation
+ * T_bm * exp(xi^) (lie.h:57-114 conventions), translation first.
+ * ranges_obs: DEVICE n_poses*W*H.  grad: DEVICE n_poses*6, loss: DEVICE
+ * n_poses (either may be NULL, not both); ranges_sim / face_ids: optional
+ * DEVICE copies of the simulated ranges and face ids.  At most 65535 poses
+ * per call.  Deterministic (fixed reduction order).  Asynchronous. */
+int rmg_range_pose_grad(const rmg_map* map, const rmg_sensor* sensor,
+                        const rmg_transform* Tsb, const rmg_transform* Tbm, uint32_t n_poses,
+                        const float* ranges_obs, float huber_delta,
+                        float* grad, float* loss, float* ranges_sim, uint32_t* face_ids, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Correspondence statistics and Umeyama.
+ *
+ * rmagine::UmeyamaReductionConstraints (types/UmeyamaReductionConstraints.hpp:46-59). */
+typedef struct rmg_umeyama_constraints {
+  float max_dist;        /* ignore correspondences at or beyond this distance */
+  uint32_t dataset_id;   /* with dataset_ids: keep only this id */
+  uint32_t model_id;     /* with model_ids: keep only this id */
+} rmg_umeyama_constraints;
+
+/* Batched statistics_p2p (statistics.cpp:19-57, statistics.cu:58-160):
+ * batch b reduces correspondences [b*n_per_batch, (b+1)*n_per_batch) of the
+ * DEVICE arrays dataset_points / model_points (+ optional masks and ids,
+ * NULL = unused) to one CrossStatistics.  Dataset points are first mapped by
+ * pre_transforms (DEVICE; NULL = identity; stride 0 = one transform for all
+ * batches, 1 = one per batch).  Filter: masks > 0, ids == params ids,
+ * ||M - D||^2 < max_dist^2.  Accumulation in binary64.  Outputs (DEVICE, NULL
+ * = not wanted): stats[n_batches] and transforms[n_batches] = the Umeyama
+ * transform of each batch (optimization.cpp:12-49, memory_math.cu:1627-1708)
+ * solved in binary64.  params is a HOST pointer.  Asynchronous. */
+int rmg_statistics_p2p(const rmg_transform* pre_transforms, uint32_t pre_transform_stride,
+                       const rmg_vec3* dataset_points, const uint8_t* dataset_mask, const uint32_t* dataset_ids,
+                       const rmg_vec3* model_points, const uint8_t* model_mask, const uint32_t* model_ids,
+                       const rmg_umeyama_constraints* params, uint32_t n_batches, uint32_t n_per_batch,
+                       rmg_cross_stats* stats, rmg_transform* transforms, void* stream);
+
+/* Batched statistics_p2l (statistics.cpp:84-126, statistics.cu:190-276):
+ * model points are plane points with model_normals; the model correspondence is
+ * the projection M = D + N ((I - D) . N), kept when |(I - D) . N| < max_dist. */
+int rmg_statistics_p2l(const rmg_transform* pre_transforms, uint32_t pre_transform_stride,
+                       const rmg_vec3* dataset_points, const uint8_t* dataset_mask, const uint32_t* dataset_ids,
+                       const rmg_vec3* model_points, const rmg_vec3* model_normals,
+                       const uint8_t* model_mask, const uint32_t* model_ids,
+                       const rmg_umeyama_constraints* params, uint32_t n_batches, uint32_t n_per_batch,
+                       rmg_cross_stats* stats, rmg_transform* transforms, void* stream);
+
+/* Batched umeyama_transform(CrossStatistics) (memory_math.cu:1646-1656,
+ * optimization.cpp:51-55): DEVICE stats[n] -> DEVICE out[n]. */
+int rmg_umeyama_transform(const rmg_cross_stats* stats, uint32_t n, rmg_transform* out, void* stream);
+
+/* Backward of statistics_p2p + Umeyama (no counterpart in the reference):
+ * given the forward's stats and upstream gradients grad_R (DEVICE, 9 floats
+ * per batch, row-major dL/dR of the rotation matrix; NULL = 0) and grad_t
+ * (DEVICE, 3 per batch; NULL = 0), writes dL/d(dataset point) and dL/d(model
+ * point) for every correspondence (DEVICE float3 arrays; NULL = skip;
+ * filtered-out correspondences get 0).  Same inputs and filter as the forward. */
+int rmg_umeyama_backward(const rmg_transform* pre_transforms, uint32_t pre_transform_stride,
+                         const rmg_vec3* dataset_points, const uint8_t* dataset_mask, const uint32_t* dataset_ids,
+                         const rmg_vec3* model_points, const uint8_t* model_mask, const uint32_t* model_ids,
+                         const rmg_umeyama_constraints* params, uint32_t n_batches, uint32_t n_per_batch,
+                         const rmg_cross_stats* stats, const float* grad_R, const float* grad_t,
+                         rmg_vec3* grad_dataset, rmg_vec3* grad_model, void* stream);
+
+/* ---------------------------------------------------------------------------
  * LBVH build without device allocation.
  * No counterpart in the reference: rmagine's maps always allocate their own
  * memory.  This is for callers that cannot call cudaMalloc -- code running

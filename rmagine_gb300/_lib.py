@@ -107,6 +107,10 @@ class LbvhBuffersC(C.Structure):
                 ("leaf_parent", C.c_void_p), ("flags", C.c_void_p)]
 
 
+class ConstraintsC(C.Structure):
+    _fields_ = [("max_dist", C.c_float), ("dataset_id", C.c_uint32), ("model_id", C.c_uint32)]
+
+
 RMG_NOALLOC_MAX_FACES = 65536
 
 # name -> (restype, argtypes); every symbol include/rmg.h declares
@@ -134,6 +138,14 @@ SIGNATURES: dict[str, tuple] = {
                                   C.POINTER(LaunchConfigC), _P]),
     "rmg_default_launch_config": (C.c_int, [_P, _P, C.POINTER(LaunchConfigC)]),
     "rmg_lbvh_build_noalloc": (C.c_int, [_P, _U32, _P, _U32, C.POINTER(LbvhBuffersC), _P]),
+    "rmg_statistics_p2p": (C.c_int, [_P, _U32, _P, _P, _P, _P, _P, _P, C.POINTER(ConstraintsC), _U32, _U32,
+                                     _P, _P, _P]),
+    "rmg_statistics_p2l": (C.c_int, [_P, _U32, _P, _P, _P, _P, _P, _P, _P, C.POINTER(ConstraintsC), _U32, _U32,
+                                     _P, _P, _P]),
+    "rmg_umeyama_transform": (C.c_int, [_P, _U32, _P, _P]),
+    "rmg_range_pose_grad": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, _P, C.c_float, _P, _P, _P, _P, _P]),
+    "rmg_umeyama_backward": (C.c_int, [_P, _U32, _P, _P, _P, _P, _P, _P, C.POINTER(ConstraintsC), _U32, _U32,
+                                       _P, _P, _P, _P, _P, _P]),
 }
 
 _lib: C.CDLL | None = None

@@ -228,3 +228,20 @@ def terrain_poses(scene: Scene, n: int, seed: int = 2, size: float = 500.0, abov
 def million_triangle_terrain(seed: int = 0) -> Scene:
     """The ~1M-triangle terrain: 708 x 708 grid (999,698 triangles) + 2000 boxes (24,000)."""
     return terrain(grid=708, n_boxes=2000, seed=seed)
+
+
+def perturb_poses(poses: np.ndarray, seed: int, sigma_t: float = 0.1, sigma_r_deg: float = 2.0) -> np.ndarray:
+    """Poses moved by R <- R exp(N(0, sigma_r)^3) and t <- t + N(0, sigma_t)^3 (seeded)."""
+    from .transforms import compose
+
+    rng = np.random.default_rng(seed)
+    n = poses.shape[0]
+    d = np.zeros((n, 8), np.float32)
+    w = rng.normal(0, np.radians(sigma_r_deg), (n, 3))
+    th = np.linalg.norm(w, axis=1, keepdims=True)
+    d[:, :3] = (w / np.maximum(th, 1e-30) * np.sin(th / 2)).astype(np.float32)
+    d[:, 3] = np.cos(th[:, 0] / 2).astype(np.float32)
+    out = compose(poses, d)
+    out[:, 4:7] += rng.normal(0, sigma_t, (n, 3)).astype(np.float32)
+    return out
+

@@ -1,0 +1,23 @@
+"""The per-ray work constants bench.py uses for its roofline (mean LBVH node visits and triangle
+tests per ray) re-derived by the oracle's instrumented traversal on smaller samples."""
+import numpy as np
+import pytest
+
+import bench
+import oracle
+
+IDENT = np.array([0, 0, 0, 1, 0, 0, 0, 0], np.float32)
+
+
+@pytest.mark.parametrize("name", ["terrain1m_spherical", "room_vlp16"])
+def test_work_per_ray_constants(name):
+    sc, model, poses, attrs, desc = bench.raycast_workload(name)
+    W, H = oracle.model_size(model)
+    n = poses.shape[0] * W * H
+    rng = np.random.default_rng(1)
+    gids = np.sort(rng.choice(n, min(n, 40000), replace=False)).astype(np.uint64)
+    o, d = oracle.Scene(sc.vertices, sc.faces).rays(model, IDENT, poses, gids)
+    v, t, _, _ = oracle.CanonicalLbvh(sc.vertices, sc.faces).count(o, d, model.range.max)
+    want = bench.WORK_PER_RAY[name]
+    assert abs(v.mean() - want["nodes"]) / want["nodes"] < 0.03
+    assert abs(t.mean() - want["tris"]) / want["tris"] < 0.05
