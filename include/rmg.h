@@ -220,6 +220,48 @@ int rmg_simulate_ex(const rmg_map* map, const rmg_sensor* sensor,
 int rmg_default_launch_config(const rmg_map* map, const rmg_sensor* sensor, rmg_launch_config* cfg);
 
 /* ---------------------------------------------------------------------------
+ * Batched heterogeneous sensors (no counterpart in the reference, where each
+ * simulator call launches once per sensor: SphereSimulatorOptix.cpp:64-81).
+ * A plan binds many (sensor, Tsb, Tbm, n_poses, outputs) jobs on one map; a
+ * launch runs ALL their rays in one persistent kernel replayed from a CUDA
+ * graph.  Outputs are bit-identical to one rmg_simulate per job.  The plan
+ * keeps the DEVICE pointers given at creation (update poses in place).
+ * ------------------------------------------------------------------------- */
+typedef struct rmg_batch_entry {
+  const rmg_sensor* sensor;
+  rmg_transform Tsb;           /* by value */
+  const rmg_transform* Tbm;    /* DEVICE, n_poses records */
+  uint32_t n_poses;
+  rmg_outputs out;             /* DEVICE buffers, as for rmg_simulate */
+} rmg_batch_entry;
+
+typedef struct rmg_batch_config {
+  uint32_t stack_depth;  /* 0, 8 or 16 */
+  uint32_t block_warps;  /* 1..8 */
+  uint32_t tile_w;       /* tile of a 2-D sensor, tile_w * tile_h == 32; 1-row sensors use 32 x 1 */
+  uint32_t tile_h;
+  uint32_t grab;         /* tiles a warp takes from the work counter at a time, 1..64 */
+  uint32_t ctas_per_sm;  /* 0 = as many as fit */
+  uint32_t use_graph;    /* 1 = replay a captured CUDA graph, 0 = direct launch */
+} rmg_batch_config;
+
+typedef struct rmg_batch rmg_batch;
+
+int rmg_batch_default_config(rmg_batch_config* cfg);
+int rmg_batch_create(const rmg_map* map, const rmg_batch_entry* entries, uint32_t n_entries, rmg_batch** out);
+int rmg_batch_set_config(rmg_batch* batch, const rmg_batch_config* cfg);
+int rmg_batch_get_config(const rmg_batch* batch, rmg_batch_config* cfg);
+int rmg_batch_info(const rmg_batch* batch, uint64_t* total_rays, uint64_t* total_tiles);
+/* Asynchronous on `stream`.  The first launch after creation or a config
+ * change captures the graph (do not call it while `stream` is capturing). */
+int rmg_batch_launch(rmg_batch* batch, void* stream);
+/* Times candidate configs on the plan itself (reps timed launches each, after
+ * a warm-up), keeps the fastest and returns it in *best (may be NULL).
+ * Runs the plan's work several times: outputs hold the last run's results. */
+int rmg_batch_autotune(rmg_batch* batch, void* stream, uint32_t reps, rmg_batch_config* best);
+int rmg_batch_destroy(rmg_batch* batch);
+
+/* ---------------------------------------------------------------------------
  * Range adjoint (no counterpart in the reference: rmagine has no
  * differentiable simulator).  Casts the rays of every pose exactly as
  * rmg_simulate does and, in the same kernel, accumulates per pose

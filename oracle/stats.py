@@ -139,6 +139,7 @@ def umeyama(st):
 
 def quat_to_rot(q):
     q = np.asarray(q, np.float64)
+    q = q / np.linalg.norm(q, axis=-1, keepdims=True)
     x, y, z, w = q[..., 0], q[..., 1], q[..., 2], q[..., 3]
     return np.stack([
         np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], -1),
@@ -148,10 +149,12 @@ def quat_to_rot(q):
 
 
 def rotation_angle(Ra, Rb):
-    """Angle (rad) of Ra^T Rb per batch."""
+    """Angle (rad) of Ra^T Rb per batch: atan2(|vee(Rd - Rd^T)| / 2, (trace - 1) / 2), which keeps
+    full precision for small angles (arccos of the trace alone resolves only ~sqrt(eps))."""
     Rd = np.einsum("bji,bjk->bik", Ra, Rb)
     c = (np.trace(Rd, axis1=1, axis2=2) - 1.0) / 2.0
-    return np.arccos(np.clip(c, -1.0, 1.0))
+    v = np.stack([Rd[:, 2, 1] - Rd[:, 1, 2], Rd[:, 0, 2] - Rd[:, 2, 0], Rd[:, 1, 0] - Rd[:, 0, 1]], axis=1)
+    return np.arctan2(np.linalg.norm(v, axis=1) / 2.0, c)
 
 
 def loss_fd_gradients(dataset, model, gR, gt, pre=None, h=1e-6, **filt):

@@ -107,6 +107,16 @@ class LbvhBuffersC(C.Structure):
                 ("leaf_parent", C.c_void_p), ("flags", C.c_void_p)]
 
 
+class BatchEntryC(C.Structure):
+    _fields_ = [("sensor", C.c_void_p), ("Tsb", TransformC), ("Tbm", C.c_void_p), ("n_poses", C.c_uint32),
+                ("out", OutputsC)]
+
+
+class BatchConfigC(C.Structure):
+    _fields_ = [("stack_depth", C.c_uint32), ("block_warps", C.c_uint32), ("tile_w", C.c_uint32),
+                ("tile_h", C.c_uint32), ("grab", C.c_uint32), ("ctas_per_sm", C.c_uint32), ("use_graph", C.c_uint32)]
+
+
 class ConstraintsC(C.Structure):
     _fields_ = [("max_dist", C.c_float), ("dataset_id", C.c_uint32), ("model_id", C.c_uint32)]
 
@@ -143,6 +153,14 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_statistics_p2l": (C.c_int, [_P, _U32, _P, _P, _P, _P, _P, _P, _P, C.POINTER(ConstraintsC), _U32, _U32,
                                      _P, _P, _P]),
     "rmg_umeyama_transform": (C.c_int, [_P, _U32, _P, _P]),
+    "rmg_batch_default_config": (C.c_int, [C.POINTER(BatchConfigC)]),
+    "rmg_batch_create": (C.c_int, [_P, C.POINTER(BatchEntryC), _U32, C.POINTER(_P)]),
+    "rmg_batch_set_config": (C.c_int, [_P, C.POINTER(BatchConfigC)]),
+    "rmg_batch_get_config": (C.c_int, [_P, C.POINTER(BatchConfigC)]),
+    "rmg_batch_info": (C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "rmg_batch_launch": (C.c_int, [_P, _P]),
+    "rmg_batch_autotune": (C.c_int, [_P, _P, _U32, C.POINTER(BatchConfigC)]),
+    "rmg_batch_destroy": (C.c_int, [_P]),
     "rmg_range_pose_grad": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, _P, C.c_float, _P, _P, _P, _P, _P]),
     "rmg_umeyama_backward": (C.c_int, [_P, _U32, _P, _P, _P, _P, _P, _P, C.POINTER(ConstraintsC), _U32, _U32,
                                        _P, _P, _P, _P, _P, _P]),

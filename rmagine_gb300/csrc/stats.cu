@@ -105,10 +105,13 @@ struct FAcc {
   }
 };
 
-__device__ __forceinline__ void fold(double* acc, FAcc& f) {
-  acc[0] += f.n;
-  for (int k = 0; k < 3; ++k) { acc[1 + k] += f.d[k]; acc[4 + k] += f.m[k]; }
-  for (int k = 0; k < 9; ++k) acc[7 + k] += f.md[k];
+// Binary64 per-thread accumulators live in shared memory, [16][threads], so the
+// registers hold only the binary32 run (keeps 3-4 CTAs resident per SM).
+__device__ __forceinline__ void fold(double (*acc)[kStatsThreads], FAcc& f) {
+  const int t = threadIdx.x;
+  acc[0][t] += f.n;
+  for (int k = 0; k < 3; ++k) { acc[1 + k][t] += f.d[k]; acc[4 + k][t] += f.m[k]; }
+  for (int k = 0; k < 9; ++k) acc[7 + k][t] += f.md[k];
   f.zero();
 }
 
@@ -145,7 +148,7 @@ __device__ void finalize(const StatsParams& P, uint32_t b, const double* acc, co
 }
 
 template <bool P2L, bool VEC>
-__global__ void __launch_bounds__(kStatsThreads) k_stats(const StatsParams P) {
+__global__ void __launch_bounds__(kStatsThreads, 3) k_stats(const StatsParams P) {
   const uint32_t b = blockIdx.x / P.chunks;
   const uint32_t c = blockIdx.x - b * P.chunks;
   const uint64_t base = (uint64_t)b * P.n_per;
@@ -157,8 +160,8 @@ __global__ void __launch_bounds__(kStatsThreads) k_stats(const StatsParams P) {
   const V sd = P.n_per ? tf_point(pre, ldv(P.dp, base)) : V{0, 0, 0};
   const V sm = P.n_per ? ldv(P.mp, base) : V{0, 0, 0};
 
-  double acc[16];
-  for (int k = 0; k < 16; ++k) acc[k] = 0.0;
+  __shared__ double acc[16][kStatsThreads];
+  for (int k = 0; k < 16; ++k) acc[k][threadIdx.x] = 0.0;
   FAcc f;
   f.zero();
   const V zero{0.f, 0.f, 0.f};
@@ -210,14 +213,11 @@ __global__ void __launch_bounds__(kStatsThreads) k_stats(const StatsParams P) {
   // CTA reduction in binary64
   __shared__ double red[kStatsThreads / 32][16];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
   for (int k = 0; k < 16; ++k) {
-    double v = acc[k];
+    double v = acc[k][threadIdx.x];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    acc[k] = v;
+    if (lane == 0) red[warp][k] = v;
   }
-  if (lane == 0)
-    for (int k = 0; k < 16; ++k) red[warp][k] = acc[k];
   __syncthreads();
   if (threadIdx.x >= 16) return;
   double v = 0.0;
