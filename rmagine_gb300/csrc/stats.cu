@@ -64,14 +64,16 @@ __device__ __forceinline__ V tf_point(const Tf& T, const V& p) {
   return V{add(r.x, T.t.x), add(r.y, T.t.y), add(r.z, T.t.z)};
 }
 
-template <bool P2L>
+// PRE = false: no pre-transform (rotating by the identity quaternion is exact, so
+// skipping it changes no bit).
+template <bool P2L, bool PRE = true>
 __device__ __forceinline__ bool correspondence(const StatsParams& P, const Tf& pre, uint64_t i, const V& dpt,
                                                const V& mpt, const V& npt, V& D, V& M) {
   if (P.dmask && P.dmask[i] == 0) return false;
   if (P.mmask && P.mmask[i] == 0) return false;
   if (P.dids && P.dids[i] != P.dataset_id) return false;
   if (P.mids && P.mids[i] != P.model_id) return false;
-  D = tf_point(pre, dpt);
+  D = PRE ? tf_point(pre, dpt) : dpt;
   if (P2L) {
     const V diff{sub(mpt.x, D.x), sub(mpt.y, D.y), sub(mpt.z, D.z)};
     const float sd = add(add(mul(diff.x, npt.x), mul(diff.y, npt.y)), mul(diff.z, npt.z));
@@ -147,7 +149,7 @@ __device__ void finalize(const StatsParams& P, uint32_t b, const double* acc, co
   }
 }
 
-template <bool P2L, bool VEC>
+template <bool P2L, bool VEC, bool PRE>
 __global__ void __launch_bounds__(kStatsThreads, 3) k_stats(const StatsParams P) {
   const uint32_t b = blockIdx.x / P.chunks;
   const uint32_t c = blockIdx.x - b * P.chunks;
@@ -192,7 +194,7 @@ __global__ void __launch_bounds__(kStatsThreads, 3) k_stats(const StatsParams P)
         if (j < lo || j >= hi) continue;
         V D, M;
         const V np = P2L ? V{nn[3 * k], nn[3 * k + 1], nn[3 * k + 2]} : zero;
-        if (correspondence<P2L>(P, pre, base + j, V{dd[3 * k], dd[3 * k + 1], dd[3 * k + 2]},
+        if (correspondence<P2L, PRE>(P, pre, base + j, V{dd[3 * k], dd[3 * k + 1], dd[3 * k + 2]},
                                 V{mmv[3 * k], mmv[3 * k + 1], mmv[3 * k + 2]}, np, D, M))
           f.add_pt(D, M, sd, sm);
       }
@@ -203,7 +205,7 @@ __global__ void __launch_bounds__(kStatsThreads, 3) k_stats(const StatsParams P)
     for (uint32_t j = lo + threadIdx.x; j < hi; j += blockDim.x) {
       V D, M;
       const V np = P2L ? ldv(P.mn, base + j) : zero;
-      if (correspondence<P2L>(P, pre, base + j, ldv(P.dp, base + j), ldv(P.mp, base + j), np, D, M))
+      if (correspondence<P2L, PRE>(P, pre, base + j, ldv(P.dp, base + j), ldv(P.mp, base + j), np, D, M))
         f.add_pt(D, M, sd, sm);
       if (++run == 4 * kFold) { fold(acc, f); run = 0; }
     }
@@ -427,12 +429,16 @@ int launch_stats(StatsParams& P, bool p2l, cudaStream_t st) {
     RMG_CUDA_TRY(cudaMemsetAsync(P.counters, 0, 4 * (size_t)P.n_batches, st));
   }
   const bool vec = vec_ok(P, p2l);
-  if (p2l) {
-    if (vec) k_stats<true, true><<<grid, kStatsThreads, 0, st>>>(P);
-    else k_stats<true, false><<<grid, kStatsThreads, 0, st>>>(P);
-  } else {
-    if (vec) k_stats<false, true><<<grid, kStatsThreads, 0, st>>>(P);
-    else k_stats<false, false><<<grid, kStatsThreads, 0, st>>>(P);
+  const int variant = (p2l ? 4 : 0) | (vec ? 2 : 0) | (P.pre ? 1 : 0);
+  switch (variant) {
+    case 0: k_stats<false, false, false><<<grid, kStatsThreads, 0, st>>>(P); break;
+    case 1: k_stats<false, false, true><<<grid, kStatsThreads, 0, st>>>(P); break;
+    case 2: k_stats<false, true, false><<<grid, kStatsThreads, 0, st>>>(P); break;
+    case 3: k_stats<false, true, true><<<grid, kStatsThreads, 0, st>>>(P); break;
+    case 4: k_stats<true, false, false><<<grid, kStatsThreads, 0, st>>>(P); break;
+    case 5: k_stats<true, false, true><<<grid, kStatsThreads, 0, st>>>(P); break;
+    case 6: k_stats<true, true, false><<<grid, kStatsThreads, 0, st>>>(P); break;
+    default: k_stats<true, true, true><<<grid, kStatsThreads, 0, st>>>(P); break;
   }
   const int s = cuda_status(cudaGetLastError(), "k_stats");
   if (scratch) cudaFreeAsync(scratch, st);

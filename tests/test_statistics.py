@@ -164,14 +164,20 @@ def test_gpu_filter_counts_single_large_batch(rs):
 def test_gpu_stats_and_umeyama_match_fp64_oracle(rs, N):
     B = 64
     src, tgt, R, t = icp_batches(B, N, seed=4)
-    for md in (np.inf, 1.0):
+    # max_dist = 1 m on clouds pre-aligned by the true pose (the ICP case): the filter drops the
+    # outliers and keeps the inliers
+    pre = np.zeros((B, 8), F32)
+    pre[:, :4] = ost.rot_to_quat(R)
+    pre[:, 4:7] = t
+    for md, pr in ((np.inf, None), (1.0, pre)):
         P = rs.UmeyamaReductionConstraints(max_dist=md)
-        got, T = gpu_stats(rs, src, tgt, params=P)
-        want = ost.stats(*ost.correspondences(src, tgt, max_dist=md))
+        got, T = gpu_stats(rs, src, tgt, pre=pr, params=P)
+        want = ost.stats(*ost.correspondences(src, tgt, pr, max_dist=md))
+        assert want["n"].min() > 0.9 * N
         check_stats(got, want)
         Ro, to, qo = ost.umeyama(want)
         Rg = ost.quat_to_rot(T[:, :4].astype(np.float64))
-        assert ost.rotation_angle(Rg, Ro).max() < 2e-6
+        assert ost.rotation_angle(Rg, Ro).max() < (2e-6 if pr is None else 2e-5)
         assert np.abs(T[:, 4:7] - to).max() < 2e-5 * (1 + np.abs(to).max())
         # the quaternion sign follows the reference's branch order
         assert np.abs(T[:, :4] - qo).max() < 1e-5
