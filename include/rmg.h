@@ -116,7 +116,7 @@ typedef struct rmg_outputs {
 
 /* Traversal launch options (the knobs the autotuner searches). */
 typedef struct rmg_launch_config {
-  uint32_t stack_depth;   /* short-stack entries per ray; 0 = stackless (parent pointers) */
+  uint32_t stack_depth;   /* short-stack entries per ray: 0 (stackless, parent pointers), 8 or 16 */
   uint32_t block_warps;   /* warps per CTA */
   uint32_t tile_w;        /* a warp covers tile_h x tile_w rays of one pose */
   uint32_t tile_h;        /* tile_w * tile_h must be 32 */

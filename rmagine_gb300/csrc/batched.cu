@@ -45,9 +45,10 @@ struct BatchParams {
   unsigned long long* counter;
   uint32_t grab;
   unsigned budget;
+  int trail_bits;
 };
 
-template <int OK, int SS>
+template <int OK, int SS, int TB>
 __device__ __forceinline__ void batched_ray(const BatchParams& B, const JobDev& J, uint64_t tile_in_job,
                                             uint32_t lane) {
   const uint32_t pose = (uint32_t)(tile_in_job / J.tiles_per_pose);
@@ -65,7 +66,7 @@ __device__ __forceinline__ void batched_ray(const BatchParams& B, const JobDev& 
   setup_ray<OK>(J.sen, Tsm, loc, dir_s, orig_s, o, d);
   Hit h;
   bool over = false;
-  trace_ray<SS>(B.map, o, d, J.sen.range_max, B.budget, h, over);
+  trace_ray<SS, TB>(B.map, o, d, J.sen.range_max, B.budget, h, over);
   if (over) atomicExch(B.map.status, (unsigned)RMG_ERR_TRAVERSAL_BUDGET);
   TraceParams P;  // the epilogue reads only map, sensor range and outputs
   P.map = B.map;
@@ -74,7 +75,7 @@ __device__ __forceinline__ void batched_ray(const BatchParams& B, const JobDev& 
   write_attributes<OK>(P, gid, h, dir_s, orig_s, Tsm);
 }
 
-template <int SS>
+template <int SS, int TB>
 __global__ void __launch_bounds__(256) k_trace_batched(const BatchParams B) {
   __shared__ unsigned long long s_begin[kMaxJobsShared + 1];
   const bool in_smem = B.n_jobs <= kMaxJobsShared;
@@ -103,34 +104,45 @@ __global__ void __launch_bounds__(256) k_trace_batched(const BatchParams B) {
       const uint64_t t = tile - J.tile_begin;
       switch (J.sen.kind) {
         case RMG_MODEL_SPHERICAL:
-        case RMG_MODEL_PINHOLE: batched_ray<ORIGIN_POSE, SS>(B, J, t, lane); break;
-        case RMG_MODEL_O1DN: batched_ray<ORIGIN_SINGLE, SS>(B, J, t, lane); break;
-        default: batched_ray<ORIGIN_TABLE, SS>(B, J, t, lane); break;
+        case RMG_MODEL_PINHOLE: batched_ray<ORIGIN_POSE, SS, TB>(B, J, t, lane); break;
+        case RMG_MODEL_O1DN: batched_ray<ORIGIN_SINGLE, SS, TB>(B, J, t, lane); break;
+        default: batched_ray<ORIGIN_TABLE, SS, TB>(B, J, t, lane); break;
       }
     }
   }
 }
 
-cudaError_t launch_batched(const BatchParams& B, int ss, unsigned grid, unsigned block, cudaStream_t st) {
-  switch (ss) {
-    case 0: k_trace_batched<0><<<grid, block, 0, st>>>(B); break;
-    case 8: k_trace_batched<8><<<grid, block, 0, st>>>(B); break;
-    case 16: k_trace_batched<16><<<grid, block, 0, st>>>(B); break;
-    default: return cudaErrorInvalidValue;
+template <int SS>
+cudaError_t launch_batched_tb(const BatchParams& B, unsigned grid, unsigned block, cudaStream_t st) {
+  switch (B.trail_bits) {
+    case 32: k_trace_batched<SS, 32><<<grid, block, 0, st>>>(B); break;
+    case 64: k_trace_batched<SS, 64><<<grid, block, 0, st>>>(B); break;
+    default: k_trace_batched<SS, 128><<<grid, block, 0, st>>>(B); break;
   }
   return cudaGetLastError();
 }
 
-template <int SS>
-const void* batched_fn() {
-  return reinterpret_cast<const void*>(k_trace_batched<SS>);
+cudaError_t launch_batched(const BatchParams& B, int ss, unsigned grid, unsigned block, cudaStream_t st) {
+  switch (ss) {
+    case 0: return launch_batched_tb<0>(B, grid, block, st);
+    case 8: return launch_batched_tb<8>(B, grid, block, st);
+    case 16: return launch_batched_tb<16>(B, grid, block, st);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
-const void* kernel_ptr(int ss) {
+template <int SS>
+const void* batched_fn(int tb) {
+  return tb == 32 ? reinterpret_cast<const void*>(k_trace_batched<SS, 32>)
+                  : tb == 64 ? reinterpret_cast<const void*>(k_trace_batched<SS, 64>)
+                             : reinterpret_cast<const void*>(k_trace_batched<SS, 128>);
+}
+
+const void* kernel_ptr(int ss, int tb) {
   switch (ss) {
-    case 0: return batched_fn<0>();
-    case 8: return batched_fn<8>();
-    default: return batched_fn<16>();
+    case 0: return batched_fn<0>(tb);
+    case 8: return batched_fn<8>(tb);
+    default: return batched_fn<16>(tb);
   }
 }
 
@@ -209,9 +221,9 @@ int build_jobs(rmg_batch* b) {
   return RMG_OK;
 }
 
-int persistent_grid(const rmg_batch_config& c, unsigned& grid) {
+int persistent_grid(const rmg_batch_config& c, int trail_bits, unsigned& grid) {
   int per_sm = 0;
-  RMG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel_ptr((int)c.stack_depth),
+  RMG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel_ptr((int)c.stack_depth, trail_bits),
                                                              32 * (int)c.block_warps, 0));
   per_sm = std::max(per_sm, 1);
   if (c.ctas_per_sm > 0) per_sm = std::min<int>(per_sm, (int)c.ctas_per_sm);
@@ -228,6 +240,7 @@ BatchParams params(const rmg_batch* b) {
   B.counter = b->counter;
   B.grab = b->cfg.grab;
   B.budget = 2u * b->map->n_nodes + 64u;
+  B.trail_bits = trail_bits_for_depth(b->map->depth);
   return B;
 }
 
@@ -235,7 +248,7 @@ BatchParams params(const rmg_batch* b) {
 int launch_direct(rmg_batch* b, cudaStream_t st) {
   if (b->total_tiles == 0) return RMG_OK;
   unsigned grid = 0;
-  int s = persistent_grid(b->cfg, grid);
+  int s = persistent_grid(b->cfg, trail_bits_for_depth(b->map->depth), grid);
   if (s != RMG_OK) return s;
   RMG_CUDA_TRY(cudaMemsetAsync(b->counter, 0, sizeof(unsigned long long), st));
   return cuda_status(launch_batched(params(b), (int)b->cfg.stack_depth, grid, 32u * b->cfg.block_warps, st),

@@ -33,7 +33,7 @@ struct GradParams {
   uint32_t ctas_per_pose;
 };
 
-template <int OK, int SS>
+template <int OK, int SS, int TB>
 __global__ void __launch_bounds__(256) k_range_grad(const GradParams G) {
   const TraceParams& P = G.T;
   const uint32_t pose = blockIdx.y;
@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(256) k_range_grad(const GradParams G) {
       setup_ray<OK>(P.sen, Tsm, loc, dir_s, orig_s, o, d);
       Hit h;
       bool over = false;
-      trace_ray<SS>(P.map, o, d, P.sen.range_max, P.budget, h, over);
+      trace_ray<SS, TB>(P.map, o, d, P.sen.range_max, P.budget, h, over);
       if (over) atomicExch(P.map.status, (unsigned)RMG_ERR_TRAVERSAL_BUDGET);
       if (P.out.ranges) P.out.ranges[gid] = h.tri >= 0 ? h.t : add(P.sen.range_max, 1.0f);
       if (P.out.face_ids) P.out.face_ids[gid] = h.tri >= 0 ? h.face : 0xffffffffu;
@@ -120,15 +120,24 @@ __global__ void k_grad_final(const float* partial, uint32_t n_poses, uint32_t ct
   }
 }
 
+template <int OK, int SS>
+cudaError_t launch_grad_tb(const GradParams& G, dim3 grid, unsigned block, cudaStream_t st) {
+  switch (G.T.trail_bits) {
+    case 32: k_range_grad<OK, SS, 32><<<grid, block, 0, st>>>(G); break;
+    case 64: k_range_grad<OK, SS, 64><<<grid, block, 0, st>>>(G); break;
+    default: k_range_grad<OK, SS, 128><<<grid, block, 0, st>>>(G); break;
+  }
+  return cudaGetLastError();
+}
+
 template <int OK>
 cudaError_t launch_grad(const GradParams& G, int ss, dim3 grid, unsigned block, cudaStream_t st) {
   switch (ss) {
-    case 0: k_range_grad<OK, 0><<<grid, block, 0, st>>>(G); break;
-    case 8: k_range_grad<OK, 8><<<grid, block, 0, st>>>(G); break;
-    case 16: k_range_grad<OK, 16><<<grid, block, 0, st>>>(G); break;
+    case 0: return launch_grad_tb<OK, 0>(G, grid, block, st);
+    case 8: return launch_grad_tb<OK, 8>(G, grid, block, st);
+    case 16: return launch_grad_tb<OK, 16>(G, grid, block, st);
     default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
 }  // namespace

@@ -16,6 +16,6 @@ cudaError_t launch_trace_single(const TraceParams& P, int stack_depth, unsigned 
 cudaError_t launch_trace_table(const TraceParams& P, int stack_depth, unsigned grid, unsigned block,
                                cudaStream_t st);
 
-inline bool valid_stack_depth(uint32_t s) { return s == 0 || s == 4 || s == 8 || s == 16 || s == 32; }
+inline bool valid_stack_depth(uint32_t s) { return s == 0 || s == 8 || s == 16; }
 
 }  // namespace rmg

@@ -18,7 +18,7 @@ int default_config(const rmg_sensor* s, rmg_launch_config* cfg) {
 
 int check_config(const rmg_launch_config& c) {
   if (!valid_stack_depth(c.stack_depth))
-    return fail(RMG_ERR_UNSUPPORTED, "launch config: stack_depth must be 0, 4, 8, 16 or 32");
+    return fail(RMG_ERR_UNSUPPORTED, "launch config: stack_depth must be 0, 8 or 16");
   if (c.block_warps < 1 || c.block_warps > 8)
     return fail(RMG_ERR_UNSUPPORTED, "launch config: block_warps must be 1..8");
   if (c.tile_w == 0 || (c.tile_w & (c.tile_w - 1)) != 0 || c.tile_w > 32 || c.tile_w * c.tile_h != 32)
@@ -50,6 +50,7 @@ int make_trace_params(const rmg_map* map, const rmg_sensor* sensor, const rmg_tr
   P.tiles_per_pose = P.tiles_x * tiles_y;
   P.n_tiles = (uint64_t)P.tiles_per_pose * n_poses;
   P.budget = 2u * map->n_nodes + 64u;
+  P.trail_bits = trail_bits_for_depth(map->depth);
   return RMG_OK;
 }
 

@@ -9,8 +9,8 @@
 //   * Every internal node carries both child boxes; a visit tests the two
 //     boxes, intersects leaf children (one triangle each) on the spot and
 //     descends into the nearer hit internal child.
-//   * A 128-bit trail records, one bit per level, whether the other child of
-//     that level is still pending.  The pending children themselves are kept
+//   * A trail of 32, 64 or 128 bits (chosen from the tree depth) records, one
+//     bit per level, whether the other child of that level is still pending.  The pending children themselves are kept
 //     in a circular short stack of SS entries (SS = 0: none).  When the stack
 //     has run dry but the trail still has pending levels, the ray climbs the
 //     parent links to the pending level and takes the sibling: stackless
@@ -55,14 +55,27 @@ __device__ __forceinline__ RayBox make_raybox(const V& o, const V& d) {
   return r;
 }
 
+// Three-input float min/max (PTX ISA 8.8, sm_100 and later); same NaN rules as
+// the two-input forms.
+__device__ __forceinline__ float fmin3f(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float fmax3f(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
 // Slab test of one box; tmin includes the ray's tnear = 0.
 __device__ __forceinline__ void slab(const RayBox& r, float lox, float hix, float loy, float hiy,
                                      float loz, float hiz, float& tmin, float& tmax) {
   const float x0 = fmaf(lox, r.ix, -r.oix), x1 = fmaf(hix, r.ix, -r.oix);
   const float y0 = fmaf(loy, r.iy, -r.oiy), y1 = fmaf(hiy, r.iy, -r.oiy);
   const float z0 = fmaf(loz, r.iz, -r.oiz), z1 = fmaf(hiz, r.iz, -r.oiz);
-  tmin = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), 0.0f));
-  tmax = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
+  tmin = fmax3f(fminf(x0, x1), fminf(y0, y1), fmaxf(fminf(z0, z1), 0.0f));
+  tmax = fmin3f(fmaxf(x0, x1), fmaxf(y0, y1), fmaxf(z0, z1));
 }
 
 __device__ __forceinline__ bool visit(float tmin, float tmax, float best) {
@@ -79,20 +92,49 @@ __device__ __forceinline__ void test_tri(const DeviceMap& map, const RayW& rw, i
   }
 }
 
-// 128-bit trail helpers.
-__device__ __forceinline__ void trail_push(uint64_t& lo, uint64_t& hi, uint64_t bit) {
-  hi = (hi << 1) | (lo >> 63);
-  lo = (lo << 1) | bit;
-}
-__device__ __forceinline__ int trail_ctz(uint64_t lo, uint64_t hi) {
-  return lo ? (__ffsll((long long)lo) - 1) : (64 + __ffsll((long long)hi) - 1);
-}
-__device__ __forceinline__ void trail_shr(uint64_t& lo, uint64_t& hi, int k) {
-  if (k >= 64) { lo = hi >> (k - 64); hi = 0; }
-  else if (k > 0) { lo = (lo >> k) | (hi << (64 - k)); hi >>= k; }
-}
+// The trail: one bit per internal level of the current path ("the other child
+// of this level is still pending").  TB bits must exceed the tree's internal
+// depth; the launcher picks 32, 64 or 128 from the depth the build measured.
+template <int TB> struct Trail;
 
-template <int SS>
+template <> struct Trail<32> {
+  uint32_t v = 0;
+  __device__ __forceinline__ void push(uint32_t bit) { v = (v << 1) | bit; }
+  __device__ __forceinline__ bool empty() const { return v == 0; }
+  __device__ __forceinline__ int ctz() const { return __ffs((int)v) - 1; }
+  __device__ __forceinline__ void shr(int k) { v >>= k; }
+  __device__ __forceinline__ void clear_low() { v ^= 1u; }
+};
+
+template <> struct Trail<64> {
+  uint64_t v = 0;
+  __device__ __forceinline__ void push(uint32_t bit) { v = (v << 1) | bit; }
+  __device__ __forceinline__ bool empty() const { return v == 0; }
+  __device__ __forceinline__ int ctz() const { return __ffsll((long long)v) - 1; }
+  __device__ __forceinline__ void shr(int k) { v >>= k; }
+  __device__ __forceinline__ void clear_low() { v ^= 1ull; }
+};
+
+template <> struct Trail<128> {
+  uint64_t lo = 0, hi = 0;
+  __device__ __forceinline__ void push(uint32_t bit) {
+    hi = (hi << 1) | (lo >> 63);
+    lo = (lo << 1) | bit;
+  }
+  __device__ __forceinline__ bool empty() const { return (lo | hi) == 0; }
+  __device__ __forceinline__ int ctz() const {
+    return lo ? (__ffsll((long long)lo) - 1) : (64 + __ffsll((long long)hi) - 1);
+  }
+  __device__ __forceinline__ void shr(int k) {
+    if (k >= 64) { lo = hi >> (k - 64); hi = 0; }
+    else if (k > 0) { lo = (lo >> k) | (hi << (64 - k)); hi >>= k; }
+  }
+  __device__ __forceinline__ void clear_low() { lo ^= 1ull; }
+};
+
+inline int trail_bits_for_depth(unsigned depth) { return depth <= 32 ? 32 : (depth <= 64 ? 64 : 128); }
+
+template <int SS, int TB>
 __device__ __forceinline__ void trace_ray(const DeviceMap& map, const V& o, const V& d, float tfar,
                                           unsigned budget, Hit& h, bool& over_budget) {
   h.t = tfar;
@@ -103,7 +145,7 @@ __device__ __forceinline__ void trace_ray(const DeviceMap& map, const V& o, cons
   const RayBox rb = make_raybox(o, d);
 
   int node = map.root;
-  uint64_t tlo = 0, thi = 0;
+  Trail<TB> trail;
   int stk[SS > 0 ? SS : 1];
   float stkt[SS > 0 ? SS : 1];
   int sp = 0, top = 0;
@@ -134,21 +176,21 @@ __device__ __forceinline__ void trace_ray(const DeviceMap& map, const V& o, cons
         stkt[top] = lf ? tminR : tminL;
         sp = sp < SS ? sp + 1 : SS;
       }
-      trail_push(tlo, thi, 1);
+      trail.push(1u);
       node = nearc;
       continue;
     }
     if (hitL || hitR) {
-      trail_push(tlo, thi, 0);
+      trail.push(0u);
       node = hitL ? ln.x : ln.y;
       continue;
     }
     // ---- backtrack to the nearest pending level ----
     bool found = false;
-    while (tlo | thi) {
-      const int k = trail_ctz(tlo, thi);
-      trail_shr(tlo, thi, k);
-      tlo ^= 1ull;
+    while (!trail.empty()) {
+      const int k = trail.ctz();
+      trail.shr(k);
+      trail.clear_low();
       if (SS > 0 && sp > 0) {
         const int cand = stk[top];
         const float ct = stkt[top];
@@ -201,6 +243,7 @@ struct TraceParams {
   uint32_t tiles_per_pose;
   uint64_t n_tiles;
   unsigned budget;
+  int trail_bits;
 };
 
 // Writes all requested attributes of one ray (SphereSimulatorEmbree.tcc:104-249).
@@ -274,7 +317,7 @@ __device__ __forceinline__ void setup_ray(const SensorDev& sen, const Tf& Tsm, u
 }
 
 // One warp = one tile of tile_h x tile_w rays of one pose.
-template <int OK, int SS>
+template <int OK, int SS, int TB>
 __global__ void __launch_bounds__(256) k_trace(const TraceParams P) {
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp >= P.n_tiles) return;
@@ -295,7 +338,7 @@ __global__ void __launch_bounds__(256) k_trace(const TraceParams P) {
   setup_ray<OK>(P.sen, Tsm, loc, dir_s, orig_s, o, d);
   Hit h;
   bool over = false;
-  trace_ray<SS>(P.map, o, d, P.sen.range_max, P.budget, h, over);
+  trace_ray<SS, TB>(P.map, o, d, P.sen.range_max, P.budget, h, over);
   if (over) atomicExch(P.map.status, (unsigned)RMG_ERR_TRAVERSAL_BUDGET);
   write_attributes<OK>(P, gid, h, dir_s, orig_s, Tsm);
 }

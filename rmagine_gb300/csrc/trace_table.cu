@@ -4,17 +4,26 @@
 
 namespace rmg {
 
+namespace {
+template <int SS>
+cudaError_t by_trail(const TraceParams& P, unsigned grid, unsigned block, cudaStream_t st) {
+  switch (P.trail_bits) {
+    case 32: k_trace<ORIGIN_TABLE, SS, 32><<<grid, block, 0, st>>>(P); break;
+    case 64: k_trace<ORIGIN_TABLE, SS, 64><<<grid, block, 0, st>>>(P); break;
+    default: k_trace<ORIGIN_TABLE, SS, 128><<<grid, block, 0, st>>>(P); break;
+  }
+  return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t launch_trace_table(const TraceParams& P, int stack_depth, unsigned grid, unsigned block,
                                cudaStream_t st) {
   switch (stack_depth) {
-    case 0: k_trace<ORIGIN_TABLE, 0><<<grid, block, 0, st>>>(P); break;
-    case 4: k_trace<ORIGIN_TABLE, 4><<<grid, block, 0, st>>>(P); break;
-    case 8: k_trace<ORIGIN_TABLE, 8><<<grid, block, 0, st>>>(P); break;
-    case 16: k_trace<ORIGIN_TABLE, 16><<<grid, block, 0, st>>>(P); break;
-    case 32: k_trace<ORIGIN_TABLE, 32><<<grid, block, 0, st>>>(P); break;
+    case 0: return by_trail<0>(P, grid, block, st);
+    case 8: return by_trail<8>(P, grid, block, st);
+    case 16: return by_trail<16>(P, grid, block, st);
     default: return cudaErrorInvalidValue;
   }
-  return cudaGetLastError();
 }
 
 }  // namespace rmg

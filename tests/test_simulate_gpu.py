@@ -171,7 +171,7 @@ def test_stack_depths_and_tiles_bitwise_identical():
     m = rm.Map(sc.vertices, sc.faces)
     model = sensors.ouster_like(64, 512)
     base = gpu_sim(m, model, poses, cfg=rm.launch_config(8, 4, 8, 4))
-    for cfg in [(0, 4, 8, 4), (4, 2, 8, 4), (16, 8, 32, 1), (32, 1, 4, 8), (8, 4, 16, 2), (0, 8, 2, 16)]:
+    for cfg in [(0, 4, 8, 4), (16, 2, 8, 4), (16, 8, 32, 1), (8, 1, 4, 8), (8, 4, 16, 2), (0, 8, 2, 16)]:
         other = gpu_sim(m, model, poses, cfg=rm.launch_config(*cfg))
         for a in ALL:
             assert np.array_equal(base[a].view(np.uint8), other[a].view(np.uint8)), (cfg, a)
