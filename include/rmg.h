@@ -120,6 +120,9 @@ typedef struct rmg_launch_config {
   uint32_t block_warps;   /* warps per CTA */
   uint32_t tile_w;        /* a warp covers tile_h x tile_w rays of one pose */
   uint32_t tile_h;        /* tile_w * tile_h must be 32 */
+  uint32_t refill;        /* 0: one tile per warp.  1..32: persistent warps that hand new rays to
+                             idle lanes whenever fewer than `refill` lanes are busy (stack_depth 8 or 16) */
+  uint32_t chunk;         /* refill mode: tiles a warp takes from the work counter at a time (>= 1) */
 } rmg_launch_config;
 
 typedef struct rmg_map_info {

@@ -16,6 +16,13 @@ cudaError_t launch_trace_single(const TraceParams& P, int stack_depth, unsigned 
 cudaError_t launch_trace_table(const TraceParams& P, int stack_depth, unsigned grid, unsigned block,
                                cudaStream_t st);
 
+cudaError_t launch_trace_refill_pose(const TraceParams& P, int stack_depth, unsigned block,
+                                     unsigned long long* counter, uint32_t chunk, uint32_t refill, cudaStream_t st);
+cudaError_t launch_trace_refill_single(const TraceParams& P, int stack_depth, unsigned block,
+                                       unsigned long long* counter, uint32_t chunk, uint32_t refill, cudaStream_t st);
+cudaError_t launch_trace_refill_table(const TraceParams& P, int stack_depth, unsigned block,
+                                      unsigned long long* counter, uint32_t chunk, uint32_t refill, cudaStream_t st);
+
 inline bool valid_stack_depth(uint32_t s) { return s == 0 || s == 8 || s == 16; }
 
 }  // namespace rmg

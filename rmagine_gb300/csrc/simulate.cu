@@ -10,6 +10,8 @@ namespace rmg {
 int default_config(const rmg_sensor* s, rmg_launch_config* cfg) {
   cfg->stack_depth = 8;
   cfg->block_warps = 4;
+  cfg->refill = 0;
+  cfg->chunk = 4;
   if (s && s->width >= 8 && s->height >= 4) { cfg->tile_w = 8; cfg->tile_h = 4; }
   else if (s && s->height < 4 && s->height > 1) { cfg->tile_w = 16; cfg->tile_h = 2; }
   else { cfg->tile_w = 32; cfg->tile_h = 1; }
@@ -23,6 +25,10 @@ int check_config(const rmg_launch_config& c) {
     return fail(RMG_ERR_UNSUPPORTED, "launch config: block_warps must be 1..8");
   if (c.tile_w == 0 || (c.tile_w & (c.tile_w - 1)) != 0 || c.tile_w > 32 || c.tile_w * c.tile_h != 32)
     return fail(RMG_ERR_UNSUPPORTED, "launch config: tile_w must be a power of two with tile_w*tile_h == 32");
+  if (c.refill > 32) return fail(RMG_ERR_UNSUPPORTED, "launch config: refill must be 0..32");
+  if (c.refill && c.stack_depth == 0)
+    return fail(RMG_ERR_UNSUPPORTED, "launch config: refill mode needs stack_depth 8 or 16");
+  if (c.refill && (c.chunk < 1 || c.chunk > 1024)) return fail(RMG_ERR_UNSUPPORTED, "launch config: chunk 1..1024");
   return RMG_OK;
 }
 
@@ -54,8 +60,31 @@ int make_trace_params(const rmg_map* map, const rmg_sensor* sensor, const rmg_tr
   return RMG_OK;
 }
 
+int launch_refill(const TraceParams& P, const rmg_sensor* sensor, const rmg_launch_config& cfg, cudaStream_t st) {
+  unsigned long long* counter = nullptr;
+  RMG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&counter), sizeof(unsigned long long), st));
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+  const unsigned block = 32u * cfg.block_warps;
+  if (e == cudaSuccess) {
+    switch (sensor->model.kind) {
+      case RMG_MODEL_SPHERICAL:
+      case RMG_MODEL_PINHOLE:
+        e = launch_trace_refill_pose(P, (int)cfg.stack_depth, block, counter, cfg.chunk, cfg.refill, st);
+        break;
+      case RMG_MODEL_O1DN:
+        e = launch_trace_refill_single(P, (int)cfg.stack_depth, block, counter, cfg.chunk, cfg.refill, st);
+        break;
+      default: e = launch_trace_refill_table(P, (int)cfg.stack_depth, block, counter, cfg.chunk, cfg.refill, st); break;
+    }
+  }
+  const int s = cuda_status(e, "trace refill launch");
+  cudaFreeAsync(counter, st);
+  return s;
+}
+
 int launch_plain(const TraceParams& P, const rmg_sensor* sensor, const rmg_launch_config& cfg,
                  cudaStream_t st) {
+  if (cfg.refill) return launch_refill(P, sensor, cfg, st);
   const uint64_t blocks = (P.n_tiles + cfg.block_warps - 1) / cfg.block_warps;
   if (blocks > 0x7fffffffull) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate: too many rays for one launch");
   const unsigned block = 32u * cfg.block_warps;

@@ -134,25 +134,60 @@ template <> struct Trail<128> {
 
 inline int trail_bits_for_depth(unsigned depth) { return depth <= 32 ? 32 : (depth <= 64 ? 64 : 128); }
 
+// One ray's traversal state.  step() performs one node visit and, when the
+// visit does not descend, the backtrack to the next pending node; it returns
+// true once the ray is finished (or out of budget, which sets `over`).  The
+// classic kernel loops step() to completion; the refill kernel interleaves the
+// steps of rays that start at different times.  Both run this same code, so
+// their results are identical.
+// The circular short stack lives in its own object (dynamically indexed arrays
+// go to local memory; keeping them apart lets the scalar state stay in registers).
+template <int SS>
+struct ShortStack {
+  int node[SS > 0 ? SS : 1];
+  float t[SS > 0 ? SS : 1];
+};
+
 template <int SS, int TB>
-__device__ __forceinline__ void trace_ray(const DeviceMap& map, const V& o, const V& d, float tfar,
-                                          unsigned budget, Hit& h, bool& over_budget) {
-  h.t = tfar;
-  h.tri = -1;
-  h.face = 0xffffffffu;
-  if (map.root < 0) return;
-  const RayW rw = make_rayw(o, d);
-  const RayBox rb = make_raybox(o, d);
-
-  int node = map.root;
+struct RayTrav {
+  RayW rw;
+  RayBox rb;
+  Hit h;
+  float tfar;
+  int node;
   Trail<TB> trail;
-  int stk[SS > 0 ? SS : 1];
-  float stkt[SS > 0 ? SS : 1];
-  int sp = 0, top = 0;
-  unsigned steps = 0;
+  int sp, top;
+  unsigned steps;
+  bool over;
 
-  for (;;) {
-    if (++steps > budget) { over_budget = true; h.tri = -1; h.t = tfar; h.face = 0xffffffffu; return; }
+  // Returns false when there is nothing to traverse (empty map).
+  __device__ __forceinline__ bool init(const DeviceMap& map, const V& o, const V& d, float tfar_) {
+    tfar = tfar_;
+    h.t = tfar_;
+    h.tri = -1;
+    h.face = 0xffffffffu;
+    over = false;
+    steps = 0;
+    sp = 0;
+    top = 0;
+    trail = Trail<TB>();
+    node = map.root;
+    if (map.root < 0) return false;
+    rw = make_rayw(o, d);
+    rb = make_raybox(o, d);
+    return true;
+  }
+
+  __device__ __forceinline__ bool fail_budget() {
+    over = true;
+    h.tri = -1;
+    h.t = tfar;
+    h.face = 0xffffffffu;
+    return true;
+  }
+
+  __device__ __forceinline__ bool step(const DeviceMap& map, unsigned budget, ShortStack<SS>& stack) {
+    if (++steps > budget) return fail_budget();
     const Node* np = map.nodes + node;
     const float4 a = __ldg(&np->a);
     const float4 b = __ldg(&np->b);
@@ -169,44 +204,40 @@ __device__ __forceinline__ void trace_ray(const DeviceMap& map, const V& o, cons
     hitR = hitR && tminR <= h.t * kWiden;
     if (hitL && hitR) {
       const bool lf = tminL <= tminR;
-      const int nearc = lf ? ln.x : ln.y;
       if (SS > 0) {
         top = (top + 1) & (SS - 1);
-        stk[top] = lf ? ln.y : ln.x;
-        stkt[top] = lf ? tminR : tminL;
+        stack.node[top] = lf ? ln.y : ln.x;
+        stack.t[top] = lf ? tminR : tminL;
         sp = sp < SS ? sp + 1 : SS;
       }
       trail.push(1u);
-      node = nearc;
-      continue;
+      node = lf ? ln.x : ln.y;
+      return false;
     }
     if (hitL || hitR) {
       trail.push(0u);
       node = hitL ? ln.x : ln.y;
-      continue;
+      return false;
     }
     // ---- backtrack to the nearest pending level ----
-    bool found = false;
     while (!trail.empty()) {
       const int k = trail.ctz();
       trail.shr(k);
       trail.clear_low();
       if (SS > 0 && sp > 0) {
-        const int cand = stk[top];
-        const float ct = stkt[top];
+        const int cand = stack.node[top];
+        const float ct = stack.t[top];
         top = (top - 1) & (SS > 0 ? SS - 1 : 0);
         --sp;
         node = cand;
-        if (ct <= h.t * kWiden) { found = true; break; }
+        if (ct <= h.t * kWiden) return false;
       } else {
         // The trail never holds more levels than the path below the root, so
         // a climb that reaches the root's parent (-1) means a corrupt tree.
         for (int j = 0; j < k && node >= 0; ++j) node = __ldg(&map.nodes[node].d.z);
         steps += (unsigned)k;
         const int p = node >= 0 ? __ldg(&map.nodes[node].d.z) : -1;
-        if (steps > budget || p < 0) {
-          over_budget = true; h.tri = -1; h.t = tfar; h.face = 0xffffffffu; return;
-        }
+        if (steps > budget || p < 0) return fail_budget();
         const Node* pp = map.nodes + p;
         const int4 pl = __ldg(&pp->d);
         float tmin, tmax;
@@ -223,11 +254,24 @@ __device__ __forceinline__ void trace_ray(const DeviceMap& map, const V& o, cons
           slab(rb, aa.x, aa.y, aa.z, aa.w, cc.x, cc.y, tmin, tmax);
         }
         node = sib;
-        if (visit(tmin, tmax, h.t)) { found = true; break; }
+        if (visit(tmin, tmax, h.t)) return false;
       }
     }
-    if (!found) return;
+    return true;
   }
+};
+
+template <int SS, int TB>
+__device__ __forceinline__ void trace_ray(const DeviceMap& map, const V& o, const V& d, float tfar,
+                                          unsigned budget, Hit& h, bool& over_budget) {
+  RayTrav<SS, TB> r;
+  ShortStack<SS> stack;
+  if (r.init(map, o, d, tfar)) {
+    while (!r.step(map, budget, stack)) {
+    }
+  }
+  h = r.h;
+  if (r.over) over_budget = true;
 }
 
 struct TraceParams {
@@ -341,6 +385,102 @@ __global__ void __launch_bounds__(256) k_trace(const TraceParams P) {
   trace_ray<SS, TB>(P.map, o, d, P.sen.range_max, P.budget, h, over);
   if (over) atomicExch(P.map.status, (unsigned)RMG_ERR_TRAVERSAL_BUDGET);
   write_attributes<OK>(P, gid, h, dir_s, orig_s, Tsm);
+}
+
+}  // namespace rmg
+
+namespace rmg {
+
+// Persistent variant with lane refill ("dynamic ray fetch").  Rays are numbered
+// tile-major (ray = tile * 32 + slot, the slot inside the tile_h x tile_w tile),
+// so consecutive numbers are neighbouring rays of one pose.  A warp takes
+// `chunk` tiles at a time from a global counter; whenever fewer than `refill`
+// of its lanes still hold an unfinished ray, the idle lanes take the next ray
+// numbers, ranked with __ballot_sync / __popc so each gets a distinct one.
+// Every lane then performs one traversal step.  A finished lane writes its
+// outputs and becomes idle.  Per ray the work is exactly that of k_trace.
+template <int OK>
+__device__ __forceinline__ bool ray_coords(const TraceParams& P, uint64_t ray, uint32_t& pose, uint32_t& loc,
+                                           uint64_t& gid) {
+  const uint64_t tile = ray >> 5;
+  const uint32_t slot = (uint32_t)(ray & 31u);
+  pose = (uint32_t)(tile / P.tiles_per_pose);
+  const uint32_t r = (uint32_t)(tile - (uint64_t)pose * P.tiles_per_pose);
+  const uint32_t ty = r / P.tiles_x, tx = r - ty * P.tiles_x;
+  const uint32_t tile_w = 1u << P.tile_w_log2;
+  const uint32_t vid = ty * P.tile_h + (slot >> P.tile_w_log2);
+  const uint32_t hid = tx * tile_w + (slot & (tile_w - 1));
+  const uint32_t W = P.sen.width, H = P.sen.height;
+  if (vid >= H || hid >= W) return false;
+  loc = vid * W + hid;
+  gid = (uint64_t)pose * W * H + loc;
+  return true;
+}
+
+template <int OK, int SS, int TB>
+__global__ void __launch_bounds__(256) k_trace_refill(const TraceParams P, unsigned long long* counter,
+                                                      uint32_t chunk, uint32_t refill) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t lt = (1u << lane) - 1u;
+  refill = refill ? refill : 1u;  // at least one idle lane triggers a fetch: the loop always progresses
+  chunk = chunk ? chunk : 1u;
+  uint64_t next = 0, end = 0;
+  bool exhausted = false, active = false;
+  uint64_t my_ray = 0;
+  RayTrav<SS, TB> R;
+  ShortStack<SS> stack;
+  for (;;) {
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!exhausted && (uint32_t)__popc(act) < refill) {
+      unsigned idle = ~act;
+      while (idle) {
+        if (next >= end) {
+          unsigned long long base = 0;
+          if (lane == 0) base = atomicAdd(counter, (unsigned long long)chunk);
+          base = __shfl_sync(0xffffffffu, base, 0);
+          if (base >= P.n_tiles) { exhausted = true; break; }
+          next = base * 32ull;
+          end = min((uint64_t)base + chunk, P.n_tiles) * 32ull;
+        }
+        const uint32_t n_idle = (uint32_t)__popc(idle);
+        const uint32_t take = (uint32_t)min((uint64_t)n_idle, end - next);
+        const uint32_t rank = (uint32_t)__popc(idle & lt);
+        const bool mine = ((idle >> lane) & 1u) && rank < take;
+        if (mine) {
+          my_ray = next + rank;
+          uint32_t pose, loc;
+          uint64_t gid;
+          if (ray_coords<OK>(P, my_ray, pose, loc, gid)) {
+            const Tf Tsm = tmul(load_tf(P.Tbm[pose]), P.Tsb);
+            V dir_s, orig_s, o, d;
+            setup_ray<OK>(P.sen, Tsm, loc, dir_s, orig_s, o, d);
+            active = true;
+            if (!R.init(P.map, o, d, P.sen.range_max)) {  // empty map: finished at once
+              write_attributes<OK>(P, gid, R.h, dir_s, orig_s, Tsm);
+              active = false;
+            }
+          }
+        }
+        idle &= ~__ballot_sync(0xffffffffu, mine);
+        next += take;
+      }
+    }
+    if (__ballot_sync(0xffffffffu, active) == 0) {
+      if (exhausted) break;
+      continue;
+    }
+    if (active && R.step(P.map, P.budget, stack)) {
+      if (R.over) atomicExch(P.map.status, (unsigned)RMG_ERR_TRAVERSAL_BUDGET);
+      uint32_t pose, loc;
+      uint64_t gid;
+      ray_coords<OK>(P, my_ray, pose, loc, gid);
+      const Tf Tsm = tmul(load_tf(P.Tbm[pose]), P.Tsb);
+      V dir_s, orig_s, o, d;
+      setup_ray<OK>(P.sen, Tsm, loc, dir_s, orig_s, o, d);
+      write_attributes<OK>(P, gid, R.h, dir_s, orig_s, Tsm);
+      active = false;
+    }
+  }
 }
 
 }  // namespace rmg

@@ -1,6 +1,9 @@
-// Instantiates the traversal kernel for ORIGIN_POSE rays (see trace.cuh).
-#include "trace.cuh"
+// Instantiates the traversal kernels for ORIGIN_POSE rays (see trace.cuh).
+#include <algorithm>
+
+#include "internal.h"
 #include "launch.h"
+#include "trace.cuh"
 
 namespace rmg {
 
@@ -14,6 +17,28 @@ cudaError_t by_trail(const TraceParams& P, unsigned grid, unsigned block, cudaSt
   }
   return cudaGetLastError();
 }
+
+template <int SS, int TB>
+cudaError_t refill_one(const TraceParams& P, unsigned block, unsigned long long* counter, uint32_t chunk,
+                       uint32_t refill, cudaStream_t st) {
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_refill<ORIGIN_POSE, SS, TB>,
+                                                                (int)block, 0);
+  if (e != cudaSuccess) return e;
+  const unsigned grid = (unsigned)(std::max(per_sm, 1) * device_sm_count());
+  k_trace_refill<ORIGIN_POSE, SS, TB><<<grid, block, 0, st>>>(P, counter, chunk, refill);
+  return cudaGetLastError();
+}
+
+template <int SS>
+cudaError_t refill_by_trail(const TraceParams& P, unsigned block, unsigned long long* counter, uint32_t chunk,
+                            uint32_t refill, cudaStream_t st) {
+  switch (P.trail_bits) {
+    case 32: return refill_one<SS, 32>(P, block, counter, chunk, refill, st);
+    case 64: return refill_one<SS, 64>(P, block, counter, chunk, refill, st);
+    default: return refill_one<SS, 128>(P, block, counter, chunk, refill, st);
+  }
+}
 }  // namespace
 
 cudaError_t launch_trace_pose(const TraceParams& P, int stack_depth, unsigned grid, unsigned block,
@@ -22,6 +47,16 @@ cudaError_t launch_trace_pose(const TraceParams& P, int stack_depth, unsigned gr
     case 0: return by_trail<0>(P, grid, block, st);
     case 8: return by_trail<8>(P, grid, block, st);
     case 16: return by_trail<16>(P, grid, block, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_trace_refill_pose(const TraceParams& P, int stack_depth, unsigned block,
+                                      unsigned long long* counter, uint32_t chunk, uint32_t refill,
+                                      cudaStream_t st) {
+  switch (stack_depth) {
+    case 8: return refill_by_trail<8>(P, block, counter, chunk, refill, st);
+    case 16: return refill_by_trail<16>(P, block, counter, chunk, refill, st);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -171,7 +171,8 @@ def test_stack_depths_and_tiles_bitwise_identical():
     m = rm.Map(sc.vertices, sc.faces)
     model = sensors.ouster_like(64, 512)
     base = gpu_sim(m, model, poses, cfg=rm.launch_config(8, 4, 8, 4))
-    for cfg in [(0, 4, 8, 4), (16, 2, 8, 4), (16, 8, 32, 1), (8, 1, 4, 8), (8, 4, 16, 2), (0, 8, 2, 16)]:
+    for cfg in [(0, 4, 8, 4), (16, 2, 8, 4), (16, 8, 32, 1), (8, 1, 4, 8), (8, 4, 16, 2), (0, 8, 2, 16),
+                (8, 4, 8, 4, 16, 4), (16, 2, 8, 4, 32, 1), (8, 8, 16, 2, 1, 7), (16, 4, 4, 8, 24, 64)]:
         other = gpu_sim(m, model, poses, cfg=rm.launch_config(*cfg))
         for a in ALL:
             assert np.array_equal(base[a].view(np.uint8), other[a].view(np.uint8)), (cfg, a)
@@ -195,11 +196,31 @@ def test_single_triangle_map():
 
 
 def test_ragged_tiles_and_single_pose():
-    """Sensor sizes that are not multiples of the tile (W=37, H=5) and one pose."""
+    """Sensor sizes that are not multiples of the tile (W=37, H=5) and one pose, in both the
+    one-tile-per-warp and the lane-refill launch modes."""
     sc = scenes.box_room(seed=2, n_boxes=30)
     m = sensors.SphericalModel(phi=sensors.DiscreteInterval(-0.2, 0.1, 5),
                                theta=sensors.DiscreteInterval(-3.0, 0.16, 37), range=sensors.Interval(0.1, 50.0))
-    check_parity(sc.vertices, sc.faces, m, scenes.room_poses(1, seed=3))
+    got, _, _ = check_parity(sc.vertices, sc.faces, m, scenes.room_poses(1, seed=3))
+    mp = rm.Map(sc.vertices, sc.faces)
+    for cfg in [(8, 4, 8, 4, 32, 1), (16, 2, 8, 4, 8, 3)]:
+        other = gpu_sim(mp, m, scenes.room_poses(1, seed=3), cfg=rm.launch_config(*cfg))
+        for a in ALL:
+            assert np.array_equal(got[a].view(np.uint8), other[a].view(np.uint8)), (cfg, a)
+
+
+def test_refill_mode_on_empty_map_and_corrupt_tree():
+    model = sensors.vlp16_900()
+    empty = rm.Map(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))
+    res = gpu_sim(empty, model, scenes.room_poses(2), cfg=rm.launch_config(8, 4, 8, 4, 16, 2))
+    assert np.all(res["hits"] == 0) and np.all(res["face_ids"] == 0xFFFFFFFF)
+    sc = scenes.box_room(seed=8, n_boxes=20)
+    m = rm.Map(sc.vertices, sc.faces)
+    g = m.export()
+    internal = int(g["links"][0][0]) if g["links"][0][0] >= 0 else int(g["links"][0][1])
+    _lib.call("rmg_map_debug_set_child", m.handle, internal, 0, 0)
+    gpu_sim(m, model, scenes.room_poses(2, seed=9), attrs=("ranges",), cfg=rm.launch_config(16, 4, 8, 4, 32, 4))
+    assert m.status(clear=True) == _lib.RMG_ERR_TRAVERSAL_BUDGET
 
 
 def test_zero_poses_and_no_outputs_are_noops():
