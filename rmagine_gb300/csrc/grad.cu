@@ -133,7 +133,6 @@ cudaError_t launch_grad_tb(const GradParams& G, dim3 grid, unsigned block, cudaS
 template <int OK>
 cudaError_t launch_grad(const GradParams& G, int ss, dim3 grid, unsigned block, cudaStream_t st) {
   switch (ss) {
-    case 0: return launch_grad_tb<OK, 0>(G, grid, block, st);
     case 8: return launch_grad_tb<OK, 8>(G, grid, block, st);
     case 16: return launch_grad_tb<OK, 16>(G, grid, block, st);
     default: return cudaErrorInvalidValue;
@@ -164,7 +163,6 @@ extern "C" int rmg_range_pose_grad(const rmg_map* map, const rmg_sensor* sensor,
   if (n_poses > 65535u) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad: at most 65535 poses per call");
   rmg_launch_config cfg;
   default_config(sensor, &cfg);
-  cfg.block_warps = 8;
   rmg_outputs out{};
   out.ranges = ranges_sim;
   out.face_ids = face_ids;

@@ -7,8 +7,10 @@
 
 namespace rmg {
 
+// Defaults from a sweep on the 1M-triangle terrain (spherical 128x1024): short
+// stack 16, 4 warps per CTA, 8 x 4 ray tiles, one tile per warp.
 int default_config(const rmg_sensor* s, rmg_launch_config* cfg) {
-  cfg->stack_depth = 8;
+  cfg->stack_depth = 16;
   cfg->block_warps = 4;
   cfg->refill = 0;
   cfg->chunk = 4;

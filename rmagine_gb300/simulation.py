@@ -219,7 +219,7 @@ def outputs_c(bundle: Bundle) -> L.OutputsC:
     return o
 
 
-def launch_config(stack_depth=8, block_warps=4, tile_w=8, tile_h=4, refill=0, chunk=4) -> L.LaunchConfigC:
+def launch_config(stack_depth=16, block_warps=4, tile_w=8, tile_h=4, refill=0, chunk=4) -> L.LaunchConfigC:
     return L.LaunchConfigC(stack_depth, block_warps, tile_w, tile_h, refill, chunk)
 
 
