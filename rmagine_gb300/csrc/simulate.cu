@@ -59,6 +59,7 @@ int make_trace_params(const rmg_map* map, const rmg_sensor* sensor, const rmg_tr
   P.n_tiles = (uint64_t)P.tiles_per_pose * n_poses;
   P.budget = 2u * map->n_nodes + 64u;
   P.trail_bits = trail_bits_for_depth(map->depth);
+  P.full_stack = map->depth <= (unsigned)kFullStack ? 1 : 0;
   return RMG_OK;
 }
 

@@ -10,8 +10,9 @@
 // dataset/model arrays (float3, 12 B each).  One or more CTAs reduce a batch.
 // Each thread accumulates, around a per-batch shift (the batch's first
 // pre-transformed dataset point and first model point), binary32 sums of
-// d', m' and m' d'^T over runs of at most 32 correspondences, then folds them
-// into binary64 accumulators; warps and the CTA combine in binary64, and
+// d', m' and m' d'^T over runs of at most 32 correspondences; the warp sums its
+// 32 runs pairwise in binary32 and folds the result into binary64 accumulators
+// (one lane, one fold per 1024 correspondences); the CTA combines in binary64, and
 // batches split over several CTAs are combined in a fixed order by the last
 // CTA to finish, so results are deterministic.  The mean and covariance are
 // formed in binary64 (cov = E[m' d'^T] - E[m'] E[d']^T), then rounded to the
@@ -107,13 +108,24 @@ struct FAcc {
   }
 };
 
-// Binary64 per-thread accumulators live in shared memory, [16][threads], so the
-// registers hold only the binary32 run (keeps 3-4 CTAs resident per SM).
-__device__ __forceinline__ void fold(double (*acc)[kStatsThreads], FAcc& f) {
-  const int t = threadIdx.x;
-  acc[0][t] += f.n;
-  for (int k = 0; k < 3; ++k) { acc[1 + k][t] += f.d[k]; acc[4 + k][t] += f.m[k]; }
-  for (int k = 0; k < 9; ++k) acc[7 + k][t] += f.md[k];
+// Folding a binary32 run into binary64: the 32 lanes' runs are first summed
+// pairwise across the warp in binary32 (a 5-level butterfly), then ONE lane
+// adds the 16 warp sums to the warp's binary64 accumulators in shared memory.
+// The GB300's binary64 pipe is narrow; this keeps it at 16 operations per 1024
+// correspondences instead of 16 per 32.  All lanes must call fold together.
+__device__ __forceinline__ void fold(double (*acc)[kStatsThreads / 32], FAcc& f) {
+  float v[16] = {f.n, f.d[0], f.d[1], f.d[2], f.m[0], f.m[1], f.m[2], f.md[0], f.md[1], f.md[2],
+                 f.md[3], f.md[4], f.md[5], f.md[6], f.md[7], f.md[8]};
+#pragma unroll
+  for (int k = 0; k < 16; ++k)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane < 16) {
+    float x = v[0];
+#pragma unroll
+    for (int k = 1; k < 16; ++k) x = lane == k ? v[k] : x;
+    acc[lane][warp] += (double)x;
+  }
   f.zero();
 }
 
@@ -162,8 +174,9 @@ __global__ void __launch_bounds__(kStatsThreads, 3) k_stats(const StatsParams P)
   const V sd = P.n_per ? tf_point(pre, ldv(P.dp, base)) : V{0, 0, 0};
   const V sm = P.n_per ? ldv(P.mp, base) : V{0, 0, 0};
 
-  __shared__ double acc[16][kStatsThreads];
-  for (int k = 0; k < 16; ++k) acc[k][threadIdx.x] = 0.0;
+  __shared__ double acc[16][kStatsThreads / 32];
+  if (threadIdx.x < 16 * (kStatsThreads / 32)) acc[threadIdx.x / (kStatsThreads / 32)][threadIdx.x % (kStatsThreads / 32)] = 0.0;
+  __syncthreads();
   FAcc f;
   f.zero();
   const V zero{0.f, 0.f, 0.f};
@@ -171,7 +184,11 @@ __global__ void __launch_bounds__(kStatsThreads, 3) k_stats(const StatsParams P)
     // thread t takes groups of 4 consecutive correspondences: 3 x 16-byte loads per array
     const uint32_t g0 = lo / 4, g1 = (hi + 3) / 4;
     int run = 0;
-    for (uint32_t g = g0 + threadIdx.x; g < g1; g += blockDim.x) {
+    // warp-uniform trip count (lanes past the end skip the loads)
+    const uint32_t iters = (g1 - g0 + blockDim.x - 1) / blockDim.x;
+    for (uint32_t it = 0; it < iters; ++it) {
+      const uint32_t g = g0 + threadIdx.x + it * blockDim.x;
+      if (g < g1) {
       const uint64_t e = base + 4ull * g;
       const float4* dv = reinterpret_cast<const float4*>(P.dp + 3 * e);
       const float4* mv = reinterpret_cast<const float4*>(P.mp + 3 * e);
@@ -198,32 +215,30 @@ __global__ void __launch_bounds__(kStatsThreads, 3) k_stats(const StatsParams P)
                                 V{mmv[3 * k], mmv[3 * k + 1], mmv[3 * k + 2]}, np, D, M))
           f.add_pt(D, M, sd, sm);
       }
+      }
       if (++run == kFold) { fold(acc, f); run = 0; }
     }
   } else {
     int run = 0;
-    for (uint32_t j = lo + threadIdx.x; j < hi; j += blockDim.x) {
-      V D, M;
-      const V np = P2L ? ldv(P.mn, base + j) : zero;
-      if (correspondence<P2L, PRE>(P, pre, base + j, ldv(P.dp, base + j), ldv(P.mp, base + j), np, D, M))
-        f.add_pt(D, M, sd, sm);
+    const uint32_t iters = (hi - lo + blockDim.x - 1) / blockDim.x;
+    for (uint32_t it = 0; it < iters; ++it) {
+      const uint32_t j = lo + threadIdx.x + it * blockDim.x;
+      if (j < hi) {
+        V D, M;
+        const V np = P2L ? ldv(P.mn, base + j) : zero;
+        if (correspondence<P2L, PRE>(P, pre, base + j, ldv(P.dp, base + j), ldv(P.mp, base + j), np, D, M))
+          f.add_pt(D, M, sd, sm);
+      }
       if (++run == 4 * kFold) { fold(acc, f); run = 0; }
     }
   }
   fold(acc, f);
 
-  // CTA reduction in binary64
-  __shared__ double red[kStatsThreads / 32][16];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int k = 0; k < 16; ++k) {
-    double v = acc[k][threadIdx.x];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) red[warp][k] = v;
-  }
+  // CTA reduction in binary64: warp accumulators in a fixed order
   __syncthreads();
   if (threadIdx.x >= 16) return;
   double v = 0.0;
-  for (int w = 0; w < kStatsThreads / 32; ++w) v += red[w][threadIdx.x];
+  for (int w = 0; w < kStatsThreads / 32; ++w) v += acc[threadIdx.x][w];
   __shared__ double tot[16];
   __shared__ bool last;
   tot[threadIdx.x] = v;

@@ -115,6 +115,12 @@ template <> struct Trail<64> {
   __device__ __forceinline__ void clear_low() { v ^= 1ull; }
 };
 
+// TB == 0: no trail at all; the traversal keeps every pending far child on a
+// full stack (used when the tree's internal depth is below the stack size).
+template <> struct Trail<0> {
+  __device__ __forceinline__ void push(uint32_t) {}
+};
+
 template <> struct Trail<128> {
   uint64_t lo = 0, hi = 0;
   __device__ __forceinline__ void push(uint32_t bit) {
@@ -204,7 +210,12 @@ struct RayTrav {
     hitR = hitR && tminR <= h.t * kWiden;
     if (hitL && hitR) {
       const bool lf = tminL <= tminR;
-      if (SS > 0) {
+      if constexpr (TB == 0) {
+        if (sp >= SS) return fail_budget();  // only a corrupt tree gets this deep
+        stack.node[sp] = lf ? ln.y : ln.x;
+        stack.t[sp] = lf ? tminR : tminL;
+        ++sp;
+      } else if (SS > 0) {
         top = (top + 1) & (SS - 1);
         stack.node[top] = lf ? ln.y : ln.x;
         stack.t[top] = lf ? tminR : tminL;
@@ -219,7 +230,17 @@ struct RayTrav {
       node = hitL ? ln.x : ln.y;
       return false;
     }
+    if constexpr (TB == 0) {
+      // ---- full stack: pop the nearest pending child that survives the cull ----
+      while (sp > 0) {
+        --sp;
+        node = stack.node[sp];
+        if (stack.t[sp] <= h.t * kWiden) return false;
+      }
+      return true;
+    }
     // ---- backtrack to the nearest pending level ----
+    if constexpr (TB != 0) {
     while (!trail.empty()) {
       const int k = trail.ctz();
       trail.shr(k);
@@ -257,6 +278,7 @@ struct RayTrav {
         if (visit(tmin, tmax, h.t)) return false;
       }
     }
+    }
     return true;
   }
 };
@@ -288,7 +310,10 @@ struct TraceParams {
   uint64_t n_tiles;
   unsigned budget;
   int trail_bits;
+  int full_stack;  // internal depth < kFullStack: the traversal may keep every pending child on a stack
 };
+
+constexpr int kFullStack = 32;
 
 // Writes all requested attributes of one ray (SphereSimulatorEmbree.tcc:104-249).
 template <int OK>

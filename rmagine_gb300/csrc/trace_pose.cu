@@ -10,6 +10,10 @@ namespace rmg {
 namespace {
 template <int SS>
 cudaError_t by_trail(const TraceParams& P, unsigned grid, unsigned block, cudaStream_t st) {
+  if (SS > 0 && P.full_stack) {  // same visits and results, without trail bookkeeping
+    k_trace<ORIGIN_POSE, kFullStack, 0><<<grid, block, 0, st>>>(P);
+    return cudaGetLastError();
+  }
   switch (P.trail_bits) {
     case 32: k_trace<ORIGIN_POSE, SS, 32><<<grid, block, 0, st>>>(P); break;
     case 64: k_trace<ORIGIN_POSE, SS, 64><<<grid, block, 0, st>>>(P); break;
