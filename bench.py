@@ -41,7 +41,12 @@ OUT_BYTES = {"hits": 1, "ranges": 4, "points": 12, "normals": 12, "face_ids": 4,
 # on a fixed 0.1% ray sample (rng seed 0) of each workload; tests/test_work_constants.py
 # re-derives them on smaller samples.
 WORK_PER_RAY = {
-    "terrain1m_spherical": {"nodes": 39.942, "tris": 1.886},
+    "terrain1m_spherical": {"nodes": 30.521, "tris": 1.800},
+    "terrain1m_pinhole": {"nodes": 27.285, "tris": 1.657},
+    "terrain2m_spherical": {"nodes": 30.580, "tris": 1.764},
+    "room_vlp16": {"nodes": 65.651, "tris": 3.919},
+    "pose_grad": {"nodes": 30.260, "tris": 1.763},
+},
     "terrain1m_pinhole": {"nodes": 36.787, "tris": 1.711},
     "terrain2m_spherical": {"nodes": 40.516, "tris": 1.860},
     "room_vlp16": {"nodes": 68.997, "tris": 4.149},

@@ -337,11 +337,10 @@ void lbvh_build(const Mesh& m, Lbvh& L) {
     const float q[3] = {cen[i].x, cen[i].y, cen[i].z};
     for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], q[k]); hi[k] = std::max(hi[k], q[k]); }
   }
-  float scale[3];
-  for (int k = 0; k < 3; ++k) {
-    const float ext = hi[k] - lo[k];
-    scale[k] = ext > 0.0f ? 2097152.0f / ext : 0.0f;
-  }
+  // one scale for all axes: the centroids' bounding cube
+  const float ext = std::max(std::max(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+  const float s1 = ext > 0.0f ? 2097152.0f / ext : 0.0f;
+  const float scale[3] = {s1, s1, s1};
   std::vector<uint64_t> key(n);
   for (int i = 0; i < n; ++i) {
     const float q[3] = {cen[i].x, cen[i].y, cen[i].z};
