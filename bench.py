@@ -46,11 +46,6 @@ WORK_PER_RAY = {
     "terrain2m_spherical": {"nodes": 30.580, "tris": 1.764},
     "room_vlp16": {"nodes": 65.651, "tris": 3.919},
     "pose_grad": {"nodes": 30.260, "tris": 1.763},
-},
-    "terrain1m_pinhole": {"nodes": 36.787, "tris": 1.711},
-    "terrain2m_spherical": {"nodes": 40.516, "tris": 1.860},
-    "room_vlp16": {"nodes": 68.997, "tris": 4.149},
-    "pose_grad": {"nodes": 40.046, "tris": 1.855},
 }
 
 # Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel,
