@@ -46,6 +46,7 @@ struct BatchParams {
   uint32_t grab;
   unsigned budget;
   int trail_bits;
+  int full_stack;
 };
 
 template <int OK, int SS, int TB>
@@ -114,6 +115,10 @@ __global__ void __launch_bounds__(256) k_trace_batched(const BatchParams B) {
 
 template <int SS>
 cudaError_t launch_batched_tb(const BatchParams& B, unsigned grid, unsigned block, cudaStream_t st) {
+  if (SS > 0 && B.full_stack) {
+    k_trace_batched<kFullStack, 0><<<grid, block, 0, st>>>(B);
+    return cudaGetLastError();
+  }
   switch (B.trail_bits) {
     case 32: k_trace_batched<SS, 32><<<grid, block, 0, st>>>(B); break;
     case 64: k_trace_batched<SS, 64><<<grid, block, 0, st>>>(B); break;
@@ -133,6 +138,7 @@ cudaError_t launch_batched(const BatchParams& B, int ss, unsigned grid, unsigned
 
 template <int SS>
 const void* batched_fn(int tb) {
+  if (tb == 0) return reinterpret_cast<const void*>(k_trace_batched<kFullStack, 0>);
   return tb == 32 ? reinterpret_cast<const void*>(k_trace_batched<SS, 32>)
                   : tb == 64 ? reinterpret_cast<const void*>(k_trace_batched<SS, 64>)
                              : reinterpret_cast<const void*>(k_trace_batched<SS, 128>);
@@ -241,6 +247,7 @@ BatchParams params(const rmg_batch* b) {
   B.grab = b->cfg.grab;
   B.budget = 2u * b->map->n_nodes + 64u;
   B.trail_bits = trail_bits_for_depth(b->map->depth);
+  B.full_stack = b->map->depth <= (unsigned)kFullStack ? 1 : 0;
   return B;
 }
 
@@ -248,7 +255,8 @@ BatchParams params(const rmg_batch* b) {
 int launch_direct(rmg_batch* b, cudaStream_t st) {
   if (b->total_tiles == 0) return RMG_OK;
   unsigned grid = 0;
-  int s = persistent_grid(b->cfg, trail_bits_for_depth(b->map->depth), grid);
+  const bool full = b->cfg.stack_depth > 0 && b->map->depth <= (unsigned)kFullStack;
+  int s = persistent_grid(b->cfg, full ? 0 : trail_bits_for_depth(b->map->depth), grid);
   if (s != RMG_OK) return s;
   RMG_CUDA_TRY(cudaMemsetAsync(b->counter, 0, sizeof(unsigned long long), st));
   return cuda_status(launch_batched(params(b), (int)b->cfg.stack_depth, grid, 32u * b->cfg.block_warps, st),

@@ -122,6 +122,10 @@ __global__ void k_grad_final(const float* partial, uint32_t n_poses, uint32_t ct
 
 template <int OK, int SS>
 cudaError_t launch_grad_tb(const GradParams& G, dim3 grid, unsigned block, cudaStream_t st) {
+  if (G.T.full_stack) {
+    k_range_grad<OK, kFullStack, 0><<<grid, block, 0, st>>>(G);
+    return cudaGetLastError();
+  }
   switch (G.T.trail_bits) {
     case 32: k_range_grad<OK, SS, 32><<<grid, block, 0, st>>>(G); break;
     case 64: k_range_grad<OK, SS, 64><<<grid, block, 0, st>>>(G); break;
