@@ -234,6 +234,7 @@ class _Simulator:
         self._Tsb = transform_c([0, 0, 0, 1, 0, 0, 0])
         self.launch_config: L.LaunchConfigC | None = None
         self._staging: dict = {}
+        self._copy_stream = None
 
     # SimulatorEmbree::setMap
     def setMap(self, map: Map) -> None:
@@ -307,6 +308,9 @@ class _Simulator:
         L.check(st, "rmg_simulate")
 
     def _simulate_host(self, Tbm: torch.Tensor, bundle: Bundle, n: int) -> Bundle:
+        """Host bundle: the poses are split into chunks; chunk k is simulated into device
+        staging memory on the current stream while chunk k-1 is copied back to the host on a
+        second stream, so the device->host copy overlaps the ray casting.  Synchronises."""
         dev = Bundle(*bundle.attrs)
         for a, t in bundle.tensors().items():
             key = (a, tuple(t.shape), t.dtype)
@@ -315,11 +319,30 @@ class _Simulator:
                 buf = torch.empty(t.shape, dtype=t.dtype, device="cuda")
                 self._staging[key] = buf
             setattr(dev, a, buf)
+        if self._copy_stream is None:
+            self._copy_stream = torch.cuda.Stream()
+        compute = torch.cuda.current_stream()
+        copy = self._copy_stream
         Tbm_d = Tbm.to("cuda", non_blocking=True).contiguous()
-        self._launch(Tbm_d, n, dev, _stream_ptr())
-        for a, t in bundle.tensors().items():
-            t.copy_(getattr(dev, a), non_blocking=True)
-        torch.cuda.current_stream().synchronize()
+        per_pose = self.sensor.width * self.sensor.height
+        out_bytes = sum(t.element_size() * t[0:1].numel() for t in bundle.tensors().values()) * per_pose
+        # chunks of ~256 MB of outputs, at least 4 when there are enough poses
+        chunk = max(1, min(n // 4 if n >= 4 else n, (256 << 20) // max(1, out_bytes)))
+        copy.wait_stream(compute)
+        for c0 in range(0, n, chunk):
+            c1 = min(n, c0 + chunk)
+            view = Bundle(*bundle.attrs)
+            for a in bundle.attrs:
+                setattr(view, a, getattr(dev, a)[c0 * per_pose:c1 * per_pose])
+            self._launch(Tbm_d[c0:c1], c1 - c0, view, _stream_ptr())
+            done = torch.cuda.Event()
+            done.record(compute)
+            copy.wait_event(done)
+            with torch.cuda.stream(copy):
+                for a, t in bundle.tensors().items():
+                    t[c0 * per_pose:c1 * per_pose].copy_(getattr(view, a), non_blocking=True)
+        compute.wait_stream(copy)
+        compute.synchronize()
         return bundle
 
 
