@@ -1,0 +1,425 @@
+// rmagine_gb300.hpp -- header-only C++ layer over the C ABI (rmg.h), with
+// rmagine's types and simulator interface, so that C++ code written against
+// rmagine's simulators (SphereSimulatorEmbree / SphereSimulatorOptix and
+// siblings) switches by changing the simulator type.
+//
+// Mirrors (uos/rmagine v2.4.2):
+//   Memory<T, RAM | VRAM_CUDA>       types/Memory.hpp:59-266, types/MemoryCuda.hpp:66-100
+//   Bundle / Hits / Ranges / ...     types/Bundle.hpp:72-131, simulation/SimulationResults.hpp:56-215
+//   resize_memory_bundle             SimulationResults.hpp:176-215
+//   SphericalModel / PinholeModel /
+//   O1DnModel / OnDnModel            types/sensor_models.h:54-502
+//   Transform / Quaternion / Vector3 math/types/Transform.hpp, Quaternion.hpp, Vector3.hpp (data layout)
+//   SimulatorX::setMap/setTsb/
+//     setModel/simulate              SimulatorEmbree.hpp:52-72, SphereSimulatorEmbree.hpp:107-159,
+//                                    SphereSimulatorOptix.hpp:122-190
+//   statistics_p2p / umeyama         math/statistics.h:72-157, math/optimization.h:61-75
+// Errors throw rmagine_gb300::Exception, as rmagine's RM_THROW does (util/exceptions.h:48).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "rmg.h"
+
+namespace rmagine_gb300 {
+
+class Exception : public std::runtime_error {
+ public:
+  Exception(int status, const std::string& what) : std::runtime_error(what), status(status) {}
+  int status;
+};
+
+inline void check(int st, const char* where) {
+  if (st != RMG_OK)
+    throw Exception(st, std::string(where) + ": " + rmg_status_string(st) + " (" + rmg_last_error() + ")");
+}
+
+inline void cuda_check(cudaError_t e, const char* where) {
+  if (e != cudaSuccess) throw Exception(RMG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// ---- plain data (byte-compatible with rmagine and with rmg.h) --------------------
+struct Vector3 {
+  float x, y, z;
+};
+struct Quaternion {
+  float x, y, z, w;
+  static Quaternion Identity() { return {0.f, 0.f, 0.f, 1.f}; }
+};
+struct Transform {
+  Quaternion R;
+  Vector3 t;
+  uint32_t stamp;
+  static Transform Identity() { return {Quaternion::Identity(), {0.f, 0.f, 0.f}, 0}; }
+};
+struct Face {
+  uint32_t v0, v1, v2;
+};
+using Vector = Vector3;
+static_assert(sizeof(Transform) == sizeof(rmg_transform), "Transform is 32 bytes");
+static_assert(sizeof(Vector3) == sizeof(rmg_vec3) && sizeof(Face) == sizeof(rmg_face), "layouts");
+
+struct Interval {
+  float min, max;
+};
+struct DiscreteInterval {
+  float min, inc;
+  uint32_t size;
+  float getValue(uint32_t i) const { return min + static_cast<float>(i) * inc; }
+};
+
+// ---- memory -----------------------------------------------------------------------
+struct RAM {};
+struct VRAM_CUDA {};
+
+template <typename T, typename MemT>
+class Memory;
+
+template <typename T>
+class Memory<T, RAM> {
+ public:
+  Memory() = default;
+  explicit Memory(size_t n) : v_(n) {}
+  void resize(size_t n) { v_.resize(n); }
+  size_t size() const { return v_.size(); }
+  T* raw() { return v_.data(); }
+  const T* raw() const { return v_.data(); }
+  T& operator[](size_t i) { return v_[i]; }
+  const T& operator[](size_t i) const { return v_[i]; }
+  Memory& operator=(const Memory<T, VRAM_CUDA>& o);
+
+ private:
+  std::vector<T> v_;
+};
+
+template <typename T>
+class Memory<T, VRAM_CUDA> {
+ public:
+  Memory() = default;
+  explicit Memory(size_t n) { resize(n); }
+  Memory(const Memory&) = delete;
+  Memory& operator=(const Memory&) = delete;
+  Memory(Memory&& o) noexcept : p_(o.p_), n_(o.n_) { o.p_ = nullptr; o.n_ = 0; }
+  ~Memory() { cudaFree(p_); }
+  void resize(size_t n) {
+    if (n == n_) return;
+    cudaFree(p_);
+    p_ = nullptr;
+    n_ = 0;
+    if (n) cuda_check(cudaMalloc(reinterpret_cast<void**>(&p_), n * sizeof(T)), "cudaMalloc");
+    n_ = n;
+  }
+  size_t size() const { return n_; }
+  T* raw() { return p_; }
+  const T* raw() const { return p_; }
+  // RAM -> VRAM assignment copies (MemoryCuda.cu:10-90 semantics)
+  Memory& operator=(const Memory<T, RAM>& o) {
+    resize(o.size());
+    if (n_) cuda_check(cudaMemcpy(p_, o.raw(), n_ * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy");
+    return *this;
+  }
+
+ private:
+  T* p_ = nullptr;
+  size_t n_ = 0;
+};
+
+template <typename T>
+Memory<T, RAM>& Memory<T, RAM>::operator=(const Memory<T, VRAM_CUDA>& o) {
+  resize(o.size());
+  if (o.size()) cuda_check(cudaMemcpy(raw(), o.raw(), o.size() * sizeof(T), cudaMemcpyDeviceToHost), "cudaMemcpy");
+  return *this;
+}
+
+// ---- result attributes and bundles ---------------------------------------------------
+template <typename MemT> struct Hits { Memory<uint8_t, MemT> hits; };
+template <typename MemT> struct Ranges { Memory<float, MemT> ranges; };
+template <typename MemT> struct Points { Memory<Vector3, MemT> points; };
+template <typename MemT> struct Normals { Memory<Vector3, MemT> normals; };
+template <typename MemT> struct FaceIds { Memory<uint32_t, MemT> face_ids; };
+template <typename MemT> struct GeomIds { Memory<uint32_t, MemT> geom_ids; };
+template <typename MemT> struct ObjectIds { Memory<uint32_t, MemT> object_ids; };
+
+template <typename... Attrs>
+struct Bundle : public Attrs... {
+  template <typename A>
+  static constexpr bool has() { return (std::is_same<A, Attrs>::value || ...); }
+};
+
+template <typename MemT>
+using IntAttrAll = Bundle<Hits<MemT>, Ranges<MemT>, Points<MemT>, Normals<MemT>, FaceIds<MemT>, GeomIds<MemT>,
+                          ObjectIds<MemT>>;
+
+template <typename MemT, typename BundleT>
+void resize_memory_bundle(BundleT& res, unsigned W, unsigned H, unsigned N = 1) {
+  const size_t n = (size_t)W * H * N;
+  if constexpr (BundleT::template has<Hits<MemT>>()) res.Hits<MemT>::hits.resize(n);
+  if constexpr (BundleT::template has<Ranges<MemT>>()) res.Ranges<MemT>::ranges.resize(n);
+  if constexpr (BundleT::template has<Points<MemT>>()) res.Points<MemT>::points.resize(n);
+  if constexpr (BundleT::template has<Normals<MemT>>()) res.Normals<MemT>::normals.resize(n);
+  if constexpr (BundleT::template has<FaceIds<MemT>>()) res.FaceIds<MemT>::face_ids.resize(n);
+  if constexpr (BundleT::template has<GeomIds<MemT>>()) res.GeomIds<MemT>::geom_ids.resize(n);
+  if constexpr (BundleT::template has<ObjectIds<MemT>>()) res.ObjectIds<MemT>::object_ids.resize(n);
+}
+
+// rmg_outputs of a device bundle: a buffer is requested iff it is non-empty
+// (set_simulation_flags_, embree_common.h:79-139).
+template <typename BundleT>
+rmg_outputs outputs_of(BundleT& b) {
+  using M = VRAM_CUDA;
+  rmg_outputs o{};
+  if constexpr (BundleT::template has<Hits<M>>()) o.hits = b.Hits<M>::hits.size() ? b.Hits<M>::hits.raw() : nullptr;
+  if constexpr (BundleT::template has<Ranges<M>>())
+    o.ranges = b.Ranges<M>::ranges.size() ? b.Ranges<M>::ranges.raw() : nullptr;
+  if constexpr (BundleT::template has<Points<M>>())
+    o.points = b.Points<M>::points.size() ? reinterpret_cast<rmg_vec3*>(b.Points<M>::points.raw()) : nullptr;
+  if constexpr (BundleT::template has<Normals<M>>())
+    o.normals = b.Normals<M>::normals.size() ? reinterpret_cast<rmg_vec3*>(b.Normals<M>::normals.raw()) : nullptr;
+  if constexpr (BundleT::template has<FaceIds<M>>())
+    o.face_ids = b.FaceIds<M>::face_ids.size() ? b.FaceIds<M>::face_ids.raw() : nullptr;
+  if constexpr (BundleT::template has<GeomIds<M>>())
+    o.geom_ids = b.GeomIds<M>::geom_ids.size() ? b.GeomIds<M>::geom_ids.raw() : nullptr;
+  if constexpr (BundleT::template has<ObjectIds<M>>())
+    o.object_ids = b.ObjectIds<M>::object_ids.size() ? b.ObjectIds<M>::object_ids.raw() : nullptr;
+  return o;
+}
+
+// ---- sensor models ---------------------------------------------------------------------
+struct SphericalModel {
+  DiscreteInterval phi, theta;
+  Interval range;
+  uint32_t getWidth() const { return theta.size; }
+  uint32_t getHeight() const { return phi.size; }
+  uint32_t size() const { return getWidth() * getHeight(); }
+  uint32_t getBufferId(uint32_t vid, uint32_t hid) const { return vid * getWidth() + hid; }
+  rmg_model to_c() const {
+    rmg_model m{};
+    m.kind = RMG_MODEL_SPHERICAL;
+    m.range = {range.min, range.max};
+    m.phi = {phi.min, phi.inc, phi.size};
+    m.theta = {theta.min, theta.inc, theta.size};
+    return m;
+  }
+};
+
+struct PinholeModel {
+  uint32_t width, height;
+  Interval range;
+  float f[2], c[2];
+  uint32_t getWidth() const { return width; }
+  uint32_t getHeight() const { return height; }
+  uint32_t size() const { return width * height; }
+  uint32_t getBufferId(uint32_t vid, uint32_t hid) const { return vid * width + hid; }
+  rmg_model to_c() const {
+    rmg_model m{};
+    m.kind = RMG_MODEL_PINHOLE;
+    m.width = width;
+    m.height = height;
+    m.range = {range.min, range.max};
+    m.f[0] = f[0]; m.f[1] = f[1]; m.c[0] = c[0]; m.c[1] = c[1];
+    return m;
+  }
+};
+
+struct O1DnModel {
+  uint32_t width, height;
+  Interval range;
+  Vector3 orig;
+  Memory<Vector3, RAM> dirs;
+  uint32_t getWidth() const { return width; }
+  uint32_t getHeight() const { return height; }
+  uint32_t size() const { return width * height; }
+  rmg_model to_c() const {
+    rmg_model m{};
+    m.kind = RMG_MODEL_O1DN;
+    m.width = width;
+    m.height = height;
+    m.range = {range.min, range.max};
+    m.orig = {orig.x, orig.y, orig.z};
+    m.dirs = reinterpret_cast<const rmg_vec3*>(dirs.raw());
+    return m;
+  }
+};
+
+struct OnDnModel {
+  uint32_t width, height;
+  Interval range;
+  Memory<Vector3, RAM> origs, dirs;
+  uint32_t getWidth() const { return width; }
+  uint32_t getHeight() const { return height; }
+  uint32_t size() const { return width * height; }
+  rmg_model to_c() const {
+    rmg_model m{};
+    m.kind = RMG_MODEL_ONDN;
+    m.width = width;
+    m.height = height;
+    m.range = {range.min, range.max};
+    m.dirs = reinterpret_cast<const rmg_vec3*>(dirs.raw());
+    m.origs = reinterpret_cast<const rmg_vec3*>(origs.raw());
+    return m;
+  }
+};
+
+// ---- map -----------------------------------------------------------------------------------
+class TriangleMap {
+ public:
+  TriangleMap(const Memory<Vector3, RAM>& V, const Memory<Face, RAM>& F, cudaStream_t s = 0) {
+    check(rmg_map_build(reinterpret_cast<const rmg_vec3*>(V.raw()), (uint32_t)V.size(),
+                        reinterpret_cast<const rmg_face*>(F.raw()), (uint32_t)F.size(), s, &h_),
+          "rmg_map_build");
+  }
+  ~TriangleMap() { rmg_map_destroy(h_); }
+  TriangleMap(const TriangleMap&) = delete;
+  TriangleMap& operator=(const TriangleMap&) = delete;
+  rmg_map* handle() const { return h_; }
+  void refit(const Memory<Vector3, RAM>& V, cudaStream_t s = 0) {
+    check(rmg_map_refit(h_, reinterpret_cast<const rmg_vec3*>(V.raw()), (uint32_t)V.size(), s), "rmg_map_refit");
+  }
+  int status(bool clear = true) { return rmg_map_status(h_, clear ? 1 : 0); }
+
+ private:
+  rmg_map* h_ = nullptr;
+};
+using MapPtr = std::shared_ptr<TriangleMap>;
+
+// ---- simulators ---------------------------------------------------------------------------
+template <typename ModelT>
+class SimulatorGB300 {
+ public:
+  SimulatorGB300() = default;
+  explicit SimulatorGB300(MapPtr map) : map_(std::move(map)) {}
+  ~SimulatorGB300() { rmg_sensor_destroy(sensor_); }
+  SimulatorGB300(const SimulatorGB300&) = delete;
+  SimulatorGB300& operator=(const SimulatorGB300&) = delete;
+
+  void setMap(MapPtr map) { map_ = std::move(map); }
+  MapPtr map() const { return map_; }
+  void setTsb(const Transform& T) { Tsb_ = T; }
+  void setModel(const ModelT& model) {
+    const rmg_model c = model.to_c();
+    rmg_sensor* s = nullptr;
+    check(rmg_sensor_create(&c, nullptr, &s), "rmg_sensor_create");
+    rmg_sensor_destroy(sensor_);
+    sensor_ = s;
+    rmg_sensor_size(sensor_, &W_, &H_);
+  }
+
+  // Device form (SphereSimulatorOptix.hpp:141-160): asynchronous on `stream`.
+  template <typename BundleT>
+  void simulate(const Memory<Transform, VRAM_CUDA>& Tbm, BundleT& ret, cudaStream_t stream = 0) const {
+    ready();
+    const rmg_outputs o = outputs_of(ret);
+    check(rmg_simulate(map_->handle(), sensor_, reinterpret_cast<const rmg_transform*>(&Tsb_),
+                       reinterpret_cast<const rmg_transform*>(Tbm.raw()), (uint32_t)Tbm.size(), &o, stream),
+          "rmg_simulate");
+  }
+
+  // Allocating device form: simulate<BundleT>(Tbm).
+  template <typename BundleT>
+  BundleT simulate(const Memory<Transform, VRAM_CUDA>& Tbm, cudaStream_t stream = 0) const {
+    BundleT res;
+    resize_memory_bundle<VRAM_CUDA>(res, W_, H_, (unsigned)Tbm.size());
+    simulate(Tbm, res, stream);
+    return res;
+  }
+
+  // Host form (SphereSimulatorEmbree.hpp:130-155): poses and results in RAM; synchronises.
+  template <typename BundleRAM>
+  void simulate(const Memory<Transform, RAM>& Tbm, BundleRAM& ret) const {
+    ready();
+    Memory<Transform, VRAM_CUDA> Td;
+    Td = Tbm;
+    IntAttrAll<VRAM_CUDA> dev;
+    const size_t n = (size_t)W_ * H_ * Tbm.size();
+    if constexpr (BundleRAM::template has<Hits<RAM>>()) if (ret.Hits<RAM>::hits.size()) dev.Hits<VRAM_CUDA>::hits.resize(n);
+    if constexpr (BundleRAM::template has<Ranges<RAM>>()) if (ret.Ranges<RAM>::ranges.size()) dev.Ranges<VRAM_CUDA>::ranges.resize(n);
+    if constexpr (BundleRAM::template has<Points<RAM>>()) if (ret.Points<RAM>::points.size()) dev.Points<VRAM_CUDA>::points.resize(n);
+    if constexpr (BundleRAM::template has<Normals<RAM>>()) if (ret.Normals<RAM>::normals.size()) dev.Normals<VRAM_CUDA>::normals.resize(n);
+    if constexpr (BundleRAM::template has<FaceIds<RAM>>()) if (ret.FaceIds<RAM>::face_ids.size()) dev.FaceIds<VRAM_CUDA>::face_ids.resize(n);
+    if constexpr (BundleRAM::template has<GeomIds<RAM>>()) if (ret.GeomIds<RAM>::geom_ids.size()) dev.GeomIds<VRAM_CUDA>::geom_ids.resize(n);
+    if constexpr (BundleRAM::template has<ObjectIds<RAM>>()) if (ret.ObjectIds<RAM>::object_ids.size()) dev.ObjectIds<VRAM_CUDA>::object_ids.resize(n);
+    simulate(Td, dev, 0);
+    cuda_check(cudaDeviceSynchronize(), "simulate");
+    if constexpr (BundleRAM::template has<Hits<RAM>>()) if (ret.Hits<RAM>::hits.size()) ret.Hits<RAM>::hits = dev.Hits<VRAM_CUDA>::hits;
+    if constexpr (BundleRAM::template has<Ranges<RAM>>()) if (ret.Ranges<RAM>::ranges.size()) ret.Ranges<RAM>::ranges = dev.Ranges<VRAM_CUDA>::ranges;
+    if constexpr (BundleRAM::template has<Points<RAM>>()) if (ret.Points<RAM>::points.size()) ret.Points<RAM>::points = dev.Points<VRAM_CUDA>::points;
+    if constexpr (BundleRAM::template has<Normals<RAM>>()) if (ret.Normals<RAM>::normals.size()) ret.Normals<RAM>::normals = dev.Normals<VRAM_CUDA>::normals;
+    if constexpr (BundleRAM::template has<FaceIds<RAM>>()) if (ret.FaceIds<RAM>::face_ids.size()) ret.FaceIds<RAM>::face_ids = dev.FaceIds<VRAM_CUDA>::face_ids;
+    if constexpr (BundleRAM::template has<GeomIds<RAM>>()) if (ret.GeomIds<RAM>::geom_ids.size()) ret.GeomIds<RAM>::geom_ids = dev.GeomIds<VRAM_CUDA>::geom_ids;
+    if constexpr (BundleRAM::template has<ObjectIds<RAM>>()) if (ret.ObjectIds<RAM>::object_ids.size()) ret.ObjectIds<RAM>::object_ids = dev.ObjectIds<VRAM_CUDA>::object_ids;
+  }
+
+  template <typename BundleRAM>
+  BundleRAM simulate(const Memory<Transform, RAM>& Tbm) const {
+    BundleRAM res;
+    resize_memory_bundle<RAM>(res, W_, H_, (unsigned)Tbm.size());
+    simulate(Tbm, res);
+    return res;
+  }
+
+  uint32_t width() const { return W_; }
+  uint32_t height() const { return H_; }
+
+ private:
+  void ready() const {
+    if (!map_) throw Exception(RMG_ERR_INVALID_ARG, "simulate: no map set");
+    if (!sensor_) throw Exception(RMG_ERR_INVALID_ARG, "simulate: no model set");
+  }
+  MapPtr map_;
+  rmg_sensor* sensor_ = nullptr;
+  Transform Tsb_ = Transform::Identity();
+  uint32_t W_ = 0, H_ = 0;
+};
+
+using SphereSimulatorGB300 = SimulatorGB300<SphericalModel>;
+using PinholeSimulatorGB300 = SimulatorGB300<PinholeModel>;
+using O1DnSimulatorGB300 = SimulatorGB300<O1DnModel>;
+using OnDnSimulatorGB300 = SimulatorGB300<OnDnModel>;
+
+// ---- statistics / Umeyama -----------------------------------------------------------------
+struct CrossStatistics {
+  Vector3 dataset_mean, model_mean;
+  float covariance[9];  // column-major, like rmagine::Matrix3x3
+  uint32_t n_meas;
+};
+static_assert(sizeof(CrossStatistics) == sizeof(rmg_cross_stats), "CrossStatistics is 64 bytes");
+
+struct UmeyamaReductionConstraints {
+  float max_dist;
+  uint32_t dataset_id, model_id;
+};
+
+// statistics_p2p over n_batches batches of n_per_batch DEVICE correspondences.
+inline void statistics_p2p(const Memory<Vector3, VRAM_CUDA>& dataset, const Memory<Vector3, VRAM_CUDA>& model,
+                           const UmeyamaReductionConstraints& params, uint32_t n_batches,
+                           Memory<CrossStatistics, VRAM_CUDA>& stats, Memory<Transform, VRAM_CUDA>* Ts = nullptr,
+                           const Memory<uint8_t, VRAM_CUDA>* dataset_mask = nullptr, cudaStream_t s = 0) {
+  const uint32_t n_per = n_batches ? (uint32_t)(dataset.size() / n_batches) : 0;
+  stats.resize(n_batches);
+  if (Ts) Ts->resize(n_batches);
+  const rmg_umeyama_constraints c{params.max_dist, params.dataset_id, params.model_id};
+  check(rmg_statistics_p2p(nullptr, 0, reinterpret_cast<const rmg_vec3*>(dataset.raw()),
+                           dataset_mask ? dataset_mask->raw() : nullptr, nullptr,
+                           reinterpret_cast<const rmg_vec3*>(model.raw()), nullptr, nullptr, &c, n_batches, n_per,
+                           reinterpret_cast<rmg_cross_stats*>(stats.raw()),
+                           Ts ? reinterpret_cast<rmg_transform*>(Ts->raw()) : nullptr, s),
+        "rmg_statistics_p2p");
+}
+
+inline void umeyama_transform(const Memory<CrossStatistics, VRAM_CUDA>& stats, Memory<Transform, VRAM_CUDA>& Ts,
+                              cudaStream_t s = 0) {
+  Ts.resize(stats.size());
+  check(rmg_umeyama_transform(reinterpret_cast<const rmg_cross_stats*>(stats.raw()), (uint32_t)stats.size(),
+                              reinterpret_cast<rmg_transform*>(Ts.raw()), s),
+        "rmg_umeyama_transform");
+}
+
+}  // namespace rmagine_gb300

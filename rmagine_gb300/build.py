@@ -80,5 +80,21 @@ def build(verbose: bool = False, ptxas_info: bool = False, jobs: int | None = No
     return out
 
 
+def build_cpp_tests() -> Path:
+    """Compiles the C++ API test program (tests/cpp/test_simulators.cpp) against the library."""
+    lib = build()
+    src = ROOT / "tests" / "cpp" / "test_simulators.cpp"
+    out = BUILD / "test_simulators"
+    deps = [src, ROOT / "include" / "rmagine_gb300.hpp", ROOT / "include" / "rmg.h", lib]
+    if out.exists() and out.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+        return out
+    cmd = [nvcc(), "-std=c++17", "-O2", "-I", str(ROOT / "include"), str(src), "-L", str(LIBDIR), "-lrmg_gb300",
+           "-Xlinker", f"-rpath={LIBDIR}", "-o", str(out)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"C++ test build failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return out
+
+
 if __name__ == "__main__":
     build(verbose=True, ptxas_info="-v" in sys.argv)

@@ -363,6 +363,14 @@ class OnDnSimulator(_Simulator):
     model_type = OnDnModel
 
 
+def pose_shard(n_poses: int, rank: int, world: int) -> tuple[int, int]:
+    """Contiguous pose range [lo, hi) of `rank` among `world` replicas: poses are independent and
+    the map is replicated, so N GPUs split the poses with no collective on the data path."""
+    base, extra = divmod(n_poses, world)
+    lo = rank * base + min(rank, extra)
+    return lo, lo + base + (1 if rank < extra else 0)
+
+
 def make_simulator(model, map: Map | None = None) -> _Simulator:
     """Simulator.hpp:52-78 (SimulatorType<ModelT, CompT>) for this backend."""
     for cls in (SphereSimulator, PinholeSimulator, O1DnSimulator, OnDnSimulator):
