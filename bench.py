@@ -50,7 +50,12 @@ WORK_PER_RAY = {
 
 # Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel,
 # from one ncu capture of the workload (profiles/).
-TRAFFIC: dict = {}
+TRAFFIC: dict = {
+    "terrain1m_spherical": 2944196608 + 4433009664,
+    "icp_stats_fwd": 6442640128 + 4728320,
+    "icp_stats_bwd": 6444127744 + 6394882560,
+    "pose_grad": 13100006912 + 351378688,
+}
 
 RAYCAST = ("terrain1m_spherical", "terrain1m_pinhole", "terrain2m_spherical", "room_vlp16")
 
