@@ -403,7 +403,7 @@ def gpu_icp(args, world):
               "parallelism": f"replicas{world}" if world > 1 else "single"}
     line = {"metric": "Gcorr/s", "unit": "Gcorr/s", "value": round(value, 3),
             "ms_per_step": round(total_ms / args.steps, 3), "dtype": "f32 (f64 accumulation)", "config": config,
-            "gpu_launches": 5 * args.steps,
+            "gpu_launches": 4 * args.steps,
             "forward_ms": round(f_ms / args.steps, 3), "backward_ms": round(b_ms / args.steps, 3),
             "e2e": {"value": round(e2e, 3), "unit": "Gcorr/s", "h2d_bytes_per_step": int(2 * 12 * corr),
                     "d2h_bytes_per_step": int(2 * 12 * corr + 32 * B)},
