@@ -45,12 +45,28 @@ def _headers() -> list[Path]:
     return sorted(list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((ROOT / "include").glob("*.h")))
 
 
+def _extra_flags() -> list[str]:
+    """Additional nvcc flags from RMG_NVCC_FLAGS (space separated), e.g. -DRMG_TRACE_MIN_BLOCKS=5."""
+    return os.environ.get("RMG_NVCC_FLAGS", "").split()
+
+
+def _build_dir() -> Path:
+    extra = _extra_flags()
+    if not extra:
+        return BUILD
+    import hashlib
+
+    return BUILD / ("flags_" + hashlib.sha1(" ".join(extra).encode()).hexdigest()[:10])
+
+
 def _compile(src: Path, extra: list[str]) -> Path:
-    obj = BUILD / (src.stem + ".o")
+    bdir = _build_dir()
+    bdir.mkdir(parents=True, exist_ok=True)
+    obj = bdir / (src.stem + ".o")
     newest_dep = max([src.stat().st_mtime] + [h.stat().st_mtime for h in _headers()])
     if obj.exists() and obj.stat().st_mtime >= newest_dep:
         return obj
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *_extra_flags(), *extra, "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src.name}:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
@@ -67,7 +83,9 @@ def build(verbose: bool = False, ptxas_info: bool = False, jobs: int | None = No
         objs = list(ex.map(lambda s: _compile(s, extra), srcs))
     out = lib_path()
     newest = max(o.stat().st_mtime for o in objs)
-    if not out.exists() or out.stat().st_mtime < newest:
+    stamp = LIBDIR / "build_flags.txt"
+    flags = " ".join(_extra_flags())
+    if not out.exists() or out.stat().st_mtime < newest or (stamp.read_text() if stamp.exists() else "") != flags:
         tmp = out.with_suffix(".so.tmp")
         cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart_static", "-lrt",
                "-lpthread", "-ldl"]
@@ -75,6 +93,7 @@ def build(verbose: bool = False, ptxas_info: bool = False, jobs: int | None = No
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, out)
+        stamp.write_text(flags)
     if verbose:
         print(f"built {out}")
     return out

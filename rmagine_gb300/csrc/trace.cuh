@@ -386,8 +386,14 @@ __device__ __forceinline__ void setup_ray(const SensorDev& sen, const Tf& Tsm, u
 }
 
 // One warp = one tile of tile_h x tile_w rays of one pose.
+// Minimum resident CTAs per SM requested from the compiler for k_trace (a
+// register cap); 1 leaves the allocation to ptxas.
+#ifndef RMG_TRACE_MIN_BLOCKS
+#define RMG_TRACE_MIN_BLOCKS 1
+#endif
+
 template <int OK, int SS, int TB>
-__global__ void __launch_bounds__(256) k_trace(const TraceParams P) {
+__global__ void __launch_bounds__(256, RMG_TRACE_MIN_BLOCKS) k_trace(const TraceParams P) {
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp >= P.n_tiles) return;
   const uint32_t lane = threadIdx.x & 31;
