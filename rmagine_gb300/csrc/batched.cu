@@ -76,8 +76,12 @@ __device__ __forceinline__ void batched_ray(const BatchParams& B, const JobDev& 
   write_attributes<OK>(P, gid, h, dir_s, orig_s, Tsm);
 }
 
+#ifndef RMG_BATCHED_MIN_BLOCKS
+#define RMG_BATCHED_MIN_BLOCKS 5
+#endif
+
 template <int SS, int TB>
-__global__ void __launch_bounds__(256) k_trace_batched(const BatchParams B) {
+__global__ void __launch_bounds__(256, RMG_BATCHED_MIN_BLOCKS) k_trace_batched(const BatchParams B) {
   __shared__ unsigned long long s_begin[kMaxJobsShared + 1];
   const bool in_smem = B.n_jobs <= kMaxJobsShared;
   if (in_smem) {

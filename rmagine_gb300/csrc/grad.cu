@@ -33,8 +33,12 @@ struct GradParams {
   uint32_t ctas_per_pose;
 };
 
+#ifndef RMG_GRAD_MIN_BLOCKS
+#define RMG_GRAD_MIN_BLOCKS 5
+#endif
+
 template <int OK, int SS, int TB>
-__global__ void __launch_bounds__(256) k_range_grad(const GradParams G) {
+__global__ void __launch_bounds__(256, RMG_GRAD_MIN_BLOCKS) k_range_grad(const GradParams G) {
   const TraceParams& P = G.T;
   const uint32_t pose = blockIdx.y;
   const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;

@@ -386,10 +386,14 @@ __device__ __forceinline__ void setup_ray(const SensorDev& sen, const Tf& Tsm, u
 }
 
 // One warp = one tile of tile_h x tile_w rays of one pose.
-// Minimum resident CTAs per SM requested from the compiler for k_trace (a
-// register cap); 1 leaves the allocation to ptxas.
+// Minimum resident CTAs per SM requested from the compiler for k_trace: 5
+// CTAs of 256 threads cap the kernel at 48 registers (a few bytes of spills
+// to L1-cached local memory) and lift occupancy from 50% to 62.5%; measured
+// 9% faster than the unconstrained 62-register build on the 1M-triangle
+// terrain (6,179 vs 5,661 Mrays/s), while 6 CTAs (40 registers) spill more
+// and lose again.
 #ifndef RMG_TRACE_MIN_BLOCKS
-#define RMG_TRACE_MIN_BLOCKS 1
+#define RMG_TRACE_MIN_BLOCKS 5
 #endif
 
 template <int OK, int SS, int TB>
