@@ -10,7 +10,10 @@ all five attributes (Hits, Ranges, Points, Normals, FaceIds): 131,072,000 rays p
 Other workloads: terrain1m_pinhole, terrain2m_spherical (2,117,058 triangles), room_vlp16;
 icp_stats (8192 batches x 32768 correspondences: statistics_p2p + Umeyama forward and the
 backward, correspondences/s); pose_grad (2.1M-triangle terrain, spherical 64 x 1024, 4096
-poses: fused ray cast + range adjoint, pose-gradient evaluations/s).
+poses: fused ray cast + range adjoint, pose-gradient evaluations/s); rcc_fused (the
+correction loop's inner step fused: model ray cast at 1,000 pose estimates paired ray by ray
+with per-pose scans into statistics_p2l + Umeyama, sensor rays/s, with the two-step
+simulate + statistics path timed beside it); batched (64 mixed sensors in one launch).
 
 Prints one JSON line (rank 0).  `--impl reference` times the CPU restatement of the reference's
 semantics on the host cores instead (see the cpu_* functions).
@@ -46,6 +49,8 @@ WORK_PER_RAY = {
     "terrain2m_spherical": {"nodes": 30.580, "tris": 1.764},
     "room_vlp16": {"nodes": 65.651, "tris": 3.919},
     "pose_grad": {"nodes": 30.260, "tris": 1.763},
+    # averaged over all sensor rays; rays without a valid dataset point (1 - data_frac) are not cast
+    "rcc_fused": {"nodes": 21.417, "tris": 1.715, "data_frac": 0.554},
 }
 
 # Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel,
@@ -510,6 +515,121 @@ def gpu_posegrad(args, world):
     return line, lambda: cpu_posegrad(sc, model, true, est, obs_h), config
 
 
+# ---- fused simulate -> statistics (RCC / MICP-L inner step) ---------------------------------
+def rcc_workload(n_poses=1000):
+    """1M-triangle terrain, spherical 128x1024, n pose estimates (the ray-cast workload's poses
+    perturbed by N(0, 0.1 m) / N(0, 2 deg)), each against the scan taken at its true pose."""
+    from rmagine_gb300 import scenes, sensors
+
+    sc = scenes.million_triangle_terrain(seed=0)
+    model = sensors.ouster_like(128, 1024, 45.0, 0.5, 130.0)
+    true = scenes.terrain_poses(sc, 1000, seed=2)[:n_poses]
+    est = scenes.perturb_poses(true, 4, 0.1, 2.0)
+    return sc, model, true, est
+
+
+def cpu_rcc(sc, model, true, est, data_h, target_s=10.0):
+    """The oracle's restatement of the step: OpenMP ray cast of the model scan + binary64 numpy
+    statistics_p2l + Umeyama, over a bounded pose sample."""
+    import oracle
+    from oracle import stats as ost
+
+    ocs = oracle.Scene(sc.vertices, sc.faces)
+    threads = oracle.lib().orc_max_threads()
+    W, H = model_size(model)
+
+    def run(n):
+        return ost.simulate_statistics(ocs, model, IDENT, est[:n], data_h["points"][:n * W * H],
+                                       dmask=data_h["hits"][:n * W * H], max_dist=0.5)
+
+    t0 = time.perf_counter()
+    run(1)
+    per = max(time.perf_counter() - t0, 1e-4)
+    n = int(max(1, min(len(est), data_h["hits"].size // (W * H), target_s / per)))
+    t0 = time.perf_counter()
+    run(n)
+    dt = time.perf_counter() - t0
+    return {"value": n * W * H / dt / 1e6, "unit": "Mrays/s", "cores": int(threads), "kind": "port",
+            "sample": f"{n} of {len(est)} poses ({n * W * H} rays): oracle OpenMP ray cast + numpy binary64 "
+                      f"statistics_p2l + Umeyama", "seconds": dt}
+
+
+def gpu_rcc(args, world):
+    import torch
+
+    import rmagine_gb300 as rm
+    from rmagine_gb300 import statistics as rs
+
+    n_poses = args.poses or 1000
+    sc, model, true, est = rcc_workload(n_poses)
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    W, H = model_size(model)
+    rays = n_poses * W * H
+    m = rm.Map(sc.vertices, sc.faces)
+    sim = rm.SphereSimulator(m)
+    sim.setModel(model)
+    data = sim.simulate(torch.from_numpy(true).to(dev), attrs=("hits", "points"))
+    dp, dm = data.points.reshape(n_poses, W * H, 3), data.hits.reshape(n_poses, W * H)
+    Est = torch.from_numpy(est).to(dev)
+    P = rs.UmeyamaReductionConstraints(max_dist=0.5)
+
+    def fused():
+        return sim.simulate_statistics(Est, dp, dataset_mask=dm, params=P)
+
+    mod = rm.Bundle("hits", "points", "normals")
+    rm.resize_memory_bundle(mod, W, H, n_poses, device=dev)
+
+    def two_step():
+        sim.simulate(Est, mod)
+        return rs.statistics_p2l(dp, mod.points.reshape(n_poses, W * H, 3), mod.normals.reshape(n_poses, W * H, 3),
+                                 params=P, dataset_mask=dm, model_mask=mod.hits.reshape(n_poses, W * H))
+
+    for _ in range(args.warmup):
+        fused()
+        two_step()
+    torch.cuda.synchronize(dev)
+    total_ms, step_ms, clocks = Timer(dev, args.steps).run(fused, world)
+    two_ms, _, _ = Timer(dev, max(3, min(args.steps, 5))).run(two_step, world)
+    two_ms /= max(3, min(args.steps, 5))
+    if m.status() != 0:
+        raise RuntimeError("device status error in the timed region")
+    value = world * rays * args.steps / (total_ms / 1e3) / 1e6
+    # end to end: estimates and scans from pinned host memory, statistics + transforms back
+    host_est = torch.from_numpy(est).pin_memory()
+    host_dp, host_dm = dp.cpu().pin_memory(), dm.cpu().pin_memory()
+    e2e_t = []
+    for _ in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        st, T = sim.simulate_statistics(host_est, host_dp, dataset_mask=host_dm, params=P)
+        st.cpu()
+        T.cpu()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e = rays / (sum(e2e_t) / len(e2e_t)) / 1e6
+    wk = WORK_PER_RAY["rcc_fused"]
+    rl = roofline(1 + wk["data_frac"] * 12 + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
+                  "per sensor ray: dataset mask 1 B + dataset point 12 B where valid + 64 B per node visit + 48 B per "
+                  "triangle test (rays without a valid dataset point are not cast); nothing is written per ray",
+                  TRAFFIC.get("rcc_fused"))
+    config = {"workload": f"fused simulate -> statistics_p2l -> Umeyama: terrain 708x708 + 2000 boxes (1,023,698 "
+                          f"tris), spherical 128x1024, {n_poses} pose estimates (perturbed N(0,0.1 m) / N(0,2 deg)) "
+                          f"each against the scan at its true pose, max_dist 0.5 m",
+              "poses": n_poses, "rays_per_step": rays, "l2": "flushed between timed steps (256 MB write)",
+              "parallelism": f"replicas{world}" if world > 1 else "single"}
+    line = {"metric": "Mrays/s", "unit": "Mrays/s", "value": round(value, 1),
+            "ms_per_step": round(total_ms / args.steps, 3), "dtype": "f32", "config": config,
+            "gpu_launches": 2 * args.steps,
+            "two_step": {"value": round(rays / (two_ms / 1e3) / 1e6, 1), "unit": "Mrays/s",
+                         "ms_per_step": round(two_ms, 3),
+                         "what": "rmg_simulate (Hits, Points, Normals) + rmg_statistics_p2l with Umeyama"},
+            "e2e": {"value": round(e2e, 1), "unit": "Mrays/s", "h2d_bytes_per_step": int(est.nbytes + 13 * rays),
+                    "d2h_bytes_per_step": int(96 * n_poses)},
+            "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
+    data_h = {"points": dp[:8].reshape(-1, 3).cpu().numpy(), "hits": dm[:8].reshape(-1).cpu().numpy()}
+    return line, lambda: cpu_rcc(sc, model, true, est, data_h), config
+
+
 # ---- batched heterogeneous sensors ------------------------------------------------------------
 def gpu_batched(args, world):
     import torch
@@ -638,6 +758,8 @@ def main():
         line, cpu, _ = gpu_posegrad(args, world)
     elif args.workload == "batched":
         line, cpu, _ = gpu_batched(args, world)
+    elif args.workload == "rcc_fused":
+        line, cpu, _ = gpu_rcc(args, world)
     else:
         raise SystemExit(f"unknown workload {args.workload}")
     if rank != 0:
@@ -676,6 +798,13 @@ def reference_arm(args, base):
         obs = oracle.Scene(sc.vertices, sc.faces).simulate(model, IDENT, true, attrs=("ranges",))["ranges"]
         run = lambda: cpu_posegrad(sc, model, true, est, obs, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
         metric, unit, config = "pose-grad evals/s", "poses/s", {"workload": "pose gradient (CPU sample)"}
+    elif args.workload == "rcc_fused":
+        import oracle
+
+        sc, model, true, est = rcc_workload(16)
+        data_h = oracle.Scene(sc.vertices, sc.faces).simulate(model, IDENT, true, attrs=("hits", "points"))
+        run = lambda: cpu_rcc(sc, model, true, est, data_h, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
+        metric, unit, config = "Mrays/s", "Mrays/s", {"workload": "fused simulate -> statistics_p2l (CPU sample)"}
     else:
         raise SystemExit(f"unknown workload {args.workload}")
     vals, leg = [], None

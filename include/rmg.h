@@ -335,6 +335,52 @@ int rmg_umeyama_backward(const rmg_transform* pre_transforms, uint32_t pre_trans
                          rmg_vec3* grad_dataset, rmg_vec3* grad_model, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Fused simulate -> statistics (the inner step of the RCC / MICP-L correction
+ * loop, tests/embree/correction_rcc.cpp:139-160).
+ *
+ * Replaces, per pose p, the sequence
+ *     simulate(Tbm[p], model bundle: Points, Normals, Hits)
+ *         (SphereSimulatorEmbree.tcc:42-253 and the other three models)
+ *     stats[p] = statistics_p2l(pre, dataset, model, params)   (statistics.cpp:84-126)
+ *          (or statistics_p2p, statistics.cpp:19-57, when point_to_plane == 0)
+ *     transforms[p] = umeyama_transform(stats[p])              (optimization.cpp:12-49)
+ * in one ray-casting launch that never writes the model bundle: ray i of pose
+ * p is paired with dataset point i of the pose's scan.  The model side of ray i
+ * is valid when it hits with range >= range.min (the Hits attribute); its point
+ * and normal equal the Points / Normals attributes of rmg_simulate bit for bit.
+ * The filter and pairing follow rmg_statistics_p2p / _p2l; the model ids filter
+ * is not applied (a simulated model cloud carries no ids in that loop:
+ * correction_rcc.cpp:143-147 builds it from points, hits and normals).
+ * Dataset rays that are masked out are not cast.  The sums may be added in a
+ * different order from rmg_simulate + rmg_statistics_p2l (binary32 partial
+ * sums folded into binary64), so the statistics agree with that pair to
+ * binary32 rounding and n_meas agrees exactly. */
+typedef struct rmg_scan {
+  const rmg_vec3* points;  /* DEVICE [n_scans][width*height], sensor frame, ray order of rmg_simulate */
+  const uint8_t* mask;     /* DEVICE, > 0 = valid (e.g. the scan's Hits), or NULL */
+  const uint32_t* ids;     /* DEVICE, compared with params->dataset_id, or NULL */
+  uint32_t per_pose;       /* 1: scan p belongs to pose p; 0: one scan for every pose */
+} rmg_scan;
+
+/* Tsb, dataset and params are HOST pointers; Tbm[n_poses], pre_transforms
+ * (NULL = identity; stride 0 = one for all poses, 1 = one per pose) and the
+ * outputs stats[n_poses] / transforms[n_poses] (NULL = not wanted, not both)
+ * are DEVICE pointers.  Asynchronous on `stream`.  No counterpart in the
+ * reference (it always materialises the model bundle). */
+int rmg_simulate_statistics(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                            const rmg_transform* Tbm, uint32_t n_poses, const rmg_scan* dataset,
+                            const rmg_transform* pre_transforms, uint32_t pre_transform_stride,
+                            const rmg_umeyama_constraints* params, int point_to_plane,
+                            rmg_cross_stats* stats, rmg_transform* transforms, void* stream);
+
+/* Batched Transform::mult (Transform.tcc:34-42; multInplace :44-56 when out
+ * aliases a): out[i] = a[i] * b[i] for i < n, all DEVICE arrays; stride 0
+ * repeats element 0 of that operand.  Lets a correction loop keep its pose
+ * estimates on the device (Tpre = Tpre * T, Tbm = Tbm * Tpre). */
+int rmg_transforms_compose(const rmg_transform* a, uint32_t a_stride, const rmg_transform* b, uint32_t b_stride,
+                           rmg_transform* out, uint32_t n, void* stream);
+
+/* ---------------------------------------------------------------------------
  * LBVH build without device allocation.
  * No counterpart in the reference: rmagine's maps always allocate their own
  * memory.  This is for callers that cannot call cudaMalloc -- code running

@@ -81,8 +81,9 @@ def correspondences(dataset, model, pre=None, dmask=None, mmask=None, dids=None,
 def stats(D, M, ok):
     """Binary64 CrossStatistics per batch: dict of dataset_mean [B,3], model_mean [B,3],
     covariance [B,3,3] (row i = model axis, col j = dataset axis), n [B]."""
-    D = D.astype(np.float64)
-    M = M.astype(np.float64)
+    # masked-out entries may hold NaN (miss rays carry NaN points): select, do not multiply by 0
+    D = np.where(ok[..., None], D.astype(np.float64), 0.0)
+    M = np.where(ok[..., None], M.astype(np.float64), 0.0)
     w = ok.astype(np.float64)
     n = w.sum(axis=1)
     nn = np.maximum(n, 1.0)[:, None]
@@ -194,3 +195,32 @@ def loss_fd_gradients(dataset, model, gR, gt, pre=None, h=1e-6, **filt):
             else:
                 g[(slice(None),) + idx] = (L(dataset, a) - L(dataset, b)) / (2 * h)
     return gd, gm
+
+
+def simulate_statistics(scene, model, Tsb, Tbm, dataset, dmask=None, dids=None, dataset_id=0, pre=None,
+                        max_dist=np.inf, point_to_plane=True):
+    """The RCC / MICP-L inner step per pose (tests/embree/correction_rcc.cpp:139-160): simulate
+    the model scan (Points, Normals, Hits) at Tbm[p] (oracle.Scene.simulate), pair it ray by ray
+    with the dataset scan (one [W*H, 3] scan for all poses or [P, W*H, 3] per pose),
+    statistics_p2l / _p2p (statistics.cpp:19-126) in binary64 and Umeyama (optimization.cpp:12-49).
+    Returns (stats dict, R, t, q, per-ray validity [P, W*H])."""
+    Tbm = np.asarray(Tbm, F32).reshape(-1, 8)
+    P = Tbm.shape[0]
+    sim = scene.simulate(model, Tsb, Tbm, attrs=("hits", "points", "normals"))
+    N = sim["hits"].size // P
+    ds = np.asarray(dataset, F32).reshape(-1, N, 3)
+    ds = np.broadcast_to(ds, (P, N, 3)) if ds.shape[0] == 1 else ds
+
+    def per_pose(a):
+        if a is None:
+            return None
+        a = np.asarray(a).reshape(-1, N)
+        return np.broadcast_to(a, (P, N)) if a.shape[0] == 1 else a
+
+    D, M, ok = correspondences(ds, sim["points"].reshape(P, N, 3), pre, dmask=per_pose(dmask),
+                               mmask=sim["hits"].reshape(P, N), dids=per_pose(dids), dataset_id=dataset_id,
+                               max_dist=max_dist,
+                               normals=sim["normals"].reshape(P, N, 3) if point_to_plane else None)
+    st = stats(D, M, ok)
+    R, t, q = umeyama(st)
+    return st, R, t, q, ok

@@ -121,6 +121,10 @@ class ConstraintsC(C.Structure):
     _fields_ = [("max_dist", C.c_float), ("dataset_id", C.c_uint32), ("model_id", C.c_uint32)]
 
 
+class ScanC(C.Structure):
+    _fields_ = [("points", C.c_void_p), ("mask", C.c_void_p), ("ids", C.c_void_p), ("per_pose", C.c_uint32)]
+
+
 RMG_NOALLOC_MAX_FACES = 65536
 
 # name -> (restype, argtypes); every symbol include/rmg.h declares
@@ -153,6 +157,9 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_statistics_p2l": (C.c_int, [_P, _U32, _P, _P, _P, _P, _P, _P, _P, C.POINTER(ConstraintsC), _U32, _U32,
                                      _P, _P, _P]),
     "rmg_umeyama_transform": (C.c_int, [_P, _U32, _P, _P]),
+    "rmg_simulate_statistics": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(ScanC), _P, _U32,
+                                          C.POINTER(ConstraintsC), C.c_int, _P, _P, _P]),
+    "rmg_transforms_compose": (C.c_int, [_P, _U32, _P, _U32, _P, _U32, _P]),
     "rmg_batch_default_config": (C.c_int, [C.POINTER(BatchConfigC)]),
     "rmg_batch_create": (C.c_int, [_P, C.POINTER(BatchEntryC), _U32, C.POINTER(_P)]),
     "rmg_batch_set_config": (C.c_int, [_P, C.POINTER(BatchConfigC)]),

@@ -25,6 +25,7 @@
 
 #include "internal.h"
 #include "linalg.cuh"
+#include "stats.cuh"
 
 namespace rmg {
 namespace {
@@ -59,12 +60,6 @@ __device__ __forceinline__ Tf batch_pre(const StatsParams& P, uint32_t b) {
   return load_tf(P.pre[P.pre_stride ? b : 0]);
 }
 
-// Transform * Vector3 = R * v + t (Transform.tcc:56-60), exact order.
-__device__ __forceinline__ V tf_point(const Tf& T, const V& p) {
-  const V r = qrot(T.R, p);
-  return V{add(r.x, T.t.x), add(r.y, T.t.y), add(r.z, T.t.z)};
-}
-
 // PRE = false: no pre-transform (rotating by the identity quaternion is exact, so
 // skipping it changes no bit).
 template <bool P2L, bool PRE = true>
@@ -75,18 +70,7 @@ __device__ __forceinline__ bool correspondence(const StatsParams& P, const Tf& p
   if (P.dids && P.dids[i] != P.dataset_id) return false;
   if (P.mids && P.mids[i] != P.model_id) return false;
   D = PRE ? tf_point(pre, dpt) : dpt;
-  if (P2L) {
-    const V diff{sub(mpt.x, D.x), sub(mpt.y, D.y), sub(mpt.z, D.z)};
-    const float sd = add(add(mul(diff.x, npt.x), mul(diff.y, npt.y)), mul(diff.z, npt.z));
-    if (!(fabsf(sd) < P.max_dist)) return false;
-    M = V{add(D.x, mul(npt.x, sd)), add(D.y, mul(npt.y, sd)), add(D.z, mul(npt.z, sd))};
-  } else {
-    M = mpt;
-    const V diff{sub(M.x, D.x), sub(M.y, D.y), sub(M.z, D.z)};
-    const float d2 = add(add(mul(diff.x, diff.x), mul(diff.y, diff.y)), mul(diff.z, diff.z));
-    if (!(d2 < mul(P.max_dist, P.max_dist))) return false;
-  }
-  return true;
+  return match<P2L>(D, mpt, npt, P.max_dist, M);
 }
 
 struct FAcc {
@@ -144,15 +128,7 @@ __device__ void finalize(const StatsParams& P, uint32_t b, const double* acc, co
     dm[0] = (double)sd.x + ds[0]; dm[1] = (double)sd.y + ds[1]; dm[2] = (double)sd.z + ds[2];
     mm[0] = (double)sm.x + ms[0]; mm[1] = (double)sm.y + ms[1]; mm[2] = (double)sm.z + ms[2];
   }
-  if (P.stats) {
-    rmg_cross_stats s;
-    s.dataset_mean = rmg_vec3{(float)dm[0], (float)dm[1], (float)dm[2]};
-    s.model_mean = rmg_vec3{(float)mm[0], (float)mm[1], (float)mm[2]};
-    for (int r = 0; r < 3; ++r)
-      for (int c = 0; c < 3; ++c) s.covariance.data[3 * c + r] = (float)C[3 * r + c];
-    s.n_meas = (uint32_t)n;
-    P.stats[b] = s;
-  }
+  if (P.stats) store_cross_stats(n, dm, mm, C, P.stats + b);
   if (P.dstats) {
     double* o = P.dstats + 16ull * b;
     for (int k = 0; k < 3; ++k) { o[k] = dm[k]; o[3 + k] = mm[k]; }
@@ -259,14 +235,6 @@ __global__ void __launch_bounds__(kStatsThreads, 3) k_stats(const StatsParams P)
   tot[threadIdx.x] = s;
   __syncwarp(0xffffu);
   if (threadIdx.x == 0) finalize(P, b, tot, sd, sm);
-}
-
-__device__ __forceinline__ void store_tf(rmg_transform* out, const double q[4], const double t[3]) {
-  rmg_transform T;
-  T.R = rmg_quat{(float)q[0], (float)q[1], (float)q[2], (float)q[3]};
-  T.t = rmg_vec3{(float)t[0], (float)t[1], (float)t[2]};
-  T.stamp = 0;
-  *out = T;
 }
 
 __global__ void k_umeyama_dstats(const double* dstats, uint32_t n, rmg_transform* out) {

@@ -315,6 +315,33 @@ struct TraceParams {
 
 constexpr int kFullStack = 32;
 
+// Hit point in the sensor frame: dir_s * t (+ orig_s for per-ray origins),
+// SphereSimulatorEmbree.tcc:127-133 / O1DnSimulatorEmbree.tcc:132.
+template <int OK>
+__device__ __forceinline__ V hit_point(const V& dir_s, const V& orig_s, float t) {
+  V p{mul(dir_s.x, t), mul(dir_s.y, t), mul(dir_s.z, t)};
+  if (OK != ORIGIN_POSE) { p.x = add(p.x, orig_s.x); p.y = add(p.y, orig_s.y); p.z = add(p.z, orig_s.z); }
+  return p;
+}
+
+// Unit face normal of the hit triangle in the sensor frame, flipped to face
+// the ray (EmbreeMesh.cpp:275-295 + SphereSimulatorEmbree.tcc:136-156).
+__device__ __forceinline__ V hit_normal(const DeviceMap& map, const Hit& h, const V& dir_s, const Tf& Tsm) {
+  const Tri* tp = map.tris + h.tri;
+  const float4 p0 = __ldg(&tp->v0), p1 = __ldg(&tp->v1), p2 = __ldg(&tp->v2);
+  const V e1{sub(p1.x, p0.x), sub(p1.y, p0.y), sub(p1.z, p0.z)};
+  const V e2{sub(p2.x, p0.x), sub(p2.y, p0.y), sub(p2.z, p0.z)};
+  V n{sub(mul(e1.y, e2.z), mul(e1.z, e2.y)), sub(mul(e1.z, e2.x), mul(e1.x, e2.z)),
+      sub(mul(e1.x, e2.y), mul(e1.y, e2.x))};
+  float len = __fsqrt_rn(add(add(mul(n.x, n.x), mul(n.y, n.y)), mul(n.z, n.z)));
+  n = V{__fdiv_rn(n.x, len), __fdiv_rn(n.y, len), __fdiv_rn(n.z, len)};
+  n = qrot(qconj(Tsm.R), n);
+  const float dp = add(add(mul(dir_s.x, n.x), mul(dir_s.y, n.y)), mul(dir_s.z, n.z));
+  if (dp > 0.0f) n = V{-n.x, -n.y, -n.z};
+  len = __fsqrt_rn(add(add(mul(n.x, n.x), mul(n.y, n.y)), mul(n.z, n.z)));
+  return V{__fdiv_rn(n.x, len), __fdiv_rn(n.y, len), __fdiv_rn(n.z, len)};
+}
+
 // Writes all requested attributes of one ray (SphereSimulatorEmbree.tcc:104-249).
 template <int OK>
 __device__ __forceinline__ void write_attributes(const TraceParams& P, uint64_t gid, const Hit& h,
@@ -326,26 +353,14 @@ __device__ __forceinline__ void write_attributes(const TraceParams& P, uint64_t 
     if (out.hits) out.hits[gid] = t >= rmin ? 1 : 0;
     if (out.ranges) out.ranges[gid] = t;
     if (out.points) {
-      V p{mul(dir_s.x, t), mul(dir_s.y, t), mul(dir_s.z, t)};
-      if (OK != ORIGIN_POSE) { p.x = add(p.x, orig_s.x); p.y = add(p.y, orig_s.y); p.z = add(p.z, orig_s.z); }
+      const V p = hit_point<OK>(dir_s, orig_s, t);
       float* po = reinterpret_cast<float*>(out.points) + 3 * gid;
       po[0] = p.x; po[1] = p.y; po[2] = p.z;
     }
     if (out.normals) {
-      const Tri* tp = P.map.tris + h.tri;
-      const float4 p0 = __ldg(&tp->v0), p1 = __ldg(&tp->v1), p2 = __ldg(&tp->v2);
-      const V e1{sub(p1.x, p0.x), sub(p1.y, p0.y), sub(p1.z, p0.z)};
-      const V e2{sub(p2.x, p0.x), sub(p2.y, p0.y), sub(p2.z, p0.z)};
-      V n{sub(mul(e1.y, e2.z), mul(e1.z, e2.y)), sub(mul(e1.z, e2.x), mul(e1.x, e2.z)),
-          sub(mul(e1.x, e2.y), mul(e1.y, e2.x))};
-      float len = __fsqrt_rn(add(add(mul(n.x, n.x), mul(n.y, n.y)), mul(n.z, n.z)));
-      n = V{__fdiv_rn(n.x, len), __fdiv_rn(n.y, len), __fdiv_rn(n.z, len)};
-      n = qrot(qconj(Tsm.R), n);
-      const float dp = add(add(mul(dir_s.x, n.x), mul(dir_s.y, n.y)), mul(dir_s.z, n.z));
-      if (dp > 0.0f) n = V{-n.x, -n.y, -n.z};
-      len = __fsqrt_rn(add(add(mul(n.x, n.x), mul(n.y, n.y)), mul(n.z, n.z)));
+      const V n = hit_normal(P.map, h, dir_s, Tsm);
       float* no = reinterpret_cast<float*>(out.normals) + 3 * gid;
-      no[0] = __fdiv_rn(n.x, len); no[1] = __fdiv_rn(n.y, len); no[2] = __fdiv_rn(n.z, len);
+      no[0] = n.x; no[1] = n.y; no[2] = n.z;
     }
     if (out.face_ids) out.face_ids[gid] = h.face;
     if (out.geom_ids) out.geom_ids[gid] = 0u;

@@ -307,6 +307,43 @@ class _Simulator:
                                      C.byref(self.launch_config), stream)
         L.check(st, "rmg_simulate")
 
+    def simulate_statistics(self, Tbm, dataset_points, dataset_mask=None, dataset_ids=None, pre=None,
+                            params=None, point_to_plane: bool = True, want_stats: bool = True,
+                            want_transforms: bool = True):
+        """Fused simulate -> statistics_p2l (or _p2p) -> umeyama_transform for every pose in Tbm:
+        the model scan is cast at Tbm[p] and paired ray by ray with the dataset scan, without
+        writing Points/Normals (rmg_simulate_statistics).  dataset_points is [W*H, 3] (one scan
+        for every pose) or [n, W*H, 3] (one per pose), in the sensor frame and ray order of
+        simulate(); dataset_mask (e.g. the scan's hits) and dataset_ids follow its shape.  pre is
+        one transform or one per pose.  Returns (stats [n,16] or None, transforms [n,8] or None)
+        on the device, asynchronously on the current stream."""
+        from . import statistics as S
+
+        self._check_ready()
+        Tbm = S._dev(Tbm, torch.float32).reshape(-1, 8)
+        n = Tbm.shape[0]
+        W, H = self.sensor.width, self.sensor.height
+        dp = S._dev(dataset_points, torch.float32)
+        per_pose = dp.dim() == 3
+        if dp.shape[-2:] != (W * H, 3) or (per_pose and dp.shape[0] != n):
+            raise L.RmgError(L.RMG_ERR_INVALID_ARG, "simulate_statistics",
+                             f"dataset points {tuple(dp.shape)} do not match {n} poses x {W * H} rays")
+        dm, di = S._u8(dataset_mask), S._i32(dataset_ids)
+        for name, t in (("mask", dm), ("ids", di)):
+            if t is not None and t.numel() != dp.numel() // 3:
+                raise L.RmgError(L.RMG_ERR_INVALID_ARG, "simulate_statistics", f"dataset {name} size mismatch")
+        pre_t, stride = S._pre(pre, n)
+        params = params or S.UmeyamaReductionConstraints()
+        stats = torch.empty((n, 16), dtype=torch.float32, device="cuda") if want_stats else None
+        T = torch.empty((n, 8), dtype=torch.float32, device="cuda") if want_transforms else None
+        scan = L.ScanC(dp.data_ptr(), None if dm is None else dm.data_ptr(), None if di is None else di.data_ptr(),
+                       1 if per_pose else 0)
+        pc = params.to_c()
+        L.call("rmg_simulate_statistics", self._map.handle, self.sensor.handle, C.byref(self._Tsb),
+               C.c_void_p(Tbm.data_ptr()), n, C.byref(scan), _ptr(pre_t), stride, C.byref(pc),
+               1 if point_to_plane else 0, _ptr(stats), _ptr(T), _stream_ptr())
+        return stats, T
+
     def _simulate_host(self, Tbm: torch.Tensor, bundle: Bundle, n: int) -> Bundle:
         """Host bundle: the poses are split into chunks; chunk k is simulated into device
         staging memory on the current stream while chunk k-1 is copied back to the host on a

@@ -21,3 +21,24 @@ def test_work_per_ray_constants(name):
     want = bench.WORK_PER_RAY[name]
     assert abs(v.mean() - want["nodes"]) / want["nodes"] < 0.03
     assert abs(t.mean() - want["tris"]) / want["tris"] < 0.05
+
+
+def test_rcc_fused_work_constants():
+    """rcc_fused casts only rays whose dataset point is valid (a hit at the true pose); its
+    constants average node visits / triangle tests at the estimates over all sensor rays."""
+    sc, model, true, est = bench.rcc_workload(1000)
+    W, H = oracle.model_size(model)
+    n = true.shape[0] * W * H
+    rng = np.random.default_rng(1)
+    gids = np.sort(rng.choice(n, 40000, replace=False)).astype(np.uint64)
+    scene = oracle.Scene(sc.vertices, sc.faces)
+    lbvh = oracle.CanonicalLbvh(sc.vertices, sc.faces)
+    o, d = scene.rays(model, IDENT, true, gids)
+    _, _, t, f = lbvh.count(o, d, model.range.max)
+    valid = (f != 0xFFFFFFFF) & (t >= model.range.min)
+    o, d = scene.rays(model, IDENT, est, gids)
+    v, tt, _, _ = lbvh.count(o, d, model.range.max)
+    want = bench.WORK_PER_RAY["rcc_fused"]
+    assert abs(valid.mean() - want["data_frac"]) < 0.01
+    assert abs(np.where(valid, v, 0).mean() - want["nodes"]) / want["nodes"] < 0.03
+    assert abs(np.where(valid, tt, 0).mean() - want["tris"]) / want["tris"] < 0.05
