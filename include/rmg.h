@@ -335,6 +335,60 @@ int rmg_umeyama_backward(const rmg_transform* pre_transforms, uint32_t pre_trans
                          rmg_vec3* grad_dataset, rmg_vec3* grad_model, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Scenes: several meshes and instances of them (two-level BVH).
+ *
+ * Replaces EmbreeScene::add / commit with EmbreeInstance::set / setTransform /
+ * setScale / apply (EmbreeScene.cpp:246-406, EmbreeInstance.cpp:33-60,
+ * EmbreeGeometry.cpp) and OptixScene's instance hierarchy (OptixScene.cpp:
+ * 396-481).  Each instance places one geometry (an rmg_map, the bottom-level
+ * tree, which the scene references and does not own) in the map frame with
+ * x_map = T * (scale (.) x_mesh), EmbreeInstance::apply's M = T * diag(scale).
+ * The scene builds a top-level LBVH over the instances' map-frame boxes.
+ *
+ * Hits report, as the reference's IntAttrAll does for instanced scenes
+ * (SphereSimulatorEmbree.tcc:160-186, SensorProgramHit.cu:220-262):
+ * face_ids = the triangle's index in its own mesh, geom_ids / object_ids =
+ * the instance's geom_id / object_id fields.  A binding that mirrors rmagine
+ * sets object_id = the instance's id in the top-level scene and geom_id = the
+ * mesh's id inside the instanced scene; for a mesh added to the scene without
+ * an instance both are the mesh's id (and T = identity, scale = 1).
+ * Normals are the hit triangle's normal taken to the map frame by the
+ * instance (R * scale^-1 (.) n, the OptiX path's
+ * optixTransformNormalFromObjectToWorldSpace, SensorProgramHit.cu:120-136),
+ * then to the sensor frame as for a single mesh.
+ * The closest hit over all instances wins; equal ranges go to the smaller
+ * instance index, then the smaller face index. */
+typedef struct rmg_scene rmg_scene;  /* opaque */
+
+typedef struct rmg_instance_desc {
+  uint32_t geometry;   /* index into the scene's geometry list */
+  uint32_t geom_id;    /* reported in GeomIds for hits on this instance */
+  uint32_t object_id;  /* reported in ObjectIds */
+  rmg_transform T;     /* instance pose in the map frame */
+  rmg_vec3 scale;      /* per-axis scale applied before T; no component may be 0 */
+} rmg_instance_desc;
+
+/* geometries: HOST array of n_geometries map handles (each built with
+ * rmg_map_build, tree depth <= 32, alive as long as the scene);
+ * instances: HOST array.  Builds the top-level tree on `stream` and
+ * synchronises with it.  n_instances == 0 gives a scene where every ray misses. */
+int rmg_scene_create(const rmg_map* const* geometries, uint32_t n_geometries,
+                     const rmg_instance_desc* instances, uint32_t n_instances, void* stream, rmg_scene** out);
+/* New instance poses, scales or ids (same count).  rebuild == 0 refits the
+ * top-level tree in place (rmg_map_refit's semantics: fast, topology kept);
+ * rebuild != 0 builds it anew.  Call it too after rmg_map_refit of a geometry
+ * (its bounds changed).  Needs exclusive use of the scene; synchronises. */
+int rmg_scene_update(rmg_scene* scene, const rmg_instance_desc* instances, uint32_t n_instances, int rebuild,
+                     void* stream);
+int rmg_scene_destroy(rmg_scene* scene);
+/* Device error word of the scene (RMG_ERR_TRAVERSAL_BUDGET after a corrupt
+ * tree), like rmg_map_status; synchronises. */
+int rmg_scene_status(rmg_scene* scene, int clear);
+/* rmg_simulate on a scene: same sensors, poses, outputs and semantics. */
+int rmg_simulate_scene(const rmg_scene* scene, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                       const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Fused simulate -> statistics (the inner step of the RCC / MICP-L correction
  * loop, tests/embree/correction_rcc.cpp:139-160).
  *

@@ -7,8 +7,8 @@ from ._lib import RmgError, load  # noqa: F401
 from .sensors import (DiscreteInterval, Interval, O1DnModel, OnDnModel, PinholeModel,  # noqa: F401
                       SphericalModel, depth_camera, example_o1dn, example_ondn, example_pinhole,
                       example_spherical, ouster_like, vlp16_360, vlp16_900)
-from .simulation import (ATTRIBUTES, Bundle, IntAttrAll, Map, O1DnSimulator,  # noqa: F401
-                         OnDnSimulator, PinholeSimulator, Sensor, SphereSimulator,
+from .simulation import (ATTRIBUTES, Bundle, Instance, IntAttrAll, Map, O1DnSimulator,  # noqa: F401
+                         OnDnSimulator, PinholeSimulator, Scene, Sensor, SphereSimulator,
                          identity_transforms, launch_config, make_simulator, make_transforms,
                          resize_memory_bundle)
 

@@ -121,6 +121,11 @@ class ConstraintsC(C.Structure):
     _fields_ = [("max_dist", C.c_float), ("dataset_id", C.c_uint32), ("model_id", C.c_uint32)]
 
 
+class InstanceDescC(C.Structure):
+    _fields_ = [("geometry", C.c_uint32), ("geom_id", C.c_uint32), ("object_id", C.c_uint32), ("T", TransformC),
+                ("scale", C.c_float * 3)]
+
+
 class ScanC(C.Structure):
     _fields_ = [("points", C.c_void_p), ("mask", C.c_void_p), ("ids", C.c_void_p), ("per_pose", C.c_uint32)]
 
@@ -160,6 +165,11 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_simulate_statistics": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(ScanC), _P, _U32,
                                           C.POINTER(ConstraintsC), C.c_int, _P, _P, _P]),
     "rmg_transforms_compose": (C.c_int, [_P, _U32, _P, _U32, _P, _U32, _P]),
+    "rmg_scene_create": (C.c_int, [_P, _U32, _P, _U32, _P, C.POINTER(_P)]),
+    "rmg_scene_update": (C.c_int, [_P, _P, _U32, C.c_int, _P]),
+    "rmg_scene_destroy": (C.c_int, [_P]),
+    "rmg_scene_status": (C.c_int, [_P, C.c_int]),
+    "rmg_simulate_scene": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(OutputsC), _P]),
     "rmg_batch_default_config": (C.c_int, [C.POINTER(BatchConfigC)]),
     "rmg_batch_create": (C.c_int, [_P, C.POINTER(BatchEntryC), _U32, C.POINTER(_P)]),
     "rmg_batch_set_config": (C.c_int, [_P, C.POINTER(BatchConfigC)]),

@@ -1,0 +1,492 @@
+// Scenes: instances of several meshes under a top-level LBVH (two-level BVH).
+//
+// Replaces the instance hierarchy of rmagine's Embree / OptiX maps
+// (EmbreeScene.cpp:246-406, EmbreeInstance.cpp:33-60, OptixScene.cpp:396-481)
+// for the simulators.  Bottom level: each geometry is an ordinary rmg_map (its
+// LBVH and packed triangles), shared by every instance that places it.  Top
+// level: an LBVH over the instances' map-frame boxes, built by the same device
+// builder as a mesh -- instance i is handed to it as the degenerate triangle
+// (lo_i, hi_i, centre_i), whose bounds are exactly the box and whose centroid
+// is the box centre -- so rmg_map_refit of that tree is the dynamic-scene
+// update.  Leaf k of the top tree is the k-th live instance (face id k).
+//
+// Traversal (k_trace_scene): the top tree is walked with a full stack; at an
+// instance leaf the ray is taken into the instance's mesh frame,
+//     o_l = s^-1 (.) R^T (o - t),   d_l = s^-1 (.) R^T d   (R^T as conj(q) sandwich),
+// which keeps the ray parameter t, and the geometry's tree is walked by the
+// plain kernel's RayTrav with tfar = the best range so far.  A hit replaces
+// the best when its range is smaller, or equal with a smaller instance index;
+// within one mesh equal ranges already go to the smaller face index, so the
+// result is the lexicographic minimum (t, instance, face) over all hits,
+// independent of the visiting order.  Both trees must be at most 32 levels deep
+// (checked at creation; the stack guards turn a corrupt tree into
+// RMG_ERR_TRAVERSAL_BUDGET in the scene's status word).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+#include "trace.cuh"
+
+struct rmg_scene;
+
+namespace rmg {
+namespace {
+
+struct InstDev {
+  float4 qinv;   // conj(q): map -> mesh rotation
+  float4 t;      // translation (w unused)
+  float4 inv_s;  // 1 / scale per axis (w unused)
+  float4 q;      // mesh -> map rotation (normals)
+  uint4 ids;     // geometry, geom_id, object_id, instance index
+};
+
+struct GeomDev {
+  const Node* nodes;
+  const Tri* tris;
+  int root;
+  unsigned budget;
+};
+
+struct SceneParams {
+  TraceParams T;  // T.map: the top-level tree, status = the scene's word
+  const InstDev* inst;
+  const GeomDev* geoms;
+};
+
+struct Best {
+  float t;
+  int tri;        // packed triangle index in the hit geometry, -1 = none
+  uint32_t face;
+  int inst;       // live-instance slot
+  uint32_t order; // instance index (tie-break)
+};
+
+__device__ __forceinline__ void instance_hit(const SceneParams& S, int k, const V& o, const V& d, Best& best,
+                                             bool& over) {
+  const uint32_t slot = __float_as_uint(__ldg(&S.T.map.tris[k].v0.w));
+  const InstDev* ip = S.inst + slot;
+  const float4 qi = __ldg(&ip->qinv), tt = __ldg(&ip->t), is = __ldg(&ip->inv_s);
+  const uint4 ids = __ldg(&ip->ids);
+  const Q qinv{qi.x, qi.y, qi.z, qi.w};
+  const V rl = qrot(qinv, V{sub(o.x, tt.x), sub(o.y, tt.y), sub(o.z, tt.z)});
+  const V ol{mul(rl.x, is.x), mul(rl.y, is.y), mul(rl.z, is.z)};
+  const V rd = qrot(qinv, d);
+  const V dl{mul(rd.x, is.x), mul(rd.y, is.y), mul(rd.z, is.z)};
+  const GeomDev* gp = S.geoms + ids.x;
+  DeviceMap bm;
+  bm.nodes = reinterpret_cast<const Node*>(__ldg(reinterpret_cast<const unsigned long long*>(&gp->nodes)));
+  bm.tris = reinterpret_cast<const Tri*>(__ldg(reinterpret_cast<const unsigned long long*>(&gp->tris)));
+  bm.root = __ldg(&gp->root);
+  bm.n_nodes = 0;
+  bm.n_tris = 0;
+  bm.status = S.T.map.status;
+  const unsigned budget = __ldg(&gp->budget);
+  RayTrav<kFullStack, 0> r;
+  ShortStack<kFullStack> stack;
+  if (!r.init(bm, ol, dl, best.t)) return;
+  while (!r.step(bm, budget, stack)) {
+  }
+  if (r.over) { over = true; return; }
+  if (r.h.tri < 0) return;
+  if (r.h.t < best.t || best.inst < 0 || ids.w < best.order) {
+    best.t = r.h.t;
+    best.tri = r.h.tri;
+    best.face = r.h.face;
+    best.inst = (int)slot;
+    best.order = ids.w;
+  }
+}
+
+// Top-level walk with a full stack (depth <= 32 checked at creation; the guard
+// below only fires on a corrupt tree).
+__device__ __forceinline__ void trace_scene(const SceneParams& S, const V& o, const V& d, float tfar, Best& best,
+                                            bool& over) {
+  best.t = tfar;
+  best.tri = -1;
+  best.face = 0xffffffffu;
+  best.inst = -1;
+  best.order = 0xffffffffu;
+  const DeviceMap& tl = S.T.map;
+  if (tl.root < 0) return;
+  const RayBox rb = make_raybox(o, d);
+  int stk_node[kFullStack];
+  float stk_t[kFullStack];
+  int sp = 0;
+  int node = tl.root;
+  unsigned steps = 0;
+  while (true) {
+    if (++steps > S.T.budget) { over = true; break; }
+    const Node* np = tl.nodes + node;
+    const float4 a = __ldg(&np->a), b = __ldg(&np->b), c = __ldg(&np->c);
+    const int4 ln = __ldg(&np->d);
+    float tminL, tmaxL, tminR, tmaxR;
+    slab(rb, a.x, a.y, a.z, a.w, c.x, c.y, tminL, tmaxL);
+    slab(rb, b.x, b.y, b.z, b.w, c.z, c.w, tminR, tmaxR);
+    bool hitL = visit(tminL, tmaxL, best.t);
+    bool hitR = visit(tminR, tmaxR, best.t);
+    if (hitL && ln.x < 0) { instance_hit(S, ~ln.x, o, d, best, over); hitL = false; }
+    if (hitR && ln.y < 0) { instance_hit(S, ~ln.y, o, d, best, over); hitR = false; }
+    if (over) break;
+    hitL = hitL && tminL <= best.t * kWiden;
+    hitR = hitR && tminR <= best.t * kWiden;
+    if (hitL && hitR) {
+      if (sp >= kFullStack) { over = true; break; }
+      const bool lf = tminL <= tminR;
+      stk_node[sp] = lf ? ln.y : ln.x;
+      stk_t[sp] = lf ? tminR : tminL;
+      ++sp;
+      node = lf ? ln.x : ln.y;
+      continue;
+    }
+    if (hitL || hitR) {
+      node = hitL ? ln.x : ln.y;
+      continue;
+    }
+    bool found = false;
+    while (sp > 0) {
+      --sp;
+      node = stk_node[sp];
+      if (stk_t[sp] <= best.t * kWiden) { found = true; break; }
+    }
+    if (!found) break;
+  }
+  if (over) {
+    best.tri = -1;
+    best.t = tfar;
+    best.face = 0xffffffffu;
+    best.inst = -1;
+  }
+}
+
+#ifndef RMG_SCENE_MIN_BLOCKS
+#define RMG_SCENE_MIN_BLOCKS 4
+#endif
+
+template <int OK>
+__global__ void __launch_bounds__(256, RMG_SCENE_MIN_BLOCKS) k_trace_scene(const SceneParams S) {
+  const TraceParams& P = S.T;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= P.n_tiles) return;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t pose = (uint32_t)(warp / P.tiles_per_pose);
+  const uint32_t r = (uint32_t)(warp - (uint64_t)pose * P.tiles_per_pose);
+  const uint32_t ty = r / P.tiles_x, tx = r - ty * P.tiles_x;
+  const uint32_t tile_w = 1u << P.tile_w_log2;
+  const uint32_t vid = ty * P.tile_h + (lane >> P.tile_w_log2);
+  const uint32_t hid = tx * tile_w + (lane & (tile_w - 1));
+  const uint32_t W = P.sen.width, H = P.sen.height;
+  if (vid >= H || hid >= W) return;
+  const uint32_t loc = vid * W + hid;
+  const uint64_t gid = (uint64_t)pose * W * H + loc;
+
+  const Tf Tsm = tmul(load_tf(P.Tbm[pose]), P.Tsb);
+  V dir_s, orig_s, o, d;
+  setup_ray<OK>(P.sen, Tsm, loc, dir_s, orig_s, o, d);
+  Best best;
+  bool over = false;
+  trace_scene(S, o, d, P.sen.range_max, best, over);
+  if (over) atomicExch(P.map.status, (unsigned)RMG_ERR_TRAVERSAL_BUDGET);
+
+  const rmg_outputs& out = P.out;
+  if (best.tri >= 0) {
+    const float t = best.t;
+    if (out.hits) out.hits[gid] = t >= P.sen.range_min ? 1 : 0;
+    if (out.ranges) out.ranges[gid] = t;
+    if (out.points) {
+      const V p = hit_point<OK>(dir_s, orig_s, t);
+      float* po = reinterpret_cast<float*>(out.points) + 3 * gid;
+      po[0] = p.x; po[1] = p.y; po[2] = p.z;
+    }
+    const InstDev* ip = S.inst + best.inst;
+    if (out.normals) {
+      const uint4 ids = __ldg(&ip->ids);
+      const Tri* tris = reinterpret_cast<const Tri*>(
+          __ldg(reinterpret_cast<const unsigned long long*>(&S.geoms[ids.x].tris)));
+      const V nl = face_normal_unit(tris + best.tri);
+      const float4 is = __ldg(&ip->inv_s), q = __ldg(&ip->q);
+      const V nm = qrot(Q{q.x, q.y, q.z, q.w}, V{mul(nl.x, is.x), mul(nl.y, is.y), mul(nl.z, is.z)});
+      const V n = normal_to_sensor(nm, dir_s, Tsm);
+      float* no = reinterpret_cast<float*>(out.normals) + 3 * gid;
+      no[0] = n.x; no[1] = n.y; no[2] = n.z;
+    }
+    if (out.face_ids) out.face_ids[gid] = best.face;
+    if (out.geom_ids || out.object_ids) {
+      const uint4 ids = __ldg(&ip->ids);
+      if (out.geom_ids) out.geom_ids[gid] = ids.y;
+      if (out.object_ids) out.object_ids[gid] = ids.z;
+    }
+  } else {
+    const float nanf_ = __int_as_float(0x7fc00000);
+    if (out.hits) out.hits[gid] = 0;
+    if (out.ranges) out.ranges[gid] = add(P.sen.range_max, 1.0f);
+    if (out.points) {
+      float* po = reinterpret_cast<float*>(out.points) + 3 * gid;
+      po[0] = nanf_; po[1] = nanf_; po[2] = nanf_;
+    }
+    if (out.normals) {
+      float* no = reinterpret_cast<float*>(out.normals) + 3 * gid;
+      no[0] = nanf_; no[1] = nanf_; no[2] = nanf_;
+    }
+    if (out.face_ids) out.face_ids[gid] = 0xffffffffu;
+    if (out.geom_ids) out.geom_ids[gid] = 0xffffffffu;
+    if (out.object_ids) out.object_ids[gid] = 0xffffffffu;
+  }
+}
+
+}  // namespace
+
+int default_config(const rmg_sensor* s, rmg_launch_config* cfg);
+int make_trace_params(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                      const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
+                      const rmg_launch_config& cfg, TraceParams& P);
+DeviceMap device_view(const rmg_map* m);
+
+}  // namespace rmg
+
+using namespace rmg;
+
+struct rmg_scene {
+  int device = 0;
+  std::vector<const rmg_map*> geoms;
+  uint32_t n_instances = 0;
+  std::vector<uint32_t> live;   // instance index of each top-level leaf
+  rmg_map* tlas = nullptr;      // NULL when no instance is live
+  InstDev* d_inst = nullptr;
+  GeomDev* d_geoms = nullptr;
+  unsigned int* d_status = nullptr;
+};
+
+namespace {
+
+void free_scene(rmg_scene* s) {
+  if (s->tlas) rmg_map_destroy(s->tlas);
+  cudaFree(s->d_inst);
+  cudaFree(s->d_geoms);
+  cudaFree(s->d_status);
+  delete s;
+}
+
+// q (x) p (x) conj(q) in binary64 with the binary32 q as given.
+void qrot_d(const rmg_quat& q, const double p[3], double out[3]) {
+  const double qx = q.x, qy = q.y, qz = q.z, qw = q.w;
+  // a = q * (p, 0)
+  const double ax = qw * p[0] + qy * p[2] - qz * p[1];
+  const double ay = qw * p[1] - qx * p[2] + qz * p[0];
+  const double az = qw * p[2] + qx * p[1] - qy * p[0];
+  const double aw = -qx * p[0] - qy * p[1] - qz * p[2];
+  // a * conj(q)
+  out[0] = -aw * qx + ax * qw - ay * qz + az * qy;
+  out[1] = -aw * qy + ax * qz + ay * qw - az * qx;
+  out[2] = -aw * qz - ax * qy + ay * qx + az * qw;
+}
+
+int check_instances(const rmg_scene* s, const rmg_instance_desc* inst, uint32_t n) {
+  if (n > 0 && !inst) return fail(RMG_ERR_INVALID_ARG, "scene: instances is NULL");
+  if (n > (1u << 24)) return fail(RMG_ERR_INVALID_ARG, "scene: too many instances");
+  for (uint32_t i = 0; i < n; ++i) {
+    const rmg_instance_desc& I = inst[i];
+    if (I.geometry >= s->geoms.size()) return fail(RMG_ERR_INVALID_ARG, "scene: instance geometry index out of range");
+    const float sc[3] = {I.scale.x, I.scale.y, I.scale.z};
+    for (float v : sc)
+      if (!(std::isfinite(v) && v != 0.0f)) return fail(RMG_ERR_INVALID_ARG, "scene: instance scale must be finite and non-zero");
+    const double qn = std::sqrt((double)I.T.R.x * I.T.R.x + (double)I.T.R.y * I.T.R.y + (double)I.T.R.z * I.T.R.z +
+                                (double)I.T.R.w * I.T.R.w);
+    if (!(std::fabs(qn - 1.0) < 1e-3)) return fail(RMG_ERR_INVALID_ARG, "scene: instance rotation is not a unit quaternion");
+    if (!(std::isfinite(I.T.t.x) && std::isfinite(I.T.t.y) && std::isfinite(I.T.t.z)))
+      return fail(RMG_ERR_INVALID_ARG, "scene: instance translation is not finite");
+  }
+  return RMG_OK;
+}
+
+// Map-frame box of every live instance as the top-level "triangles"
+// (lo, hi, centre), padded by 1e-5 of the coordinates' magnitude so that the
+// binary32 ray transform of a hit near the mesh's bounds can never fall outside.
+void instance_boxes(const rmg_scene* s, const rmg_instance_desc* inst, uint32_t n, std::vector<uint32_t>& live,
+                    std::vector<rmg_vec3>& verts, std::vector<rmg_face>& faces, std::vector<InstDev>& rec) {
+  live.clear();
+  verts.clear();
+  faces.clear();
+  rec.clear();
+  for (uint32_t i = 0; i < n; ++i) {
+    const rmg_instance_desc& I = inst[i];
+    const rmg_map* g = s->geoms[I.geometry];
+    if (g->n_faces == 0) continue;
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    double mag = 1.0;
+    for (int c = 0; c < 8; ++c) {
+      const double p[3] = {(double)I.scale.x * ((c & 1) ? g->hi[0] : g->lo[0]),
+                           (double)I.scale.y * ((c & 2) ? g->hi[1] : g->lo[1]),
+                           (double)I.scale.z * ((c & 4) ? g->hi[2] : g->lo[2])};
+      double w[3];
+      qrot_d(I.T.R, p, w);
+      w[0] += I.T.t.x; w[1] += I.T.t.y; w[2] += I.T.t.z;
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = std::min(lo[k], w[k]);
+        hi[k] = std::max(hi[k], w[k]);
+        mag = std::max(mag, std::fabs(w[k]));
+      }
+    }
+    const double pad = 1e-5 * mag;
+    rmg_vec3 vlo, vhi, vc;
+    float* fl = &vlo.x;
+    float* fh = &vhi.x;
+    float* fc = &vc.x;
+    for (int k = 0; k < 3; ++k) {
+      fl[k] = std::nextafter((float)(lo[k] - pad), -INFINITY);
+      fh[k] = std::nextafter((float)(hi[k] + pad), INFINITY);
+      fc[k] = (float)(0.5 * ((double)fl[k] + (double)fh[k]));
+    }
+    const uint32_t b = (uint32_t)verts.size();
+    verts.push_back(vlo);
+    verts.push_back(vhi);
+    verts.push_back(vc);
+    faces.push_back(rmg_face{b, b + 1, b + 2});
+    InstDev r;
+    r.qinv = make_float4(-I.T.R.x, -I.T.R.y, -I.T.R.z, I.T.R.w);
+    r.t = make_float4(I.T.t.x, I.T.t.y, I.T.t.z, 0.0f);
+    r.inv_s = make_float4(1.0f / I.scale.x, 1.0f / I.scale.y, 1.0f / I.scale.z, 0.0f);
+    r.q = make_float4(I.T.R.x, I.T.R.y, I.T.R.z, I.T.R.w);
+    r.ids = make_uint4(I.geometry, I.geom_id, I.object_id, i);
+    rec.push_back(r);
+    live.push_back(i);
+  }
+}
+
+int upload_instances(rmg_scene* s, const std::vector<InstDev>& rec, cudaStream_t st) {
+  cudaFree(s->d_inst);
+  s->d_inst = nullptr;
+  if (rec.empty()) return RMG_OK;
+  int r = dev_alloc(&s->d_inst, rec.size(), "scene instances");
+  if (r != RMG_OK) return r;
+  RMG_CUDA_TRY(cudaMemcpyAsync(s->d_inst, rec.data(), sizeof(InstDev) * rec.size(), cudaMemcpyHostToDevice, st));
+  return RMG_OK;
+}
+
+int build_top(rmg_scene* s, const rmg_instance_desc* inst, uint32_t n, bool rebuild, cudaStream_t st) {
+  std::vector<uint32_t> live;
+  std::vector<rmg_vec3> verts;
+  std::vector<rmg_face> faces;
+  std::vector<InstDev> rec;
+  instance_boxes(s, inst, n, live, verts, faces, rec);
+  int r = RMG_OK;
+  const bool same = s->tlas && live.size() == s->live.size() && !live.empty();
+  if (!rebuild && same) {
+    r = rmg_map_refit(s->tlas, verts.data(), (uint32_t)verts.size(), st);
+  } else {
+    if (s->tlas) { rmg_map_destroy(s->tlas); s->tlas = nullptr; }
+    if (!live.empty()) {
+      r = rmg_map_build(verts.data(), (uint32_t)verts.size(), faces.data(), (uint32_t)faces.size(), st, &s->tlas);
+      if (r == RMG_OK && s->tlas->depth > (unsigned)kFullStack)
+        r = fail(RMG_ERR_UNSUPPORTED, "scene: top-level tree deeper than 32 levels");
+    }
+  }
+  if (r != RMG_OK) return r;
+  r = upload_instances(s, rec, st);
+  if (r != RMG_OK) return r;
+  RMG_CUDA_TRY(cudaStreamSynchronize(st));
+  s->live = live;
+  s->n_instances = n;
+  return RMG_OK;
+}
+
+}  // namespace
+
+extern "C" int rmg_scene_create(const rmg_map* const* geometries, uint32_t n_geometries,
+                                const rmg_instance_desc* instances, uint32_t n_instances, void* stream,
+                                rmg_scene** out) {
+  if (!out) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_create: out is NULL");
+  *out = nullptr;
+  if (n_geometries > 0 && !geometries) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_create: geometries is NULL");
+  rmg_scene* s = new (std::nothrow) rmg_scene;
+  if (!s) return fail(RMG_ERR_OOM, "rmg_scene_create: host allocation");
+  cudaGetDevice(&s->device);
+  for (uint32_t g = 0; g < n_geometries; ++g) {
+    if (!geometries[g]) { delete s; return fail(RMG_ERR_INVALID_ARG, "rmg_scene_create: NULL geometry"); }
+    if (geometries[g]->n_faces > 0 && geometries[g]->depth > (unsigned)kFullStack) {
+      delete s;
+      return fail(RMG_ERR_UNSUPPORTED, "rmg_scene_create: a geometry's tree is deeper than 32 levels");
+    }
+    s->geoms.push_back(geometries[g]);
+  }
+  int r = check_instances(s, instances, n_instances);
+  if (r != RMG_OK) { delete s; return r; }
+  cudaStream_t st = as_stream(stream);
+  r = dev_alloc(&s->d_status, 1, "scene status");
+  if (r == RMG_OK) r = cuda_status(cudaMemsetAsync(s->d_status, 0, 4, st), "memset");
+  if (r == RMG_OK && n_geometries > 0) {
+    std::vector<GeomDev> g(n_geometries);
+    for (uint32_t i = 0; i < n_geometries; ++i) {
+      const DeviceMap dm = device_view(geometries[i]);
+      g[i] = GeomDev{dm.nodes, dm.tris, dm.root, 2u * geometries[i]->n_nodes + 64u};
+    }
+    r = dev_alloc(&s->d_geoms, n_geometries, "scene geometries");
+    if (r == RMG_OK)
+      r = cuda_status(cudaMemcpyAsync(s->d_geoms, g.data(), sizeof(GeomDev) * n_geometries, cudaMemcpyHostToDevice, st),
+                      "copy geometries");
+  }
+  if (r == RMG_OK) r = build_top(s, instances, n_instances, true, st);
+  if (r != RMG_OK) { free_scene(s); return r; }
+  *out = s;
+  return RMG_OK;
+}
+
+extern "C" int rmg_scene_update(rmg_scene* s, const rmg_instance_desc* instances, uint32_t n_instances, int rebuild,
+                                void* stream) {
+  if (!s) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_update: scene is NULL");
+  if (n_instances != s->n_instances) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_update: instance count differs");
+  int r = check_instances(s, instances, n_instances);
+  if (r != RMG_OK) return r;
+  return build_top(s, instances, n_instances, rebuild != 0, as_stream(stream));
+}
+
+extern "C" int rmg_scene_destroy(rmg_scene* s) {
+  if (!s) return RMG_OK;
+  free_scene(s);
+  return RMG_OK;
+}
+
+extern "C" int rmg_scene_status(rmg_scene* s, int clear) {
+  if (!s) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_status: scene is NULL");
+  unsigned int word = 0;
+  RMG_CUDA_TRY(cudaMemcpy(&word, s->d_status, 4, cudaMemcpyDeviceToHost));
+  if (clear) RMG_CUDA_TRY(cudaMemset(s->d_status, 0, 4));
+  if (word != 0) {
+    set_error("a kernel recorded a device error on this scene");
+    return (int)word;
+  }
+  return RMG_OK;
+}
+
+extern "C" int rmg_simulate_scene(const rmg_scene* s, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                                  const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out, void* stream) {
+  if (!s || !sensor || !Tsb || !out)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene: NULL scene, sensor, Tsb or outputs");
+  if (n_poses == 0) return RMG_OK;
+  if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene: Tbm is NULL");
+  if (!out->hits && !out->ranges && !out->points && !out->normals && !out->face_ids && !out->geom_ids &&
+      !out->object_ids)
+    return RMG_OK;
+  rmg_launch_config cfg;
+  default_config(sensor, &cfg);
+  SceneParams S;
+  // the top-level tree's launch geometry; an empty scene uses a zero-face stand-in view
+  rmg_map empty;
+  std::memset(&empty, 0, sizeof(empty));
+  const rmg_map* top = s->tlas ? s->tlas : &empty;
+  make_trace_params(top, sensor, Tsb, Tbm, n_poses, out, cfg, S.T);
+  S.T.map.status = s->d_status;
+  S.inst = s->d_inst;
+  S.geoms = s->d_geoms;
+  const uint64_t blocks = (S.T.n_tiles + cfg.block_warps - 1) / cfg.block_warps;
+  if (blocks > 0x7fffffffull) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene: too many rays for one launch");
+  const unsigned block = 32u * cfg.block_warps;
+  cudaStream_t st = as_stream(stream);
+  switch (sensor->model.kind) {
+    case RMG_MODEL_SPHERICAL:
+    case RMG_MODEL_PINHOLE: k_trace_scene<ORIGIN_POSE><<<(unsigned)blocks, block, 0, st>>>(S); break;
+    case RMG_MODEL_O1DN: k_trace_scene<ORIGIN_SINGLE><<<(unsigned)blocks, block, 0, st>>>(S); break;
+    default: k_trace_scene<ORIGIN_TABLE><<<(unsigned)blocks, block, 0, st>>>(S); break;
+  }
+  return cuda_status(cudaGetLastError(), "k_trace_scene");
+}

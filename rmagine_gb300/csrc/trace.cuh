@@ -324,22 +324,32 @@ __device__ __forceinline__ V hit_point(const V& dir_s, const V& orig_s, float t)
   return p;
 }
 
-// Unit face normal of the hit triangle in the sensor frame, flipped to face
-// the ray (EmbreeMesh.cpp:275-295 + SphereSimulatorEmbree.tcc:136-156).
-__device__ __forceinline__ V hit_normal(const DeviceMap& map, const Hit& h, const V& dir_s, const Tf& Tsm) {
-  const Tri* tp = map.tris + h.tri;
+// Unit geometric normal e1 x e2 of a packed triangle in its mesh frame
+// (EmbreeMesh.cpp:275-295: Embree's Ng, normalised).
+__device__ __forceinline__ V face_normal_unit(const Tri* tp) {
   const float4 p0 = __ldg(&tp->v0), p1 = __ldg(&tp->v1), p2 = __ldg(&tp->v2);
   const V e1{sub(p1.x, p0.x), sub(p1.y, p0.y), sub(p1.z, p0.z)};
   const V e2{sub(p2.x, p0.x), sub(p2.y, p0.y), sub(p2.z, p0.z)};
-  V n{sub(mul(e1.y, e2.z), mul(e1.z, e2.y)), sub(mul(e1.z, e2.x), mul(e1.x, e2.z)),
-      sub(mul(e1.x, e2.y), mul(e1.y, e2.x))};
-  float len = __fsqrt_rn(add(add(mul(n.x, n.x), mul(n.y, n.y)), mul(n.z, n.z)));
-  n = V{__fdiv_rn(n.x, len), __fdiv_rn(n.y, len), __fdiv_rn(n.z, len)};
-  n = qrot(qconj(Tsm.R), n);
+  const V n{sub(mul(e1.y, e2.z), mul(e1.z, e2.y)), sub(mul(e1.z, e2.x), mul(e1.x, e2.z)),
+            sub(mul(e1.x, e2.y), mul(e1.y, e2.x))};
+  const float len = __fsqrt_rn(add(add(mul(n.x, n.x), mul(n.y, n.y)), mul(n.z, n.z)));
+  return V{__fdiv_rn(n.x, len), __fdiv_rn(n.y, len), __fdiv_rn(n.z, len)};
+}
+
+// Map-frame normal -> sensor frame, flipped to face the ray, normalised
+// (SphereSimulatorEmbree.tcc:136-156).
+__device__ __forceinline__ V normal_to_sensor(const V& n_map, const V& dir_s, const Tf& Tsm) {
+  V n = qrot(qconj(Tsm.R), n_map);
   const float dp = add(add(mul(dir_s.x, n.x), mul(dir_s.y, n.y)), mul(dir_s.z, n.z));
   if (dp > 0.0f) n = V{-n.x, -n.y, -n.z};
-  len = __fsqrt_rn(add(add(mul(n.x, n.x), mul(n.y, n.y)), mul(n.z, n.z)));
+  const float len = __fsqrt_rn(add(add(mul(n.x, n.x), mul(n.y, n.y)), mul(n.z, n.z)));
   return V{__fdiv_rn(n.x, len), __fdiv_rn(n.y, len), __fdiv_rn(n.z, len)};
+}
+
+// Unit face normal of the hit triangle in the sensor frame, flipped to face
+// the ray (EmbreeMesh.cpp:275-295 + SphereSimulatorEmbree.tcc:136-156).
+__device__ __forceinline__ V hit_normal(const DeviceMap& map, const Hit& h, const V& dir_s, const Tf& Tsm) {
+  return normal_to_sensor(face_normal_unit(map.tris + h.tri), dir_s, Tsm);
 }
 
 // Writes all requested attributes of one ray (SphereSimulatorEmbree.tcc:104-249).

@@ -135,6 +135,87 @@ class Map:
             pass
 
 
+class Instance:
+    """One placement of a geometry in a Scene: x_map = T * (scale (.) x_mesh)
+    (EmbreeInstance::setTransform / setScale / apply, EmbreeInstance.cpp:46-60), reporting
+    geom_id / object_id for its hits."""
+
+    def __init__(self, geometry: int, T=None, scale=(1.0, 1.0, 1.0), geom_id: int = 0, object_id: int = 0):
+        self.geometry = int(geometry)
+        self.T = np.array([0, 0, 0, 1, 0, 0, 0, 0], np.float32) if T is None else \
+            np.asarray(T, np.float32).reshape(-1)[:8].copy()
+        if self.T.size == 7:
+            self.T = np.concatenate([self.T, np.zeros(1, np.float32)])
+        self.scale = np.asarray(scale, np.float32).reshape(3).copy()
+        self.geom_id = int(geom_id)
+        self.object_id = int(object_id)
+
+    def to_c(self) -> L.InstanceDescC:
+        d = L.InstanceDescC()
+        d.geometry, d.geom_id, d.object_id = self.geometry, self.geom_id, self.object_id
+        d.T = transform_c(self.T)
+        d.scale[:] = [float(x) for x in self.scale]
+        return d
+
+
+def _instances_c(instances):
+    arr = (L.InstanceDescC * max(1, len(instances)))()
+    for i, inst in enumerate(instances):
+        arr[i] = inst.to_c()
+    return arr
+
+
+class Scene:
+    """Several meshes and instances of them under a top-level tree (rmg_scene): EmbreeScene /
+    OptixScene with instance children.  Usable wherever a Map is (setMap)."""
+
+    def __init__(self, geometries, instances, stream=None):
+        self._h = None
+        self.geometries = list(geometries)  # keeps the meshes alive as long as the scene
+        self.instances = list(instances)
+        handles = (C.c_void_p * max(1, len(self.geometries)))(*[g.handle.value for g in self.geometries])
+        h = C.c_void_p()
+        L.call("rmg_scene_create", handles, len(self.geometries), _instances_c(self.instances), len(self.instances),
+               stream if stream is not None else _stream_ptr(), C.byref(h))
+        self._h = h
+
+    @classmethod
+    def from_meshes(cls, meshes, instances=None):
+        """meshes: list of (vertices, faces).  instances: list of Instance; default one identity
+        instance per mesh with geom_id = object_id = the mesh index (meshes added without instancing)."""
+        geoms = [Map(v, f) for v, f in meshes]
+        if instances is None:
+            instances = [Instance(i, geom_id=i, object_id=i) for i in range(len(geoms))]
+        return cls(geoms, instances)
+
+    @property
+    def handle(self) -> C.c_void_p:
+        if self._h is None:
+            raise L.RmgError(L.RMG_ERR_INVALID_ARG, "Scene", "scene was destroyed")
+        return self._h
+
+    def update(self, instances, rebuild: bool = False, stream=None) -> None:
+        """New instance poses / scales / ids (same count): refits the top-level tree, or rebuilds it."""
+        instances = list(instances)
+        L.call("rmg_scene_update", self.handle, _instances_c(instances), len(instances), 1 if rebuild else 0,
+               stream if stream is not None else _stream_ptr())
+        self.instances = instances
+
+    def status(self, clear: bool = True) -> int:
+        return int(L.load().rmg_scene_status(self.handle, 1 if clear else 0))
+
+    def destroy(self) -> None:
+        if self._h is not None:
+            L.load().rmg_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
 class Sensor:
     """A sensor model with its device direction table (rmg_sensor)."""
 
@@ -236,8 +317,8 @@ class _Simulator:
         self._staging: dict = {}
         self._copy_stream = None
 
-    # SimulatorEmbree::setMap
-    def setMap(self, map: Map) -> None:
+    # SimulatorEmbree::setMap (a Map or a Scene)
+    def setMap(self, map: "Map | Scene") -> None:
         self._map = map
 
     def map(self) -> Map | None:
@@ -298,6 +379,11 @@ class _Simulator:
     def _launch(self, Tbm_d: torch.Tensor, n: int, bundle: Bundle, stream) -> None:
         out = outputs_c(bundle)
         lib = L.load()
+        if isinstance(self._map, Scene):
+            st = lib.rmg_simulate_scene(self._map.handle, self.sensor.handle, C.byref(self._Tsb),
+                                        C.c_void_p(Tbm_d.data_ptr()), n, C.byref(out), stream)
+            L.check(st, "rmg_simulate_scene")
+            return
         if self.launch_config is None:
             st = lib.rmg_simulate(self._map.handle, self.sensor.handle, C.byref(self._Tsb),
                                   C.c_void_p(Tbm_d.data_ptr()), n, C.byref(out), stream)
@@ -320,6 +406,8 @@ class _Simulator:
         from . import statistics as S
 
         self._check_ready()
+        if isinstance(self._map, Scene):
+            raise L.RmgError(L.RMG_ERR_UNSUPPORTED, "simulate_statistics", "needs a single-mesh Map")
         Tbm = S._dev(Tbm, torch.float32).reshape(-1, 8)
         n = Tbm.shape[0]
         W, H = self.sensor.width, self.sensor.height

@@ -1,0 +1,286 @@
+"""Instanced scenes (two-level BVH): the oracle's brute-force restatement pinned on the CPU, and
+rmg_simulate_scene against it on the GPU.
+
+rmagine builds such maps from files (make_embree_scene, EmbreeScene.cpp:326-406: one instance per
+node with meshes, plain meshes added directly) and reports instance ids as ObjectIds and mesh ids
+as GeomIds (SphereSimulatorEmbree.tcc:160-186); its own tests cover only single-mesh maps, so the
+scene results are pinned here by (a) equality with the single-mesh path for identity instances,
+(b) the reference's cube known answers through an instance, and (c) the brute-force oracle."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle.scene import InstancedScene
+from rmagine_gb300 import scenes, sensors, transforms
+
+GOLD = json.loads((Path(__file__).parent / "golden" / "known_answers.json").read_text())
+IDENT = transforms.identity()
+ALL = ("hits", "ranges", "points", "normals", "face_ids", "geom_ids", "object_ids")
+
+
+def quat(axis, angle):
+    axis = np.asarray(axis, np.float64)
+    axis = axis / np.linalg.norm(axis)
+    return np.concatenate([axis * np.sin(angle / 2), [np.cos(angle / 2)]]).astype(np.float32)
+
+
+def pose(q, t):
+    T = IDENT.copy()
+    T[:4] = q
+    T[4:7] = t
+    return T
+
+
+def random_instances(n, n_geoms, seed, spread=8.0, scale_range=(0.5, 2.0)):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        q = rng.standard_normal(4)
+        q = (q / np.linalg.norm(q)).astype(np.float32)
+        t = rng.uniform(-spread, spread, 3).astype(np.float32)
+        t[2] = rng.uniform(0.0, 3.0)
+        s = rng.uniform(*scale_range, 3).astype(np.float32)
+        out.append(dict(geometry=int(rng.integers(0, n_geoms)), T=pose(q, t), scale=s, geom_id=int(rng.integers(0, 4)),
+                        object_id=100 + i))
+    return out
+
+
+def mesh_library():
+    cube_v, cube_f = scenes.gen_cube()
+    box_v, box_f = scenes.box_mesh([-0.3, -0.2, 0.0], [0.3, 0.2, 1.5])
+    room = scenes.box_room(seed=4, n_boxes=6, half=3.0, height=2.5)
+    return [(cube_v, cube_f), (box_v, box_f), (room.vertices, room.faces)]
+
+
+# ---- CPU: pin the scene oracle -----------------------------------------------------------
+def test_oracle_identity_instance_equals_the_single_mesh_path():
+    room = scenes.box_room(seed=0, n_boxes=10)
+    sc = InstancedScene([(room.vertices, room.faces)], [dict(geometry=0, T=IDENT, geom_id=0, object_id=0)])
+    model = sensors.vlp16_900()
+    poses = scenes.room_poses(2, seed=1)
+    a = sc.simulate(model, IDENT, poses)
+    b = oracle.Scene(room.vertices, room.faces).simulate(model, IDENT, poses)
+    for k in ALL:
+        assert np.array_equal(a[k], b[k], equal_nan=True), k
+
+
+@pytest.mark.parametrize("name", ["spherical_cube_range", "o1dn_cube_range", "ondn_cube_range"])
+def test_oracle_cube_known_answers_through_an_instance(name):
+    """The reference's genCube known answers, with the cube placed by an instance that rotates it
+    by 90 deg about z and moves it by (5, -2, 1) and a sensor moved by the same transform."""
+    g = GOLD[name]
+    model = {"example_spherical": sensors.example_spherical, "example_o1dn": sensors.example_o1dn,
+             "example_ondn": sensors.example_ondn}[g["model"]]()
+    v, f = scenes.gen_cube()
+    Tinst = pose(quat([0, 0, 1], np.pi / 2), [5.0, -2.0, 1.0])
+    sc = InstancedScene([(v, f)], [dict(geometry=0, T=Tinst, object_id=7)])
+    res = sc.simulate(model, IDENT, Tinst[None])
+    W, H = oracle.model_size(model)
+    if g.get("vid") == "phi.size/2":
+        gid = (H // 2) * W + int(g["hid"])
+    else:
+        gid = int(g.get("ray", 0))
+    assert abs(float(res["ranges"][gid]) - g["expect"]) < g["tol"]
+    assert res["object_ids"][gid] == 7
+
+
+def test_oracle_nearest_instance_wins_and_ids_follow_it():
+    v, f = scenes.gen_cube()
+    insts = [dict(geometry=0, T=pose(IDENT[:4], [4.0, 0, 0]), geom_id=1, object_id=11),
+             dict(geometry=0, T=pose(IDENT[:4], [2.0, 0, 0]), scale=(0.5, 0.5, 0.5), geom_id=2, object_id=22)]
+    sc = InstancedScene([(v, f)], insts)
+    model = sensors.OnDnModel(width=1, height=1, range=sensors.Interval(0.0, 100.0),
+                              origs=np.zeros((1, 3), np.float32), dirs=np.array([[1, 0, 0]], np.float32))
+    r = sc.simulate(model, IDENT, IDENT[None])
+    # the half-size cube at x = 2 has its near face at x = 1.75
+    assert abs(float(r["ranges"][0]) - 1.75) < 1e-6
+    assert r["object_ids"][0] == 22 and r["geom_ids"][0] == 2
+    assert np.allclose(r["normals"][0], [-1, 0, 0])
+
+
+def test_oracle_scaled_rotated_instance_matches_a_baked_mesh():
+    """An instance equals the same mesh with its vertices moved by T * diag(s) up to binary32
+    rounding (the ray is transformed instead of the mesh)."""
+    v, f = scenes.gen_cube()
+    T = pose(quat([1, 2, 3], 0.7), [1.0, -3.0, 0.5])
+    s = np.array([2.0, 0.5, 1.5], np.float32)
+    sc = InstancedScene([(v, f)], [dict(geometry=0, T=T, scale=s)])
+    baked = transforms.apply(T[None], (v * s).astype(np.float32))
+    plain = oracle.Scene(baked, f)
+    model = sensors.vlp16_900()
+    P = np.stack([pose(IDENT[:4], [1.0 - 5.0, -3.0, 0.5]), pose(IDENT[:4], [1.0 + 5.0, -3.0, 0.5]),
+                  pose(quat([0, 0, 1], 1.0), [1.0, 2.0, 0.5])])
+    a = sc.simulate(model, IDENT, P)
+    b = plain.simulate(model, IDENT, P)
+    same = a["face_ids"] == b["face_ids"]
+    assert same.mean() > 0.999 and a["hits"].sum() > 1000
+    assert np.abs(a["ranges"][same] - b["ranges"][same]).max() < 1e-4
+    hit = same & (a["hits"] > 0)
+    assert np.abs(a["normals"][hit] - b["normals"][hit]).max() < 1e-5
+
+
+# ---- GPU ---------------------------------------------------------------------------------
+def _gpu_scene(meshes, insts):
+    import rmagine_gb300 as rm
+
+    geoms = [rm.Map(v, f) for v, f in meshes]
+    return rm.Scene(geoms, [rm.Instance(i["geometry"], i["T"], i.get("scale", (1, 1, 1)), i.get("geom_id", 0),
+                                        i.get("object_id", 0)) for i in insts])
+
+
+def _run(scene, model, poses, attrs=ALL, Tsb=IDENT):
+    import torch
+
+    import rmagine_gb300 as rm
+
+    sim = rm.make_simulator(model, scene)
+    sim.setTsb(Tsb)
+    res = sim.simulate(torch.from_numpy(np.ascontiguousarray(poses, np.float32)).cuda(), attrs=attrs)
+    torch.cuda.synchronize()
+    out = {}
+    for a in attrs:
+        t = getattr(res, a).cpu().numpy()
+        out[a] = t.view(np.uint32) if a in ("face_ids", "geom_ids", "object_ids") else t
+    return out
+
+
+def _agree(got, want, rep):
+    """Exact equality of every attribute on the rays the certifier did not dispute."""
+    bad = (got["face_ids"] != want["face_ids"]) | (got["object_ids"] != want["object_ids"]) | \
+        (np.abs(got["ranges"].astype(np.float64) - want["ranges"].astype(np.float64)) > 1e-4)
+    ok = ~bad
+    assert rep["unexcused"] == 0, rep
+    for k in got:
+        assert np.array_equal(got[k][ok], want[k][ok], equal_nan=True), k
+
+
+@pytest.mark.gpu
+def test_identity_instance_scene_equals_the_map_bitwise(built):
+    import torch
+
+    import rmagine_gb300 as rm
+
+    torch.cuda.set_device(0)
+    room = scenes.box_room(seed=0, n_boxes=30)
+    model = sensors.vlp16_900()
+    poses = scenes.room_poses(8, seed=1)
+    scene = _gpu_scene([(room.vertices, room.faces)], [dict(geometry=0, T=IDENT, geom_id=3, object_id=9)])
+    a = _run(scene, model, poses)
+    b = _run(rm.Map(room.vertices, room.faces), model, poses)
+    hit = b["face_ids"] != 0xFFFFFFFF
+    for k in ("hits", "ranges", "points", "normals", "face_ids"):
+        assert np.array_equal(a[k], b[k], equal_nan=True), k
+    assert np.all(a["geom_ids"][hit] == 3) and np.all(a["object_ids"][hit] == 9)
+    assert np.all(a["geom_ids"][~hit] == 0xFFFFFFFF)
+    assert scene.status() == 0
+
+
+def _models():
+    rng = np.random.default_rng(3)
+    d = rng.standard_normal((4096, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return {"spherical": sensors.vlp16_900(), "pinhole": sensors.depth_camera(200, 150),
+            "o1dn": sensors.O1DnModel(width=4096, height=1, range=sensors.Interval(0.2, 80.0), orig=(0.05, 0.0, 0.1),
+                                      dirs=d),
+            "ondn": sensors.OnDnModel(width=2048, height=2, range=sensors.Interval(0.2, 80.0),
+                                      origs=rng.uniform(-0.1, 0.1, (4096, 3)).astype(np.float32), dirs=d)}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["spherical", "pinhole", "o1dn", "ondn"])
+def test_random_instanced_scene_matches_the_oracle(built, kind):
+    import torch
+
+    torch.cuda.set_device(0)
+    meshes = mesh_library()
+    insts = random_instances(40, len(meshes), seed=5)
+    scene = _gpu_scene(meshes, insts)
+    model = _models()[kind]
+    poses = np.stack([pose(quat([0, 0, 1], a), [np.cos(a) * 3, np.sin(a) * 3, 1.2])
+                      for a in np.linspace(0, 2 * np.pi, 4, endpoint=False)])
+    got = _run(scene, model, poses)
+    osc = InstancedScene(meshes, insts)
+    want = osc.simulate(model, IDENT, poses)
+    assert got["hits"].sum() > 0.05 * got["hits"].size
+    assert len(np.unique(got["object_ids"])) >= 6
+    rep = osc.certify(model, IDENT, poses, got, want)
+    _agree(got, {k: want[k] for k in got}, rep)
+    assert scene.status() == 0
+
+
+@pytest.mark.gpu
+def test_update_refit_and_rebuild_follow_moving_instances(built):
+    import torch
+
+    import rmagine_gb300 as rm
+
+    torch.cuda.set_device(0)
+    meshes = mesh_library()
+    insts = random_instances(24, len(meshes), seed=8)
+    scene = _gpu_scene(meshes, insts)
+    model = sensors.vlp16_900()
+    poses = np.stack([pose(IDENT[:4], [0.0, 0.0, 1.0]), pose(quat([0, 0, 1], 1.0), [2.0, 1.0, 1.5])])
+    moved = random_instances(24, len(meshes), seed=9)
+    for i, m in enumerate(moved):
+        m["geometry"] = insts[i]["geometry"]
+    new = [rm.Instance(m["geometry"], m["T"], m["scale"], m["geom_id"], m["object_id"]) for m in moved]
+    scene.update(new)                      # refit
+    a = _run(scene, model, poses)
+    scene.update(new, rebuild=True)        # rebuild
+    b = _run(scene, model, poses)
+    for k in ALL:
+        assert np.array_equal(a[k], b[k], equal_nan=True), k
+    osc = InstancedScene(meshes, moved)
+    want = osc.simulate(model, IDENT, poses)
+    _agree(a, {k: want[k] for k in a}, osc.certify(model, IDENT, poses, a, want))
+
+
+@pytest.mark.gpu
+def test_geometry_refit_then_scene_update(built):
+    import torch
+
+    import rmagine_gb300 as rm
+
+    torch.cuda.set_device(0)
+    v, f = scenes.gen_cube()
+    g = rm.Map(v, f)
+    insts = [rm.Instance(0, pose(IDENT[:4], [3.0, 0, 0]), object_id=1),
+             rm.Instance(0, pose(IDENT[:4], [-3.0, 0, 0]), object_id=2)]
+    scene = rm.Scene([g], insts)
+    model = sensors.vlp16_900()
+    v2 = (v * np.float32(2.0)).astype(np.float32)  # the mesh grows: bounds change
+    g.refit(v2)
+    scene.update(insts)
+    got = _run(scene, model, IDENT[None])
+    osc = InstancedScene([(v2, f)], [dict(geometry=0, T=i.T, object_id=i.object_id) for i in insts])
+    want = osc.simulate(model, IDENT, IDENT[None])
+    _agree(got, {k: want[k] for k in got}, osc.certify(model, IDENT, IDENT[None], got, want))
+
+
+@pytest.mark.gpu
+def test_empty_scenes_and_bad_instances(built):
+    import torch
+
+    import rmagine_gb300 as rm
+
+    torch.cuda.set_device(0)
+    model = sensors.vlp16_900()
+    empty = rm.Scene([], [])
+    r = _run(empty, model, IDENT[None])
+    assert r["hits"].sum() == 0 and np.all(r["face_ids"] == 0xFFFFFFFF)
+    assert np.all(r["ranges"] == np.float32(model.range.max) + np.float32(1))
+    g0 = rm.Map(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))
+    only_empty = rm.Scene([g0], [rm.Instance(0)])
+    assert _run(only_empty, model, IDENT[None])["hits"].sum() == 0
+    v, f = scenes.gen_cube()
+    g = rm.Map(v, f)
+    for bad in (rm.Instance(1), rm.Instance(0, scale=(1.0, 0.0, 1.0)),
+                rm.Instance(0, T=np.array([0, 0, 0, 2, 0, 0, 0, 0], np.float32))):
+        with pytest.raises(rm.RmgError):
+            rm.Scene([g], [bad])
+    sc = rm.Scene([g], [rm.Instance(0)])
+    with pytest.raises(rm.RmgError):
+        sc.update([rm.Instance(0), rm.Instance(0)])
