@@ -230,6 +230,31 @@ def million_triangle_terrain(seed: int = 0) -> Scene:
     return terrain(grid=708, n_boxes=2000, seed=seed)
 
 
+def instanced_terrain(grid: int = 708, n_boxes: int = 2000, seed: int = 0, size: float = 500.0):
+    """terrain(grid, n_boxes=n_boxes, seed) as an instanced scene: the heightfield is geometry 0
+    (one identity instance, ids 0), the boxes are instances of one unit box (geometry 1,
+    [-0.5, 0.5]^2 x [0, 1]) scaled by their edge lengths and moved to their centre and base, with
+    geom_id 0 and object_id 1 + i -- the same boxes, to binary32 rounding, that terrain() bakes
+    into the mesh.  Returns (meshes [(vertices, faces)], instances [dict]) and the baked Scene."""
+    baked = terrain(grid=grid, size=size, n_boxes=n_boxes, seed=seed)
+    n_terrain_v = grid * grid
+    n_terrain_f = 2 * (grid - 1) ** 2
+    tv = baked.vertices[:n_terrain_v]
+    tf = baked.faces[:n_terrain_f]
+    ub_v, ub_f = box_mesh([-0.5, -0.5, 0.0], [0.5, 0.5, 1.0])
+    rng = np.random.default_rng(seed + 1)
+    c = rng.uniform(-0.45 * size, 0.45 * size, (n_boxes, 2)).astype(np.float32)
+    e = rng.uniform(0.2, 2.0, (n_boxes, 3)).astype(np.float32)
+    base = baked.height_at(c[:, 0], c[:, 1]) - F32(0.1)
+    ident = np.array([0, 0, 0, 1, 0, 0, 0, 0], np.float32)
+    insts = [dict(geometry=0, T=ident.copy(), scale=np.ones(3, np.float32), geom_id=0, object_id=0)]
+    for i in range(n_boxes):
+        T = ident.copy()
+        T[4:7] = (c[i, 0], c[i, 1], base[i])
+        insts.append(dict(geometry=1, T=T, scale=e[i].copy(), geom_id=0, object_id=1 + i))
+    return [(tv, tf), (ub_v, ub_f)], insts, baked
+
+
 def perturb_poses(poses: np.ndarray, seed: int, sigma_t: float = 0.1, sigma_r_deg: float = 2.0) -> np.ndarray:
     """Poses moved by R <- R exp(N(0, sigma_r)^3) and t <- t + N(0, sigma_t)^3 (seeded)."""
     from .transforms import compose

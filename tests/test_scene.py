@@ -284,3 +284,23 @@ def test_empty_scenes_and_bad_instances(built):
     sc = rm.Scene([g], [rm.Instance(0)])
     with pytest.raises(rm.RmgError):
         sc.update([rm.Instance(0), rm.Instance(0)])
+
+
+def test_oracle_instanced_terrain_equals_the_baked_terrain():
+    """scenes.instanced_terrain places the boxes by instances; ranges agree with the baked mesh
+    to binary32 rounding, and box hits report object ids 1 + box index."""
+    meshes, insts, baked = scenes.instanced_terrain(grid=64, n_boxes=60, seed=3, size=60.0)
+    osc = InstancedScene(meshes, insts)
+    model = sensors.vlp16_900()
+    P = scenes.terrain_poses(baked, 3, seed=4, size=60.0)
+    a = osc.simulate(model, IDENT, P)
+    b = oracle.Scene(baked.vertices, baked.faces).simulate(model, IDENT, P)
+    both = (a["hits"] > 0) & (b["hits"] > 0)
+    assert both.mean() > 0.4
+    close = np.abs(a["ranges"][both] - b["ranges"][both]) < 1e-4
+    assert close.mean() > 0.999
+    n_terrain = meshes[0][1].shape[0]
+    on_box = both & (b["face_ids"] >= n_terrain)
+    box_of_face = (b["face_ids"][on_box] - n_terrain) // 12
+    agree = a["object_ids"][on_box] == 1 + box_of_face
+    assert on_box.sum() > 20 and agree.mean() > 0.99
