@@ -369,6 +369,55 @@ def gpu_scene(args, world):
     return line, lambda: cpu_raycast(baked, model, poses, SCENE_ATTRS), config
 
 
+# ---- range noise ---------------------------------------------------------------------------------
+def gpu_noise(args, world):
+    """Gaussian range noise over the Ranges of one 1M-terrain step (131,072,000 floats), in place:
+    an HBM stream of 8 bytes per range."""
+    import torch
+
+    from rmagine_gb300 import noise
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n = 131_072_000
+    r = torch.rand(n, device=dev) * 100.0
+    nz = noise.GaussianNoise(0.0, 0.02, noise.NoiseOptions(seed=42, max_range=130.0))
+    for _ in range(args.warmup):
+        nz.apply(r)
+    torch.cuda.synchronize(dev)
+    total_ms, step_ms, clocks = Timer(dev, args.steps).run(lambda: nz.apply(r), world)
+    value = world * n * args.steps / (total_ms / 1e3) / 1e9
+    rl = roofline(8.0, n, total_ms / args.steps / 1e3, "read + write of one float per range", None)
+    host = r[: n // 8].cpu().pin_memory()
+    e2e_t = []
+    for _ in range(3):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        d = host.to(dev, non_blocking=True)
+        nz.apply(d)
+        d.cpu()
+        e2e_t.append(time.perf_counter() - t0)
+    line = {"metric": "Granges/s", "unit": "Granges/s", "value": round(value, 2),
+            "ms_per_step": round(total_ms / args.steps, 3), "dtype": "f32",
+            "config": {"workload": "GaussianNoise(0, 0.02) on 131,072,000 ranges in HBM", "l2": "inputs > L2"},
+            "gpu_launches": args.steps,
+            "e2e": {"value": round(n // 8 / (sum(e2e_t) / 3) / 1e9, 3), "unit": "Granges/s",
+                    "h2d_bytes_per_step": 4 * (n // 8), "d2h_bytes_per_step": 4 * (n // 8)},
+            "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
+
+    def cpu():
+        from oracle import noise as on
+
+        rr = np.random.default_rng(0).uniform(0, 100, 4_000_000).astype(np.float32)
+        t0 = time.perf_counter()
+        on.apply(0, rr, seed=42, call=0, stddev=0.02, max_range=130.0)
+        dt = time.perf_counter() - t0
+        return {"value": rr.size / dt / 1e9, "unit": "Granges/s", "cores": 1, "kind": "port",
+                "sample": "4,000,000 ranges, numpy restatement (binary64), one thread", "seconds": dt}
+
+    return line, cpu, line["config"]
+
+
 # ---- ICP statistics + Umeyama (forward and backward) -----------------------------------------
 def icp_data(B, N, dev, seed=0):
     """Source points U([-25,25]^3); targets = R src + t + N(0, 0.01) with 5% outliers + U(-5,5)^3;
@@ -841,6 +890,8 @@ def main():
         line, cpu, _ = gpu_rcc(args, world)
     elif args.workload == "scene_terrain1m":
         line, cpu, _ = gpu_scene(args, world)
+    elif args.workload == "noise":
+        line, cpu, _ = gpu_noise(args, world)
     else:
         raise SystemExit(f"unknown workload {args.workload}")
     if rank != 0:

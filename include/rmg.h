@@ -335,6 +335,41 @@ int rmg_umeyama_backward(const rmg_transform* pre_transforms, uint32_t pre_trans
                          rmg_vec3* grad_dataset, rmg_vec3* grad_model, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Range noise, applied in place to a DEVICE Ranges buffer.
+ *
+ * Replaces GaussianNoiseCuda / RelGaussianNoiseCuda / UniformDustNoiseCuda
+ * ::apply (src/rmagine_cuda/src/noise/GaussianNoiseCuda.cu:9-52,
+ * RelGaussianNoiseCuda.cu:9-58, UniformDustNoiseCuda.cu:8-73) with the same
+ * per-element arithmetic and Noise::Options (seed, max_range;
+ * noise/Noise.hpp:52-55).  Random numbers come from the counter-based
+ * Philox4x32-10 generator keyed by `seed`, with `call` as the upper counter
+ * words: a pure function of (seed, call, element), no per-element state.
+ * Increment `call` for each apply to draw fresh noise (the reference's
+ * curand states advance instead).  Asynchronous. */
+typedef enum rmg_noise_kind {
+  RMG_NOISE_GAUSSIAN = 0,      /* r <= max_range: r += z * stddev + mean */
+  RMG_NOISE_REL_GAUSSIAN = 1,  /* r <= max_range: r += z * (stddev * r^range_exp) + mean */
+  RMG_NOISE_UNIFORM_DUST = 2   /* early returns with probability 1 - (1 - hit_probability)^r ... */
+} rmg_noise_kind;
+
+typedef struct rmg_noise {
+  uint32_t kind;
+  float mean;
+  float stddev;
+  float range_exp;
+  float hit_probability;      /* dust: hit probability per metre */
+  float return_probability;   /* dust: return probability per metre */
+  float max_range;            /* Noise::Options::max_range (10000 by default) */
+  uint64_t seed;              /* Noise::Options::seed (42 by default) */
+  uint64_t call;              /* apply-call counter */
+} rmg_noise;
+
+int rmg_noise_apply(const rmg_noise* noise, float* ranges, uint64_t n, void* stream);
+/* The generator itself (for tests): out[4*i .. 4*i+3] = Philox4x32-10 of
+ * counter (i, call) and key seed, i < n_blocks; DEVICE out. */
+int rmg_noise_philox(const rmg_noise* noise, uint32_t* out, uint64_t n_blocks, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Scenes: several meshes and instances of them (two-level BVH).
  *
  * Replaces EmbreeScene::add / commit with EmbreeInstance::set / setTransform /

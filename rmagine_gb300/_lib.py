@@ -126,6 +126,15 @@ class InstanceDescC(C.Structure):
                 ("scale", C.c_float * 3)]
 
 
+class NoiseC(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("mean", C.c_float), ("stddev", C.c_float), ("range_exp", C.c_float),
+                ("hit_probability", C.c_float), ("return_probability", C.c_float), ("max_range", C.c_float),
+                ("seed", C.c_uint64), ("call", C.c_uint64)]
+
+
+RMG_NOISE_GAUSSIAN, RMG_NOISE_REL_GAUSSIAN, RMG_NOISE_UNIFORM_DUST = 0, 1, 2
+
+
 class ScanC(C.Structure):
     _fields_ = [("points", C.c_void_p), ("mask", C.c_void_p), ("ids", C.c_void_p), ("per_pose", C.c_uint32)]
 
@@ -165,6 +174,8 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_simulate_statistics": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(ScanC), _P, _U32,
                                           C.POINTER(ConstraintsC), C.c_int, _P, _P, _P]),
     "rmg_transforms_compose": (C.c_int, [_P, _U32, _P, _U32, _P, _U32, _P]),
+    "rmg_noise_apply": (C.c_int, [C.POINTER(NoiseC), _P, C.c_uint64, _P]),
+    "rmg_noise_philox": (C.c_int, [C.POINTER(NoiseC), _P, C.c_uint64, _P]),
     "rmg_scene_create": (C.c_int, [_P, _U32, _P, _U32, _P, C.POINTER(_P)]),
     "rmg_scene_update": (C.c_int, [_P, _P, _U32, C.c_int, _P]),
     "rmg_scene_destroy": (C.c_int, [_P]),
