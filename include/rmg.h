@@ -335,6 +335,39 @@ int rmg_umeyama_backward(const rmg_transform* pre_transforms, uint32_t pre_trans
                          rmg_vec3* grad_dataset, rmg_vec3* grad_model, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Mesh files and map files.
+ *
+ * rmg_mesh_read stands in for AssimpIO::ReadFile (map/AssimpIO.hpp:50-66) as
+ * used by import_embree_map / import_optix_map (EmbreeMap.hpp:94-117) for
+ * the mesh formats maps come in: PLY (ascii, binary little / big endian),
+ * Wavefront OBJ and STL (binary, ascii), chosen by the file extension.
+ * Polygons are split into triangle fans; OBJ objects / groups become groups
+ * (face_group), the separate meshes Assimp makes of them; STL triangles keep
+ * their own three vertices.  The arrays are HOST memory owned by the library:
+ * release them with rmg_mesh_free.  Malformed files: RMG_ERR_INVALID_ARG. */
+typedef struct rmg_mesh {
+  rmg_vec3* vertices;
+  uint32_t n_vertices;
+  rmg_face* faces;
+  uint32_t n_faces;
+  uint32_t* face_group;  /* group of each face (0 for PLY / STL) */
+  uint32_t n_groups;
+} rmg_mesh;
+
+int rmg_mesh_read(const char* path, rmg_mesh* out);
+void rmg_mesh_free(rmg_mesh* mesh);
+/* Binary PLY (host byte order) of HOST arrays, readable by rmg_mesh_read. */
+int rmg_mesh_write_ply(const char* path, const rmg_vec3* vertices, uint32_t n_vertices,
+                       const rmg_face* faces, uint32_t n_faces);
+
+/* The built map (mesh + tree) to a file and back, without a rebuild.  No
+ * counterpart in the reference (it rebuilds on every import).  A load checks
+ * sizes, a checksum and every index the kernels follow before uploading;
+ * a damaged file gives RMG_ERR_INVALID_ARG.  Both synchronise. */
+int rmg_map_save(const rmg_map* map, const char* path);
+int rmg_map_load(const char* path, void* stream, rmg_map** out);
+
+/* ---------------------------------------------------------------------------
  * Range noise, applied in place to a DEVICE Ranges buffer.
  *
  * Replaces GaussianNoiseCuda / RelGaussianNoiseCuda / UniformDustNoiseCuda

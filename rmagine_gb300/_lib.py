@@ -135,6 +135,11 @@ class NoiseC(C.Structure):
 RMG_NOISE_GAUSSIAN, RMG_NOISE_REL_GAUSSIAN, RMG_NOISE_UNIFORM_DUST = 0, 1, 2
 
 
+class MeshC(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("n_vertices", C.c_uint32), ("faces", C.c_void_p), ("n_faces", C.c_uint32),
+                ("face_group", C.c_void_p), ("n_groups", C.c_uint32)]
+
+
 class ScanC(C.Structure):
     _fields_ = [("points", C.c_void_p), ("mask", C.c_void_p), ("ids", C.c_void_p), ("per_pose", C.c_uint32)]
 
@@ -174,6 +179,11 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_simulate_statistics": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(ScanC), _P, _U32,
                                           C.POINTER(ConstraintsC), C.c_int, _P, _P, _P]),
     "rmg_transforms_compose": (C.c_int, [_P, _U32, _P, _U32, _P, _U32, _P]),
+    "rmg_mesh_read": (C.c_int, [C.c_char_p, C.POINTER(MeshC)]),
+    "rmg_mesh_free": (None, [C.POINTER(MeshC)]),
+    "rmg_mesh_write_ply": (C.c_int, [C.c_char_p, _P, _U32, _P, _U32]),
+    "rmg_map_save": (C.c_int, [_P, C.c_char_p]),
+    "rmg_map_load": (C.c_int, [C.c_char_p, _P, C.POINTER(_P)]),
     "rmg_noise_apply": (C.c_int, [C.POINTER(NoiseC), _P, C.c_uint64, _P]),
     "rmg_noise_philox": (C.c_int, [C.POINTER(NoiseC), _P, C.c_uint64, _P]),
     "rmg_scene_create": (C.c_int, [_P, _U32, _P, _U32, _P, C.POINTER(_P)]),

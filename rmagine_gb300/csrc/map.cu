@@ -514,6 +514,225 @@ extern "C" int rmg_map_export(const rmg_map* m, void* nodes, void* tris, uint32_
   return RMG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Map files: the built tree saved and loaded without a rebuild.  No
+// counterpart in the reference (Embree / OptiX rebuild from the mesh on every
+// import); for large maps a load is a file read plus host->device copies.
+//
+// Layout (little-endian):
+//   char magic[8] = "RMGLBVH1"; uint32 version = 1;
+//   uint32 n_vertices, n_faces, n_nodes, depth;
+//   uint64 payload_bytes; uint64 fnv1a64(payload);
+//   payload: vertices 12 B each, faces 12 B, nodes 64 B, packed triangles 48 B,
+//            leaf order 4 B, leaf parents 4 B.
+// A load checks the sizes, the checksum and every index the kernels follow
+// (children, parents, face ids, leaf order, face vertex indices) on the host
+// before anything reaches the device, so a damaged or crafted file is
+// rejected with RMG_ERR_INVALID_ARG instead of steering a kernel out of bounds;
+// the tree depth is recomputed from the links.
+namespace {
+
+constexpr char kMapMagic[8] = {'R', 'M', 'G', 'L', 'B', 'V', 'H', '1'};
+
+struct MapFileHeader {
+  char magic[8];
+  uint32_t version;
+  uint32_t n_vertices, n_faces, n_nodes, depth;
+  uint32_t pad;
+  uint64_t payload_bytes;
+  uint64_t checksum;
+};
+static_assert(sizeof(MapFileHeader) == 48, "map file header is 48 B");
+
+uint64_t fnv1a64(const unsigned char* p, size_t n) {
+  uint64_t h = 1469598103934665603ull;
+  for (size_t i = 0; i < n; ++i) {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+uint64_t payload_size(uint64_t nv, uint64_t nf, uint64_t nn) {
+  return 12 * nv + 12 * nf + sizeof(Node) * nn + sizeof(Tri) * nf + 4 * nf + 4 * nf;
+}
+
+// Index checks and depth of a loaded tree; returns RMG_OK or INVALID_ARG.
+int check_tree(const MapFileHeader& h, const uint32_t* faces, const Node* nodes, const Tri* tris,
+               const uint32_t* order, const int* leaf_parent, uint32_t* depth_out) {
+  const uint32_t nv = h.n_vertices, nf = h.n_faces, nn = h.n_nodes;
+  const uint32_t want_nodes = nf >= 2 ? nf - 1 : (nf == 1 ? 1 : 0);
+  if (nn != want_nodes) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: node count does not match the face count");
+  for (uint64_t i = 0; i < 3ull * nf; ++i)
+    if (faces[i] >= nv) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: face vertex index out of range");
+  for (uint32_t k = 0; k < nf; ++k) {
+    uint32_t fid;
+    std::memcpy(&fid, &tris[k].v0.w, 4);
+    if (fid >= nf || order[k] >= nf) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: face id out of range");
+    if (leaf_parent[k] < -1 || leaf_parent[k] >= (int)nn)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: leaf parent out of range");
+  }
+  std::vector<uint32_t> refs_node(nn, 0), refs_leaf(nf, 0);
+  for (uint32_t i = 0; i < nn; ++i) {
+    const int c[2] = {nodes[i].d.x, nodes[i].d.y};
+    for (int k = 0; k < 2; ++k) {
+      if (c[k] >= 0) {
+        if ((uint32_t)c[k] >= nn || c[k] == 0) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: child out of range");
+        ++refs_node[c[k]];
+      } else {
+        const uint32_t leaf = (uint32_t)(~c[k]);
+        if (leaf >= nf) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: leaf out of range");
+        ++refs_leaf[leaf];
+      }
+    }
+    const int p = nodes[i].d.z;
+    if (p < -1 || p >= (int)nn || (i == 0) != (p == -1)) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: bad parent link");
+  }
+  for (uint32_t i = 1; i < nn; ++i)
+    if (refs_node[i] != 1) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: node not referenced exactly once");
+  if (nf >= 2)
+    for (uint32_t k = 0; k < nf; ++k)
+      if (refs_leaf[k] != 1) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: leaf not referenced exactly once");
+  // depth (edges) by an explicit walk from the root; every node is reached once
+  uint32_t depth = nf ? 1 : 0;
+  if (nn > 1) {
+    std::vector<std::pair<int, uint32_t>> st;
+    st.push_back({0, 0});
+    size_t visited = 0;
+    while (!st.empty()) {
+      const auto [n, dd] = st.back();
+      st.pop_back();
+      if (++visited > nn) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: links do not form a tree");
+      const int c[2] = {nodes[n].d.x, nodes[n].d.y};
+      for (int k = 0; k < 2; ++k) {
+        if (c[k] >= 0) st.push_back({c[k], dd + 1});
+        else depth = std::max(depth, dd + 1);
+      }
+    }
+    if (visited != nn) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: unreachable nodes");
+  }
+  *depth_out = depth;
+  return RMG_OK;
+}
+
+}  // namespace
+
+extern "C" int rmg_map_save(const rmg_map* m, const char* path) {
+  if (!m || !path) return fail(RMG_ERR_INVALID_ARG, "rmg_map_save: NULL argument");
+  const uint64_t nv = m->n_vertices, nf = m->n_faces, nn = m->n_nodes;
+  std::vector<unsigned char> payload(payload_size(nv, nf, nn));
+  unsigned char* p = payload.data();
+  auto dl = [&](const void* src, size_t bytes) -> int {
+    if (bytes) RMG_CUDA_TRY(cudaMemcpy(p, src, bytes, cudaMemcpyDeviceToHost));
+    p += bytes;
+    return RMG_OK;
+  };
+  int s = RMG_OK;
+  if (s == RMG_OK) s = dl(m->d_vertices, 12 * nv);
+  if (s == RMG_OK) s = dl(m->d_faces, 12 * nf);
+  if (s == RMG_OK) s = dl(m->d_nodes, sizeof(Node) * nn);
+  if (s == RMG_OK) s = dl(m->d_tris, sizeof(Tri) * nf);
+  if (s == RMG_OK) s = dl(m->d_leaf_order, 4 * nf);
+  if (s == RMG_OK) s = dl(m->d_leaf_parent, 4 * nf);
+  if (s != RMG_OK) return s;
+  MapFileHeader h;
+  std::memset(&h, 0, sizeof(h));
+  std::memcpy(h.magic, kMapMagic, 8);
+  h.version = 1;
+  h.n_vertices = m->n_vertices;
+  h.n_faces = m->n_faces;
+  h.n_nodes = m->n_nodes;
+  h.depth = m->depth;
+  h.payload_bytes = payload.size();
+  h.checksum = fnv1a64(payload.data(), payload.size());
+  FILE* fp = std::fopen(path, "wb");
+  if (!fp) return fail(RMG_ERR_INVALID_ARG, std::string("rmg_map_save: cannot write ") + path);
+  bool ok = std::fwrite(&h, sizeof(h), 1, fp) == 1;
+  ok = ok && (payload.empty() || std::fwrite(payload.data(), 1, payload.size(), fp) == payload.size());
+  ok = (std::fclose(fp) == 0) && ok;
+  return ok ? RMG_OK : fail(RMG_ERR_INVALID_ARG, "rmg_map_save: write failed");
+}
+
+extern "C" int rmg_map_load(const char* path, void* stream, rmg_map** out) {
+  if (!path || !out) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: NULL argument");
+  *out = nullptr;
+  FILE* fp = std::fopen(path, "rb");
+  if (!fp) return fail(RMG_ERR_INVALID_ARG, std::string("rmg_map_load: cannot read ") + path);
+  MapFileHeader h;
+  bool ok = std::fread(&h, sizeof(h), 1, fp) == 1;
+  if (!ok || std::memcmp(h.magic, kMapMagic, 8) != 0 || h.version != 1) {
+    std::fclose(fp);
+    return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: not a map file of this version");
+  }
+  if (h.n_faces > (1u << 30) || h.payload_bytes != payload_size(h.n_vertices, h.n_faces, h.n_nodes)) {
+    std::fclose(fp);
+    return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: sizes in the header do not agree");
+  }
+  std::vector<unsigned char> payload(h.payload_bytes);
+  ok = payload.empty() || std::fread(payload.data(), 1, payload.size(), fp) == payload.size();
+  const bool trailing = std::fgetc(fp) != EOF;
+  std::fclose(fp);
+  if (!ok || trailing) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: file size does not match the header");
+  if (fnv1a64(payload.data(), payload.size()) != h.checksum)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: checksum mismatch (damaged file)");
+  const uint64_t nv = h.n_vertices, nf = h.n_faces, nn = h.n_nodes;
+  const unsigned char* p = payload.data();
+  const unsigned char* pv = p;
+  const unsigned char* pf = pv + 12 * nv;
+  const unsigned char* pn = pf + 12 * nf;
+  const unsigned char* pt = pn + sizeof(Node) * nn;
+  const unsigned char* po = pt + sizeof(Tri) * nf;
+  const unsigned char* pp = po + 4 * nf;
+  // aligned host copies for the checks
+  std::vector<uint32_t> faces(3 * nf), order(nf);
+  std::vector<Node> nodes(nn);
+  std::vector<Tri> tris(nf);
+  std::vector<int> parents(nf);
+  if (nf) std::memcpy(faces.data(), pf, 12 * nf);
+  if (nn) std::memcpy(nodes.data(), pn, sizeof(Node) * nn);
+  if (nf) {
+    std::memcpy(tris.data(), pt, sizeof(Tri) * nf);
+    std::memcpy(order.data(), po, 4 * nf);
+    std::memcpy(parents.data(), pp, 4 * nf);
+  }
+  uint32_t depth = 0;
+  int s = check_tree(h, faces.data(), nodes.data(), tris.data(), order.data(), parents.data(), &depth);
+  if (s != RMG_OK) return s;
+  cudaStream_t st = as_stream(stream);
+  rmg_map* m = new (std::nothrow) rmg_map;
+  if (!m) return fail(RMG_ERR_OOM, "rmg_map_load: host allocation");
+  std::memset(m, 0, sizeof(*m));
+  cudaGetDevice(&m->device);
+  m->n_vertices = h.n_vertices;
+  m->n_faces = h.n_faces;
+  m->n_nodes = h.n_nodes;
+  m->depth = depth;
+  auto check = [&](int r) { if (s == RMG_OK) s = r; };
+  check(dev_alloc(&m->d_status, 1, "status"));
+  check(dev_alloc(&m->d_vertices, 3 * nv, "vertices"));
+  check(dev_alloc(&m->d_faces, 3 * nf, "faces"));
+  check(dev_alloc(&m->d_nodes, nn, "nodes"));
+  check(dev_alloc(&m->d_tris, nf, "tris"));
+  check(dev_alloc(&m->d_leaf_order, nf, "leaf order"));
+  check(dev_alloc(&m->d_leaf_parent, nf, "leaf parent"));
+  check(dev_alloc(&m->d_flags, nn, "flags"));
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    if (s == RMG_OK && bytes) s = cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st), "upload");
+  };
+  if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(m->d_status, 0, 4, st), "memset");
+  up(m->d_vertices, pv, 12 * nv);
+  up(m->d_faces, faces.data(), 12 * nf);
+  up(m->d_nodes, nodes.data(), sizeof(Node) * nn);
+  up(m->d_tris, tris.data(), sizeof(Tri) * nf);
+  up(m->d_leaf_order, order.data(), 4 * nf);
+  up(m->d_leaf_parent, parents.data(), 4 * nf);
+  if (s == RMG_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
+  if (s != RMG_OK) { free_map(m); return s; }
+  update_info(m, st);
+  *out = m;
+  return RMG_OK;
+}
+
 extern "C" int rmg_map_status(rmg_map* m, int clear) {
   if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_status: map is NULL");
   unsigned int word = 0;

@@ -123,6 +123,19 @@ class Map:
     def status(self, clear: bool = True) -> int:
         return int(L.load().rmg_map_status(self.handle, 1 if clear else 0))
 
+    def save(self, path) -> None:
+        """The built map (mesh + tree) to a file (rmg_map_save)."""
+        from .meshio import save_map
+
+        save_map(self, path)
+
+    @classmethod
+    def load(cls, path) -> "Map":
+        """A map saved by save(), without a rebuild (rmg_map_load)."""
+        from .meshio import load_map
+
+        return load_map(path)
+
     def destroy(self) -> None:
         if self._h is not None:
             L.load().rmg_map_destroy(self._h)
