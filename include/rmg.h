@@ -123,6 +123,8 @@ typedef struct rmg_launch_config {
   uint32_t refill;        /* 0: one tile per warp.  1..32: persistent warps that hand new rays to
                              idle lanes whenever fewer than `refill` lanes are busy (stack_depth 8 or 16) */
   uint32_t chunk;         /* refill mode: tiles a warp takes from the work counter at a time (>= 1) */
+  uint32_t bvh_width;     /* 2: walk the binary tree; 4: the 4-wide tree collapsed from it (when the map
+                             has one and refill == 0); 0: the default.  Results are identical. */
 } rmg_launch_config;
 
 typedef struct rmg_map_info {
@@ -130,7 +132,7 @@ typedef struct rmg_map_info {
   uint32_t n_faces;
   uint32_t n_nodes;       /* internal BVH nodes */
   uint32_t depth;         /* longest root-to-leaf path (edges) */
-  uint64_t device_bytes;  /* BVH nodes + packed triangles + vertices + faces */
+  uint64_t device_bytes;  /* BVH nodes (binary and 4-wide) + packed triangles + vertices + faces */
   float bounds_lo[3];
   float bounds_hi[3];
 } rmg_map_info;
@@ -178,7 +180,10 @@ int rmg_map_export(const rmg_map* map, void* nodes, void* tris, uint32_t* leaf_o
 int rmg_map_status(rmg_map* map, int clear);
 /* Test hook: overwrite one child link of one BVH node (synchronous).  Used
  * to check that a corrupt tree ends in RMG_ERR_TRAVERSAL_BUDGET, not a
- * fault; values are range-checked so every link stays inside the arrays. */
+ * fault; values are range-checked so every link stays inside the arrays.
+ * which 0 / 1: left / right link of binary node `node` (the map then drops
+ * its 4-wide tree, so the damaged binary tree is the one walked);
+ * which 2..5: slot which-2 of 4-wide node `node`. */
 int rmg_map_debug_set_child(rmg_map* map, uint32_t node, uint32_t which, int32_t child);
 
 /* ---------------------------------------------------------------------------

@@ -87,7 +87,7 @@ class OutputsC(C.Structure):
 
 class LaunchConfigC(C.Structure):
     _fields_ = [("stack_depth", C.c_uint32), ("block_warps", C.c_uint32), ("tile_w", C.c_uint32),
-                ("tile_h", C.c_uint32), ("refill", C.c_uint32), ("chunk", C.c_uint32)]
+                ("tile_h", C.c_uint32), ("refill", C.c_uint32), ("chunk", C.c_uint32), ("bvh_width", C.c_uint32)]
 
 
 class MapInfoC(C.Structure):

@@ -40,11 +40,26 @@ struct __align__(16) Tri {
   float4 v0, v1, v2;
 };
 
+// 4-wide node, 128 B (one cache line), collapsed from the binary tree:
+// the four child boxes as structure of arrays (component k = child k), the
+// child links (>= 0 wide node, < 0 leaf ~packed triangle, kEmpty4 = no child,
+// whose box is a point at 1e30 that no ray reaches), and meta = (children,
+// parent wide node or -1, 0, 0).
+constexpr int kEmpty4 = (int)0x80000000;
+
+struct __align__(16) Node4 {
+  float4 lox, hix, loy, hiy, loz, hiz;
+  int4 child;
+  int4 meta;
+};
+
 static_assert(sizeof(Node) == 64, "node record is 64 B");
+static_assert(sizeof(Node4) == 128, "wide node record is 128 B");
 static_assert(sizeof(Tri) == 48, "triangle record is 48 B");
 
 // Device error word values are rmg_status codes.
 struct DeviceMap {
+  const Node4* nodes4;  // the 4-wide tree, or NULL
   const Node* nodes;
   const Tri* tris;
   int n_nodes;

@@ -25,6 +25,11 @@ struct rmg_map {
   int* d_leaf_parent;         // n_faces: parent node of each leaf
   unsigned int* d_flags;      // n_nodes refit visit counters
   unsigned int* d_status;     // 1 word: device error status
+  // 4-wide tree collapsed from the binary one (wide.cu)
+  rmg::Node4* d_nodes4;       // n_nodes4
+  int* d_src4;                // 4*n_nodes4: binary record (2*parent + side) of each slot, -1 empty
+  uint32_t n_nodes4;
+  uint32_t depth4;            // levels of the wide tree
 };
 
 struct rmg_sensor {
@@ -66,6 +71,9 @@ int dev_alloc(T** p, size_t count, const char* what) {
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 DeviceMap device_view(const rmg_map* m);
+int wide_build(rmg_map* m, cudaStream_t st);
+int wide_refit(rmg_map* m, cudaStream_t st);
+void wide_free(rmg_map* m);
 SensorDev device_view(const rmg_sensor* s);
 
 int device_sm_count();

@@ -270,6 +270,7 @@ void free_map(rmg_map* m) {
   cudaFree(m->d_leaf_parent);
   cudaFree(m->d_flags);
   cudaFree(m->d_status);
+  wide_free(m);
   delete m;
 }
 
@@ -323,6 +324,7 @@ void update_info(rmg_map* m, cudaStream_t st) {
 
 DeviceMap device_view(const rmg_map* m) {
   DeviceMap d;
+  d.nodes4 = m->d_nodes4;
   d.nodes = m->d_nodes;
   d.tris = m->d_tris;
   d.n_nodes = (int)m->n_nodes;
@@ -404,6 +406,8 @@ extern "C" int rmg_map_build(const rmg_vec3* vertices, uint32_t n_vertices, cons
     if (s == RMG_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
     if (s != RMG_OK) { free_map(m); return s; }
     m->depth = 1;
+    s = wide_build(m, st);
+    if (s != RMG_OK) { free_map(m); return s; }
     update_info(m, st);
     *out = m;
     return RMG_OK;
@@ -464,6 +468,8 @@ extern "C" int rmg_map_build(const rmg_vec3* vertices, uint32_t n_vertices, cons
   cudaFree(d_vals); cudaFree(d_vals2); cudaFree(d_depth); cudaFree(d_temp);
   if (s != RMG_OK) { free_map(m); return s; }
   m->depth = depth;
+  s = wide_build(m, st);
+  if (s != RMG_OK) { free_map(m); return s; }
   update_info(m, st);
   *out = m;
   return RMG_OK;
@@ -479,6 +485,7 @@ extern "C" int rmg_map_refit(rmg_map* m, const rmg_vec3* vertices, uint32_t n_ve
   RMG_CUDA_TRY(cudaMemcpyAsync(m->d_vertices, vertices, 12 * (size_t)n_vertices,
                                cudaMemcpyHostToDevice, st));
   int s = repack_and_refit(m, st, m->d_leaf_order);
+  if (s == RMG_OK) s = wide_refit(m, st);
   if (s != RMG_OK) return s;
   RMG_CUDA_TRY(cudaStreamSynchronize(st));
   update_info(m, st);
@@ -498,7 +505,8 @@ extern "C" int rmg_map_info_get(const rmg_map* m, rmg_map_info* out) {
   out->n_nodes = m->n_nodes;
   out->depth = m->depth;
   out->device_bytes = (uint64_t)m->n_nodes * sizeof(Node) + (uint64_t)m->n_faces * sizeof(Tri) +
-                      12ull * m->n_vertices + 12ull * m->n_faces;
+                      12ull * m->n_vertices + 12ull * m->n_faces +
+                      (uint64_t)m->n_nodes4 * (sizeof(Node4) + 4 * sizeof(int));
   for (int k = 0; k < 3; ++k) { out->bounds_lo[k] = m->lo[k]; out->bounds_hi[k] = m->hi[k]; }
   return RMG_OK;
 }
@@ -727,6 +735,7 @@ extern "C" int rmg_map_load(const char* path, void* stream, rmg_map** out) {
   up(m->d_leaf_order, order.data(), 4 * nf);
   up(m->d_leaf_parent, parents.data(), 4 * nf);
   if (s == RMG_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
+  if (s == RMG_OK) s = wide_build(m, st);
   if (s != RMG_OK) { free_map(m); return s; }
   update_info(m, st);
   *out = m;
@@ -747,13 +756,24 @@ extern "C" int rmg_map_status(rmg_map* m, int clear) {
 
 extern "C" int rmg_map_debug_set_child(rmg_map* m, uint32_t node, uint32_t which, int32_t child) {
   if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: map is NULL");
-  if (node >= m->n_nodes || which > 1)
+  if (which >= 2) {  // a slot of the 4-wide tree
+    if (!m->d_nodes4 || node >= m->n_nodes4 || which > 5)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: wide node/slot out of range");
+    if (child >= 0 ? (uint32_t)child >= m->n_nodes4 : (uint32_t)(~child) >= m->n_faces)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: child out of range");
+    const size_t off = offsetof(Node4, child) + sizeof(int) * (which - 2);
+    RMG_CUDA_TRY(cudaMemcpy(reinterpret_cast<char*>(m->d_nodes4 + node) + off, &child, sizeof(int),
+                            cudaMemcpyHostToDevice));
+    return RMG_OK;
+  }
+  if (node >= m->n_nodes)
     return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: node/which out of range");
   if (child >= 0 ? (uint32_t)child >= m->n_nodes : (uint32_t)(~child) >= m->n_faces)
     return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: child out of range");
   const size_t off = offsetof(Node, d) + (which ? sizeof(int) : 0);
   RMG_CUDA_TRY(cudaMemcpy(reinterpret_cast<char*>(m->d_nodes + node) + off, &child, sizeof(int),
                           cudaMemcpyHostToDevice));
+  wide_free(m);  // the binary tree is the one damaged: walk it from now on
   return RMG_OK;
 }
 

@@ -5,6 +5,14 @@
 #include "launch.h"
 #include "trace.cuh"
 
+// Walk the 4-wide tree when the launch config leaves the choice open.  Off:
+// on the 1M-triangle terrain the binary walk is faster (spherical 6,296 vs
+// 5,736 Mrays/s, pinhole 9,200 vs 8,035); the 4-wide walk wins on small maps
+// (2,412-triangle room: 3,563 vs 3,281) and is chosen there with bvh_width = 4.
+#ifndef RMG_DEFAULT_WIDE
+#define RMG_DEFAULT_WIDE 0
+#endif
+
 namespace rmg {
 
 // Defaults from a sweep on the 1M-triangle terrain (spherical 128x1024): short
@@ -14,6 +22,7 @@ int default_config(const rmg_sensor* s, rmg_launch_config* cfg) {
   cfg->block_warps = 4;
   cfg->refill = 0;
   cfg->chunk = 4;
+  cfg->bvh_width = 0;
   if (s && s->width >= 8 && s->height >= 4) { cfg->tile_w = 8; cfg->tile_h = 4; }
   else if (s && s->height < 4 && s->height > 1) { cfg->tile_w = 16; cfg->tile_h = 2; }
   else { cfg->tile_w = 32; cfg->tile_h = 1; }
@@ -31,6 +40,8 @@ int check_config(const rmg_launch_config& c) {
   if (c.refill && c.stack_depth == 0)
     return fail(RMG_ERR_UNSUPPORTED, "launch config: refill mode needs stack_depth 8 or 16");
   if (c.refill && (c.chunk < 1 || c.chunk > 1024)) return fail(RMG_ERR_UNSUPPORTED, "launch config: chunk 1..1024");
+  if (c.bvh_width != 0 && c.bvh_width != 2 && c.bvh_width != 4)
+    return fail(RMG_ERR_UNSUPPORTED, "launch config: bvh_width must be 0, 2 or 4");
   return RMG_OK;
 }
 
@@ -60,6 +71,10 @@ int make_trace_params(const rmg_map* map, const rmg_sensor* sensor, const rmg_tr
   P.budget = 2u * map->n_nodes + 64u;
   P.trail_bits = trail_bits_for_depth(map->depth);
   P.full_stack = map->depth <= (unsigned)kFullStack ? 1 : 0;
+  // 4-wide walk: 3 pushes per level at most, so 21 levels fit its 64-entry stack
+  P.wide = (cfg.bvh_width != 2 && cfg.refill == 0 && map->d_nodes4 && 3 * map->depth4 <= (unsigned)kStack4 &&
+            RMG_DEFAULT_WIDE) ? 1 : 0;
+  if (cfg.bvh_width == 4 && cfg.refill == 0 && map->d_nodes4 && 3 * map->depth4 <= (unsigned)kStack4) P.wide = 1;
   return RMG_OK;
 }
 

@@ -10,6 +10,10 @@ namespace rmg {
 namespace {
 template <int SS>
 cudaError_t by_trail(const TraceParams& P, unsigned grid, unsigned block, cudaStream_t st) {
+  if (P.wide) {  // the 4-wide tree: same results, fewer and wider visits
+    k_trace<ORIGIN_POSE, 0, kWideTB><<<grid, block, 0, st>>>(P);
+    return cudaGetLastError();
+  }
   if (SS > 0 && P.full_stack) {  // same visits and results, without trail bookkeeping
     k_trace<ORIGIN_POSE, kFullStack, 0><<<grid, block, 0, st>>>(P);
     return cudaGetLastError();

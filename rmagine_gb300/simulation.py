@@ -313,8 +313,8 @@ def outputs_c(bundle: Bundle) -> L.OutputsC:
     return o
 
 
-def launch_config(stack_depth=16, block_warps=4, tile_w=8, tile_h=4, refill=0, chunk=4) -> L.LaunchConfigC:
-    return L.LaunchConfigC(stack_depth, block_warps, tile_w, tile_h, refill, chunk)
+def launch_config(stack_depth=16, block_warps=4, tile_w=8, tile_h=4, refill=0, chunk=4, bvh_width=0) -> L.LaunchConfigC:
+    return L.LaunchConfigC(stack_depth, block_warps, tile_w, tile_h, refill, chunk, bvh_width)
 
 
 # ---- simulators -------------------------------------------------------------------

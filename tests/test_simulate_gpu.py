@@ -170,8 +170,11 @@ def test_stack_depths_and_tiles_bitwise_identical():
     poses = scenes.terrain_poses(sc, 4, seed=13)
     m = rm.Map(sc.vertices, sc.faces)
     model = sensors.ouster_like(64, 512)
-    base = gpu_sim(m, model, poses, cfg=rm.launch_config(8, 4, 8, 4))
-    for cfg in [(0, 4, 8, 4), (16, 2, 8, 4), (16, 8, 32, 1), (8, 1, 4, 8), (8, 4, 16, 2), (0, 8, 2, 16),
+    base = gpu_sim(m, model, poses, cfg=rm.launch_config(8, 4, 8, 4, bvh_width=2))
+    assert m.info()["depth"] <= 32
+    for cfg in [(0, 4, 8, 4, 0, 4, 2), (16, 2, 8, 4, 0, 4, 2), (16, 8, 32, 1, 0, 4, 2), (8, 1, 4, 8, 0, 4, 2),
+                (8, 4, 16, 2, 0, 4, 2), (0, 8, 2, 16, 0, 4, 2),
+                (16, 4, 8, 4, 0, 4, 4), (16, 2, 16, 2, 0, 4, 4), (16, 8, 32, 1, 0, 4, 4), (16, 4, 8, 4),
                 (8, 4, 8, 4, 16, 4), (16, 2, 8, 4, 32, 1), (8, 8, 16, 2, 1, 7), (16, 4, 4, 8, 24, 64)]:
         other = gpu_sim(m, model, poses, cfg=rm.launch_config(*cfg))
         for a in ALL:
@@ -285,6 +288,20 @@ def test_corrupt_tree_reports_budget_error_not_a_fault():
     ok = rm.Map(sc.vertices, sc.faces)
     gpu_sim(ok, model, scenes.room_poses(1), attrs=("ranges",))
     assert ok.status() == 0
+
+
+def test_corrupt_wide_tree_reports_budget_error_not_a_fault():
+    """A slot of the 4-wide tree bent back to its root: the wide walk stops at its budget (or its
+    stack guard) and reports RMG_ERR_TRAVERSAL_BUDGET; the binary walk of the same map is intact."""
+    sc = scenes.box_room(seed=8, n_boxes=20)
+    m = rm.Map(sc.vertices, sc.faces)
+    model = sensors.vlp16_900()
+    want = gpu_sim(m, model, scenes.room_poses(2, seed=9), attrs=("ranges",), cfg=rm.launch_config(bvh_width=2))
+    _lib.call("rmg_map_debug_set_child", m.handle, 0, 2, 0)  # wide root, slot 0 -> wide root
+    gpu_sim(m, model, scenes.room_poses(2, seed=9), attrs=("ranges",), cfg=rm.launch_config(bvh_width=4))
+    assert m.status(clear=True) == _lib.RMG_ERR_TRAVERSAL_BUDGET
+    got = gpu_sim(m, model, scenes.room_poses(2, seed=9), attrs=("ranges",), cfg=rm.launch_config(bvh_width=2))
+    assert m.status() == 0 and np.array_equal(got["ranges"], want["ranges"])
 
 
 def test_stream_wait_timeout_and_success():
