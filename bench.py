@@ -250,6 +250,7 @@ def gpu_raycast(args, world):
     sim = rm.make_simulator(model, m)
     Tbm = torch.from_numpy(poses).to(dev)
     bundle = rm.resize_memory_bundle(rm.Bundle(*attrs), W, H, n, device=dev)
+    tuned = sim.autotune(Tbm, bundle, reps=3)  # fastest launch configuration for this map, sensor and poses
     for _ in range(args.warmup):
         sim.simulate(Tbm, bundle)
     torch.cuda.synchronize(dev)
@@ -280,7 +281,8 @@ def gpu_raycast(args, world):
                       "node and triangle fetches are served mostly from L1/L2, so this exceeds the HBM roof",
                       TRAFFIC.get(args.workload))
     config = dict(desc)
-    config.update({"poses": int(n), "rays_per_step": int(rays), "triangles": int(sc.n_faces),
+    config.update({"launch": {k: int(getattr(tuned, k)) for k, _ in tuned._fields_},
+                   "poses": int(n), "rays_per_step": int(rays), "triangles": int(sc.n_faces),
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas{world}" if world > 1 else "single"})
     line = {"metric": "Mrays/s", "unit": "Mrays/s", "value": round(value, 2), "ms_per_step": round(total_ms / args.steps, 3),

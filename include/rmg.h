@@ -125,6 +125,9 @@ typedef struct rmg_launch_config {
   uint32_t chunk;         /* refill mode: tiles a warp takes from the work counter at a time (>= 1) */
   uint32_t bvh_width;     /* 2: walk the binary tree; 4: the 4-wide tree collapsed from it (when the map
                              has one and refill == 0); 0: the default.  Results are identical. */
+  uint32_t packet;        /* 1: the warp walks the binary tree together (a node is visited when any of
+                             its 32 rays needs it; refill == 0, bvh_width != 4); 0: each ray walks alone;
+                             2: the default.  Results are identical. */
 } rmg_launch_config;
 
 typedef struct rmg_map_info {
@@ -226,6 +229,15 @@ int rmg_simulate_ex(const rmg_map* map, const rmg_sensor* sensor,
                     const rmg_outputs* out, const rmg_launch_config* cfg, void* stream);
 /* Fills *cfg with the library default for this sensor/map. */
 int rmg_default_launch_config(const rmg_map* map, const rmg_sensor* sensor, rmg_launch_config* cfg);
+
+/* Times a fixed set of launch configurations (per-ray binary walk, warp
+ * packet walk, 4-wide walk; tiles 8x4, 16x2, 4x8; 4 or 2 warps per CTA) on
+ * the caller's poses and output buffers -- all write the same results -- and
+ * returns the fastest (median of `reps` runs after a warm-up).  Same pointer
+ * rules as rmg_simulate; synchronises.  No counterpart in the reference. */
+int rmg_autotune_launch_config(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                               const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
+                               uint32_t reps, rmg_launch_config* best, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Batched heterogeneous sensors (no counterpart in the reference, where each

@@ -87,7 +87,8 @@ class OutputsC(C.Structure):
 
 class LaunchConfigC(C.Structure):
     _fields_ = [("stack_depth", C.c_uint32), ("block_warps", C.c_uint32), ("tile_w", C.c_uint32),
-                ("tile_h", C.c_uint32), ("refill", C.c_uint32), ("chunk", C.c_uint32), ("bvh_width", C.c_uint32)]
+                ("tile_h", C.c_uint32), ("refill", C.c_uint32), ("chunk", C.c_uint32), ("bvh_width", C.c_uint32),
+                ("packet", C.c_uint32)]
 
 
 class MapInfoC(C.Structure):
@@ -170,6 +171,8 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_simulate_ex": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(OutputsC),
                                   C.POINTER(LaunchConfigC), _P]),
     "rmg_default_launch_config": (C.c_int, [_P, _P, C.POINTER(LaunchConfigC)]),
+    "rmg_autotune_launch_config": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(OutputsC), _U32,
+                                             C.POINTER(LaunchConfigC), _P]),
     "rmg_lbvh_build_noalloc": (C.c_int, [_P, _U32, _P, _U32, C.POINTER(LbvhBuffersC), _P]),
     "rmg_statistics_p2p": (C.c_int, [_P, _U32, _P, _P, _P, _P, _P, _P, C.POINTER(ConstraintsC), _U32, _U32,
                                      _P, _P, _P]),

@@ -1,5 +1,7 @@
 // rmg_simulate: the C entry point of the plain (one sensor, many poses) path.
+#include <algorithm>
 #include <string>
+#include <vector>
 
 #include "internal.h"
 #include "launch.h"
@@ -13,6 +15,11 @@
 #define RMG_DEFAULT_WIDE 0
 #endif
 
+// Warp-synchronous packet walk when the launch config leaves the choice open.
+#ifndef RMG_DEFAULT_PACKET
+#define RMG_DEFAULT_PACKET 0
+#endif
+
 namespace rmg {
 
 // Defaults from a sweep on the 1M-triangle terrain (spherical 128x1024): short
@@ -23,6 +30,7 @@ int default_config(const rmg_sensor* s, rmg_launch_config* cfg) {
   cfg->refill = 0;
   cfg->chunk = 4;
   cfg->bvh_width = 0;
+  cfg->packet = 2;
   if (s && s->width >= 8 && s->height >= 4) { cfg->tile_w = 8; cfg->tile_h = 4; }
   else if (s && s->height < 4 && s->height > 1) { cfg->tile_w = 16; cfg->tile_h = 2; }
   else { cfg->tile_w = 32; cfg->tile_h = 1; }
@@ -42,6 +50,7 @@ int check_config(const rmg_launch_config& c) {
   if (c.refill && (c.chunk < 1 || c.chunk > 1024)) return fail(RMG_ERR_UNSUPPORTED, "launch config: chunk 1..1024");
   if (c.bvh_width != 0 && c.bvh_width != 2 && c.bvh_width != 4)
     return fail(RMG_ERR_UNSUPPORTED, "launch config: bvh_width must be 0, 2 or 4");
+  if (c.packet > 2) return fail(RMG_ERR_UNSUPPORTED, "launch config: packet must be 0, 1 or 2");
   return RMG_OK;
 }
 
@@ -75,6 +84,9 @@ int make_trace_params(const rmg_map* map, const rmg_sensor* sensor, const rmg_tr
   P.wide = (cfg.bvh_width != 2 && cfg.refill == 0 && map->d_nodes4 && 3 * map->depth4 <= (unsigned)kStack4 &&
             RMG_DEFAULT_WIDE) ? 1 : 0;
   if (cfg.bvh_width == 4 && cfg.refill == 0 && map->d_nodes4 && 3 * map->depth4 <= (unsigned)kStack4) P.wide = 1;
+  // warp-synchronous packet walk: binary tree, full stack
+  const bool want_packet = cfg.packet == 1 || (cfg.packet == 2 && RMG_DEFAULT_PACKET);
+  P.packet = (want_packet && !P.wide && cfg.refill == 0 && P.full_stack) ? 1 : 0;
   return RMG_OK;
 }
 
@@ -150,4 +162,71 @@ extern "C" int rmg_simulate(const rmg_map* map, const rmg_sensor* sensor, const 
                             const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
                             void* stream) {
   return rmg_simulate_ex(map, sensor, Tsb, Tbm, n_poses, out, nullptr, stream);
+}
+
+// Launch autotuner for one (map, sensor, pose set): times a fixed list of
+// candidate configurations -- per-ray binary walk, warp packet walk and 4-wide
+// walk, each with three tile shapes and two CTA sizes -- on the caller's own
+// poses and output buffers (every candidate writes the same results) and
+// returns the fastest by median of `reps` timed runs after one warm-up run.
+// Synchronises.  No counterpart in the reference.
+extern "C" int rmg_autotune_launch_config(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                                          const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
+                                          uint32_t reps, rmg_launch_config* best, void* stream) {
+  if (!map || !sensor || !Tsb || !Tbm || !out || !best || n_poses == 0)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_autotune_launch_config: NULL argument or no poses");
+  reps = std::max(1u, std::min(reps, 50u));
+  cudaStream_t st = as_stream(stream);
+  rmg_launch_config base;
+  default_config(sensor, &base);
+  struct Walk { uint32_t bvh_width, packet; };
+  const Walk walks[3] = {{2, 0}, {2, 1}, {4, 0}};
+  const uint32_t tiles[3][2] = {{8, 4}, {16, 2}, {4, 8}};
+  const uint32_t warps[2] = {4, 2};
+  cudaEvent_t e0, e1;
+  RMG_CUDA_TRY(cudaEventCreate(&e0));
+  RMG_CUDA_TRY(cudaEventCreate(&e1));
+  float best_ms = 1e30f;
+  int s = RMG_OK;
+  bool any = false;
+  for (const Walk& w : walks) {
+    for (const auto& t : tiles) {
+      for (uint32_t bw : warps) {
+        rmg_launch_config c = base;
+        c.bvh_width = w.bvh_width;
+        c.packet = w.packet;
+        c.tile_w = t[0];
+        c.tile_h = t[1];
+        c.block_warps = bw;
+        if (c.tile_w > sensor->width && c.tile_w != base.tile_w) continue;
+        if (check_config(c) != RMG_OK) continue;
+        TraceParams P;
+        make_trace_params(map, sensor, Tsb, Tbm, n_poses, out, c, P);
+        if ((w.bvh_width == 4 && !P.wide) || (w.packet == 1 && !P.packet)) continue;  // not available here
+        s = launch_plain(P, sensor, c, st);
+        if (s != RMG_OK) break;
+        std::vector<float> ms;
+        for (uint32_t r = 0; r < reps && s == RMG_OK; ++r) {
+          s = cuda_status(cudaEventRecord(e0, st), "event");
+          if (s == RMG_OK) s = launch_plain(P, sensor, c, st);
+          if (s == RMG_OK) s = cuda_status(cudaEventRecord(e1, st), "event");
+          if (s == RMG_OK) s = cuda_status(cudaEventSynchronize(e1), "event sync");
+          float x = 0.f;
+          if (s == RMG_OK) s = cuda_status(cudaEventElapsedTime(&x, e0, e1), "event time");
+          ms.push_back(x);
+        }
+        if (s != RMG_OK) break;
+        std::sort(ms.begin(), ms.end());
+        const float med = ms[ms.size() / 2];
+        if (med < best_ms) { best_ms = med; *best = c; any = true; }
+      }
+      if (s != RMG_OK) break;
+    }
+    if (s != RMG_OK) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (s != RMG_OK) return s;
+  if (!any) *best = base;
+  return RMG_OK;
 }

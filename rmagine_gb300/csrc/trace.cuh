@@ -328,6 +328,9 @@ struct RayTrav {
   }
 };
 
+// Full-stack size of the binary walks (tree depth <= 32).
+constexpr int kFullStack = 32;
+
 // Trail tag of the 4-wide traversal (trace_ray4); the other tags are trail widths.
 constexpr int kWideTB = 4;
 // Stack of the 4-wide traversal: a visit pushes at most three children, so a
@@ -413,6 +416,96 @@ __device__ __forceinline__ void trace_ray4(const DeviceMap& map, const V& o, con
   }
 }
 
+// Trail tag of the warp-synchronous packet walk (trace_ray_packet).
+constexpr int kPacketTB = 1;
+
+// Warp-synchronous walk of the binary tree for the 32 rays of one tile: the
+// warp moves through the tree together and visits a node when any lane's ray
+// needs it (__any_sync), so every node is loaded once per warp (a broadcast)
+// and all branching is uniform; each lane keeps its own culling distance and
+// closest hit, so every ray's result is the same as in its own walk.  The
+// nearer child goes first when more lanes enter it first.  Lanes without a
+// ray (ragged tiles) take part with no culling distance at all.  All 32 lanes
+// must call this together.  Pending nodes: one index per level for the warp
+// (held by every lane), each lane's own entry distance (+inf where its ray did
+// not enter the node).  It pays when a tile's rays share most of their paths
+// (measured: 2,412-triangle room with VLP-16 +33%, 1M-triangle terrain with a
+// 640 x 480 camera +6%) and loses where they part early (the terrain with the
+// 128 x 1024 spherical sensor, whose near-horizon rows reach very different
+// ranges: -9%).  A variant that let the lanes go their own ways once few of
+// them shared the path was slower everywhere (lanes never regroup).
+__device__ __forceinline__ void trace_ray_packet(const DeviceMap& map, const V& o, const V& d, float tfar,
+                                                 bool active, unsigned budget, Hit& h, bool& over_budget) {
+  h.t = active ? tfar : -1.0f;
+  h.tri = -1;
+  h.face = 0xffffffffu;
+  if (map.root < 0) {
+    h.t = tfar;
+    return;
+  }
+  const RayW rw = make_rayw(o, d);
+  const RayBox rb = make_raybox(o, d);
+  int stk_node[kFullStack];
+  float stk_t[kFullStack];
+  int sp = 0;
+  int node = map.root;
+  unsigned steps = 0;
+  const float inf = __int_as_float(0x7f800000);
+  while (true) {
+    if (++steps > budget) { over_budget = true; break; }
+    const Node* np = map.nodes + node;
+    const float4 a = __ldg(&np->a);
+    const float4 b = __ldg(&np->b);
+    const float4 c = __ldg(&np->c);
+    const int4 ln = __ldg(&np->d);
+    float tminL, tmaxL, tminR, tmaxR;
+    slab(rb, a.x, a.y, a.z, a.w, c.x, c.y, tminL, tmaxL);
+    slab(rb, b.x, b.y, b.z, b.w, c.z, c.w, tminR, tmaxR);
+    bool hitL = visit(tminL, tmaxL, h.t);
+    bool hitR = visit(tminR, tmaxR, h.t);
+    if (ln.x < 0) {  // uniform: the node is the same for the whole warp
+      if (hitL) test_tri(map, rw, ~ln.x, h);
+      hitL = false;
+    }
+    if (ln.y < 0) {
+      if (hitR) test_tri(map, rw, ~ln.y, h);
+      hitR = false;
+    }
+    const float cull = h.t * kWiden;
+    hitL = hitL && tminL <= cull;
+    hitR = hitR && tminR <= cull;
+    const bool anyL = __any_sync(0xffffffffu, hitL), anyR = __any_sync(0xffffffffu, hitR);
+    if (anyL && anyR) {
+      if (sp >= kFullStack) { over_budget = true; break; }  // only a corrupt tree gets this deep
+      const bool prefL = hitL && (!hitR || tminL <= tminR);
+      const bool prefR = hitR && !prefL;
+      const bool leftFirst = __popc(__ballot_sync(0xffffffffu, prefL)) >= __popc(__ballot_sync(0xffffffffu, prefR));
+      stk_node[sp] = leftFirst ? ln.y : ln.x;
+      stk_t[sp] = leftFirst ? (hitR ? tminR : inf) : (hitL ? tminL : inf);
+      ++sp;
+      node = leftFirst ? ln.x : ln.y;
+      continue;
+    }
+    if (anyL || anyR) {
+      node = anyL ? ln.x : ln.y;
+      continue;
+    }
+    bool found = false;
+    while (sp > 0) {
+      --sp;
+      const bool want = stk_t[sp] <= h.t * kWiden;
+      if (__any_sync(0xffffffffu, want)) { node = stk_node[sp]; found = true; break; }
+    }
+    if (!found) break;
+  }
+  if (!active) h.t = tfar;
+  if (over_budget) {
+    h.tri = -1;
+    h.t = tfar;
+    h.face = 0xffffffffu;
+  }
+}
+
 template <int SS, int TB>
 __device__ __forceinline__ void trace_ray(const DeviceMap& map, const V& o, const V& d, float tfar,
                                           unsigned budget, Hit& h, bool& over_budget) {
@@ -446,9 +539,9 @@ struct TraceParams {
   int trail_bits;
   int full_stack;  // internal depth < kFullStack: the traversal may keep every pending child on a stack
   int wide;        // walk the 4-wide tree (map.nodes4)
+  int packet;      // warp-synchronous packet walk of the binary tree
 };
 
-constexpr int kFullStack = 32;
 
 // Hit point in the sensor frame: dir_s * t (+ orig_s for per-ray origins),
 // SphereSimulatorEmbree.tcc:127-133 / O1DnSimulatorEmbree.tcc:132.
@@ -568,8 +661,9 @@ __global__ void __launch_bounds__(256, RMG_TRACE_MIN_BLOCKS) k_trace(const Trace
   const uint32_t vid = ty * P.tile_h + (lane >> P.tile_w_log2);
   const uint32_t hid = tx * tile_w + (lane & (tile_w - 1));
   const uint32_t W = P.sen.width, H = P.sen.height;
-  if (vid >= H || hid >= W) return;
-  const uint32_t loc = vid * W + hid;
+  const bool inside = vid < H && hid < W;
+  if (TB != kPacketTB && !inside) return;  // the packet walk needs every lane
+  const uint32_t loc = inside ? vid * W + hid : 0;
   const uint64_t gid = (uint64_t)pose * W * H + loc;
 
   const Tf Tsm = tmul(load_tf(P.Tbm[pose]), P.Tsb);
@@ -577,7 +671,12 @@ __global__ void __launch_bounds__(256, RMG_TRACE_MIN_BLOCKS) k_trace(const Trace
   setup_ray<OK>(P.sen, Tsm, loc, dir_s, orig_s, o, d);
   Hit h;
   bool over = false;
-  trace_ray<SS, TB>(P.map, o, d, P.sen.range_max, P.budget, h, over);
+  if constexpr (TB == kPacketTB) {
+    trace_ray_packet(P.map, o, d, P.sen.range_max, inside, P.budget, h, over);
+    if (!inside) return;
+  } else {
+    trace_ray<SS, TB>(P.map, o, d, P.sen.range_max, P.budget, h, over);
+  }
   if (over) atomicExch(P.map.status, (unsigned)RMG_ERR_TRAVERSAL_BUDGET);
   write_attributes<OK>(P, gid, h, dir_s, orig_s, Tsm);
 }

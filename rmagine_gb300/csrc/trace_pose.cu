@@ -14,6 +14,10 @@ cudaError_t by_trail(const TraceParams& P, unsigned grid, unsigned block, cudaSt
     k_trace<ORIGIN_POSE, 0, kWideTB><<<grid, block, 0, st>>>(P);
     return cudaGetLastError();
   }
+  if (P.packet) {  // the warp walks together: same results
+    k_trace<ORIGIN_POSE, 0, kPacketTB><<<grid, block, 0, st>>>(P);
+    return cudaGetLastError();
+  }
   if (SS > 0 && P.full_stack) {  // same visits and results, without trail bookkeeping
     k_trace<ORIGIN_POSE, kFullStack, 0><<<grid, block, 0, st>>>(P);
     return cudaGetLastError();

@@ -313,8 +313,9 @@ def outputs_c(bundle: Bundle) -> L.OutputsC:
     return o
 
 
-def launch_config(stack_depth=16, block_warps=4, tile_w=8, tile_h=4, refill=0, chunk=4, bvh_width=0) -> L.LaunchConfigC:
-    return L.LaunchConfigC(stack_depth, block_warps, tile_w, tile_h, refill, chunk, bvh_width)
+def launch_config(stack_depth=16, block_warps=4, tile_w=8, tile_h=4, refill=0, chunk=4, bvh_width=0,
+                  packet=2) -> L.LaunchConfigC:
+    return L.LaunchConfigC(stack_depth, block_warps, tile_w, tile_h, refill, chunk, bvh_width, packet)
 
 
 # ---- simulators -------------------------------------------------------------------
@@ -405,6 +406,27 @@ class _Simulator:
                                      C.c_void_p(Tbm_d.data_ptr()), n, C.byref(out),
                                      C.byref(self.launch_config), stream)
         L.check(st, "rmg_simulate")
+
+    def autotune(self, Tbm, bundle: Bundle | None = None, attrs: Iterable[str] | None = None, reps: int = 3):
+        """Times the launch configurations of rmg_autotune_launch_config on these poses (and this
+        bundle, or one with `attrs`) and keeps the fastest in self.launch_config.  Single-mesh maps
+        only; results do not depend on the choice."""
+        if isinstance(self._map, Scene):
+            raise L.RmgError(L.RMG_ERR_UNSUPPORTED, "autotune", "needs a single-mesh Map")
+        self._check_ready()
+        if not isinstance(Tbm, torch.Tensor):
+            Tbm = torch.as_tensor(np.asarray(Tbm, np.float32).reshape(-1, 8))
+        Tbm_d = Tbm.reshape(-1, 8).to("cuda").contiguous()
+        n = Tbm_d.shape[0]
+        if bundle is None:
+            bundle = Bundle(*(attrs if attrs is not None else ATTRIBUTES))
+            resize_memory_bundle(bundle, self.sensor.width, self.sensor.height, n, device="cuda")
+        out = outputs_c(bundle)
+        best = L.LaunchConfigC()
+        L.call("rmg_autotune_launch_config", self._map.handle, self.sensor.handle, C.byref(self._Tsb),
+               C.c_void_p(Tbm_d.data_ptr()), n, C.byref(out), int(reps), C.byref(best), _stream_ptr())
+        self.launch_config = best
+        return best
 
     def simulate_statistics(self, Tbm, dataset_points, dataset_mask=None, dataset_ids=None, pre=None,
                             params=None, point_to_plane: bool = True, want_stats: bool = True,

@@ -175,6 +175,8 @@ def test_stack_depths_and_tiles_bitwise_identical():
     for cfg in [(0, 4, 8, 4, 0, 4, 2), (16, 2, 8, 4, 0, 4, 2), (16, 8, 32, 1, 0, 4, 2), (8, 1, 4, 8, 0, 4, 2),
                 (8, 4, 16, 2, 0, 4, 2), (0, 8, 2, 16, 0, 4, 2),
                 (16, 4, 8, 4, 0, 4, 4), (16, 2, 16, 2, 0, 4, 4), (16, 8, 32, 1, 0, 4, 4), (16, 4, 8, 4),
+                (16, 4, 8, 4, 0, 4, 2, 1), (16, 2, 16, 2, 0, 4, 2, 1), (16, 8, 32, 1, 0, 4, 2, 1),
+                (16, 4, 4, 8, 0, 4, 0, 1),
                 (8, 4, 8, 4, 16, 4), (16, 2, 8, 4, 32, 1), (8, 8, 16, 2, 1, 7), (16, 4, 4, 8, 24, 64)]:
         other = gpu_sim(m, model, poses, cfg=rm.launch_config(*cfg))
         for a in ALL:
@@ -206,7 +208,7 @@ def test_ragged_tiles_and_single_pose():
                                theta=sensors.DiscreteInterval(-3.0, 0.16, 37), range=sensors.Interval(0.1, 50.0))
     got, _, _ = check_parity(sc.vertices, sc.faces, m, scenes.room_poses(1, seed=3))
     mp = rm.Map(sc.vertices, sc.faces)
-    for cfg in [(8, 4, 8, 4, 32, 1), (16, 2, 8, 4, 8, 3)]:
+    for cfg in [(8, 4, 8, 4, 32, 1), (16, 2, 8, 4, 8, 3), (16, 4, 8, 4, 0, 4, 2, 1), (16, 4, 16, 2, 0, 4, 4, 0)]:
         other = gpu_sim(mp, m, scenes.room_poses(1, seed=3), cfg=rm.launch_config(*cfg))
         for a in ALL:
             assert np.array_equal(got[a].view(np.uint8), other[a].view(np.uint8)), (cfg, a)
@@ -281,7 +283,7 @@ def test_corrupt_tree_reports_budget_error_not_a_fault():
     internal = int(root_links[0]) if root_links[0] >= 0 else int(root_links[1])
     _lib.call("rmg_map_debug_set_child", m.handle, internal, 0, 0)  # child -> root: a cycle
     model = sensors.vlp16_900()
-    for cfg in [(0, 4, 8, 4), (8, 4, 8, 4)]:
+    for cfg in [(0, 4, 8, 4), (8, 4, 8, 4), (16, 4, 8, 4, 0, 4, 2, 1)]:
         gpu_sim(m, model, scenes.room_poses(2, seed=9), attrs=("ranges",), cfg=rm.launch_config(*cfg))
         assert m.status(clear=True) == _lib.RMG_ERR_TRAVERSAL_BUDGET
     # the device is still healthy
@@ -302,6 +304,20 @@ def test_corrupt_wide_tree_reports_budget_error_not_a_fault():
     assert m.status(clear=True) == _lib.RMG_ERR_TRAVERSAL_BUDGET
     got = gpu_sim(m, model, scenes.room_poses(2, seed=9), attrs=("ranges",), cfg=rm.launch_config(bvh_width=2))
     assert m.status() == 0 and np.array_equal(got["ranges"], want["ranges"])
+
+
+def test_autotune_returns_a_config_with_identical_results():
+    sc = scenes.box_room(seed=3, n_boxes=40)
+    m = rm.Map(sc.vertices, sc.faces)
+    model = sensors.vlp16_900()
+    poses = scenes.room_poses(6, seed=4)
+    want = gpu_sim(m, model, poses)
+    sim = rm.make_simulator(model, m)
+    cfg = sim.autotune(torch.from_numpy(poses).cuda(), attrs=ALL, reps=2)
+    assert cfg.tile_w * cfg.tile_h == 32 and cfg.bvh_width in (2, 4) and cfg.packet in (0, 1)
+    got = gpu_sim(m, model, poses, cfg=cfg)
+    for a in ALL:
+        assert np.array_equal(got[a].view(np.uint8), want[a].view(np.uint8)), a
 
 
 def test_stream_wait_timeout_and_success():
