@@ -56,7 +56,8 @@ WORK_PER_RAY = {
 # Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the dominant kernel,
 # from one ncu capture of the workload (profiles/).
 TRAFFIC: dict = {
-    "terrain1m_spherical": 2944196608 + 4433009664,
+    # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
+    "terrain1m_spherical": 10 * (315226112 + 437777920),
     "icp_stats_fwd": 6442640128 + 4728320,
     "icp_stats_bwd": 6444127744 + 6394882560,
     "pose_grad": 13100006912 + 351378688,
@@ -250,7 +251,11 @@ def gpu_raycast(args, world):
     sim = rm.make_simulator(model, m)
     Tbm = torch.from_numpy(poses).to(dev)
     bundle = rm.resize_memory_bundle(rm.Bundle(*attrs), W, H, n, device=dev)
-    tuned = sim.autotune(Tbm, bundle, reps=3)  # fastest launch configuration for this map, sensor and poses
+    if args.no_autotune:
+        tuned = rm.launch_config()
+        sim.launch_config = tuned
+    else:
+        tuned = sim.autotune(Tbm, bundle, reps=3)  # fastest launch configuration for this map, sensor and poses
     for _ in range(args.warmup):
         sim.simulate(Tbm, bundle)
     torch.cuda.synchronize(dev)
@@ -862,6 +867,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="terrain1m_spherical")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="ray-cast workloads: the default launch configuration")
     ap.add_argument("--poses", type=int, default=0, help="use only the first N poses / batches (profiling case)")
     args = ap.parse_args()
 
