@@ -13,7 +13,12 @@
 //   SimulatorX::setMap/setTsb/
 //     setModel/simulate              SimulatorEmbree.hpp:52-72, SphereSimulatorEmbree.hpp:107-159,
 //                                    SphereSimulatorOptix.hpp:122-190
-//   statistics_p2p / umeyama         math/statistics.h:72-157, math/optimization.h:61-75
+//   statistics_p2p / _p2l / umeyama  math/statistics.h:72-157, math/optimization.h:61-75
+//   InstancedScene / Instance        EmbreeScene / EmbreeInstance (map/embree/EmbreeScene.hpp,
+//                                    EmbreeInstance.hpp), OptixScene instances
+//   GaussianNoiseGB300 / ...         noise/GaussianNoiseCuda.hpp, RelGaussianNoiseCuda.hpp,
+//                                    UniformDustNoiseCuda.hpp, Noise.hpp (Options)
+//   read_mesh / import_map           AssimpIO::ReadFile + import_embree_map (EmbreeMap.hpp:94-117)
 // Errors throw rmagine_gb300::Exception, as rmagine's RM_THROW does (util/exceptions.h:48).
 #pragma once
 
@@ -276,6 +281,8 @@ class TriangleMap {
                         reinterpret_cast<const rmg_face*>(F.raw()), (uint32_t)F.size(), s, &h_),
           "rmg_map_build");
   }
+  // adopts a handle (rmg_map_load); used by load()
+  explicit TriangleMap(rmg_map* h) : h_(h) {}
   ~TriangleMap() { rmg_map_destroy(h_); }
   TriangleMap(const TriangleMap&) = delete;
   TriangleMap& operator=(const TriangleMap&) = delete;
@@ -284,11 +291,113 @@ class TriangleMap {
     check(rmg_map_refit(h_, reinterpret_cast<const rmg_vec3*>(V.raw()), (uint32_t)V.size(), s), "rmg_map_refit");
   }
   int status(bool clear = true) { return rmg_map_status(h_, clear ? 1 : 0); }
+  // the built map (mesh + tree) to a file, and back without a rebuild
+  void save(const std::string& path) const { check(rmg_map_save(h_, path.c_str()), "rmg_map_save"); }
+  static std::shared_ptr<TriangleMap> load(const std::string& path, cudaStream_t s = 0) {
+    rmg_map* h = nullptr;
+    check(rmg_map_load(path.c_str(), s, &h), "rmg_map_load");
+    return std::make_shared<TriangleMap>(h);
+  }
 
  private:
   rmg_map* h_ = nullptr;
 };
 using MapPtr = std::shared_ptr<TriangleMap>;
+
+// ---- mesh files ---------------------------------------------------------------------
+struct MeshData {
+  Memory<Vector3, RAM> vertices;
+  Memory<Face, RAM> faces;
+  Memory<uint32_t, RAM> groups;  // group (OBJ object / group) of each face
+  uint32_t n_groups = 0;
+};
+
+inline MeshData read_mesh(const std::string& path) {
+  rmg_mesh m{};
+  check(rmg_mesh_read(path.c_str(), &m), "rmg_mesh_read");
+  MeshData out;
+  out.vertices.resize(m.n_vertices);
+  out.faces.resize(m.n_faces);
+  out.groups.resize(m.n_faces);
+  if (m.n_vertices) std::memcpy(out.vertices.raw(), m.vertices, sizeof(Vector3) * m.n_vertices);
+  if (m.n_faces) {
+    std::memcpy(out.faces.raw(), m.faces, sizeof(Face) * m.n_faces);
+    std::memcpy(out.groups.raw(), m.face_group, 4ull * m.n_faces);
+  }
+  out.n_groups = m.n_groups;
+  rmg_mesh_free(&m);
+  return out;
+}
+
+inline void write_ply(const std::string& path, const Memory<Vector3, RAM>& V, const Memory<Face, RAM>& F) {
+  check(rmg_mesh_write_ply(path.c_str(), reinterpret_cast<const rmg_vec3*>(V.raw()), (uint32_t)V.size(),
+                           reinterpret_cast<const rmg_face*>(F.raw()), (uint32_t)F.size()),
+        "rmg_mesh_write_ply");
+}
+
+// import_embree_map for one mesh: every face of the file in one map.
+inline MapPtr import_map(const std::string& path, cudaStream_t s = 0) {
+  const MeshData m = read_mesh(path);
+  return std::make_shared<TriangleMap>(m.vertices, m.faces, s);
+}
+
+// ---- instanced scenes ---------------------------------------------------------------
+struct Instance {
+  uint32_t geometry = 0;  // index into the scene's geometries
+  uint32_t geom_id = 0;   // GeomIds of its hits
+  uint32_t object_id = 0; // ObjectIds of its hits
+  Transform T = Transform::Identity();
+  Vector3 scale{1.f, 1.f, 1.f};
+};
+
+class InstancedScene {
+ public:
+  InstancedScene(std::vector<MapPtr> geometries, const std::vector<Instance>& instances, cudaStream_t s = 0)
+      : geoms_(std::move(geometries)) {
+    std::vector<const rmg_map*> h;
+    for (const auto& g : geoms_) h.push_back(g->handle());
+    const auto c = to_c(instances);
+    check(rmg_scene_create(h.data(), (uint32_t)h.size(), c.data(), (uint32_t)c.size(), s, &h_), "rmg_scene_create");
+  }
+  ~InstancedScene() { rmg_scene_destroy(h_); }
+  InstancedScene(const InstancedScene&) = delete;
+  InstancedScene& operator=(const InstancedScene&) = delete;
+  void update(const std::vector<Instance>& instances, bool rebuild = false, cudaStream_t s = 0) {
+    const auto c = to_c(instances);
+    check(rmg_scene_update(h_, c.data(), (uint32_t)c.size(), rebuild ? 1 : 0, s), "rmg_scene_update");
+  }
+  int status(bool clear = true) { return rmg_scene_status(h_, clear ? 1 : 0); }
+  rmg_scene* handle() const { return h_; }
+
+ private:
+  static std::vector<rmg_instance_desc> to_c(const std::vector<Instance>& in) {
+    std::vector<rmg_instance_desc> c(in.size());
+    for (size_t i = 0; i < in.size(); ++i) {
+      c[i].geometry = in[i].geometry;
+      c[i].geom_id = in[i].geom_id;
+      c[i].object_id = in[i].object_id;
+      std::memcpy(&c[i].T, &in[i].T, sizeof(rmg_transform));
+      c[i].scale = rmg_vec3{in[i].scale.x, in[i].scale.y, in[i].scale.z};
+    }
+    return c;
+  }
+  std::vector<MapPtr> geoms_;  // the scene references them
+  rmg_scene* h_ = nullptr;
+};
+using ScenePtr = std::shared_ptr<InstancedScene>;
+
+// ---- statistics types (used by the simulators' fused step) ------------------------------
+struct CrossStatistics {
+  Vector3 dataset_mean, model_mean;
+  float covariance[9];  // column-major, like rmagine::Matrix3x3
+  uint32_t n_meas;
+};
+static_assert(sizeof(CrossStatistics) == sizeof(rmg_cross_stats), "CrossStatistics is 64 bytes");
+
+struct UmeyamaReductionConstraints {
+  float max_dist;
+  uint32_t dataset_id, model_id;
+};
 
 // ---- simulators ---------------------------------------------------------------------------
 template <typename ModelT>
@@ -300,8 +409,51 @@ class SimulatorGB300 {
   SimulatorGB300(const SimulatorGB300&) = delete;
   SimulatorGB300& operator=(const SimulatorGB300&) = delete;
 
-  void setMap(MapPtr map) { map_ = std::move(map); }
+  void setMap(MapPtr map) { map_ = std::move(map); scene_.reset(); }
+  // an instanced map (EmbreeMap over a scene with instances)
+  void setMap(ScenePtr scene) { scene_ = std::move(scene); map_.reset(); }
   MapPtr map() const { return map_; }
+  ScenePtr scene() const { return scene_; }
+  // Fastest launch configuration for these poses and outputs (rmg_autotune_launch_config);
+  // kept for later simulate calls.  Single-mesh maps.
+  template <typename BundleT>
+  rmg_launch_config autotune(const Memory<Transform, VRAM_CUDA>& Tbm, BundleT& ret, uint32_t reps = 3,
+                             cudaStream_t stream = 0) {
+    ready();
+    if (!map_) throw Exception(RMG_ERR_UNSUPPORTED, "autotune: needs a single-mesh map");
+    const rmg_outputs o = outputs_of(ret);
+    rmg_launch_config c{};
+    check(rmg_autotune_launch_config(map_->handle(), sensor_, reinterpret_cast<const rmg_transform*>(&Tsb_),
+                                     reinterpret_cast<const rmg_transform*>(Tbm.raw()), (uint32_t)Tbm.size(), &o,
+                                     reps, &c, stream),
+          "rmg_autotune_launch_config");
+    cfg_ = c;
+    tuned_ = true;
+    return c;
+  }
+  // The correction loop's inner step fused (rmg_simulate_statistics): simulate at Tbm,
+  // statistics_p2l (p2l) or _p2p against `dataset` (one scan of width*height points for every
+  // pose, or one per pose when per_pose), optionally pre-transformed, and Umeyama.
+  void simulateStatistics(const Memory<Transform, VRAM_CUDA>& Tbm, const Memory<Vector3, VRAM_CUDA>& dataset,
+                          const Memory<uint8_t, VRAM_CUDA>* dataset_mask, bool per_pose,
+                          const Memory<Transform, VRAM_CUDA>* pre, const UmeyamaReductionConstraints& params,
+                          bool p2l, Memory<CrossStatistics, VRAM_CUDA>* stats, Memory<Transform, VRAM_CUDA>* Ts,
+                          cudaStream_t stream = 0) const {
+    ready();
+    if (!map_) throw Exception(RMG_ERR_UNSUPPORTED, "simulateStatistics: needs a single-mesh map");
+    if (stats) stats->resize(Tbm.size());
+    if (Ts) Ts->resize(Tbm.size());
+    const rmg_scan scan{reinterpret_cast<const rmg_vec3*>(dataset.raw()), dataset_mask ? dataset_mask->raw() : nullptr,
+                        nullptr, per_pose ? 1u : 0u};
+    const rmg_umeyama_constraints c{params.max_dist, params.dataset_id, params.model_id};
+    check(rmg_simulate_statistics(map_->handle(), sensor_, reinterpret_cast<const rmg_transform*>(&Tsb_),
+                                  reinterpret_cast<const rmg_transform*>(Tbm.raw()), (uint32_t)Tbm.size(), &scan,
+                                  pre ? reinterpret_cast<const rmg_transform*>(pre->raw()) : nullptr,
+                                  pre && pre->size() > 1 ? 1u : 0u, &c, p2l ? 1 : 0,
+                                  stats ? reinterpret_cast<rmg_cross_stats*>(stats->raw()) : nullptr,
+                                  Ts ? reinterpret_cast<rmg_transform*>(Ts->raw()) : nullptr, stream),
+          "rmg_simulate_statistics");
+  }
   void setTsb(const Transform& T) { Tsb_ = T; }
   void setModel(const ModelT& model) {
     const rmg_model c = model.to_c();
@@ -317,9 +469,16 @@ class SimulatorGB300 {
   void simulate(const Memory<Transform, VRAM_CUDA>& Tbm, BundleT& ret, cudaStream_t stream = 0) const {
     ready();
     const rmg_outputs o = outputs_of(ret);
-    check(rmg_simulate(map_->handle(), sensor_, reinterpret_cast<const rmg_transform*>(&Tsb_),
-                       reinterpret_cast<const rmg_transform*>(Tbm.raw()), (uint32_t)Tbm.size(), &o, stream),
-          "rmg_simulate");
+    const auto* T = reinterpret_cast<const rmg_transform*>(Tbm.raw());
+    const auto* Tsb = reinterpret_cast<const rmg_transform*>(&Tsb_);
+    if (scene_)
+      check(rmg_simulate_scene(scene_->handle(), sensor_, Tsb, T, (uint32_t)Tbm.size(), &o, stream),
+            "rmg_simulate_scene");
+    else if (tuned_)
+      check(rmg_simulate_ex(map_->handle(), sensor_, Tsb, T, (uint32_t)Tbm.size(), &o, &cfg_, stream),
+            "rmg_simulate_ex");
+    else
+      check(rmg_simulate(map_->handle(), sensor_, Tsb, T, (uint32_t)Tbm.size(), &o, stream), "rmg_simulate");
   }
 
   // Allocating device form: simulate<BundleT>(Tbm).
@@ -370,10 +529,13 @@ class SimulatorGB300 {
 
  private:
   void ready() const {
-    if (!map_) throw Exception(RMG_ERR_INVALID_ARG, "simulate: no map set");
+    if (!map_ && !scene_) throw Exception(RMG_ERR_INVALID_ARG, "simulate: no map set");
     if (!sensor_) throw Exception(RMG_ERR_INVALID_ARG, "simulate: no model set");
   }
   MapPtr map_;
+  ScenePtr scene_;
+  rmg_launch_config cfg_{};
+  bool tuned_ = false;
   rmg_sensor* sensor_ = nullptr;
   Transform Tsb_ = Transform::Identity();
   uint32_t W_ = 0, H_ = 0;
@@ -385,17 +547,6 @@ using O1DnSimulatorGB300 = SimulatorGB300<O1DnModel>;
 using OnDnSimulatorGB300 = SimulatorGB300<OnDnModel>;
 
 // ---- statistics / Umeyama -----------------------------------------------------------------
-struct CrossStatistics {
-  Vector3 dataset_mean, model_mean;
-  float covariance[9];  // column-major, like rmagine::Matrix3x3
-  uint32_t n_meas;
-};
-static_assert(sizeof(CrossStatistics) == sizeof(rmg_cross_stats), "CrossStatistics is 64 bytes");
-
-struct UmeyamaReductionConstraints {
-  float max_dist;
-  uint32_t dataset_id, model_id;
-};
 
 // statistics_p2p over n_batches batches of n_per_batch DEVICE correspondences.
 inline void statistics_p2p(const Memory<Vector3, VRAM_CUDA>& dataset, const Memory<Vector3, VRAM_CUDA>& model,
@@ -421,5 +572,89 @@ inline void umeyama_transform(const Memory<CrossStatistics, VRAM_CUDA>& stats, M
                               reinterpret_cast<rmg_transform*>(Ts.raw()), s),
         "rmg_umeyama_transform");
 }
+
+// statistics_p2l over n_batches batches of n_per_batch DEVICE correspondences (model points with normals).
+inline void statistics_p2l(const Memory<Vector3, VRAM_CUDA>& dataset, const Memory<Vector3, VRAM_CUDA>& model,
+                           const Memory<Vector3, VRAM_CUDA>& model_normals,
+                           const UmeyamaReductionConstraints& params, uint32_t n_batches,
+                           Memory<CrossStatistics, VRAM_CUDA>& stats, Memory<Transform, VRAM_CUDA>* Ts = nullptr,
+                           const Memory<uint8_t, VRAM_CUDA>* dataset_mask = nullptr,
+                           const Memory<uint8_t, VRAM_CUDA>* model_mask = nullptr, cudaStream_t s = 0) {
+  const uint32_t n_per = n_batches ? (uint32_t)(dataset.size() / n_batches) : 0;
+  stats.resize(n_batches);
+  if (Ts) Ts->resize(n_batches);
+  const rmg_umeyama_constraints c{params.max_dist, params.dataset_id, params.model_id};
+  check(rmg_statistics_p2l(nullptr, 0, reinterpret_cast<const rmg_vec3*>(dataset.raw()),
+                           dataset_mask ? dataset_mask->raw() : nullptr, nullptr,
+                           reinterpret_cast<const rmg_vec3*>(model.raw()),
+                           reinterpret_cast<const rmg_vec3*>(model_normals.raw()),
+                           model_mask ? model_mask->raw() : nullptr, nullptr, &c, n_batches, n_per,
+                           reinterpret_cast<rmg_cross_stats*>(stats.raw()),
+                           Ts ? reinterpret_cast<rmg_transform*>(Ts->raw()) : nullptr, s),
+        "rmg_statistics_p2l");
+}
+
+// out[i] = a[i] * b[i] on the device (Transform::mult); a one-element operand is repeated.
+inline void compose(const Memory<Transform, VRAM_CUDA>& a, const Memory<Transform, VRAM_CUDA>& b,
+                    Memory<Transform, VRAM_CUDA>& out, cudaStream_t s = 0) {
+  const size_t n = a.size() > b.size() ? a.size() : b.size();
+  if (out.raw() != a.raw()) out.resize(n);
+  check(rmg_transforms_compose(reinterpret_cast<const rmg_transform*>(a.raw()), a.size() > 1 ? 1u : 0u,
+                               reinterpret_cast<const rmg_transform*>(b.raw()), b.size() > 1 ? 1u : 0u,
+                               reinterpret_cast<rmg_transform*>(out.raw()), (uint32_t)n, s),
+        "rmg_transforms_compose");
+}
+
+// ---- range noise --------------------------------------------------------------------------
+struct NoiseOptions {  // Noise::Options
+  uint64_t seed = 42;
+  float max_range = 10000.0f;
+};
+
+class NoiseGB300 {
+ public:
+  // adds noise to DEVICE ranges in place; every call draws fresh numbers
+  void apply(Memory<float, VRAM_CUDA>& ranges, cudaStream_t s = 0) {
+    rmg_noise p = p_;
+    p.call = call_++;
+    check(rmg_noise_apply(&p, ranges.raw(), ranges.size(), s), "rmg_noise_apply");
+  }
+
+ protected:
+  NoiseGB300(uint32_t kind, const NoiseOptions& o) {
+    p_.kind = kind;
+    p_.seed = o.seed;
+    p_.max_range = o.max_range;
+  }
+  rmg_noise p_{};
+  uint64_t call_ = 0;
+};
+
+class GaussianNoiseGB300 : public NoiseGB300 {
+ public:
+  GaussianNoiseGB300(float mean, float stddev, const NoiseOptions& o = {}) : NoiseGB300(RMG_NOISE_GAUSSIAN, o) {
+    p_.mean = mean;
+    p_.stddev = stddev;
+  }
+};
+
+class RelGaussianNoiseGB300 : public NoiseGB300 {
+ public:
+  RelGaussianNoiseGB300(float mean, float stddev, float range_exp, const NoiseOptions& o = {})
+      : NoiseGB300(RMG_NOISE_REL_GAUSSIAN, o) {
+    p_.mean = mean;
+    p_.stddev = stddev;
+    p_.range_exp = range_exp;
+  }
+};
+
+class UniformDustNoiseGB300 : public NoiseGB300 {
+ public:
+  UniformDustNoiseGB300(float hit_probability, float return_probability, const NoiseOptions& o = {})
+      : NoiseGB300(RMG_NOISE_UNIFORM_DUST, o) {
+    p_.hit_probability = hit_probability;
+    p_.return_probability = return_probability;
+  }
+};
 
 }  // namespace rmagine_gb300

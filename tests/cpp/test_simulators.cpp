@@ -1,9 +1,14 @@
 // C++ API test: rmagine's own simulation known answers (tests/embree/simulation_*.cpp,
 // tests/optix/simulation_o1dn.cpp) and the CrossStatistics paper example
 // (tests/core/math_statistics.cpp:322-384), through include/rmagine_gb300.hpp, written
-// the way rmagine's tests are: an executable that throws on failure.
+// the way rmagine's tests are: an executable that throws on failure.  Then the
+// layer's other parts: an instanced scene, the fused correction step, noise,
+// mesh and map files, and the launch autotuner.
 #include <cmath>
 #include <cstdio>
+#include <cstring>
+#include <memory>
+#include <vector>
 #include <sstream>
 
 #include "rmagine_gb300.hpp"
@@ -123,6 +128,137 @@ static void test_stats_paper() {
           "statistics_p2p: paper example");
 }
 
+static rm::SphericalModel vlp16() {
+  rm::SphericalModel model;  // vlp16_900 (sensors.cpp:6-20)
+  model.theta = {(float)-M_PI, (float)(0.4 * M_PI / 180.0), 900};
+  model.phi = {(float)(-15.0 * M_PI / 180.0), (float)(2.0 * M_PI / 180.0), 16};
+  model.range = {0.5f, 130.0f};
+  return model;
+}
+
+// The cube placed by one identity instance gives the single-mesh results bit for bit.
+static void test_scene_identity_instance(const rm::MapPtr& map) {
+  rm::Instance inst;
+  inst.geom_id = 3;
+  inst.object_id = 9;
+  auto scene = std::make_shared<rm::InstancedScene>(std::vector<rm::MapPtr>{map}, std::vector<rm::Instance>{inst});
+  rm::SphereSimulatorGB300 a(map), b;
+  a.setModel(vlp16());
+  b.setModel(vlp16());
+  b.setMap(scene);
+  auto ra = a.simulate<rm::IntAttrAll<rm::RAM>>(identity_poses(2));
+  auto rb = b.simulate<rm::IntAttrAll<rm::RAM>>(identity_poses(2));
+  size_t hits = 0;
+  for (size_t i = 0; i < ra.ranges.size(); ++i) {
+    fail_if(std::memcmp(&ra.ranges[i], &rb.ranges[i], 4) != 0 || ra.face_ids[i] != rb.face_ids[i], "scene: ranges");
+    if (ra.hits[i]) {
+      ++hits;
+      fail_if(rb.object_ids[i] != 9 || rb.geom_ids[i] != 3, "scene: ids");
+    }
+  }
+  fail_if(hits == 0 || scene->status() != 0, "scene: no hits or device error");
+}
+
+// The fused step at the pose the dataset scan was taken from: identity transform.
+static void test_fused_step(const rm::MapPtr& map) {
+  rm::SphereSimulatorGB300 sim(map);
+  sim.setModel(vlp16());
+  rm::Memory<rm::Transform, rm::VRAM_CUDA> Td;
+  Td = identity_poses(1);
+  auto data = sim.simulate<rm::Bundle<rm::Hits<rm::VRAM_CUDA>, rm::Points<rm::VRAM_CUDA>>>(Td);
+  rm::Memory<rm::CrossStatistics, rm::VRAM_CUDA> st;
+  rm::Memory<rm::Transform, rm::VRAM_CUDA> T;
+  sim.simulateStatistics(Td, data.points, &data.hits, false, nullptr, {1.0f, 0, 0}, true, &st, &T);
+  rm::cuda_check(cudaDeviceSynchronize(), "sync");
+  rm::Memory<rm::CrossStatistics, rm::RAM> s;
+  s = st;
+  rm::Memory<rm::Transform, rm::RAM> t;
+  t = T;
+  rm::Memory<uint8_t, rm::RAM> h;
+  h = data.hits;
+  uint32_t n = 0;
+  for (size_t i = 0; i < h.size(); ++i) n += h[i] ? 1 : 0;
+  fail_if(s[0].n_meas != n || n == 0, "fused: n_meas");
+  fail_if(std::fabs(t[0].t.x) + std::fabs(t[0].t.y) + std::fabs(t[0].t.z) > 1e-5f ||
+              std::fabs(t[0].R.w - 1.0f) > 1e-6f,
+          "fused: not the identity");
+  // compose on the device: identity * T == T
+  rm::Memory<rm::Transform, rm::VRAM_CUDA> out;
+  rm::compose(Td, T, out);
+  rm::Memory<rm::Transform, rm::RAM> o;
+  o = out;
+  fail_if(std::memcmp(&o[0], &t[0], 28) != 0, "compose");
+}
+
+// Noise: two objects with the same seed draw the same numbers; the next call differs.
+static void test_noise() {
+  rm::Memory<float, rm::RAM> r(1001);
+  for (size_t i = 0; i < r.size(); ++i) r[i] = 1.0f + 0.01f * (float)i;
+  rm::Memory<float, rm::VRAM_CUDA> a, b;
+  a = r;
+  b = r;
+  rm::GaussianNoiseGB300 na(0.0f, 0.1f, {7, 10000.0f}), nb(0.0f, 0.1f, {7, 10000.0f});
+  na.apply(a);
+  nb.apply(b);
+  rm::Memory<float, rm::RAM> ha, hb;
+  ha = a;
+  hb = b;
+  fail_if(std::memcmp(ha.raw(), hb.raw(), 4 * ha.size()) != 0, "noise: not deterministic");
+  double sum = 0.0;
+  for (size_t i = 0; i < r.size(); ++i) sum += ha[i] - r[i];
+  fail_if(std::fabs(sum / r.size()) > 0.02, "noise: mean");
+  na.apply(a);
+  ha = a;
+  fail_if(std::memcmp(ha.raw(), hb.raw(), 4 * ha.size()) == 0, "noise: second call repeated");
+  rm::UniformDustNoiseGB300 dust(0.01f, 0.9f);
+  dust.apply(b);
+  rm::cuda_check(cudaDeviceSynchronize(), "sync");
+}
+
+// Mesh and map files round trip.
+static void test_files(const rm::MapPtr& map) {
+  rm::Memory<rm::Vector3, rm::RAM> V(8);
+  rm::Memory<rm::Face, rm::RAM> F(12);
+  const float c[8][3] = {{-0.5f, -0.5f, -0.5f}, {-0.5f, -0.5f, 0.5f}, {-0.5f, 0.5f, 0.5f}, {-0.5f, 0.5f, -0.5f},
+                         {0.5f, 0.5f, -0.5f},   {0.5f, 0.5f, 0.5f},   {0.5f, -0.5f, 0.5f}, {0.5f, -0.5f, -0.5f}};
+  for (int i = 0; i < 8; ++i) V[i] = {c[i][0], c[i][1], c[i][2]};
+  for (int i = 0; i < 12; ++i) F[i] = {(uint32_t)i % 8, (uint32_t)(i + 1) % 8, (uint32_t)(i + 3) % 8};
+  const std::string ply = "rmg_cpp_test_cube.ply", mp = "rmg_cpp_test_cube.rmgmap";
+  rm::write_ply(ply, V, F);
+  const rm::MeshData m = rm::read_mesh(ply);
+  fail_if(m.vertices.size() != 8 || m.faces.size() != 12 ||
+              std::memcmp(m.vertices.raw(), V.raw(), sizeof(rm::Vector3) * 8) != 0 ||
+              std::memcmp(m.faces.raw(), F.raw(), sizeof(rm::Face) * 12) != 0,
+          "files: PLY round trip");
+  map->save(mp);
+  auto loaded = rm::TriangleMap::load(mp);
+  rm::SphereSimulatorGB300 a(map), b(loaded);
+  a.setModel(vlp16());
+  b.setModel(vlp16());
+  auto ra = a.simulate<rm::IntAttrAll<rm::RAM>>(identity_poses(1));
+  auto rb = b.simulate<rm::IntAttrAll<rm::RAM>>(identity_poses(1));
+  fail_if(std::memcmp(ra.ranges.raw(), rb.ranges.raw(), 4 * ra.ranges.size()) != 0, "files: loaded map differs");
+  std::remove(ply.c_str());
+  std::remove(mp.c_str());
+}
+
+// The autotuner picks a configuration; results stay the same.
+static void test_autotune(const rm::MapPtr& map) {
+  rm::SphereSimulatorGB300 sim(map);
+  sim.setModel(vlp16());
+  rm::Memory<rm::Transform, rm::VRAM_CUDA> Td;
+  Td = identity_poses(4);
+  auto before = sim.simulate<rm::Bundle<rm::Ranges<rm::VRAM_CUDA>>>(Td);
+  const rmg_launch_config c = sim.autotune(Td, before, 2);
+  fail_if(c.tile_w * c.tile_h != 32, "autotune: config");
+  auto after = sim.simulate<rm::Bundle<rm::Ranges<rm::VRAM_CUDA>>>(Td);
+  rm::cuda_check(cudaDeviceSynchronize(), "sync");
+  rm::Memory<float, rm::RAM> x, y;
+  x = before.ranges;
+  y = after.ranges;
+  fail_if(std::memcmp(x.raw(), y.raw(), 4 * x.size()) != 0, "autotune: results changed");
+}
+
 int main() {
   try {
     auto map = make_cube_map();
@@ -131,6 +267,11 @@ int main() {
     test_o1dn(map);
     test_ondn_single_ray(map);
     test_stats_paper();
+    test_scene_identity_instance(map);
+    test_fused_step(map);
+    test_noise();
+    test_files(map);
+    test_autotune(map);
     fail_if(map->status() != 0, "device status");
   } catch (const std::exception& e) {
     std::fprintf(stderr, "FAILED: %s\n", e.what());
