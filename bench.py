@@ -776,7 +776,8 @@ def gpu_batched(args, world):
     torch.cuda.set_device(dev)
     sc = scenes.terrain(grid=1024, n_boxes=2000, seed=0)
     m = rm.Map(sc.vertices, sc.faces)
-    spec = batched.mixed_sensor_set(64, seed=0)
+    small = args.workload == "batched_small"
+    spec = batched.small_sensor_set(1024, seed=0) if small else batched.mixed_sensor_set(64, seed=0)
     if args.poses:
         spec = [(mod, min(c, args.poses)) for mod, c in spec]
     attrs = ("hits", "ranges")
@@ -813,6 +814,26 @@ def gpu_batched(args, world):
     torch.cuda.synchronize(dev)
     plain_ms, _, _ = Timer(dev, max(2, args.steps // 2)).run(plain, world)
     plain_ms = plain_ms / max(2, args.steps // 2)
+
+    # the same launches through the C ABI with every argument built beforehand: launch cost only
+    import ctypes as C
+
+    from rmagine_gb300 import _lib
+    from rmagine_gb300.simulation import _stream_ptr, outputs_c
+
+    lib = _lib.load()
+    prebuilt = [(sim.sensor.handle, C.byref(sim._Tsb), C.c_void_p(p.data_ptr()), p.shape[0], outputs_c(b))
+                for sim, p, b in jobs]
+    stream = _stream_ptr()
+
+    def plain_abi():
+        for sh, tsb, tp, n, out in prebuilt:
+            lib.rmg_simulate(m.handle, sh, tsb, tp, n, C.byref(out), stream)
+
+    plain_abi()
+    torch.cuda.synchronize(dev)
+    abi_ms, _, _ = Timer(dev, max(2, args.steps // 2)).run(plain_abi, world)
+    abi_ms = abi_ms / max(2, args.steps // 2)
     if m.status() != 0:
         raise RuntimeError("device status error in the timed region")
     value = world * rays * args.steps / (total_ms / 1e3) / 1e6
@@ -834,8 +855,10 @@ def gpu_batched(args, world):
     rl = roofline(5 + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
                   "per ray: Hits+Ranges 5 B + 64 B per node visit + 48 B per triangle test (work per ray of the "
                   "2.1M-triangle terrain's spherical workload used as the estimate)", TRAFFIC.get("batched"))
-    config = {"workload": "batched: terrain 1024x1024 + 2000 boxes (2,117,058 tris), 64 sensors from {VLP-16 16x900, "
-                          "spherical 128x2048, pinhole 640x480, O1Dn 10k dirs}, poses log-uniform [1,4096], Hits+Ranges",
+    config = {"workload": ("batched small sensors: terrain 1024x1024 + 2000 boxes (2,117,058 tris), 1024 sensors "
+                           "(O1Dn 256 dirs / pinhole 32x8, alternating), poses log-uniform [1,8], Hits+Ranges") if small
+              else ("batched: terrain 1024x1024 + 2000 boxes (2,117,058 tris), 64 sensors from {VLP-16 16x900, "
+                    "spherical 128x2048, pinhole 640x480, O1Dn 10k dirs}, poses log-uniform [1,4096], Hits+Ranges"),
               "sensors": len(jobs), "poses": int(sum(p.shape[0] for _, p, _ in jobs)), "rays_per_step": int(rays),
               "autotuned": {"stack_depth": best.stack_depth, "block_warps": best.block_warps,
                             "tile": f"{best.tile_w}x{best.tile_h}", "grab": best.grab, "tuning_s": round(tune_s, 2)},
@@ -847,6 +870,10 @@ def gpu_batched(args, world):
             "plain_one_launch_per_sensor": {"value": round(rays / (plain_ms / 1e3) / 1e6, 2), "unit": "Mrays/s",
                                             "ms_per_step": round(plain_ms, 3), "launches_per_step": len(jobs)},
             "speedup_vs_plain": round(plain_ms / (total_ms / args.steps), 3),
+            "plain_c_abi_loop": {"value": round(rays / (abi_ms / 1e3) / 1e6, 2), "unit": "Mrays/s",
+                                 "ms_per_step": round(abi_ms, 3),
+                                 "what": "one rmg_simulate per sensor, arguments built before the timed region"},
+            "speedup_vs_c_abi_loop": round(abi_ms / (total_ms / args.steps), 3),
             "e2e": {"value": round(e2e, 2), "unit": "Mrays/s",
                     "h2d_bytes_per_step": int(sum(p.numel() * 4 for _, p, _ in jobs)),
                     "d2h_bytes_per_step": int(5 * rays)},
@@ -892,7 +919,7 @@ def main():
         line, cpu, _ = gpu_icp(args, world)
     elif args.workload == "pose_grad":
         line, cpu, _ = gpu_posegrad(args, world)
-    elif args.workload == "batched":
+    elif args.workload in ("batched", "batched_small"):
         line, cpu, _ = gpu_batched(args, world)
     elif args.workload == "rcc_fused":
         line, cpu, _ = gpu_rcc(args, world)

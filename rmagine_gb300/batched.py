@@ -150,3 +150,24 @@ def mixed_sensor_set(n_sensors: int, seed: int, max_poses: int = 4096):
             m = o1
         out.append((m, int(max(1, c))))
     return out
+
+
+def small_sensor_set(n_sensors: int, seed: int, max_poses: int = 8):
+    """Many small sensors, where one launch per sensor is launch-bound: O1Dn sensors of 256
+    directions (each its own set, uniform on the sphere, origin (0.05, 0, 0.1)) and 32x8 pinhole
+    cameras, alternating, with floor(exp(U(ln 1, ln max_poses))) poses per sensor."""
+    import numpy as np
+
+    from . import sensors
+
+    rng = np.random.default_rng(seed)
+    counts = np.floor(np.exp(rng.uniform(0.0, np.log(max_poses), n_sensors))).astype(int)
+    out = []
+    for i, c in enumerate(counts):
+        if i % 2 == 0:
+            m = sensors.O1DnModel(width=256, height=1, range=sensors.Interval(0.3, 130.0), orig=(0.05, 0.0, 0.1),
+                                  dirs=sensors.sphere_directions(256, seed=seed + 1000 + i))
+        else:
+            m = sensors.depth_camera(32, 8, 60.0, 0.3, 130.0)
+        out.append((m, int(max(1, c))))
+    return out
