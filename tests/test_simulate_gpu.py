@@ -183,6 +183,48 @@ def test_stack_depths_and_tiles_bitwise_identical():
             assert np.array_equal(base[a].view(np.uint8), other[a].view(np.uint8)), (cfg, a)
 
 
+def comb_mesh(extra_at_deepest=0):
+    """Tiny triangles whose centroids sit at 2^i on each axis (i = 0..19): their Morton codes are
+    single bits, so the radix tree is a chain (depth ~55, beyond the 32-level full stack); with
+    `extra_at_deepest` more triangles on the first centroid the duplicate keys add index-split
+    levels below it (depth > 64: the 128-bit trail)."""
+    pts = [np.eye(3)[a] * 2.0 ** i for i in range(20) for a in range(3)] + [np.full(3, 2.0 ** 20)]
+    pts += [pts[0]] * extra_at_deepest
+    s = 0.05
+    v = np.concatenate([[p + [-s, -s, 0], p + [s, -s, 0], p + [0, s, 0]] for p in pts]).astype(np.float32)
+    f = np.arange(3 * len(pts), dtype=np.uint32).reshape(-1, 3)
+    return v, f, np.array(pts[:61], np.float32)
+
+
+@pytest.mark.parametrize("extra,min_depth,max_depth", [(0, 33, 64), (2048, 65, 128)])
+def test_deep_trees_trail_walks(extra, min_depth, max_depth):
+    """Trees deeper than the 32-level full stack run the trail walks (64- and 128-bit trails with
+    the short stack or none): parity with the oracle, and every stack setting bit-identical."""
+    v, f, centres = comb_mesh(extra)
+    m = rm.Map(v, f)
+    depth = m.info()["depth"]
+    assert min_depth <= depth <= max_depth, depth
+    origin = np.array([-3.0, -2.0, -1.0], np.float32)
+    dirs = centres - origin
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    rng = np.random.default_rng(4)
+    rnd = rng.standard_normal((195, 3)).astype(np.float32)
+    rnd /= np.linalg.norm(rnd, axis=1, keepdims=True)
+    d = np.concatenate([dirs, rnd]).astype(np.float32)
+    model = sensors.OnDnModel(width=64, height=4, range=sensors.Interval(0.0, 4.0e6),
+                              origs=np.tile(origin, (256, 1)), dirs=d)
+    poses = np.tile(IDENT, (3, 1))
+    poses[1, 4:7] = (0.5, -0.25, 0.125)
+    poses[2, :4] = scenes.euler_to_quat([0.0], [0.0], [0.01])[0]
+    got, _, _ = check_parity(v, f, model, poses)
+    assert got["hits"][:61].sum() >= 55  # the aimed rays reach their triangles
+    for cfg in [(0, 4, 8, 4), (8, 4, 8, 4), (16, 2, 16, 2), (16, 4, 8, 4, 16, 2), (16, 4, 8, 4, 0, 4, 4)]:
+        other = gpu_sim(m, model, poses, cfg=rm.launch_config(*cfg))
+        for a in ALL:
+            assert np.array_equal(got[a].view(np.uint8), other[a].view(np.uint8)), (cfg, a)
+    assert m.status() == 0
+
+
 # ---- edge cases -----------------------------------------------------------------------------
 def test_empty_map_writes_misses():
     m = rm.Map(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))
