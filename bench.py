@@ -65,7 +65,7 @@ TRAFFIC: dict = {
     "rcc_fused": 10 * (310600448 + 23166208),
 }
 
-RAYCAST = ("terrain1m_spherical", "terrain1m_pinhole", "terrain2m_spherical", "room_vlp16")
+RAYCAST = ("terrain1m_spherical", "terrain1m_pinhole", "terrain2m_spherical", "terrain33m_spherical", "room_vlp16")
 
 
 def raycast_workload(name: str):
@@ -77,6 +77,9 @@ def raycast_workload(name: str):
     elif name == "terrain2m_spherical":
         sc = scenes.terrain(grid=1024, n_boxes=2000, seed=0)
         tri = "terrain 1024x1024 + 2000 boxes (2,117,058 tris)"
+    elif name == "terrain33m_spherical":
+        sc = scenes.terrain(grid=4096, size=2000.0, n_boxes=2000, seed=0)
+        tri = "terrain 4096x4096 over 2 km + 2000 boxes (33,562,050 tris)"
     elif name == "room_vlp16":
         sc = scenes.box_room(seed=0, n_boxes=200)
         model = sensors.vlp16_900()
@@ -91,7 +94,7 @@ def raycast_workload(name: str):
     else:
         model = sensors.ouster_like(128, 1024, 45.0, 0.5, 130.0)
         mdesc = "spherical 128x1024 (+-22.5 deg)"
-    poses = scenes.terrain_poses(sc, 1000, seed=2)
+    poses = scenes.terrain_poses(sc, 1000, seed=2, size=2000.0 if name.startswith("terrain33m") else 500.0)
     return sc, model, poses, ALL, {"workload": f"{tri}, {mdesc}, 1000 poses, Hits+Ranges+Points+Normals+FaceIds"}
 
 
