@@ -39,8 +39,12 @@ def perturb(Tbm: torch.Tensor, xi: torch.Tensor) -> torch.Tensor:
 
 def range_pose_grad(sim: _Simulator, Tbm: torch.Tensor, ranges_obs: torch.Tensor, delta: float = 0.2,
                     want_sim: bool = False):
-    """Returns (grad [N,6], loss [N]) and, with want_sim, the simulated (ranges, face_ids)."""
+    """Returns (grad [N,6], loss [N]) and, with want_sim, the simulated (ranges, face_ids), on the
+    device.  Observed ranges in host memory are uploaded in pose chunks on a second stream while the
+    previous chunk is computed (the result is the same as one call on device data)."""
     sim._check_ready()
+    if isinstance(ranges_obs, torch.Tensor) and not ranges_obs.is_cuda:
+        return _range_pose_grad_host(sim, Tbm, ranges_obs, delta, want_sim)
     Tbm = Tbm.reshape(-1, 8).to("cuda").contiguous()
     n = Tbm.shape[0]
     W, H = sim.sensor.width, sim.sensor.height
@@ -54,6 +58,44 @@ def range_pose_grad(sim: _Simulator, Tbm: torch.Tensor, ranges_obs: torch.Tensor
     p = lambda t: None if t is None else C.c_void_p(t.data_ptr())  # noqa: E731
     L.call("rmg_range_pose_grad", sim._map.handle, sim.sensor.handle, C.byref(sim._Tsb), p(Tbm), n, p(obs),
            float(delta), p(grad), p(loss), p(rs), p(fs), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if want_sim:
+        return grad, loss, rs, fs
+    return grad, loss
+
+
+def _range_pose_grad_host(sim, Tbm, ranges_obs, delta, want_sim, chunks: int = 8):
+    Tbm_d = Tbm.reshape(-1, 8).to("cuda", non_blocking=True).contiguous()
+    n = Tbm_d.shape[0]
+    W, H = sim.sensor.width, sim.sensor.height
+    per = W * H
+    obs_h = ranges_obs.reshape(-1)
+    if obs_h.dtype != torch.float32:
+        obs_h = obs_h.to(torch.float32)
+    if obs_h.numel() != n * per:
+        raise L.RmgError(L.RMG_ERR_INVALID_ARG, "range_pose_grad", "ranges_obs must hold n_poses*W*H values")
+    obs_d = torch.empty((n * per,), dtype=torch.float32, device="cuda")
+    grad = torch.empty((n, 6), dtype=torch.float32, device="cuda")
+    loss = torch.empty((n,), dtype=torch.float32, device="cuda")
+    rs = torch.empty((n * per,), dtype=torch.float32, device="cuda") if want_sim else None
+    fs = torch.empty((n * per,), dtype=torch.int32, device="cuda") if want_sim else None
+    if getattr(sim, "_copy_stream", None) is None:
+        sim._copy_stream = torch.cuda.Stream()
+    compute = torch.cuda.current_stream()
+    copy = sim._copy_stream
+    copy.wait_stream(compute)
+    step = max(1, -(-n // chunks))
+    p = lambda t: None if t is None else C.c_void_p(t.data_ptr())  # noqa: E731
+    for c0 in range(0, n, step):
+        c1 = min(n, c0 + step)
+        with torch.cuda.stream(copy):
+            obs_d[c0 * per:c1 * per].copy_(obs_h[c0 * per:c1 * per], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(copy)
+        compute.wait_event(ev)
+        L.call("rmg_range_pose_grad", sim._map.handle, sim.sensor.handle, C.byref(sim._Tsb), p(Tbm_d[c0:c1]),
+               c1 - c0, p(obs_d[c0 * per:c1 * per]), float(delta), p(grad[c0:c1]), p(loss[c0:c1]),
+               None if rs is None else p(rs[c0 * per:c1 * per]), None if fs is None else p(fs[c0 * per:c1 * per]),
+               C.c_void_p(compute.cuda_stream))
     if want_sim:
         return grad, loss, rs, fs
     return grad, loss

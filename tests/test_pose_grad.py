@@ -99,6 +99,34 @@ def test_gpu_gradient_matches_fp64_reference_and_fd(rm_mod):
 
 
 @gpu
+def test_host_observations_give_the_device_result_bitwise(rm_mod):
+    """Observed ranges in pinned host memory go through the pipelined path (pose chunks uploaded
+    while the previous chunk computes); gradient, loss and the simulated ranges equal one call on
+    device data bit for bit, for pose counts that do and do not divide into the chunks."""
+    import torch
+
+    from rmagine_gb300 import grad as rg
+
+    rm = rm_mod
+    sc, model, true, est = problem(seed=21, n_poses=11)
+    m = rm.Map(sc.vertices, sc.faces)
+    sim = rm.SphereSimulator(m)
+    sim.setModel(model)
+    obs = sim.simulate(torch.from_numpy(true).cuda(), attrs=("ranges",)).ranges
+    for n in (11, 8, 1):
+        Td = torch.from_numpy(est[:n].copy()).cuda()
+        per = obs.numel() // 11
+        g0, l0, r0, f0 = rg.range_pose_grad(sim, Td, obs[:n * per], DELTA, want_sim=True)
+        host = obs[:n * per].cpu().pin_memory()
+        g1, l1, r1, f1 = rg.range_pose_grad(sim, torch.from_numpy(est[:n].copy()).pin_memory(), host, DELTA,
+                                            want_sim=True)
+        torch.cuda.synchronize()
+        for a, b in ((g0, g1), (l0, l1), (r0, r1), (f0, f1)):
+            assert torch.equal(a, b), n
+    assert m.status() == 0
+
+
+@gpu
 def test_gpu_gradient_on_a_plane_matches_fd_of_retraced_ranges(rm_mod):
     """Flat ground (two coplanar triangles): every ray's range is a smooth function of the pose,
     so GPU gradients compare directly with binary64 central differences of re-traced ranges."""
