@@ -437,12 +437,18 @@ class _Simulator:
         for every pose) or [n, W*H, 3] (one per pose), in the sensor frame and ray order of
         simulate(); dataset_mask (e.g. the scan's hits) and dataset_ids follow its shape.  pre is
         one transform or one per pose.  Returns (stats [n,16] or None, transforms [n,8] or None)
-        on the device, asynchronously on the current stream."""
+        on the device, asynchronously on the current stream.  Per-pose scans in host memory are
+        uploaded in pose chunks on a second stream while the previous chunk is computed (the same
+        result as one call on device data: every pose is reduced on its own)."""
         from . import statistics as S
 
         self._check_ready()
         if isinstance(self._map, Scene):
             raise L.RmgError(L.RMG_ERR_UNSUPPORTED, "simulate_statistics", "needs a single-mesh Map")
+        if (isinstance(dataset_points, torch.Tensor) and not dataset_points.is_cuda and dataset_points.dim() == 3
+                and dataset_points.shape[0] > 1):
+            return self._simulate_statistics_host(Tbm, dataset_points, dataset_mask, dataset_ids, pre, params,
+                                                  point_to_plane, want_stats, want_transforms)
         Tbm = S._dev(Tbm, torch.float32).reshape(-1, 8)
         n = Tbm.shape[0]
         W, H = self.sensor.width, self.sensor.height
@@ -465,6 +471,53 @@ class _Simulator:
         L.call("rmg_simulate_statistics", self._map.handle, self.sensor.handle, C.byref(self._Tsb),
                C.c_void_p(Tbm.data_ptr()), n, C.byref(scan), _ptr(pre_t), stride, C.byref(pc),
                1 if point_to_plane else 0, _ptr(stats), _ptr(T), _stream_ptr())
+        return stats, T
+
+    def _simulate_statistics_host(self, Tbm, dp_h, dm_h, di_h, pre, params, point_to_plane, want_stats,
+                                  want_transforms, chunks: int = 8):
+        from . import statistics as S
+
+        Tbm = S._dev(Tbm, torch.float32).reshape(-1, 8)
+        n = Tbm.shape[0]
+        W, H = self.sensor.width, self.sensor.height
+        per = W * H
+        if tuple(dp_h.shape) != (n, per, 3):
+            raise L.RmgError(L.RMG_ERR_INVALID_ARG, "simulate_statistics",
+                             f"dataset points {tuple(dp_h.shape)} do not match {n} poses x {per} rays")
+        host = {"points": dp_h.to(torch.float32).reshape(n, per, 3)}
+        if dm_h is not None:
+            host["mask"] = torch.as_tensor(dm_h).reshape(n, per).to(torch.uint8)
+        if di_h is not None:
+            host["ids"] = (di_h if isinstance(di_h, torch.Tensor) else
+                           torch.as_tensor(np.asarray(di_h).astype(np.uint32).view(np.int32))).reshape(n, per).to(torch.int32)
+        dev = {k: torch.empty(v.shape, dtype=v.dtype, device="cuda") for k, v in host.items()}
+        pre_t, stride = S._pre(pre, n)
+        params = params or S.UmeyamaReductionConstraints()
+        stats = torch.empty((n, 16), dtype=torch.float32, device="cuda") if want_stats else None
+        T = torch.empty((n, 8), dtype=torch.float32, device="cuda") if want_transforms else None
+        if self._copy_stream is None:
+            self._copy_stream = torch.cuda.Stream()
+        compute = torch.cuda.current_stream()
+        copy = self._copy_stream
+        copy.wait_stream(compute)
+        pc = params.to_c()
+        step = max(1, -(-n // chunks))
+        for c0 in range(0, n, step):
+            c1 = min(n, c0 + step)
+            with torch.cuda.stream(copy):
+                for k in dev:
+                    dev[k][c0:c1].copy_(host[k][c0:c1], non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(copy)
+            compute.wait_event(ev)
+            scan = L.ScanC(dev["points"][c0].data_ptr(), dev["mask"][c0].data_ptr() if "mask" in dev else None,
+                           dev["ids"][c0].data_ptr() if "ids" in dev else None, 1)
+            L.call("rmg_simulate_statistics", self._map.handle, self.sensor.handle, C.byref(self._Tsb),
+                   C.c_void_p(Tbm[c0].data_ptr()), c1 - c0, C.byref(scan),
+                   None if pre_t is None else C.c_void_p(pre_t[c0 if stride else 0].data_ptr()), stride,
+                   C.byref(pc), 1 if point_to_plane else 0,
+                   None if stats is None else C.c_void_p(stats[c0].data_ptr()),
+                   None if T is None else C.c_void_p(T[c0].data_ptr()), C.c_void_p(compute.cuda_stream))
         return stats, T
 
     def _simulate_host(self, Tbm: torch.Tensor, bundle: Bundle, n: int) -> Bundle:

@@ -334,3 +334,28 @@ def test_batched_correction_matches_the_two_step_loop(built):
     e0 = np.linalg.norm(est0[:, 4:7] - true[:, 4:7], axis=1)
     e1 = np.linalg.norm(fused[:, 4:7] - true[:, 4:7], axis=1)
     assert np.median(e1) < 0.5 * np.median(e0), (np.median(e0), np.median(e1))
+
+
+@pytest.mark.gpu
+def test_host_scans_give_the_device_result_bitwise(built):
+    """Per-pose scans in pinned host memory are uploaded in pose chunks overlapped with the fused
+    launches; every pose is reduced on its own, so the statistics and transforms equal one call on
+    device data bit for bit (pose counts that do and do not divide into the chunks)."""
+    import torch
+
+    from rmagine_gb300 import statistics as rs
+
+    torch.cuda.set_device(0)
+    n = 11
+    sc, model, m, sim, true, est, data, pre = _room_problem("spherical", n, seed=31)
+    W, H = sim.sensor.width, sim.sensor.height
+    P = rs.UmeyamaReductionConstraints(max_dist=0.5)
+    dp, dm = data.points.reshape(n, W * H, 3), data.hits.reshape(n, W * H)
+    for k in (11, 9, 2):
+        E = torch.from_numpy(est[:k].copy()).cuda()
+        s0, T0 = sim.simulate_statistics(E, dp[:k], dataset_mask=dm[:k], pre=pre[:k], params=P)
+        s1, T1 = sim.simulate_statistics(E, dp[:k].cpu().pin_memory(), dataset_mask=dm[:k].cpu().pin_memory(),
+                                         pre=pre[:k], params=P)
+        torch.cuda.synchronize()
+        assert torch.equal(s0, s1) and torch.equal(T0, T1), k
+    assert m.status() == 0
