@@ -269,7 +269,8 @@ def gpu_raycast(args, world):
         raise RuntimeError("device status error in the timed region")
     value = world * rays * args.steps / (total_ms / 1e3) / 1e6
 
-    # e2e through the public API: pinned host poses in, pinned host bundle out, synchronous
+    # e2e through the host-buffer C entry point (rmg_simulate_host, behind the simulator's RAM-bundle
+    # overload): pinned host poses in, pinned host bundle out, synchronous
     host_poses = torch.from_numpy(poses).pin_memory()
     hb = rm.resize_memory_bundle(rm.Bundle(*attrs), W, H, n, device="cpu", pin_memory=True)
     sim.simulate(host_poses, hb)
@@ -296,7 +297,7 @@ def gpu_raycast(args, world):
     line = {"metric": "Mrays/s", "unit": "Mrays/s", "value": round(value, 2), "ms_per_step": round(total_ms / args.steps, 3),
             "dtype": "f32", "config": config, "gpu_launches": args.steps,
             "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": int(poses.nbytes),
-                    "d2h_bytes_per_step": int(rays * out_b)},
+                    "d2h_bytes_per_step": int(rays * out_b), "step_ms": [round(1e3 * x, 3) for x in e2e_t]},
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms],
             "map": {k: m.info()[k] for k in ("n_faces", "n_nodes", "depth", "device_bytes")}}
     return line, lambda: cpu_raycast(sc, model, poses, attrs), config
@@ -347,6 +348,7 @@ def gpu_scene(args, world):
     baked_ms, _, _ = Timer(dev, reps).run(lambda: bsim.simulate(Tbm, bundle), world)
     baked_ms /= reps
     del bsim, m
+    # e2e through rmg_simulate_scene_host: pinned host poses in, pinned host bundle out, synchronous
     host_poses = torch.from_numpy(poses).pin_memory()
     hb = rm.resize_memory_bundle(rm.Bundle(*SCENE_ATTRS), W, H, n, device="cpu", pin_memory=True)
     sim.simulate(host_poses, hb)
@@ -374,7 +376,7 @@ def gpu_scene(args, world):
             "baked_single_mesh": {"value": round(rays / (baked_ms / 1e3) / 1e6, 2), "unit": "Mrays/s",
                                   "ms_per_step": round(baked_ms, 3)},
             "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": int(poses.nbytes),
-                    "d2h_bytes_per_step": int(rays * out_b)},
+                    "d2h_bytes_per_step": int(rays * out_b), "step_ms": [round(1e3 * x, 3) for x in e2e_t]},
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
     return line, lambda: cpu_raycast(baked, model, poses, SCENE_ATTRS), config
 

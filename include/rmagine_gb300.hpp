@@ -175,11 +175,10 @@ void resize_memory_bundle(BundleT& res, unsigned W, unsigned H, unsigned N = 1) 
   if constexpr (BundleT::template has<ObjectIds<MemT>>()) res.ObjectIds<MemT>::object_ids.resize(n);
 }
 
-// rmg_outputs of a device bundle: a buffer is requested iff it is non-empty
+// rmg_outputs of a bundle's MemT buffers: a buffer is requested iff it is non-empty
 // (set_simulation_flags_, embree_common.h:79-139).
-template <typename BundleT>
+template <typename M = VRAM_CUDA, typename BundleT>
 rmg_outputs outputs_of(BundleT& b) {
-  using M = VRAM_CUDA;
   rmg_outputs o{};
   if constexpr (BundleT::template has<Hits<M>>()) o.hits = b.Hits<M>::hits.size() ? b.Hits<M>::hits.raw() : nullptr;
   if constexpr (BundleT::template has<Ranges<M>>())
@@ -195,6 +194,19 @@ rmg_outputs outputs_of(BundleT& b) {
   if constexpr (BundleT::template has<ObjectIds<M>>())
     o.object_ids = b.ObjectIds<M>::object_ids.size() ? b.ObjectIds<M>::object_ids.raw() : nullptr;
   return o;
+}
+
+// Resizes every non-empty MemT buffer of a bundle to n elements (the requested ones).
+template <typename M, typename BundleT>
+void resize_requested(BundleT& b, size_t n) {
+  if constexpr (BundleT::template has<Hits<M>>()) if (b.Hits<M>::hits.size()) b.Hits<M>::hits.resize(n);
+  if constexpr (BundleT::template has<Ranges<M>>()) if (b.Ranges<M>::ranges.size()) b.Ranges<M>::ranges.resize(n);
+  if constexpr (BundleT::template has<Points<M>>()) if (b.Points<M>::points.size()) b.Points<M>::points.resize(n);
+  if constexpr (BundleT::template has<Normals<M>>()) if (b.Normals<M>::normals.size()) b.Normals<M>::normals.resize(n);
+  if constexpr (BundleT::template has<FaceIds<M>>()) if (b.FaceIds<M>::face_ids.size()) b.FaceIds<M>::face_ids.resize(n);
+  if constexpr (BundleT::template has<GeomIds<M>>()) if (b.GeomIds<M>::geom_ids.size()) b.GeomIds<M>::geom_ids.resize(n);
+  if constexpr (BundleT::template has<ObjectIds<M>>())
+    if (b.ObjectIds<M>::object_ids.size()) b.ObjectIds<M>::object_ids.resize(n);
 }
 
 // ---- sensor models ---------------------------------------------------------------------
@@ -490,30 +502,23 @@ class SimulatorGB300 {
     return res;
   }
 
-  // Host form (SphereSimulatorEmbree.hpp:130-155): poses and results in RAM; synchronises.
+  // Host form (SphereSimulatorEmbree.hpp:130-155): poses and results in RAM; the non-empty
+  // buffers are filled through rmg_simulate_host (pose chunks cast on `stream` while earlier
+  // chunks are copied back).  Synchronises.
   template <typename BundleRAM>
-  void simulate(const Memory<Transform, RAM>& Tbm, BundleRAM& ret) const {
+  void simulate(const Memory<Transform, RAM>& Tbm, BundleRAM& ret, cudaStream_t stream = 0) const {
     ready();
-    Memory<Transform, VRAM_CUDA> Td;
-    Td = Tbm;
-    IntAttrAll<VRAM_CUDA> dev;
-    const size_t n = (size_t)W_ * H_ * Tbm.size();
-    if constexpr (BundleRAM::template has<Hits<RAM>>()) if (ret.Hits<RAM>::hits.size()) dev.Hits<VRAM_CUDA>::hits.resize(n);
-    if constexpr (BundleRAM::template has<Ranges<RAM>>()) if (ret.Ranges<RAM>::ranges.size()) dev.Ranges<VRAM_CUDA>::ranges.resize(n);
-    if constexpr (BundleRAM::template has<Points<RAM>>()) if (ret.Points<RAM>::points.size()) dev.Points<VRAM_CUDA>::points.resize(n);
-    if constexpr (BundleRAM::template has<Normals<RAM>>()) if (ret.Normals<RAM>::normals.size()) dev.Normals<VRAM_CUDA>::normals.resize(n);
-    if constexpr (BundleRAM::template has<FaceIds<RAM>>()) if (ret.FaceIds<RAM>::face_ids.size()) dev.FaceIds<VRAM_CUDA>::face_ids.resize(n);
-    if constexpr (BundleRAM::template has<GeomIds<RAM>>()) if (ret.GeomIds<RAM>::geom_ids.size()) dev.GeomIds<VRAM_CUDA>::geom_ids.resize(n);
-    if constexpr (BundleRAM::template has<ObjectIds<RAM>>()) if (ret.ObjectIds<RAM>::object_ids.size()) dev.ObjectIds<VRAM_CUDA>::object_ids.resize(n);
-    simulate(Td, dev, 0);
-    cuda_check(cudaDeviceSynchronize(), "simulate");
-    if constexpr (BundleRAM::template has<Hits<RAM>>()) if (ret.Hits<RAM>::hits.size()) ret.Hits<RAM>::hits = dev.Hits<VRAM_CUDA>::hits;
-    if constexpr (BundleRAM::template has<Ranges<RAM>>()) if (ret.Ranges<RAM>::ranges.size()) ret.Ranges<RAM>::ranges = dev.Ranges<VRAM_CUDA>::ranges;
-    if constexpr (BundleRAM::template has<Points<RAM>>()) if (ret.Points<RAM>::points.size()) ret.Points<RAM>::points = dev.Points<VRAM_CUDA>::points;
-    if constexpr (BundleRAM::template has<Normals<RAM>>()) if (ret.Normals<RAM>::normals.size()) ret.Normals<RAM>::normals = dev.Normals<VRAM_CUDA>::normals;
-    if constexpr (BundleRAM::template has<FaceIds<RAM>>()) if (ret.FaceIds<RAM>::face_ids.size()) ret.FaceIds<RAM>::face_ids = dev.FaceIds<VRAM_CUDA>::face_ids;
-    if constexpr (BundleRAM::template has<GeomIds<RAM>>()) if (ret.GeomIds<RAM>::geom_ids.size()) ret.GeomIds<RAM>::geom_ids = dev.GeomIds<VRAM_CUDA>::geom_ids;
-    if constexpr (BundleRAM::template has<ObjectIds<RAM>>()) if (ret.ObjectIds<RAM>::object_ids.size()) ret.ObjectIds<RAM>::object_ids = dev.ObjectIds<VRAM_CUDA>::object_ids;
+    resize_requested<RAM>(ret, (size_t)W_ * H_ * Tbm.size());
+    const rmg_outputs o = outputs_of<RAM>(ret);
+    const auto* T = reinterpret_cast<const rmg_transform*>(Tbm.raw());
+    const auto* Tsb = reinterpret_cast<const rmg_transform*>(&Tsb_);
+    if (scene_)
+      check(rmg_simulate_scene_host(scene_->handle(), sensor_, Tsb, T, (uint32_t)Tbm.size(), &o, stream),
+            "rmg_simulate_scene_host");
+    else
+      check(rmg_simulate_host(map_->handle(), sensor_, Tsb, T, (uint32_t)Tbm.size(), &o, tuned_ ? &cfg_ : nullptr,
+                              stream),
+            "rmg_simulate_host");
   }
 
   template <typename BundleRAM>

@@ -230,6 +230,28 @@ int rmg_simulate_ex(const rmg_map* map, const rmg_sensor* sensor,
 /* Fills *cfg with the library default for this sensor/map. */
 int rmg_default_launch_config(const rmg_map* map, const rmg_sensor* sensor, rmg_launch_config* cfg);
 
+/* Host form of rmg_simulate: the RAM-bundle overload of the Embree simulators
+ * (SphereSimulatorEmbree.hpp:130-155, simulate(Memory<Transform,RAM>, Bundle
+ * of RAM buffers)).  Tbm and every non-NULL output are HOST pointers (pinned
+ * or pageable; device pointers also work).  The poses are uploaded once and
+ * the rays cast in pose chunks into device staging memory on `stream`; each
+ * chunk's outputs are copied to the host on a second stream while the next
+ * chunks are cast.  Results are bit-identical to rmg_simulate.  Synchronous:
+ * returns when `out` holds every result.  cfg may be NULL (library default).
+ * Staging comes from a per-device stream-ordered pool that keeps its memory
+ * between calls (rmg_host_staging_trim releases it). */
+int rmg_simulate_host(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                      const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
+                      const rmg_launch_config* cfg, void* stream);
+/* Pipeline shape of the host forms (process-wide): output bytes per pose
+ * chunk (0 = the default, 128 MiB; at least one pose per chunk) and compute
+ * streams the chunks alternate over (0 = the default, 2; at most 3), so that
+ * one chunk's last warps overlap the next chunk's first ones.  Results do not
+ * depend on either. */
+int rmg_host_set_pipeline(uint64_t chunk_bytes, uint32_t compute_streams);
+/* Returns the host forms' cached staging memory to the driver. */
+int rmg_host_staging_trim(void);
+
 /* Times a fixed set of launch configurations (per-ray binary walk, warp
  * packet walk, 4-wide walk; tiles 8x4, 16x2, 4x8; 4 or 2 warps per CTA) on
  * the caller's poses and output buffers -- all write the same results -- and
@@ -472,6 +494,10 @@ int rmg_scene_status(rmg_scene* scene, int clear);
 /* rmg_simulate on a scene: same sensors, poses, outputs and semantics. */
 int rmg_simulate_scene(const rmg_scene* scene, const rmg_sensor* sensor, const rmg_transform* Tsb,
                        const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out, void* stream);
+/* Host form of rmg_simulate_scene (host poses and outputs), pipelined and
+ * synchronous like rmg_simulate_host. */
+int rmg_simulate_scene_host(const rmg_scene* scene, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                            const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Fused simulate -> statistics (the inner step of the RCC / MICP-L correction

@@ -171,6 +171,10 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_simulate_ex": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(OutputsC),
                                   C.POINTER(LaunchConfigC), _P]),
     "rmg_default_launch_config": (C.c_int, [_P, _P, C.POINTER(LaunchConfigC)]),
+    "rmg_simulate_host": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(OutputsC),
+                                    C.POINTER(LaunchConfigC), _P]),
+    "rmg_host_set_pipeline": (C.c_int, [C.c_uint64, _U32]),
+    "rmg_host_staging_trim": (C.c_int, []),
     "rmg_autotune_launch_config": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(OutputsC), _U32,
                                              C.POINTER(LaunchConfigC), _P]),
     "rmg_lbvh_build_noalloc": (C.c_int, [_P, _U32, _P, _U32, C.POINTER(LbvhBuffersC), _P]),
@@ -194,6 +198,7 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_scene_destroy": (C.c_int, [_P]),
     "rmg_scene_status": (C.c_int, [_P, C.c_int]),
     "rmg_simulate_scene": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(OutputsC), _P]),
+    "rmg_simulate_scene_host": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(OutputsC), _P]),
     "rmg_batch_default_config": (C.c_int, [C.POINTER(BatchConfigC)]),
     "rmg_batch_create": (C.c_int, [_P, C.POINTER(BatchEntryC), _U32, C.POINTER(_P)]),
     "rmg_batch_set_config": (C.c_int, [_P, C.POINTER(BatchConfigC)]),

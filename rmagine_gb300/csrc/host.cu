@@ -1,0 +1,265 @@
+// Host-buffer forms of rmg_simulate and rmg_simulate_scene: poses and results
+// in host memory, like the Embree simulators' RAM bundles
+// (SphereSimulatorEmbree.hpp:130-155).  The poses are uploaded once; the rays
+// are cast in pose chunks into device staging slots, alternating between the
+// caller's stream and further compute streams so that one chunk's last warps
+// overlap the next chunk's first ones (a small launch is otherwise as long as
+// its slowest warp), and each chunk's outputs are copied to the host on a copy
+// stream while later chunks are cast.  Chunks are launched ahead of the copies
+// that free their slots' predecessors, so a pageable destination (whose
+// device->host copy returns to the host only when it is done) still overlaps
+// with the casting.
+#include <atomic>
+#include <algorithm>
+#include <functional>
+#include <mutex>
+
+#include "internal.h"
+
+namespace rmg {
+namespace {
+
+constexpr int kMaxCompute = 3;   // compute streams at most (the caller's and up to two more)
+constexpr int kSlots = 4;        // staging chunks in flight; more than the compute streams (see host_pipeline)
+constexpr int kMaxDevices = 64;
+constexpr size_t kDefaultChunkBytes = size_t(128) << 20;
+constexpr int kDefaultCompute = 2;
+std::atomic<size_t> g_chunk_bytes{kDefaultChunkBytes};
+std::atomic<int> g_compute{kDefaultCompute};
+
+// Staging memory comes from one stream-ordered pool per device that keeps what
+// it holds between calls (release threshold: everything), so a repeated call
+// allocates nothing from the driver; rmg_host_staging_trim gives it back.
+std::mutex g_pool_mu;
+cudaMemPool_t g_pool[kMaxDevices] = {};
+
+int staging_pool(cudaMemPool_t* out) {
+  int dev = 0;
+  RMG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(RMG_ERR_UNSUPPORTED, "host staging: device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  if (!g_pool[dev]) {
+    cudaMemPoolProps p{};
+    p.allocType = cudaMemAllocationTypePinned;
+    p.handleTypes = cudaMemHandleTypeNone;
+    p.location.type = cudaMemLocationTypeDevice;
+    p.location.id = dev;
+    cudaMemPool_t pool;
+    RMG_CUDA_TRY(cudaMemPoolCreate(&pool, &p));
+    uint64_t keep = UINT64_MAX;
+    const cudaError_t e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e != cudaSuccess) {
+      cudaMemPoolDestroy(pool);
+      return cuda_status(e, "cudaMemPoolSetAttribute");
+    }
+    g_pool[dev] = pool;
+  }
+  *out = g_pool[dev];
+  return RMG_OK;
+}
+
+// The seven output attributes as (pointer, bytes per ray) pairs, rmg_outputs order.
+struct AttrList {
+  char* ptr[7];
+  size_t size[7];
+};
+
+AttrList attrs_of(const rmg_outputs& o) {
+  return AttrList{{reinterpret_cast<char*>(o.hits), reinterpret_cast<char*>(o.ranges),
+                   reinterpret_cast<char*>(o.points), reinterpret_cast<char*>(o.normals),
+                   reinterpret_cast<char*>(o.face_ids), reinterpret_cast<char*>(o.geom_ids),
+                   reinterpret_cast<char*>(o.object_ids)},
+                  {1, 4, 12, 12, 4, 4, 4}};
+}
+
+rmg_outputs outputs_at(const AttrList& a) {
+  rmg_outputs o;
+  o.hits = reinterpret_cast<uint8_t*>(a.ptr[0]);
+  o.ranges = reinterpret_cast<float*>(a.ptr[1]);
+  o.points = reinterpret_cast<rmg_vec3*>(a.ptr[2]);
+  o.normals = reinterpret_cast<rmg_vec3*>(a.ptr[3]);
+  o.face_ids = reinterpret_cast<uint32_t*>(a.ptr[4]);
+  o.geom_ids = reinterpret_cast<uint32_t*>(a.ptr[5]);
+  o.object_ids = reinterpret_cast<uint32_t*>(a.ptr[6]);
+  return o;
+}
+
+using Launch = std::function<int(const rmg_transform* Tbm, uint32_t n, const rmg_outputs* out, cudaStream_t st)>;
+
+// Streams and events of one call; released in every exit path.
+struct Pipeline {
+  cudaStream_t side[kMaxCompute - 1] = {};  // compute streams besides the caller's
+  cudaStream_t copy = nullptr;
+  cudaEvent_t cast[kSlots] = {};     // chunk in slot s written (its compute stream)
+  cudaEvent_t copied[kSlots] = {};   // chunk in slot s read back (copy stream)
+  cudaEvent_t ready = nullptr;       // poses uploaded (caller's stream)
+  cudaEvent_t side_done[kMaxCompute - 1] = {};
+  cudaEvent_t done = nullptr;
+  ~Pipeline() {
+    for (int s = 0; s < kSlots; ++s) {
+      if (cast[s]) cudaEventDestroy(cast[s]);
+      if (copied[s]) cudaEventDestroy(copied[s]);
+    }
+    for (int k = 0; k < kMaxCompute - 1; ++k) {
+      if (side_done[k]) cudaEventDestroy(side_done[k]);
+      if (side[k]) cudaStreamDestroy(side[k]);
+    }
+    for (cudaEvent_t e : {ready, done})
+      if (e) cudaEventDestroy(e);
+    if (copy) cudaStreamDestroy(copy);
+  }
+};
+
+// Chunk k is cast on compute stream k % nc into slot k % kSlots (nc compute
+// streams).  Chunks 0..nc-1 are launched first; then iteration k launches
+// chunk k+nc and issues chunk k's copies.  The launch of chunk j waits for the
+// copy of chunk j-kSlots (same slot), which was issued at iteration j-kSlots <
+// j-nc, i.e. before the wait is enqueued, because kSlots > nc.
+int host_pipeline(const char* what, uint64_t rays_per_pose, const rmg_transform* Tbm_host, uint32_t n_poses,
+                  const rmg_outputs& out_host, cudaStream_t st, const Launch& launch) {
+  static_assert(kSlots > kMaxCompute, "a slot is reused only after its copy was issued");
+  const uint32_t nc = (uint32_t)std::min(std::max(g_compute.load(), 1), kMaxCompute);
+  const AttrList host = attrs_of(out_host);
+  size_t bytes_per_ray = 0;
+  for (int a = 0; a < 7; ++a)
+    if (host.ptr[a]) bytes_per_ray += host.size[a];
+  if (bytes_per_ray == 0 || rays_per_pose == 0) return RMG_OK;
+  const size_t bytes_per_pose = bytes_per_ray * rays_per_pose;
+  // at least one pose, at most ceil(n/2) so that two chunks overlap
+  size_t chunk = std::max<size_t>(1, g_chunk_bytes.load() / bytes_per_pose);
+  chunk = std::min<size_t>(chunk, std::max<uint32_t>(1u, (n_poses + 1) / 2));
+  const uint32_t n_chunks = (uint32_t)((n_poses + chunk - 1) / chunk);
+  const int slots = (int)std::min<uint32_t>(kSlots, n_chunks);
+
+  cudaMemPool_t pool;
+  int s = staging_pool(&pool);
+  if (s != RMG_OK) return s;
+  Pipeline pl;
+  for (uint32_t k = 0; k + 1 < nc; ++k) {
+    RMG_CUDA_TRY(cudaStreamCreateWithFlags(&pl.side[k], cudaStreamNonBlocking));
+    RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.side_done[k], cudaEventDisableTiming));
+  }
+  RMG_CUDA_TRY(cudaStreamCreateWithFlags(&pl.copy, cudaStreamNonBlocking));
+  for (int k = 0; k < slots; ++k) {
+    RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.cast[k], cudaEventDisableTiming));
+    RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.copied[k], cudaEventDisableTiming));
+  }
+  RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.ready, cudaEventDisableTiming));
+  RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.done, cudaEventDisableTiming));
+  cudaStream_t compute[kMaxCompute] = {st};
+  for (uint32_t k = 0; k + 1 < nc; ++k) compute[k + 1] = pl.side[k];
+
+  // staging: all poses, then `slots` output chunks, every array 256-byte aligned
+  const size_t pose_bytes = ((size_t)n_poses * sizeof(rmg_transform) + 255) & ~size_t(255);
+  size_t slot_bytes = 0;
+  size_t offset[7] = {};
+  for (int a = 0; a < 7; ++a) {
+    if (!host.ptr[a]) continue;
+    offset[a] = slot_bytes;
+    slot_bytes += (chunk * rays_per_pose * host.size[a] + 255) & ~size_t(255);
+  }
+  char* staging = nullptr;
+  RMG_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&staging), pose_bytes + slots * slot_bytes, pool, st));
+  const auto* Tbm_dev = reinterpret_cast<const rmg_transform*>(staging);
+  s = cuda_status(cudaMemcpyAsync(staging, Tbm_host, (size_t)n_poses * sizeof(rmg_transform), cudaMemcpyDefault, st),
+                  what);
+  if (s == RMG_OK) s = cuda_status(cudaEventRecord(pl.ready, st), what);
+  for (uint32_t k = 0; s == RMG_OK && k + 1 < nc; ++k) s = cuda_status(cudaStreamWaitEvent(pl.side[k], pl.ready, 0), what);
+
+  auto slot_outputs = [&](int slot) {
+    AttrList d = host;
+    for (int a = 0; a < 7; ++a)
+      d.ptr[a] = host.ptr[a] ? staging + pose_bytes + slot * slot_bytes + offset[a] : nullptr;
+    return d;
+  };
+  auto cast_chunk = [&](uint32_t k) -> int {
+    const int slot = (int)(k % slots);
+    const cudaStream_t cs = compute[k % nc];
+    const uint32_t p0 = (uint32_t)(k * chunk), np = (uint32_t)std::min<size_t>(chunk, n_poses - p0);
+    if (k >= (uint32_t)slots) RMG_CUDA_TRY(cudaStreamWaitEvent(cs, pl.copied[slot], 0));
+    const rmg_outputs o = outputs_at(slot_outputs(slot));
+    const int r = launch(Tbm_dev + p0, np, &o, cs);
+    if (r != RMG_OK) return r;
+    RMG_CUDA_TRY(cudaEventRecord(pl.cast[slot], cs));
+    return RMG_OK;
+  };
+  auto copy_chunk = [&](uint32_t k) -> int {
+    const int slot = (int)(k % slots);
+    const uint64_t p0 = (uint64_t)k * chunk, np = std::min<uint64_t>(chunk, n_poses - p0);
+    RMG_CUDA_TRY(cudaStreamWaitEvent(pl.copy, pl.cast[slot], 0));
+    const AttrList d = slot_outputs(slot);
+    for (int a = 0; a < 7; ++a) {
+      if (!host.ptr[a]) continue;
+      const size_t row = rays_per_pose * host.size[a];
+      RMG_CUDA_TRY(cudaMemcpyAsync(host.ptr[a] + p0 * row, d.ptr[a], np * row, cudaMemcpyDefault, pl.copy));
+    }
+    RMG_CUDA_TRY(cudaEventRecord(pl.copied[slot], pl.copy));
+    return RMG_OK;
+  };
+
+  for (uint32_t k = 0; s == RMG_OK && k < std::min<uint32_t>(nc, n_chunks); ++k) s = cast_chunk(k);
+  for (uint32_t k = 0; s == RMG_OK && k < n_chunks; ++k) {
+    if (k + nc < n_chunks) s = cast_chunk(k + nc);
+    if (s == RMG_OK) s = copy_chunk(k);
+  }
+  // the staging is freed in stream order after the last copy and the side
+  // streams' last launches, whatever happened
+  cudaEventRecord(pl.done, pl.copy);
+  cudaStreamWaitEvent(st, pl.done, 0);
+  for (uint32_t k = 0; k + 1 < nc; ++k) {
+    cudaEventRecord(pl.side_done[k], pl.side[k]);
+    cudaStreamWaitEvent(st, pl.side_done[k], 0);
+  }
+  cudaFreeAsync(staging, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (s != RMG_OK) return s;
+  return cuda_status(e, what);
+}
+
+uint64_t rays_of(const rmg_sensor* sensor) { return (uint64_t)sensor->width * sensor->height; }
+
+}  // namespace
+}  // namespace rmg
+
+using namespace rmg;
+
+extern "C" int rmg_simulate_host(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                                 const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
+                                 const rmg_launch_config* cfg, void* stream) {
+  if (!map || !sensor || !Tsb || !out)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_host: NULL map, sensor, Tsb or outputs");
+  if (n_poses == 0) return RMG_OK;
+  if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_host: Tbm is NULL");
+  return host_pipeline("rmg_simulate_host", rays_of(sensor), Tbm, n_poses, *out, as_stream(stream),
+                       [&](const rmg_transform* T, uint32_t n, const rmg_outputs* o, cudaStream_t st) {
+                         return rmg_simulate_ex(map, sensor, Tsb, T, n, o, cfg, st);
+                       });
+}
+
+extern "C" int rmg_simulate_scene_host(const rmg_scene* scene, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                                       const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
+                                       void* stream) {
+  if (!scene || !sensor || !Tsb || !out)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene_host: NULL scene, sensor, Tsb or outputs");
+  if (n_poses == 0) return RMG_OK;
+  if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene_host: Tbm is NULL");
+  return host_pipeline("rmg_simulate_scene_host", rays_of(sensor), Tbm, n_poses, *out, as_stream(stream),
+                       [&](const rmg_transform* T, uint32_t n, const rmg_outputs* o, cudaStream_t st) {
+                         return rmg_simulate_scene(scene, sensor, Tsb, T, n, o, st);
+                       });
+}
+
+extern "C" int rmg_host_set_pipeline(uint64_t chunk_bytes, uint32_t compute_streams) {
+  if (compute_streams > (uint32_t)kMaxCompute)
+    return fail(RMG_ERR_UNSUPPORTED, "rmg_host_set_pipeline: compute_streams must be 0..3");
+  g_chunk_bytes.store(chunk_bytes ? (size_t)chunk_bytes : kDefaultChunkBytes);
+  g_compute.store(compute_streams ? (int)compute_streams : kDefaultCompute);
+  return RMG_OK;
+}
+
+extern "C" int rmg_host_staging_trim(void) {
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  for (int d = 0; d < kMaxDevices; ++d)
+    if (g_pool[d]) RMG_CUDA_TRY(cudaMemPoolTrimTo(g_pool[d], 0));
+  return RMG_OK;
+}

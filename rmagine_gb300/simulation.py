@@ -328,7 +328,6 @@ class _Simulator:
         self._model = None
         self._Tsb = transform_c([0, 0, 0, 1, 0, 0, 0])
         self.launch_config: L.LaunchConfigC | None = None
-        self._staging: dict = {}
         self._copy_stream = None
 
     # SimulatorEmbree::setMap (a Map or a Scene)
@@ -521,41 +520,21 @@ class _Simulator:
         return stats, T
 
     def _simulate_host(self, Tbm: torch.Tensor, bundle: Bundle, n: int) -> Bundle:
-        """Host bundle: the poses are split into chunks; chunk k is simulated into device
-        staging memory on the current stream while chunk k-1 is copied back to the host on a
-        second stream, so the device->host copy overlaps the ray casting.  Synchronises."""
-        dev = Bundle(*bundle.attrs)
+        """Host bundle (the Embree simulators' RAM form): rmg_simulate_host / rmg_simulate_scene_host
+        cast the poses in chunks into device staging memory and copy each chunk back on a second
+        stream while the next ones are cast.  Synchronises."""
         for a, t in bundle.tensors().items():
-            key = (a, tuple(t.shape), t.dtype)
-            buf = self._staging.get(key)
-            if buf is None:
-                buf = torch.empty(t.shape, dtype=t.dtype, device="cuda")
-                self._staging[key] = buf
-            setattr(dev, a, buf)
-        if self._copy_stream is None:
-            self._copy_stream = torch.cuda.Stream()
-        compute = torch.cuda.current_stream()
-        copy = self._copy_stream
-        Tbm_d = Tbm.to("cuda", non_blocking=True).contiguous()
-        per_pose = self.sensor.width * self.sensor.height
-        out_bytes = sum(t.element_size() * t[0:1].numel() for t in bundle.tensors().values()) * per_pose
-        # chunks of ~256 MB of outputs, at least 4 when there are enough poses
-        chunk = max(1, min(n // 4 if n >= 4 else n, (256 << 20) // max(1, out_bytes)))
-        copy.wait_stream(compute)
-        for c0 in range(0, n, chunk):
-            c1 = min(n, c0 + chunk)
-            view = Bundle(*bundle.attrs)
-            for a in bundle.attrs:
-                setattr(view, a, getattr(dev, a)[c0 * per_pose:c1 * per_pose])
-            self._launch(Tbm_d[c0:c1], c1 - c0, view, _stream_ptr())
-            done = torch.cuda.Event()
-            done.record(compute)
-            copy.wait_event(done)
-            with torch.cuda.stream(copy):
-                for a, t in bundle.tensors().items():
-                    t[c0 * per_pose:c1 * per_pose].copy_(getattr(view, a), non_blocking=True)
-        compute.wait_stream(copy)
-        compute.synchronize()
+            if not t.is_contiguous():
+                raise L.RmgError(L.RMG_ERR_INVALID_ARG, "simulate", f"{a} is not contiguous")
+        T = Tbm.to(torch.float32).contiguous()
+        out = outputs_c(bundle)
+        if isinstance(self._map, Scene):
+            L.call("rmg_simulate_scene_host", self._map.handle, self.sensor.handle, C.byref(self._Tsb),
+                   C.c_void_p(T.data_ptr()), n, C.byref(out), _stream_ptr())
+        else:
+            L.call("rmg_simulate_host", self._map.handle, self.sensor.handle, C.byref(self._Tsb),
+                   C.c_void_p(T.data_ptr()), n, C.byref(out),
+                   None if self.launch_config is None else C.byref(self.launch_config), _stream_ptr())
         return bundle
 
 
