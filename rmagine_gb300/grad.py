@@ -40,8 +40,9 @@ def perturb(Tbm: torch.Tensor, xi: torch.Tensor) -> torch.Tensor:
 def range_pose_grad(sim: _Simulator, Tbm: torch.Tensor, ranges_obs: torch.Tensor, delta: float = 0.2,
                     want_sim: bool = False):
     """Returns (grad [N,6], loss [N]) and, with want_sim, the simulated (ranges, face_ids), on the
-    device.  Observed ranges in host memory are uploaded in pose chunks on a second stream while the
-    previous chunk is computed (the result is the same as one call on device data)."""
+    device.  Observed ranges in host memory are uploaded in pose chunks on a copy stream while earlier
+    chunks are computed, the launches alternating between two compute streams (the result is the
+    same as one call on device data)."""
     sim._check_ready()
     if isinstance(ranges_obs, torch.Tensor) and not ranges_obs.is_cuda:
         return _range_pose_grad_host(sim, Tbm, ranges_obs, delta, want_sim)
@@ -80,13 +81,14 @@ def _range_pose_grad_host(sim, Tbm, ranges_obs, delta, want_sim, chunks: int = 8
     fs = torch.empty((n * per,), dtype=torch.int32, device="cuda") if want_sim else None
     if getattr(sim, "_copy_stream", None) is None:
         sim._copy_stream = torch.cuda.Stream()
-    compute = torch.cuda.current_stream()
+    streams = sim._compute_streams()
     copy = sim._copy_stream
-    copy.wait_stream(compute)
+    copy.wait_stream(streams[0])
     step = max(1, -(-n // chunks))
     p = lambda t: None if t is None else C.c_void_p(t.data_ptr())  # noqa: E731
-    for c0 in range(0, n, step):
+    for i, c0 in enumerate(range(0, n, step)):
         c1 = min(n, c0 + step)
+        compute = streams[i % len(streams)]
         with torch.cuda.stream(copy):
             obs_d[c0 * per:c1 * per].copy_(obs_h[c0 * per:c1 * per], non_blocking=True)
         ev = torch.cuda.Event()
@@ -96,6 +98,7 @@ def _range_pose_grad_host(sim, Tbm, ranges_obs, delta, want_sim, chunks: int = 8
                c1 - c0, p(obs_d[c0 * per:c1 * per]), float(delta), p(grad[c0:c1]), p(loss[c0:c1]),
                None if rs is None else p(rs[c0 * per:c1 * per]), None if fs is None else p(fs[c0 * per:c1 * per]),
                C.c_void_p(compute.cuda_stream))
+    sim._join_streams(streams)
     if want_sim:
         return grad, loss, rs, fs
     return grad, loss

@@ -329,6 +329,7 @@ class _Simulator:
         self._Tsb = transform_c([0, 0, 0, 1, 0, 0, 0])
         self.launch_config: L.LaunchConfigC | None = None
         self._copy_stream = None
+        self._side_streams: list | None = None
 
     # SimulatorEmbree::setMap (a Map or a Scene)
     def setMap(self, map: "Map | Scene") -> None:
@@ -359,6 +360,23 @@ class _Simulator:
         if self._sensor is None:
             raise L.RmgError(L.RMG_ERR_INVALID_ARG, "simulate", "no model set")
         return self._sensor
+
+    def _compute_streams(self, k: int = 2) -> list:
+        """The current stream and k-1 cached side streams (each made to wait for the current one)
+        that the chunked host paths alternate their launches over: a launch of a few poses lasts
+        as long as its slowest warps, and the next chunk's launch on another stream fills the SMs
+        those stragglers leave idle.  The caller joins them with _join_streams."""
+        cur = torch.cuda.current_stream()
+        if self._side_streams is None or len(self._side_streams) != k - 1:
+            self._side_streams = [torch.cuda.Stream() for _ in range(k - 1)]
+        for s in self._side_streams:
+            s.wait_stream(cur)
+        return [cur] + self._side_streams
+
+    @staticmethod
+    def _join_streams(streams: list) -> None:
+        for s in streams[1:]:
+            streams[0].wait_stream(s)
 
     def _check_ready(self) -> None:
         if self._map is None:
@@ -437,8 +455,9 @@ class _Simulator:
         simulate(); dataset_mask (e.g. the scan's hits) and dataset_ids follow its shape.  pre is
         one transform or one per pose.  Returns (stats [n,16] or None, transforms [n,8] or None)
         on the device, asynchronously on the current stream.  Per-pose scans in host memory are
-        uploaded in pose chunks on a second stream while the previous chunk is computed (the same
-        result as one call on device data: every pose is reduced on its own)."""
+        uploaded in pose chunks on a copy stream while earlier chunks are computed, the launches
+        alternating between two compute streams (the same result as one call on device data: every
+        pose is reduced on its own)."""
         from . import statistics as S
 
         self._check_ready()
@@ -473,7 +492,7 @@ class _Simulator:
         return stats, T
 
     def _simulate_statistics_host(self, Tbm, dp_h, dm_h, di_h, pre, params, point_to_plane, want_stats,
-                                  want_transforms, chunks: int = 8):
+                                  want_transforms, chunks: int = 16):
         from . import statistics as S
 
         Tbm = S._dev(Tbm, torch.float32).reshape(-1, 8)
@@ -496,13 +515,14 @@ class _Simulator:
         T = torch.empty((n, 8), dtype=torch.float32, device="cuda") if want_transforms else None
         if self._copy_stream is None:
             self._copy_stream = torch.cuda.Stream()
-        compute = torch.cuda.current_stream()
+        streams = self._compute_streams()
         copy = self._copy_stream
-        copy.wait_stream(compute)
+        copy.wait_stream(streams[0])
         pc = params.to_c()
         step = max(1, -(-n // chunks))
-        for c0 in range(0, n, step):
+        for i, c0 in enumerate(range(0, n, step)):
             c1 = min(n, c0 + step)
+            compute = streams[i % len(streams)]
             with torch.cuda.stream(copy):
                 for k in dev:
                     dev[k][c0:c1].copy_(host[k][c0:c1], non_blocking=True)
@@ -517,6 +537,7 @@ class _Simulator:
                    C.byref(pc), 1 if point_to_plane else 0,
                    None if stats is None else C.c_void_p(stats[c0].data_ptr()),
                    None if T is None else C.c_void_p(T[c0].data_ptr()), C.c_void_p(compute.cuda_stream))
+        self._join_streams(streams)
         return stats, T
 
     def _simulate_host(self, Tbm: torch.Tensor, bundle: Bundle, n: int) -> Bundle:
