@@ -32,6 +32,9 @@ def lib() -> C.CDLL:
             "orc_dirs_spherical": (None, [C.c_float, C.c_float, C.c_uint32, C.c_float, C.c_float, C.c_uint32, _P]),
             "orc_dirs_pinhole": (None, [C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_float, C.c_float, _P]),
             "orc_bvh_build": (_P, [_P, C.c_uint32, _P, C.c_uint32]),
+            "orc_bvh_build_ex": (_P, [_P, C.c_uint32, _P, C.c_uint32, C.c_int]),
+            "orc_bvh_count": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_float, _P, _P, _P, _P, C.c_int]),
+            "orc_bvh_save_map": (C.c_int, [_P, C.c_char_p]),
             "orc_bvh_free": (None, [_P]),
             "orc_bvh_num_nodes": (C.c_uint32, [_P]),
             "orc_simulate": (C.c_int, [_P, C.c_int, C.c_uint32, C.c_uint32, C.c_float, C.c_float, _P, _P, _P,
@@ -96,10 +99,10 @@ def directions(model) -> np.ndarray:
 class Scene:
     """A mesh with the oracle's binned-SAH BVH."""
 
-    def __init__(self, vertices, faces):
+    def __init__(self, vertices, faces, max_leaf: int = 4):
         self.v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
         self.f = np.ascontiguousarray(faces, np.uint32).reshape(-1, 3)
-        self.h = lib().orc_bvh_build(_p(self.v), self.v.shape[0], _p(self.f), self.f.shape[0])
+        self.h = lib().orc_bvh_build_ex(_p(self.v), self.v.shape[0], _p(self.f), self.f.shape[0], int(max_leaf))
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -108,6 +111,27 @@ class Scene:
 
     def num_nodes(self) -> int:
         return int(lib().orc_bvh_num_nodes(self.h))
+
+    def save_map(self, path) -> int:
+        """Writes this tree (built with max_leaf=1) as a GPU map file (rmg_map_load reads it);
+        returns its depth."""
+        d = int(lib().orc_bvh_save_map(self.h, str(path).encode()))
+        if d < 0:
+            raise ValueError("save_map needs a one-triangle-per-leaf tree and a writable path")
+        return d
+
+    def count(self, o, d, tfar: float, nthreads: int = 0):
+        """Per-ray internal-node visits and triangle tests through this SAH tree (nearest child
+        first, t-culling), with the hit t and face: the tree-quality yardstick for the LBVH counts."""
+        o = np.ascontiguousarray(o, np.float32).reshape(-1, 3)
+        d = np.ascontiguousarray(d, np.float32).reshape(-1, 3)
+        n = o.shape[0]
+        visits = np.zeros(n, np.uint32)
+        tests = np.zeros(n, np.uint32)
+        t = np.zeros(n, np.float32)
+        f = np.zeros(n, np.uint32)
+        lib().orc_bvh_count(self.h, _p(o), _p(d), n, float(tfar), _p(visits), _p(tests), _p(t), _p(f), int(nthreads))
+        return visits, tests, t, f
 
     def _model_args(self, model):
         k = model_kind(model)

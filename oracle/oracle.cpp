@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <limits>
@@ -171,6 +172,7 @@ struct BuildCtx {
   std::vector<double> cen;  // 3 per tri
   std::vector<uint32_t>* prims;
   std::vector<SahNode>* nodes;
+  int max_leaf = 4;  // triangles per leaf at most
 };
 
 int build_sah(BuildCtx& c, int first, int count) {
@@ -184,7 +186,7 @@ int build_sah(BuildCtx& c, int first, int count) {
     for (int k = 0; k < 3; ++k) { cb.lo[k] = std::min(cb.lo[k], q[k]); cb.hi[k] = std::max(cb.hi[k], q[k]); }
   }
   (*c.nodes)[idx].box = b;
-  if (count <= 4) {
+  if (count <= c.max_leaf) {
     (*c.nodes)[idx].first = first; (*c.nodes)[idx].count = count;
     (*c.nodes)[idx].left = (*c.nodes)[idx].right = -1;
     return idx;
@@ -256,7 +258,10 @@ bool box_hit(const RayD& r, const BoxD& b, double pad, double tfar, double& tmin
 
 struct HitF { float t; uint32_t face; bool hit; };
 
-HitF closest_hit(const SahBvh& bvh, const V3& o, const V3& d, float tfar, uint64_t* tri_tests) {
+// Nearest child first with t-culling, like the GPU walk; `node_visits` (when
+// non-NULL) counts the internal nodes whose two child boxes were tested.
+HitF closest_hit(const SahBvh& bvh, const V3& o, const V3& d, float tfar, uint64_t* tri_tests,
+                 uint64_t* node_visits = nullptr) {
   HitF h{tfar, 0xffffffffu, false};
   if (bvh.nodes.empty()) return h;
   const RayW rw = make_rayw(o, d);
@@ -280,6 +285,7 @@ HitF closest_hit(const SahBvh& bvh, const V3& o, const V3& d, float tfar, uint64
         if (tri_tests) ++*tri_tests;
       }
     } else {
+      if (node_visits) ++*node_visits;
       double tl, tr;
       const bool hl = box_hit(rd, bvh.nodes[n.left].box, bvh.pad, (double)h.t, tl);
       const bool hr = box_hit(rd, bvh.nodes[n.right].box, bvh.pad, (double)h.t, tr);
@@ -584,7 +590,14 @@ void orc_dirs_pinhole(uint32_t W, uint32_t H, float fx, float fy, float cx, floa
   }
 }
 
+void* orc_bvh_build_ex(const float* verts, uint32_t nv, const uint32_t* faces, uint32_t nf, int max_leaf);
+
 void* orc_bvh_build(const float* verts, uint32_t nv, const uint32_t* faces, uint32_t nf) {
+  return orc_bvh_build_ex(verts, nv, faces, nf, 4);
+}
+
+// Binned-SAH tree with at most max_leaf (>= 1) triangles per leaf.
+void* orc_bvh_build_ex(const float* verts, uint32_t nv, const uint32_t* faces, uint32_t nf, int max_leaf) {
   SahBvh* b = new SahBvh;
   b->mesh.v.resize(nv);
   for (uint32_t i = 0; i < nv; ++i) b->mesh.v[i] = V3{verts[3 * i], verts[3 * i + 1], verts[3 * i + 2]};
@@ -607,6 +620,7 @@ void* orc_bvh_build(const float* verts, uint32_t nv, const uint32_t* faces, uint
   }
   c.prims = &b->prims;
   c.nodes = &b->nodes;
+  c.max_leaf = std::max(1, max_leaf);
   b->nodes.reserve(2 * (size_t)nf);
   build_sah(c, 0, (int)nf);
   return b;
@@ -776,5 +790,134 @@ int orc_lbvh_count(void* p, const float* o, const float* d, uint64_t n, float tf
 
 // SAH-tree node count (the tree-quality yardstick).
 uint32_t orc_bvh_num_nodes(void* p) { return (uint32_t)static_cast<SahBvh*>(p)->nodes.size(); }
+
+// Writes a one-triangle-per-leaf SAH tree (max_leaf 1) as a GPU map file
+// (the RMGLBVH1 layout of rmg_map_save: 48-byte header, then vertices, faces,
+// 64-byte nodes, 48-byte packed triangles, leaf order, leaf parents, with an
+// FNV-1a 64 checksum of the payload).  Internal nodes are numbered in depth-
+// first preorder from the root (0), leaf k holds prims[k]; child boxes are the
+// exact binary32 bounds of their triangles.  Returns the tree depth (edges to
+// the deepest leaf), or -1 when the tree has a leaf of more than one triangle
+// or the file cannot be written.  Used by tests to load a second topology of
+// the same mesh into the GPU library.
+int orc_bvh_save_map(void* p, const char* path) {
+  const SahBvh& b = *static_cast<SahBvh*>(p);
+  const uint32_t nv = (uint32_t)b.mesh.v.size(), nf = (uint32_t)(b.mesh.f.size() / 3);
+  if (nf < 2) return -1;
+  for (const SahNode& n : b.nodes)
+    if (n.count > 1) return -1;
+  struct FBox { float lo[3], hi[3]; };
+  const uint32_t nn = nf - 1;
+  std::vector<int32_t> id(b.nodes.size(), 0);  // SAH node -> internal id, or ~leaf
+  {
+    int32_t next = 0;
+    std::vector<int> st{0};
+    while (!st.empty()) {
+      const int k = st.back();
+      st.pop_back();
+      const SahNode& n = b.nodes[k];
+      if (n.count == 1) { id[k] = ~n.first; continue; }
+      id[k] = next++;
+      st.push_back(n.right);
+      st.push_back(n.left);
+    }
+  }
+  std::vector<uint32_t> words(16 * (size_t)nn, 0);
+  std::vector<float> tris(12 * (size_t)nf);
+  std::vector<uint32_t> order(nf);
+  std::vector<int32_t> leaf_parent(nf, -1);
+  std::vector<FBox> box(b.nodes.size());
+  int depth = 0;
+  // post-order: boxes bottom-up; pre-order ids already assigned
+  std::vector<std::pair<int, int>> st{{0, 0}};
+  std::vector<int> post;
+  std::vector<int> level(b.nodes.size(), 0);
+  while (!st.empty()) {
+    const auto [k, lv] = st.back();
+    st.pop_back();
+    level[k] = lv;
+    post.push_back(k);
+    const SahNode& n = b.nodes[k];
+    if (n.count == 1) { depth = std::max(depth, lv); continue; }
+    st.push_back({n.left, lv + 1});
+    st.push_back({n.right, lv + 1});
+  }
+  for (auto it = post.rbegin(); it != post.rend(); ++it) {
+    const int k = *it;
+    const SahNode& n = b.nodes[k];
+    FBox fb;
+    if (n.count == 1) {
+      const uint32_t f = b.prims[n.first];
+      for (int a = 0; a < 3; ++a) { fb.lo[a] = INFINITY; fb.hi[a] = -INFINITY; }
+      for (int v = 0; v < 3; ++v) {
+        const V3 q = b.mesh.vert(f, v);
+        const float c[3] = {q.x, q.y, q.z};
+        for (int a = 0; a < 3; ++a) { fb.lo[a] = std::min(fb.lo[a], c[a]); fb.hi[a] = std::max(fb.hi[a], c[a]); }
+        tris[12 * (size_t)n.first + 4 * v + 0] = q.x;
+        tris[12 * (size_t)n.first + 4 * v + 1] = q.y;
+        tris[12 * (size_t)n.first + 4 * v + 2] = q.z;
+        tris[12 * (size_t)n.first + 4 * v + 3] = 0.0f;
+      }
+      std::memcpy(&tris[12 * (size_t)n.first + 3], &f, 4);
+      order[n.first] = f;
+    } else {
+      const FBox& L = box[n.left];
+      const FBox& R = box[n.right];
+      for (int a = 0; a < 3; ++a) { fb.lo[a] = std::min(L.lo[a], R.lo[a]); fb.hi[a] = std::max(L.hi[a], R.hi[a]); }
+      uint32_t* w = &words[16 * (size_t)id[k]];
+      const float fa[12] = {L.lo[0], L.hi[0], L.lo[1], L.hi[1], R.lo[0], R.hi[0], R.lo[1], R.hi[1],
+                            L.lo[2], L.hi[2], R.lo[2], R.hi[2]};
+      std::memcpy(w, fa, 48);
+      const int32_t links[4] = {id[n.left], id[n.right], -1, 0};
+      std::memcpy(w + 12, links, 16);
+      for (int c : {n.left, n.right}) {
+        if (id[c] >= 0) std::memcpy(&words[16 * (size_t)id[c] + 14], &id[k], 4);
+        else leaf_parent[~id[c]] = id[k];
+      }
+    }
+    box[k] = fb;
+  }
+  std::vector<unsigned char> payload;
+  auto put = [&](const void* src, size_t bytes) {
+    const unsigned char* q = static_cast<const unsigned char*>(src);
+    payload.insert(payload.end(), q, q + bytes);
+  };
+  for (const V3& v : b.mesh.v) { const float q[3] = {v.x, v.y, v.z}; put(q, 12); }
+  put(b.mesh.f.data(), 4 * b.mesh.f.size());
+  put(words.data(), 4 * words.size());
+  put(tris.data(), 4 * tris.size());
+  put(order.data(), 4 * order.size());
+  put(leaf_parent.data(), 4 * leaf_parent.size());
+  uint64_t h = 1469598103934665603ull;
+  for (unsigned char c : payload) { h ^= c; h *= 1099511628211ull; }
+  unsigned char hdr[48] = {'R', 'M', 'G', 'L', 'B', 'V', 'H', '1'};
+  const uint32_t hw[6] = {1u, nv, nf, nn, (uint32_t)depth, 0u};
+  std::memcpy(hdr + 8, hw, 24);
+  const uint64_t tail[2] = {(uint64_t)payload.size(), h};
+  std::memcpy(hdr + 32, tail, 16);
+  FILE* fp = std::fopen(path, "wb");
+  if (!fp) return -1;
+  bool ok = std::fwrite(hdr, 48, 1, fp) == 1 && std::fwrite(payload.data(), 1, payload.size(), fp) == payload.size();
+  ok = (std::fclose(fp) == 0) && ok;
+  return ok ? depth : -1;
+}
+
+// Per-ray internal-node visits and triangle tests of explicit rays through the
+// SAH tree (the tree-quality yardstick beside orc_lbvh_count), plus the hit.
+int orc_bvh_count(void* p, const float* o, const float* d, uint64_t n, float tfar, uint32_t* visits,
+                  uint32_t* tests, float* t_out, uint32_t* face_out, int nthreads) {
+  const SahBvh& bvh = *static_cast<SahBvh*>(p);
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads_or_default(nthreads))
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    uint64_t v = 0, t = 0;
+    const HitF h = closest_hit(bvh, V3{o[3 * i], o[3 * i + 1], o[3 * i + 2]}, V3{d[3 * i], d[3 * i + 1], d[3 * i + 2]},
+                               tfar, &t, &v);
+    visits[i] = (uint32_t)v;
+    tests[i] = (uint32_t)t;
+    if (t_out) t_out[i] = h.hit ? h.t : INFINITY;
+    if (face_out) face_out[i] = h.face;
+  }
+  return 0;
+}
 
 }  // extern "C"

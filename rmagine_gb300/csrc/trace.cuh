@@ -16,7 +16,8 @@
 //     parent links to the pending level and takes the sibling: stackless
 //     backtracking in the manner of Hapala et al. 2011 / Afra and
 //     Szirmay-Kalos 2014, so any SS gives the same visits and results.
-//   * Box tests widen the interval by 2^-22 relative; triangle tests are the
+//   * Box tests widen every plane distance outward by |o/d| 2^-21 and the
+//     interval by 2^-22 relative (RayBox); triangle tests are the
 //     watertight test of common.cuh.  Closest-hit ties are broken by the
 //     smaller face id, so the result does not depend on traversal order.
 //   * Every ray has a step budget (2 * internal nodes + 64 node visits and
@@ -46,12 +47,23 @@ struct Hit {
   uint32_t face;    // original face id
 };
 
+// Slab constants of one ray.  A plane at coordinate c is crossed at
+// t = fma(c, 1/d, -o/d).  Rounding o/d leaves an absolute error of up to
+// |o/d| * 2^-24 in every such t -- far more than a relative widening covers
+// when the origin is far from the coordinate origin and d is small in that
+// axis -- so each plane's addend carries an outward offset e = |o/d| * 2^-21
+// (the near plane earlier, the far plane later).  The remaining error of a
+// plane distance is below 2 ulp of t plus 2 |o/d| 2^-24 (rounded 1/d and
+// o/d, rounded addend, one rounding of the fma), inside e plus the relative
+// widening kWiden, so a box that the ray truly meets within (0, tfar] is never
+// culled and the closest hit does not depend on the tree.
 struct RayBox {
   float ix, iy, iz;     // 1/d (zero components replaced by +-1e20)
-  float oix, oiy, oiz;  // o/d
+  float clx, cly, clz;  // addend of the lo plane: -o/d -+ e (minus when 1/d > 0)
+  float chx, chy, chz;  // addend of the hi plane: -o/d +- e
 #if RMG_SLAB_F32X2
   unsigned long long pix, piy, piz;     // (1/d, 1/d) per axis, packed for fma.rn.f32x2
-  unsigned long long noix, noiy, noiz;  // (-o/d, -o/d)
+  unsigned long long cx, cy, cz;        // (lo addend, hi addend) per axis
 #endif
 };
 
@@ -68,16 +80,20 @@ __device__ __forceinline__ RayBox make_raybox(const V& o, const V& d) {
   r.ix = fabsf(d.x) > 1e-20f ? __frcp_rn(d.x) : copysignf(1e20f, d.x);
   r.iy = fabsf(d.y) > 1e-20f ? __frcp_rn(d.y) : copysignf(1e20f, d.y);
   r.iz = fabsf(d.z) > 1e-20f ? __frcp_rn(d.z) : copysignf(1e20f, d.z);
-  r.oix = o.x * r.ix;
-  r.oiy = o.y * r.iy;
-  r.oiz = o.z * r.iz;
+  const float oix = o.x * r.ix, oiy = o.y * r.iy, oiz = o.z * r.iz;
+  const float kE = 4.76837158e-7f;  // 2^-21
+  const float ex = copysignf(fabsf(oix) * kE, r.ix), ey = copysignf(fabsf(oiy) * kE, r.iy),
+              ez = copysignf(fabsf(oiz) * kE, r.iz);
+  r.clx = -oix - ex; r.chx = -oix + ex;
+  r.cly = -oiy - ey; r.chy = -oiy + ey;
+  r.clz = -oiz - ez; r.chz = -oiz + ez;
 #if RMG_SLAB_F32X2
   r.pix = pack2(r.ix, r.ix);
   r.piy = pack2(r.iy, r.iy);
   r.piz = pack2(r.iz, r.iz);
-  r.noix = pack2(-r.oix, -r.oix);
-  r.noiy = pack2(-r.oiy, -r.oiy);
-  r.noiz = pack2(-r.oiz, -r.oiz);
+  r.cx = pack2(r.clx, r.chx);
+  r.cy = pack2(r.cly, r.chy);
+  r.cz = pack2(r.clz, r.chz);
 #endif
   return r;
 }
@@ -96,12 +112,12 @@ __device__ __forceinline__ float fmax3f(float a, float b, float c) {
 }
 
 #if RMG_SLAB_F32X2
-// (lo, hi) * (1/d, 1/d) + (-o/d, -o/d) for one axis in one packed FMA
-// (fma.rn.f32x2, sm_100 and later: two IEEE single-precision FMAs).
-__device__ __forceinline__ void slab_axis(float lo, float hi, unsigned long long inv, unsigned long long noi,
+// (lo, hi) * (1/d, 1/d) + (lo addend, hi addend) for one axis in one packed
+// FMA (fma.rn.f32x2, sm_100 and later: two IEEE single-precision FMAs).
+__device__ __forceinline__ void slab_axis(float lo, float hi, unsigned long long inv, unsigned long long add,
                                           float& t0, float& t1) {
   unsigned long long r;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(pack2(lo, hi)), "l"(inv), "l"(noi));
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(pack2(lo, hi)), "l"(inv), "l"(add));
   asm("mov.b64 {%0, %1}, %2;" : "=f"(t0), "=f"(t1) : "l"(r));
 }
 #endif
@@ -111,13 +127,13 @@ __device__ __forceinline__ void slab(const RayBox& r, float lox, float hix, floa
                                      float loz, float hiz, float& tmin, float& tmax) {
 #if RMG_SLAB_F32X2
   float x0, x1, y0, y1, z0, z1;
-  slab_axis(lox, hix, r.pix, r.noix, x0, x1);
-  slab_axis(loy, hiy, r.piy, r.noiy, y0, y1);
-  slab_axis(loz, hiz, r.piz, r.noiz, z0, z1);
+  slab_axis(lox, hix, r.pix, r.cx, x0, x1);
+  slab_axis(loy, hiy, r.piy, r.cy, y0, y1);
+  slab_axis(loz, hiz, r.piz, r.cz, z0, z1);
 #else
-  const float x0 = fmaf(lox, r.ix, -r.oix), x1 = fmaf(hix, r.ix, -r.oix);
-  const float y0 = fmaf(loy, r.iy, -r.oiy), y1 = fmaf(hiy, r.iy, -r.oiy);
-  const float z0 = fmaf(loz, r.iz, -r.oiz), z1 = fmaf(hiz, r.iz, -r.oiz);
+  const float x0 = fmaf(lox, r.ix, r.clx), x1 = fmaf(hix, r.ix, r.chx);
+  const float y0 = fmaf(loy, r.iy, r.cly), y1 = fmaf(hiy, r.iy, r.chy);
+  const float z0 = fmaf(loz, r.iz, r.clz), z1 = fmaf(hiz, r.iz, r.chz);
 #endif
   tmin = fmax3f(fminf(x0, x1), fminf(y0, y1), fmaxf(fminf(z0, z1), 0.0f));
   tmax = fmin3f(fmaxf(x0, x1), fmaxf(y0, y1), fmaxf(z0, z1));

@@ -42,3 +42,26 @@ def test_rcc_fused_work_constants():
     assert abs(valid.mean() - want["data_frac"]) < 0.01
     assert abs(np.where(valid, v, 0).mean() - want["nodes"]) / want["nodes"] < 0.03
     assert abs(np.where(valid, tt, 0).mean() - want["tris"]) / want["tris"] < 0.05
+
+
+# SAH yardstick (oracle binned-SAH tree, one triangle per leaf, same visiting order and culling)
+SAH_YARDSTICK = {"terrain1m_spherical": {"nodes": 25.206, "tris": 1.721}, "room_vlp16": {"nodes": 24.502, "tris": 3.124}}
+
+
+@pytest.mark.parametrize("name", ["terrain1m_spherical", "room_vlp16"])
+def test_sah_yardstick(name):
+    """The tree-quality yardstick beside the LBVH constants: mean node visits and triangle tests per
+    ray through the oracle's binned-SAH tree (one triangle per leaf) on the same rays, which must
+    find the same closest faces as the LBVH."""
+    sc, model, poses, attrs, desc = bench.raycast_workload(name)
+    W, H = oracle.model_size(model)
+    n = poses.shape[0] * W * H
+    rng = np.random.default_rng(1)
+    gids = np.sort(rng.choice(n, min(n, 40000), replace=False)).astype(np.uint64)
+    o, d = oracle.Scene(sc.vertices, sc.faces).rays(model, IDENT, poses, gids)
+    _, _, _, lf = oracle.CanonicalLbvh(sc.vertices, sc.faces).count(o, d, model.range.max)
+    v, t, _, f = oracle.Scene(sc.vertices, sc.faces, max_leaf=1).count(o, d, model.range.max)
+    assert np.array_equal(f, lf)
+    want = SAH_YARDSTICK[name]
+    assert abs(v.mean() - want["nodes"]) / want["nodes"] < 0.03
+    assert abs(t.mean() - want["tris"]) / want["tris"] < 0.05
