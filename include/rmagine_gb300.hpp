@@ -288,10 +288,12 @@ struct OnDnModel {
 // ---- map -----------------------------------------------------------------------------------
 class TriangleMap {
  public:
-  TriangleMap(const Memory<Vector3, RAM>& V, const Memory<Face, RAM>& F, cudaStream_t s = 0) {
-    check(rmg_map_build(reinterpret_cast<const rmg_vec3*>(V.raw()), (uint32_t)V.size(),
-                        reinterpret_cast<const rmg_face*>(F.raw()), (uint32_t)F.size(), s, &h_),
-          "rmg_map_build");
+  // builder: RMG_BUILD_SAH (the default) or RMG_BUILD_LBVH; queries give the same results with either
+  TriangleMap(const Memory<Vector3, RAM>& V, const Memory<Face, RAM>& F, cudaStream_t s = 0,
+              rmg_builder builder = RMG_BUILD_SAH) {
+    check(rmg_map_build_ex(reinterpret_cast<const rmg_vec3*>(V.raw()), (uint32_t)V.size(),
+                           reinterpret_cast<const rmg_face*>(F.raw()), (uint32_t)F.size(), builder, s, &h_),
+          "rmg_map_build_ex");
   }
   // adopts a handle (rmg_map_load); used by load()
   explicit TriangleMap(rmg_map* h) : h_(h) {}

@@ -157,7 +157,7 @@ int rmg_device_info(int* sm_count, int* cc_major, int* cc_minor);
 int rmg_stream_wait(void* stream, uint32_t timeout_ms);
 
 /* ---------------------------------------------------------------------------
- * Map: triangle mesh + LBVH.
+ * Map: triangle mesh + BVH.
  * Replaces EmbreeMesh::init/computeFaceNormals/apply + EmbreeScene::commit
  * (src/rmagine_embree/src/map/embree/EmbreeMesh.cpp:162-335,
  *  EmbreeScene.cpp:187-191) and OptixScene::commit (OptixScene.cpp:242-481).
@@ -168,6 +168,20 @@ int rmg_stream_wait(void* stream, uint32_t timeout_ms);
 int rmg_map_build(const rmg_vec3* vertices, uint32_t n_vertices,
                   const rmg_face* faces, uint32_t n_faces,
                   void* stream, rmg_map** out);
+
+/* Tree builders.  Results of every query are the same for both (the closest
+ * hit does not depend on the tree); they differ in build time and in how many
+ * nodes a ray visits. */
+typedef enum rmg_builder {
+  RMG_BUILD_SAH = 0,   /* top-down binned surface area heuristic, one triangle per leaf, depth <= 32
+                          (the quality class of Embree's default build, EmbreeScene.hpp:61-83); the
+                          default of rmg_map_build */
+  RMG_BUILD_LBVH = 1   /* linear BVH over 63-bit Morton codes (Karras 2012): fastest build */
+} rmg_builder;
+/* rmg_map_build with an explicit builder. */
+int rmg_map_build_ex(const rmg_vec3* vertices, uint32_t n_vertices,
+                     const rmg_face* faces, uint32_t n_faces, uint32_t builder,
+                     void* stream, rmg_map** out);
 /* Moves the vertices (same count, same faces) and refits every box of the
  * existing tree bottom-up without re-sorting.  Needs exclusive use of the
  * map (no simulate in flight).  Synchronises with `stream`. */

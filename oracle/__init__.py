@@ -35,6 +35,8 @@ def lib() -> C.CDLL:
             "orc_bvh_build_ex": (_P, [_P, C.c_uint32, _P, C.c_uint32, C.c_int]),
             "orc_bvh_count": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_float, _P, _P, _P, _P, C.c_int]),
             "orc_bvh_save_map": (C.c_int, [_P, C.c_char_p]),
+            "orc_tree_count": (C.c_int, [_P, _P, C.c_uint32, _P, _P, C.c_uint64, C.c_float, _P, _P, _P, _P,
+                                         C.c_int]),
             "orc_bvh_free": (None, [_P]),
             "orc_bvh_num_nodes": (C.c_uint32, [_P]),
             "orc_simulate": (C.c_int, [_P, C.c_int, C.c_uint32, C.c_uint32, C.c_float, C.c_float, _P, _P, _P,
@@ -225,6 +227,24 @@ class CanonicalLbvh:
         f = np.zeros(n, np.uint32)
         lib().orc_lbvh_count(self.h, _p(o), _p(d), n, float(tfar), _p(visits), _p(tests), _p(t), _p(f), int(nthreads))
         return visits, tests, t, f
+
+
+def tree_count(export: dict, o, d, tfar: float, nthreads: int = 0):
+    """Per-ray node visits, triangle tests, hit t and face through a GPU map's exported tree
+    (rmg_map_export / Map.export()), in the kernel's visiting order."""
+    nodes = np.ascontiguousarray(np.concatenate([export["boxes"], export["links"].view(np.float32)], axis=1),
+                                 np.float32)
+    tris = np.ascontiguousarray(export["tris"], np.float32)
+    o = np.ascontiguousarray(o, np.float32).reshape(-1, 3)
+    d = np.ascontiguousarray(d, np.float32).reshape(-1, 3)
+    n = o.shape[0]
+    visits = np.zeros(n, np.uint32)
+    tests = np.zeros(n, np.uint32)
+    t = np.zeros(n, np.float32)
+    f = np.zeros(n, np.uint32)
+    lib().orc_tree_count(_p(nodes), _p(tris), tris.shape[0], _p(o), _p(d), n, float(tfar), _p(visits), _p(tests),
+                         _p(t), _p(f), int(nthreads))
+    return visits, tests, t, f
 
 
 def certify(scene: Scene, model, Tsb, Tbm, got: dict, want: dict, band: float = 1e-6, tol: float = 1e-4):

@@ -457,11 +457,13 @@ void lbvh_build(const Mesh& m, Lbvh& L) {
 // same form), instrumented: counts internal-node visits and triangle tests.
 const float kWiden = 1.00000024f;
 
-void slab(const float inv[3], const float oi[3], const float lo[3], const float hi[3], float& tmin, float& tmax) {
+// cl / ch: the lo / hi plane addends, -o/d widened outward by |o/d| 2^-21.
+void slab(const float inv[3], const float cl[3], const float ch[3], const float lo[3], const float hi[3], float& tmin,
+          float& tmax) {
   float t0[3], t1[3];
   for (int k = 0; k < 3; ++k) {
-    t0[k] = std::fmaf(lo[k], inv[k], -oi[k]);
-    t1[k] = std::fmaf(hi[k], inv[k], -oi[k]);
+    t0[k] = std::fmaf(lo[k], inv[k], cl[k]);
+    t1[k] = std::fmaf(hi[k], inv[k], ch[k]);
   }
   tmin = std::max(std::max(std::min(t0[0], t1[0]), std::min(t0[1], t1[1])), std::max(std::min(t0[2], t1[2]), 0.0f));
   tmax = std::min(std::min(std::max(t0[0], t1[0]), std::max(t0[1], t1[1])), std::max(t0[2], t1[2]));
@@ -472,10 +474,13 @@ HitF lbvh_trace(const Lbvh& L, const V3& o, const V3& d, float tfar, uint64_t& v
   if (L.nodes.empty()) return h;
   const RayW rw = make_rayw(o, d);
   const float dd[3] = {d.x, d.y, d.z}, oo[3] = {o.x, o.y, o.z};
-  float inv[3], oi[3];
+  float inv[3], cl[3], ch[3];
   for (int k = 0; k < 3; ++k) {
     inv[k] = std::fabs(dd[k]) > 1e-20f ? 1.0f / dd[k] : std::copysign(1e20f, dd[k]);
-    oi[k] = oo[k] * inv[k];
+    const float oi = oo[k] * inv[k];
+    const float e = std::copysign(std::fabs(oi) * 4.76837158e-7f, inv[k]);
+    cl[k] = -oi - e;
+    ch[k] = -oi + e;
   }
   auto test = [&](int k) {
     const float* t = &L.tris[12 * (size_t)k];
@@ -495,8 +500,8 @@ HitF lbvh_trace(const Lbvh& L, const V3& o, const V3& d, float tfar, uint64_t& v
     const float llo[3] = {n.a[0], n.a[2], n.c[0]}, lhi[3] = {n.a[1], n.a[3], n.c[1]};
     const float rlo[3] = {n.b[0], n.b[2], n.c[2]}, rhi[3] = {n.b[1], n.b[3], n.c[3]};
     float tl, tL, tr, tR;
-    slab(inv, oi, llo, lhi, tl, tL);
-    slab(inv, oi, rlo, rhi, tr, tR);
+    slab(inv, cl, ch, llo, lhi, tl, tL);
+    slab(inv, cl, ch, rlo, rhi, tr, tR);
     bool hl = tl <= std::min(tL, h.t) * kWiden;
     bool hr = tr <= std::min(tR, h.t) * kWiden;
     if (hl && n.d[0] < 0) { test(~n.d[0]); hl = false; }
@@ -775,6 +780,31 @@ void orc_lbvh_export(void* p, void* nodes, float* tris, uint32_t* order) {
 int orc_lbvh_count(void* p, const float* o, const float* d, uint64_t n, float tfar, uint32_t* visits,
                    uint32_t* tests, float* t_out, uint32_t* face_out, int nthreads) {
   const Lbvh& L = *static_cast<Lbvh*>(p);
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads_or_default(nthreads))
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    uint64_t v = 0, t = 0;
+    const HitF h = lbvh_trace(L, V3{o[3 * i], o[3 * i + 1], o[3 * i + 2]}, V3{d[3 * i], d[3 * i + 1], d[3 * i + 2]},
+                              tfar, v, t);
+    visits[i] = (uint32_t)v;
+    tests[i] = (uint32_t)t;
+    if (t_out) t_out[i] = h.hit ? h.t : INFINITY;
+    if (face_out) face_out[i] = h.face;
+  }
+  return 0;
+}
+
+// Node visits, triangle tests and hits of explicit rays through any tree in
+// the GPU library's layout (nodes: n_faces - 1 records of 16 words, tris:
+// n_faces records of 12 floats, as rmg_map_export writes them), walked like
+// orc_lbvh_count walks the canonical LBVH.
+int orc_tree_count(const void* nodes, const float* tris, uint32_t n_faces, const float* o, const float* d, uint64_t n,
+                   float tfar, uint32_t* visits, uint32_t* tests, float* t_out, uint32_t* face_out, int nthreads) {
+  Lbvh L;
+  if (n_faces >= 2) {
+    L.nodes.resize(n_faces - 1);
+    std::memcpy(L.nodes.data(), nodes, sizeof(LNode) * L.nodes.size());
+    L.tris.assign(tris, tris + 12 * (size_t)n_faces);
+  }
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads_or_default(nthreads))
   for (int64_t i = 0; i < (int64_t)n; ++i) {
     uint64_t v = 0, t = 0;

@@ -29,6 +29,8 @@ RMG_ERR_TIMEOUT = 4
 RMG_ERR_TRAVERSAL_BUDGET = 5
 RMG_ERR_NO_DEVICE = 6
 RMG_ERR_UNSUPPORTED = 7
+RMG_BUILD_SAH = 0
+RMG_BUILD_LBVH = 1
 
 RMG_MODEL_SPHERICAL = 0
 RMG_MODEL_PINHOLE = 1
@@ -157,6 +159,7 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_device_info": (C.c_int, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "rmg_stream_wait": (C.c_int, [_P, _U32]),
     "rmg_map_build": (C.c_int, [_P, _U32, _P, _U32, _P, C.POINTER(_P)]),
+    "rmg_map_build_ex": (C.c_int, [_P, _U32, _P, _U32, _U32, _P, C.POINTER(_P)]),
     "rmg_map_refit": (C.c_int, [_P, _P, _U32, _P]),
     "rmg_map_destroy": (C.c_int, [_P]),
     "rmg_map_info_get": (C.c_int, [_P, C.POINTER(MapInfoC)]),

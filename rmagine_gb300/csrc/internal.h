@@ -72,6 +72,8 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 
 DeviceMap device_view(const rmg_map* m);
 int wide_build(rmg_map* m, cudaStream_t st);
+// Binned-SAH topology of a map's n >= 2 faces (csrc/sah.cu); synchronises.
+int sah_build_topology(rmg_map* m, cudaStream_t st, uint32_t* d_order);
 int wide_refit(rmg_map* m, cudaStream_t st);
 void wide_free(rmg_map* m);
 SensorDev device_view(const rmg_sensor* s);

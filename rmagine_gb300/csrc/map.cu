@@ -340,7 +340,15 @@ using namespace rmg;
 
 extern "C" int rmg_map_build(const rmg_vec3* vertices, uint32_t n_vertices, const rmg_face* faces,
                              uint32_t n_faces, void* stream, rmg_map** out) {
+  return rmg_map_build_ex(vertices, n_vertices, faces, n_faces, RMG_BUILD_SAH, stream, out);
+}
+
+extern "C" int rmg_map_build_ex(const rmg_vec3* vertices, uint32_t n_vertices, const rmg_face* faces,
+                                uint32_t n_faces, uint32_t builder, void* stream, rmg_map** out) {
   if (!out) return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: out is NULL");
+  *out = nullptr;
+  if (builder != RMG_BUILD_SAH && builder != RMG_BUILD_LBVH)
+    return fail(RMG_ERR_UNSUPPORTED, "rmg_map_build_ex: builder must be RMG_BUILD_SAH or RMG_BUILD_LBVH");
   *out = nullptr;
   if (n_faces > 0 && (!vertices || !faces))
     return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: vertices/faces are NULL");
@@ -413,8 +421,31 @@ extern "C" int rmg_map_build(const rmg_vec3* vertices, uint32_t n_vertices, cons
     return RMG_OK;
   }
 
-  // ---- scratch ----------------------------------------------------------
   const uint32_t n = n_faces;
+  if (builder == RMG_BUILD_SAH) {
+    s = sah_build_topology(m, st, m->d_leaf_order);
+    if (s == RMG_OK) s = repack_and_refit(m, st, m->d_leaf_order);
+    unsigned int* d_depth = nullptr;
+    if (s == RMG_OK) s = dev_alloc(&d_depth, 1, "depth");
+    if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(d_depth, 0, 4, st), "memset");
+    if (s == RMG_OK) {
+      k_depth<<<grid_for(n), kBlock, 0, st>>>(m->d_nodes, m->d_leaf_parent, n, d_depth);
+      s = cuda_status(cudaGetLastError(), "depth");
+    }
+    unsigned int depth = 0;
+    if (s == RMG_OK) s = cuda_status(cudaMemcpyAsync(&depth, d_depth, 4, cudaMemcpyDeviceToHost, st), "depth copy");
+    if (s == RMG_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
+    cudaFree(d_depth);
+    if (s != RMG_OK) { free_map(m); return s; }
+    m->depth = depth;
+    s = wide_build(m, st);
+    if (s != RMG_OK) { free_map(m); return s; }
+    update_info(m, st);
+    *out = m;
+    return RMG_OK;
+  }
+
+  // ---- LBVH scratch -----------------------------------------------------
   const int nb = std::min<int>((int)grid_for(n), 4 * device_sm_count());
   float* d_partial = nullptr;
   float* d_bounds = nullptr;

@@ -124,7 +124,7 @@ def test_lbvh_matches_canonical_build(which):
     else:  # many identical triangles: equal Morton codes, index tie-break
         v, f = scenes.gen_cube()
         v, f = scenes.merge([(v, f)] * 40)
-    m = rm.Map(v, f)
+    m = rm.Map(v, f, builder="lbvh")
     g = m.export()
     c = oracle.CanonicalLbvh(v, f).export()
     assert np.array_equal(g["leaf_order"], c["leaf_order"])
@@ -201,7 +201,7 @@ def test_deep_trees_trail_walks(extra, min_depth, max_depth):
     """Trees deeper than the 32-level full stack run the trail walks (64- and 128-bit trails with
     the short stack or none): parity with the oracle, and every stack setting bit-identical."""
     v, f, centres = comb_mesh(extra)
-    m = rm.Map(v, f)
+    m = rm.Map(v, f, builder="lbvh")
     depth = m.info()["depth"]
     assert min_depth <= depth <= max_depth, depth
     origin = np.array([-3.0, -2.0, -1.0], np.float32)
@@ -297,9 +297,11 @@ def test_host_bundle_matches_device_bundle():
         assert np.array_equal(getattr(hb, a).numpy().view(np.uint8), dev[a].view(np.uint8)), a
 
 
-def test_refit_moves_geometry():
+@pytest.mark.parametrize("builder", ["lbvh", "sah"])
+def test_refit_moves_geometry(builder):
     sc = scenes.box_room(seed=6, n_boxes=60)
-    m = rm.Map(sc.vertices, sc.faces)
+    m = rm.Map(sc.vertices, sc.faces, builder=builder)
+    links = m.export()["links"]
     moved = sc.vertices + np.array([0.3, -0.2, 0.1], np.float32)
     m.refit(moved)
     model = sensors.vlp16_900()
@@ -311,8 +313,10 @@ def test_refit_moves_geometry():
     assert rep["unexcused"] == 0, rep
     # the refitted tree keeps the original topology and carries the new boxes
     g = m.export()
-    c = oracle.CanonicalLbvh(sc.vertices, sc.faces).export()
-    assert np.array_equal(g["links"], c["links"])
+    assert np.array_equal(g["links"], links)
+    if builder == "lbvh":
+        c = oracle.CanonicalLbvh(sc.vertices, sc.faces).export()
+        assert np.array_equal(g["links"], c["links"])
 
 
 def test_corrupt_tree_reports_budget_error_not_a_fault():
