@@ -57,7 +57,7 @@ WORK_PER_RAY = {
 # from one ncu capture of the workload (profiles/).
 TRAFFIC: dict = {
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
-    "terrain1m_spherical": 10 * (315226112 + 437777920),
+    "terrain1m_spherical": 10 * (289994240 + 438243328),
     "icp_stats_fwd": 6442640128 + 4728320,
     "icp_stats_bwd": 6444127744 + 6394882560,
     "pose_grad": 13100006912 + 351378688,
@@ -250,7 +250,10 @@ def gpu_raycast(args, world):
     W, H = model_size(model)
     n = poses.shape[0]
     rays = n * W * H
-    m = rm.Map(sc.vertices, sc.faces)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    m = rm.Map(sc.vertices, sc.faces)  # binned-SAH tree (the default builder); includes the host->device copy
+    build_ms = 1e3 * (time.perf_counter() - t0)
     sim = rm.make_simulator(model, m)
     Tbm = torch.from_numpy(poses).to(dev)
     bundle = rm.resize_memory_bundle(rm.Bundle(*attrs), W, H, n, device=dev)
@@ -275,23 +278,25 @@ def gpu_raycast(args, world):
     hb = rm.resize_memory_bundle(rm.Bundle(*attrs), W, H, n, device="cpu", pin_memory=True)
     sim.simulate(host_poses, hb)
     e2e_t = []
-    for _ in range(max(1, min(args.steps, 3))):
+    for _ in range(max(3, min(args.steps, 5))):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         sim.simulate(host_poses, hb)
         e2e_t.append(time.perf_counter() - t0)
-    e2e = rays / (sum(e2e_t) / len(e2e_t)) / 1e6
+    e2e = rays / float(np.median(e2e_t)) / 1e6
     out_b = sum(OUT_BYTES[a] for a in attrs)
     wk = WORK_PER_RAY.get(args.workload)
     rl = None
     if wk:
         rl = roofline(out_b + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
-                      "algorithmic bytes per ray = outputs + 64 B per node visit + 48 B per triangle test; "
-                      "node and triangle fetches are served mostly from L1/L2, so this exceeds the HBM roof",
+                      "algorithmic bytes per ray = outputs + 64 B per node visit + 48 B per triangle test, with the "
+                      "canonical LBVH's visit counts (the default SAH tree visits about 17% fewer nodes for the same "
+                      "rays); node and triangle fetches are served mostly from L1/L2, so this exceeds the HBM roof",
                       TRAFFIC.get(args.workload))
     config = dict(desc)
     config.update({"launch": {k: int(getattr(tuned, k)) for k, _ in tuned._fields_},
                    "poses": int(n), "rays_per_step": int(rays), "triangles": int(sc.n_faces),
+                   "tree": {"builder": m.builder, "depth": int(m.info()["depth"]), "build_ms": round(build_ms, 1)},
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas{world}" if world > 1 else "single"})
     line = {"metric": "Mrays/s", "unit": "Mrays/s", "value": round(value, 2), "ms_per_step": round(total_ms / args.steps, 3),
@@ -353,12 +358,12 @@ def gpu_scene(args, world):
     hb = rm.resize_memory_bundle(rm.Bundle(*SCENE_ATTRS), W, H, n, device="cpu", pin_memory=True)
     sim.simulate(host_poses, hb)
     e2e_t = []
-    for _ in range(max(1, min(args.steps, 3))):
+    for _ in range(max(3, min(args.steps, 5))):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         sim.simulate(host_poses, hb)
         e2e_t.append(time.perf_counter() - t0)
-    e2e = rays / (sum(e2e_t) / len(e2e_t)) / 1e6
+    e2e = rays / float(np.median(e2e_t)) / 1e6
     out_b = sum(OUT_BYTES[a] for a in SCENE_ATTRS)
     wk = WORK_PER_RAY["terrain1m_spherical"]
     rl = roofline(out_b + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
