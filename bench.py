@@ -60,9 +60,9 @@ TRAFFIC: dict = {
     "terrain1m_spherical": 10 * (289994240 + 438243328),
     "icp_stats_fwd": 6442640128 + 4728320,
     "icp_stats_bwd": 6444127744 + 6394882560,
-    "pose_grad": 13100006912 + 351378688,
+    "pose_grad": 12633964800 + 681905664,
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
-    "rcc_fused": 10 * (310600448 + 23166208),
+    "rcc_fused": 10 * (295375872 + 23611136),
 }
 
 RAYCAST = ("terrain1m_spherical", "terrain1m_pinhole", "terrain2m_spherical", "terrain33m_spherical", "room_vlp16")
