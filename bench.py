@@ -885,18 +885,31 @@ def gpu_batched(args, world):
     if m.status() != 0:
         raise RuntimeError("device status error in the timed region")
     value = world * rays * args.steps / (total_ms / 1e3) / 1e6
-    # e2e: host poses in, host hits+ranges out, through the plan
+    # e2e: host poses in, host hits+ranges out, through the chunked plan (16 pose ranges of every
+    # job; each range's outputs copy to the host while the next range is cast)
     host_poses = all_poses.cpu().pin_memory()
     host_out = {a: torch.empty(t.shape, dtype=t.dtype, pin_memory=True) for a, t in all_out.items()}
+    host_jobs = []
+    r0 = 0
+    for nr in n_rays:
+        hb = rm.Bundle(*attrs)
+        for a in attrs:
+            setattr(hb, a, host_out[a][r0:r0 + nr])
+        host_jobs.append(hb)
+        r0 += nr
+    e2e_chunks = 16
+    cplan = batched.ChunkedBatchPlan(m, jobs, e2e_chunks, best)
+
+    def e2e_step():
+        all_poses.copy_(host_poses, non_blocking=True)
+        cplan.run_to_host(host_jobs)
+
+    e2e_step()
     e2e_t = []
     for _ in range(3):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        all_poses.copy_(host_poses, non_blocking=True)
-        plan.launch()
-        for a in attrs:
-            host_out[a].copy_(all_out[a], non_blocking=True)
-        torch.cuda.synchronize(dev)
+        e2e_step()
         e2e_t.append(time.perf_counter() - t0)
     e2e = rays / float(np.median(e2e_t)) / 1e6
     wk = WORK_PER_RAY.get("terrain2m_spherical")

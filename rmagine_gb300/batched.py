@@ -121,6 +121,65 @@ class BatchPlan:
             pass
 
 
+class ChunkedBatchPlan:
+    """Host-result form of a batch: every job's poses are split into n_chunks ranges and one
+    BatchPlan is built per range.  run_to_host() launches the plans in order on the current stream
+    and copies each plan's outputs to host memory on a second stream while the next plan runs, so
+    the device->host copy of all but the last range overlaps the ray casting.  Outputs are
+    bit-identical to one BatchPlan over all poses (every ray is independent).  Jobs are given as
+    for BatchPlan, with device Tbm and device bundles; a job with fewer poses than n_chunks sits in
+    the first ranges only."""
+
+    def __init__(self, map: Map, jobs, n_chunks: int = 4, config: L.BatchConfigC | None = None):
+        self.jobs = list(jobs)
+        self.plans: list[BatchPlan] = []
+        self.slices: list[list[tuple[int, int, int]]] = []  # per plan: (job, first ray, end ray)
+        for k in range(max(1, int(n_chunks))):
+            sub, sl = [], []
+            for j, job in enumerate(self.jobs):
+                who, Tbm, bundle = job[0], job[1].reshape(-1, 8), job[2]
+                n = Tbm.shape[0]
+                p0, p1 = n * k // n_chunks, n * (k + 1) // n_chunks
+                if p1 <= p0:
+                    continue
+                sensor = who.sensor if isinstance(who, _Simulator) else who
+                per = sensor.width * sensor.height
+                b = Bundle(*bundle.attrs)
+                for a, t in bundle.tensors().items():
+                    setattr(b, a, t[p0 * per:p1 * per])
+                sub.append((who, Tbm[p0:p1], b) + tuple(job[3:]))
+                sl.append((j, p0 * per, p1 * per))
+            if sub:
+                self.plans.append(BatchPlan(map, sub, config))
+                self.slices.append(sl)
+        self._copy = None
+
+    def launch(self) -> None:
+        """All ranges on the device, asynchronously on the current stream."""
+        for p in self.plans:
+            p.launch()
+
+    def run_to_host(self, host_bundles) -> None:
+        """host_bundles[j]: host Bundle of job j (same attributes and sizes as its device bundle;
+        pinned memory copies fastest).  Synchronous."""
+        if self._copy is None:
+            self._copy = torch.cuda.Stream()
+        cur = torch.cuda.current_stream()
+        self._copy.wait_stream(cur)
+        for plan, sl in zip(self.plans, self.slices):
+            plan.launch()
+            ev = torch.cuda.Event()
+            ev.record(cur)
+            self._copy.wait_event(ev)
+            with torch.cuda.stream(self._copy):
+                for j, r0, r1 in sl:
+                    host = host_bundles[j]
+                    for a, t in self.jobs[j][2].tensors().items():
+                        getattr(host, a)[r0:r1].copy_(t[r0:r1], non_blocking=True)
+        cur.wait_stream(self._copy)
+        cur.synchronize()
+
+
 def batch_config(stack_depth=8, block_warps=4, tile_w=8, tile_h=4, grab=2, ctas_per_sm=0, use_graph=1):
     return L.BatchConfigC(stack_depth, block_warps, tile_w, tile_h, grab, ctas_per_sm, use_graph)
 

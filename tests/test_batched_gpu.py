@@ -89,3 +89,30 @@ def test_empty_plan_and_zero_pose_entries(setup):
     plan.launch()
     torch.cuda.synchronize()
     assert plan.info()["rays"] == 0
+
+
+@pytest.mark.parametrize("n_chunks", [1, 3, 8])
+def test_chunked_plan_to_host_equals_plain(setup, n_chunks):
+    """ChunkedBatchPlan.run_to_host: every job's poses in n_chunks ranges (jobs with fewer poses sit
+    in the first ranges), outputs copied to pinned and pageable host bundles bit-identical to one
+    plain simulate per sensor; launch() alone fills the device bundles the same way."""
+    m, jobs, plains = setup
+    cp = batched.ChunkedBatchPlan(m, jobs, n_chunks)
+    for pin in (True, False):
+        hosts = []
+        for sim, poses, b in jobs:
+            hb = rm.resize_memory_bundle(rm.Bundle(*ATTRS), sim.sensor.width, sim.sensor.height, poses.shape[0],
+                                         device="cpu", pin_memory=pin)
+            for t in hb.tensors().values():
+                t.view(torch.uint8).fill_(0xA5)
+            hosts.append(hb)
+        clear(jobs)
+        cp.run_to_host(hosts)
+        for hb, p in zip(hosts, plains):
+            for a in ATTRS:
+                assert torch.equal(getattr(hb, a).view(torch.uint8), getattr(p, a).cpu().view(torch.uint8)), a
+    clear(jobs)
+    cp.launch()
+    torch.cuda.synchronize()
+    assert_same(jobs, plains)
+    assert m.status() == 0
