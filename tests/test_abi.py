@@ -72,3 +72,9 @@ def test_invalid_arguments_fail_without_touching_the_gpu(built):
     st = lib.rmg_map_build(v.ctypes.data_as(ctypes.c_void_p), 3, f.ctypes.data_as(ctypes.c_void_p), 1, None,
                            ctypes.byref(out))
     assert st == _lib.RMG_ERR_INVALID_ARG
+    # an unknown tree builder is rejected before any device work
+    st = lib.rmg_map_build_ex(v.ctypes.data_as(ctypes.c_void_p), 3, f.ctypes.data_as(ctypes.c_void_p), 1, 7, None,
+                              ctypes.byref(out))
+    assert st == _lib.RMG_ERR_UNSUPPORTED
+    assert lib.rmg_host_set_pipeline(0, 9) == _lib.RMG_ERR_UNSUPPORTED
+    assert lib.rmg_host_set_pipeline(0, 0) == _lib.RMG_OK
