@@ -33,7 +33,10 @@
 namespace rmg {
 namespace {
 
-constexpr int kNB = 16;               // bins per axis
+#ifndef RMG_SAH_BINS
+#define RMG_SAH_BINS 16
+#endif
+constexpr int kNB = RMG_SAH_BINS;     // bins per axis
 constexpr int kBlk = 256;
 constexpr uint32_t kBatch = 32768;    // tasks whose bins are held at once
 constexpr uint32_t kMaxDepth = 32;    // leaves at most this many edges below the root
