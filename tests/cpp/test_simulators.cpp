@@ -259,6 +259,54 @@ static void test_autotune(const rm::MapPtr& map) {
   fail_if(std::memcmp(x.raw(), y.raw(), 4 * x.size()) != 0, "autotune: results changed");
 }
 
+// A bumpy 64 x 64 heightfield: both tree builders and the host (RAM) and device forms of
+// simulate give bit-identical results.
+static void test_builders_and_host_form() {
+  const int G = 64;
+  rm::Memory<rm::Vector3, rm::RAM> V(G * G);
+  for (int y = 0; y < G; ++y)
+    for (int x = 0; x < G; ++x)
+      V[y * G + x] = {(float)x - G / 2, (float)y - G / 2, 0.7f * std::sin(0.31f * x) * std::cos(0.23f * y) - 2.0f};
+  rm::Memory<rm::Face, rm::RAM> F(2 * (G - 1) * (G - 1));
+  size_t k = 0;
+  for (int y = 0; y + 1 < G; ++y)
+    for (int x = 0; x + 1 < G; ++x) {
+      const uint32_t a = y * G + x, b = a + 1, c = a + G, d = c + 1;
+      F[k++] = {a, b, d};
+      F[k++] = {a, d, c};
+    }
+  auto sah = std::make_shared<rm::TriangleMap>(V, F, (cudaStream_t)0, RMG_BUILD_SAH);
+  auto lbvh = std::make_shared<rm::TriangleMap>(V, F, (cudaStream_t)0, RMG_BUILD_LBVH);
+  rm::Memory<rm::Transform, rm::RAM> T(5);
+  for (size_t i = 0; i < T.size(); ++i) {
+    T[i] = rm::Transform::Identity();
+    T[i].t = {-10.0f + 4.0f * i, 3.0f - 1.5f * i, 0.5f};
+  }
+  rm::SphereSimulatorGB300 host_sim(sah);
+  host_sim.setModel(vlp16());
+  auto host = host_sim.simulate<rm::Bundle<rm::Ranges<rm::RAM>, rm::Normals<rm::RAM>, rm::FaceIds<rm::RAM>>>(T);
+  rm::SphereSimulatorGB300 dev_sim(lbvh);
+  dev_sim.setModel(vlp16());
+  rm::Memory<rm::Transform, rm::VRAM_CUDA> Td;
+  Td = T;
+  auto dev = dev_sim.simulate<rm::Bundle<rm::Ranges<rm::VRAM_CUDA>, rm::Normals<rm::VRAM_CUDA>,
+                                         rm::FaceIds<rm::VRAM_CUDA>>>(Td);
+  rm::cuda_check(cudaDeviceSynchronize(), "sync");
+  rm::Memory<float, rm::RAM> r;
+  rm::Memory<rm::Vector3, rm::RAM> n;
+  rm::Memory<uint32_t, rm::RAM> f;
+  r = dev.ranges;
+  n = dev.normals;
+  f = dev.face_ids;
+  fail_if(r.size() != host.ranges.size() || std::memcmp(r.raw(), host.ranges.raw(), 4 * r.size()) != 0,
+          "builders/host form: ranges differ");
+  fail_if(std::memcmp(n.raw(), host.normals.raw(), 12 * n.size()) != 0, "builders/host form: normals differ");
+  fail_if(std::memcmp(f.raw(), host.face_ids.raw(), 4 * f.size()) != 0, "builders/host form: face ids differ");
+  size_t hits = 0;
+  for (size_t i = 0; i < f.size(); ++i) hits += f[i] != 0xffffffffu;
+  fail_if(hits == 0, "builders/host form: no ray hit the heightfield");
+}
+
 int main() {
   try {
     auto map = make_cube_map();
@@ -272,6 +320,7 @@ int main() {
     test_noise();
     test_files(map);
     test_autotune(map);
+    test_builders_and_host_form();
     fail_if(map->status() != 0, "device status");
   } catch (const std::exception& e) {
     std::fprintf(stderr, "FAILED: %s\n", e.what());
