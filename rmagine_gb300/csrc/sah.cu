@@ -1,5 +1,7 @@
 // Top-down binned-SAH build of a binary BVH with one triangle per leaf, on the
-// GPU, level by level.
+// GPU, level by level: the binned surface area heuristic of Wald ("On fast
+// construction of SAH-based bounding volume hierarchies", IEEE RT 2007),
+// breadth-first over all nodes of a level at once.
 //
 // Every internal node of the current level is a task: a contiguous range of
 // the triangle permutation plus the bounds of its triangles' centroids.  Per
