@@ -524,7 +524,8 @@ def gpu_icp(args, world):
     b_ms, _, _ = Timer(dev, args.steps).run(bwd, world)
     value = world * corr * args.steps / (total_ms / 1e3) / 1e9
     # e2e: host (pinned) clouds in, transforms + gradients back, through the public API; batches in
-    # 8 chunks whose uploads, statistics + backward and downloads overlap on three streams
+    # chunks whose uploads, statistics + backward and downloads overlap on three streams (the copies
+    # in the two directions share the host link: 340 GB/s together against 193-211 GB/s alone)
     hs, ht = src.cpu().pin_memory(), tgt.cpu().pin_memory()
     hgd = torch.empty(hs.shape, dtype=torch.float32, pin_memory=True)
     hgm = torch.empty(hs.shape, dtype=torch.float32, pin_memory=True)
@@ -532,7 +533,7 @@ def gpu_icp(args, world):
     ds, dt_ = torch.empty_like(src), torch.empty_like(tgt)
     up, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
     compute = torch.cuda.current_stream(dev)
-    cstep = max(1, B // 8)
+    cstep = max(1, B // 32)  # 32 chunks: 6.74 Gcorr/s; 8 / 16 / 64: 6.44 / 6.69 / 6.68
 
     def e2e_step():
         up.wait_stream(compute)
@@ -560,13 +561,13 @@ def gpu_icp(args, world):
 
     e2e_step()
     e2e_t = []
-    for _ in range(max(1, min(args.steps, 3))):
+    for _ in range(max(3, min(args.steps, 5))):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         e2e_step()
         torch.cuda.synchronize(dev)
         e2e_t.append(time.perf_counter() - t0)
-    e2e = corr / (sum(e2e_t) / len(e2e_t)) / 1e9
+    e2e = corr / float(np.median(e2e_t)) / 1e9
     fwd_s, bwd_s = f_ms / args.steps / 1e3, b_ms / args.steps / 1e3
     rl_f = roofline(24, corr, fwd_s, "k_stats: 24 B per correspondence read (dataset + model points)",
                     TRAFFIC.get("icp_stats_fwd"))
