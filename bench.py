@@ -418,7 +418,7 @@ def gpu_noise(args, world):
             "ms_per_step": round(total_ms / args.steps, 3), "dtype": "f32",
             "config": {"workload": "GaussianNoise(0, 0.02) on 131,072,000 ranges in HBM", "l2": "inputs > L2"},
             "gpu_launches": args.steps,
-            "e2e": {"value": round(n // 8 / (sum(e2e_t) / 3) / 1e9, 3), "unit": "Granges/s",
+            "e2e": {"value": round(n // 8 / float(np.median(e2e_t)) / 1e9, 3), "unit": "Granges/s",
                     "h2d_bytes_per_step": 4 * (n // 8), "d2h_bytes_per_step": 4 * (n // 8)},
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
 
@@ -659,14 +659,14 @@ def gpu_posegrad(args, world):
     host_est = torch.from_numpy(est).pin_memory()
     host_obs = obs.cpu().pin_memory()
     e2e_t = []
-    for _ in range(max(1, min(args.steps, 3))):
+    for _ in range(max(3, min(args.steps, 5))):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         g, l_ = rg.range_pose_grad(sim, host_est, host_obs, 0.2)
         g.cpu()
         l_.cpu()
         e2e_t.append(time.perf_counter() - t0)
-    e2e = n_poses / (sum(e2e_t) / len(e2e_t))
+    e2e = n_poses / float(np.median(e2e_t))
     wk = WORK_PER_RAY["pose_grad"]
     rl = roofline(4 + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
                   "per ray: observed range 4 B + 64 B per node visit + 48 B per triangle test (the adjoint re-reads "
@@ -771,14 +771,14 @@ def gpu_rcc(args, world):
     host_est = torch.from_numpy(est).pin_memory()
     host_dp, host_dm = dp.cpu().pin_memory(), dm.cpu().pin_memory()
     e2e_t = []
-    for _ in range(max(1, min(args.steps, 3))):
+    for _ in range(max(3, min(args.steps, 5))):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
         st, T = sim.simulate_statistics(host_est, host_dp, dataset_mask=host_dm, params=P)
         st.cpu()
         T.cpu()
         e2e_t.append(time.perf_counter() - t0)
-    e2e = rays / (sum(e2e_t) / len(e2e_t)) / 1e6
+    e2e = rays / float(np.median(e2e_t)) / 1e6
     wk = WORK_PER_RAY["rcc_fused"]
     rl = roofline(1 + wk["data_frac"] * 12 + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
                   "per sensor ray: dataset mask 1 B + dataset point 12 B where valid + 64 B per node visit + 48 B per "
