@@ -469,6 +469,11 @@ class SimulatorGB300 {
           "rmg_simulate_statistics");
   }
   void setTsb(const Transform& T) { Tsb_ = T; }
+  // setModel(MemoryView<ModelT, RAM>) (SphereSimulatorEmbree.hpp:115): the first model.
+  void setModel(const Memory<ModelT, RAM>& models) {
+    if (models.size() == 0) throw Exception(RMG_ERR_INVALID_ARG, "setModel: no model");
+    setModel(models[0]);
+  }
   void setModel(const ModelT& model) {
     const rmg_model c = model.to_c();
     rmg_sensor* s = nullptr;
@@ -529,6 +534,21 @@ class SimulatorGB300 {
     resize_memory_bundle<RAM>(res, W_, H_, (unsigned)Tbm.size());
     simulate(Tbm, res);
     return res;
+  }
+
+  // One pose (SphereSimulatorEmbree.hpp:128-135): results in RAM; synchronises.
+  template <typename BundleRAM>
+  void simulate(const Transform& Tbm, BundleRAM& ret) const {
+    Memory<Transform, RAM> T(1);
+    T[0] = Tbm;
+    simulate(T, ret);
+  }
+
+  template <typename BundleRAM>
+  BundleRAM simulate(const Transform& Tbm) const {
+    Memory<Transform, RAM> T(1);
+    T[0] = Tbm;
+    return simulate<BundleRAM>(T);
   }
 
   uint32_t width() const { return W_; }

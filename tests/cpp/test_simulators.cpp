@@ -305,6 +305,16 @@ static void test_builders_and_host_form() {
   size_t hits = 0;
   for (size_t i = 0; i < f.size(); ++i) hits += f[i] != 0xffffffffu;
   fail_if(hits == 0, "builders/host form: no ray hit the heightfield");
+  // the single-pose overloads give the pose's slice of the batch
+  rm::Memory<rm::SphericalModel, rm::RAM> models(1);
+  models[0] = vlp16();
+  rm::SphereSimulatorGB300 one(sah);
+  one.setModel(models);
+  auto single = one.simulate<rm::Bundle<rm::Ranges<rm::RAM>>>(T[3]);
+  const size_t per = (size_t)one.width() * one.height();
+  fail_if(single.ranges.size() != per ||
+              std::memcmp(single.ranges.raw(), host.ranges.raw() + 3 * per, 4 * per) != 0,
+          "single-pose simulate differs from the batch");
 }
 
 int main() {
