@@ -65,3 +65,18 @@ def test_sah_yardstick(name):
     want = SAH_YARDSTICK[name]
     assert abs(v.mean() - want["nodes"]) / want["nodes"] < 0.03
     assert abs(t.mean() - want["tris"]) / want["tris"] < 0.05
+
+
+def test_tree_count_of_an_exported_tree_equals_the_canonical_walk():
+    """oracle.tree_count (any tree in the GPU layout) walks like CanonicalLbvh.count: on the
+    canonical tree's own export the counts and hits agree exactly."""
+    sc, model, poses, _, _ = bench.raycast_workload("room_vlp16")
+    poses = poses[:5]
+    W, H = oracle.model_size(model)
+    gids = np.arange(poses.shape[0] * W * H, dtype=np.uint64)[::3]
+    o, d = oracle.Scene(sc.vertices, sc.faces).rays(model, IDENT, poses, gids)
+    lb = oracle.CanonicalLbvh(sc.vertices, sc.faces)
+    v1, t1, h1, f1 = lb.count(o, d, model.range.max)
+    v2, t2, h2, f2 = oracle.tree_count(lb.export(), o, d, model.range.max)
+    assert np.array_equal(v1, v2) and np.array_equal(t1, t2) and np.array_equal(f1, f2)
+    assert np.array_equal(h1.view(np.uint32), h2.view(np.uint32))
