@@ -63,6 +63,10 @@ TRAFFIC: dict = {
     "pose_grad": 12633964800 + 681905664,
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
     "rcc_fused": 10 * (295375872 + 23611136),
+    # full-size launch (131,072,000 ranges)
+    "noise": 524372992 + 463147776,
+    # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
+    "scene_terrain1m": 10 * (351828992 + 659708416),
 }
 
 RAYCAST = ("terrain1m_spherical", "terrain1m_pinhole", "terrain2m_spherical", "terrain33m_spherical", "room_vlp16")
@@ -404,7 +408,7 @@ def gpu_noise(args, world):
     torch.cuda.synchronize(dev)
     total_ms, step_ms, clocks = Timer(dev, args.steps).run(lambda: nz.apply(r), world)
     value = world * n * args.steps / (total_ms / 1e3) / 1e9
-    rl = roofline(8.0, n, total_ms / args.steps / 1e3, "read + write of one float per range", None)
+    rl = roofline(8.0, n, total_ms / args.steps / 1e3, "read + write of one float per range", TRAFFIC.get("noise"))
     host = r[: n // 8].cpu().pin_memory()
     e2e_t = []
     for _ in range(3):

@@ -21,7 +21,8 @@
 // Gaussian kinds draw one Philox block (4 numbers -> 4 normals) per group of 4
 // consecutive elements (counter = group index); dust draws one block per
 // element (counter = element index).  The kernel streams the buffer once with
-// 16-byte accesses: HBM-bound, 8 bytes per element.
+// 16-byte accesses, 8 bytes per element; the generator's integer multiplies
+// and the stream's latency bound it, at about 70% of the HBM roof.
 #include "internal.h"
 
 namespace rmg {
@@ -53,13 +54,50 @@ __device__ __forceinline__ float uniform01(uint32_t x) {
   return __fmul_rn((float)((x >> 8) | 1u), 5.9604644775390625e-08f);  // odd k * 2^-24, exact
 }
 
-// Box-Muller: (u1, u2) -> two standard normals.
+// Box-Muller: (u1, u2) -> two standard normals, on the special-function unit
+// (PTX lg2/sqrt/sin/cos .approx: relative error of lg2 below 2^-22, absolute
+// error of sin/cos below 2^-20 on [-pi, pi]), which leaves each normal within
+// about 1e-6 of the exact transform of the same uniforms -- far inside the
+// noise it models -- at a third of the instructions of the correctly rounded
+// functions.  u1 is in (0, 1): log(u1) = lg2(u1) * ln 2 is finite and <= 0.
+#ifndef RMG_NOISE_APPROX
+#define RMG_NOISE_APPROX 1
+#endif
+__device__ __forceinline__ float lg2_approx(float x) {
+  float y;
+  asm("lg2.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float y;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float sin_approx(float x) {
+  float y;
+  asm("sin.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float cos_approx(float x) {
+  float y;
+  asm("cos.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __device__ __forceinline__ void box_muller(float u1, float u2, float& z0, float& z1) {
+#if RMG_NOISE_APPROX
+  const float r = sqrt_approx(-1.38629436f * lg2_approx(u1));  // -2 ln 2 * log2(u1)
+  // angle 2 pi u2 - pi in [-pi, pi): the same circle point up to a half turn, i.e. (-cos, -sin)
+  const float a = fmaf(6.28318531f, u2, -3.14159265f);
+  z0 = -r * cos_approx(a);
+  z1 = -r * sin_approx(a);
+#else
   const float r = sqrtf(-2.0f * logf(u1));
   float s, c;
   sincospif(2.0f * u2, &s, &c);
   z0 = r * c;
   z1 = r * s;
+#endif
 }
 
 struct NoiseDev {
@@ -88,37 +126,52 @@ __device__ __forceinline__ float dust_one(const NoiseDev& p, float r, uint64_t i
   return r;
 }
 
-__global__ void __launch_bounds__(256) k_noise(float* data, uint64_t n, const NoiseDev p) {
+// Noise of one group of four consecutive ranges (group index g, first element 4 g).
+__device__ __forceinline__ void noise_group(const NoiseDev& p, uint64_t g, float v[4]) {
+  const uint64_t i0 = 4 * g;
+  if (p.kind == RMG_NOISE_UNIFORM_DUST) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = dust_one(p, v[k], i0 + k);
+  } else {
+    const U4 b = philox4x32_10(U4{(uint32_t)g, (uint32_t)(g >> 32), p.call0, p.call1}, p.key0, p.key1);
+    float z[4];
+    box_muller(uniform01(b.x), uniform01(b.y), z[0], z[1]);
+    box_muller(uniform01(b.z), uniform01(b.w), z[2], z[3]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = gauss_one(p, v[k], z[k]);
+  }
+}
+
+// Resident CTAs per SM requested from the compiler: 4 (64 registers) measured
+// best; 6 (40 registers) and 8 spill and lose (607 / 551 / 388 Granges/s).
+#ifndef RMG_NOISE_MIN_BLOCKS
+#define RMG_NOISE_MIN_BLOCKS 4
+#endif
+
+// Grid-stride over groups of four ranges: with a 16-byte aligned buffer the full
+// groups stream as float4 (a second load kept in flight per thread measured
+// slower: 560 against 600 Granges/s); the last partial group, and every group
+// of an unaligned buffer, take scalar accesses.
+__global__ void __launch_bounds__(256, RMG_NOISE_MIN_BLOCKS) k_noise(float* data, uint64_t n, const NoiseDev p) {
   const uint64_t groups = (n + 3) / 4;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool vec = (reinterpret_cast<uintptr_t>(data) & 15u) == 0;
-  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < groups;
-       g += (uint64_t)gridDim.x * blockDim.x) {
+  const uint64_t full_groups = vec ? n / 4 : 0;
+  float4* d4 = reinterpret_cast<float4*>(data);
+  for (uint64_t g = tid; g < full_groups; g += stride) {
+    const float4 q = __ldcs(d4 + g);
+    float v[4] = {q.x, q.y, q.z, q.w};
+    noise_group(p, g, v);
+    __stcs(d4 + g, make_float4(v[0], v[1], v[2], v[3]));
+  }
+  for (uint64_t g = full_groups + tid; g < groups; g += stride) {
     const uint64_t i0 = 4 * g;
     float v[4];
-    const bool full = vec && i0 + 4 <= n;
-    if (full) {
-      const float4 q = __ldcs(reinterpret_cast<const float4*>(data) + g);
-      v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
-    } else {
-      for (int k = 0; k < 4; ++k) v[k] = i0 + k < n ? data[i0 + k] : 0.0f;
-    }
-    if (p.kind == RMG_NOISE_UNIFORM_DUST) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) v[k] = dust_one(p, v[k], i0 + k);
-    } else {
-      const U4 b = philox4x32_10(U4{(uint32_t)g, (uint32_t)(g >> 32), p.call0, p.call1}, p.key0, p.key1);
-      float z[4];
-      box_muller(uniform01(b.x), uniform01(b.y), z[0], z[1]);
-      box_muller(uniform01(b.z), uniform01(b.w), z[2], z[3]);
-#pragma unroll
-      for (int k = 0; k < 4; ++k) v[k] = gauss_one(p, v[k], z[k]);
-    }
-    if (full) {
-      __stcs(reinterpret_cast<float4*>(data) + g, make_float4(v[0], v[1], v[2], v[3]));
-    } else {
-      for (int k = 0; k < 4; ++k)
-        if (i0 + k < n) data[i0 + k] = v[k];
-    }
+    for (int k = 0; k < 4; ++k) v[k] = i0 + k < n ? data[i0 + k] : 0.0f;
+    noise_group(p, g, v);
+    for (int k = 0; k < 4; ++k)
+      if (i0 + k < n) data[i0 + k] = v[k];
   }
 }
 
