@@ -776,7 +776,8 @@ def gpu_rcc(args, world):
     if m.status() != 0:
         raise RuntimeError("device status error in the timed region")
     value = world * rays * args.steps / (total_ms / 1e3) / 1e6
-    # end to end: estimates and scans from pinned host memory, statistics + transforms back
+    # end to end through rmg_simulate_statistics_host: estimates and scans from pinned host memory,
+    # statistics + transforms back in host memory
     host_est = torch.from_numpy(est).pin_memory()
     host_dp, host_dm = dp.cpu().pin_memory(), dm.cpu().pin_memory()
     e2e_t = []

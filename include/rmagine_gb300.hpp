@@ -468,6 +468,27 @@ class SimulatorGB300 {
                                   Ts ? reinterpret_cast<rmg_transform*>(Ts->raw()) : nullptr, stream),
           "rmg_simulate_statistics");
   }
+  // Host form of simulateStatistics (rmg_simulate_statistics_host): poses, scans and results in
+  // RAM; per-pose scans are uploaded in chunks while earlier chunks are reduced.  Synchronises.
+  void simulateStatistics(const Memory<Transform, RAM>& Tbm, const Memory<Vector3, RAM>& dataset,
+                          const Memory<uint8_t, RAM>* dataset_mask, bool per_pose, const Memory<Transform, RAM>* pre,
+                          const UmeyamaReductionConstraints& params, bool p2l, Memory<CrossStatistics, RAM>* stats,
+                          Memory<Transform, RAM>* Ts, cudaStream_t stream = 0) const {
+    ready();
+    if (!map_) throw Exception(RMG_ERR_UNSUPPORTED, "simulateStatistics: needs a single-mesh map");
+    if (stats) stats->resize(Tbm.size());
+    if (Ts) Ts->resize(Tbm.size());
+    const rmg_scan scan{reinterpret_cast<const rmg_vec3*>(dataset.raw()), dataset_mask ? dataset_mask->raw() : nullptr,
+                        nullptr, per_pose ? 1u : 0u};
+    const rmg_umeyama_constraints c{params.max_dist, params.dataset_id, params.model_id};
+    check(rmg_simulate_statistics_host(map_->handle(), sensor_, reinterpret_cast<const rmg_transform*>(&Tsb_),
+                                       reinterpret_cast<const rmg_transform*>(Tbm.raw()), (uint32_t)Tbm.size(), &scan,
+                                       pre ? reinterpret_cast<const rmg_transform*>(pre->raw()) : nullptr,
+                                       pre && pre->size() > 1 ? 1u : 0u, &c, p2l ? 1 : 0,
+                                       stats ? reinterpret_cast<rmg_cross_stats*>(stats->raw()) : nullptr,
+                                       Ts ? reinterpret_cast<rmg_transform*>(Ts->raw()) : nullptr, stream),
+          "rmg_simulate_statistics_host");
+  }
   void setTsb(const Transform& T) { Tsb_ = T; }
   // setModel(MemoryView<ModelT, RAM>) (SphereSimulatorEmbree.hpp:115): the first model.
   void setModel(const Memory<ModelT, RAM>& models) {

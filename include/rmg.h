@@ -552,6 +552,18 @@ int rmg_simulate_statistics(const rmg_map* map, const rmg_sensor* sensor, const 
                             const rmg_umeyama_constraints* params, int point_to_plane,
                             rmg_cross_stats* stats, rmg_transform* transforms, void* stream);
 
+/* Host form of rmg_simulate_statistics: Tbm, the dataset's arrays,
+ * pre_transforms and the outputs are HOST pointers (pinned or pageable).
+ * Per-pose scans are uploaded in pose chunks while earlier chunks are
+ * reduced; results are bit-identical to rmg_simulate_statistics on the same
+ * data.  Synchronous.  rmg_host_set_pipeline shapes the chunks (input bytes
+ * per chunk) and the compute streams. */
+int rmg_simulate_statistics_host(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                                 const rmg_transform* Tbm, uint32_t n_poses, const rmg_scan* dataset,
+                                 const rmg_transform* pre_transforms, uint32_t pre_transform_stride,
+                                 const rmg_umeyama_constraints* params, int point_to_plane,
+                                 rmg_cross_stats* stats, rmg_transform* transforms, void* stream);
+
 /* Batched Transform::mult (Transform.tcc:34-42; multInplace :44-56 when out
  * aliases a): out[i] = a[i] * b[i] for i < n, all DEVICE arrays; stride 0
  * repeats element 0 of that operand.  Lets a correction loop keep its pose

@@ -188,6 +188,8 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_umeyama_transform": (C.c_int, [_P, _U32, _P, _P]),
     "rmg_simulate_statistics": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(ScanC), _P, _U32,
                                           C.POINTER(ConstraintsC), C.c_int, _P, _P, _P]),
+    "rmg_simulate_statistics_host": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(ScanC), _P, _U32,
+                                               C.POINTER(ConstraintsC), C.c_int, _P, _P, _P]),
     "rmg_transforms_compose": (C.c_int, [_P, _U32, _P, _U32, _P, _U32, _P]),
     "rmg_mesh_read": (C.c_int, [C.c_char_p, C.POINTER(MeshC)]),
     "rmg_mesh_free": (None, [C.POINTER(MeshC)]),

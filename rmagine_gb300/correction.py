@@ -49,6 +49,9 @@ def correct_rcc(sim: _Simulator, dataset_points, Tbm_est, dataset_mask=None, n_o
     dataset scan(s) (see _Simulator.simulate_statistics for the shapes) and returns the
     corrected estimates [n, 8] on the device."""
     Tbm = S._dev(Tbm_est, torch.float32).reshape(-1, 8).clone()
+    # the scans are read n_outer * n_inner times: upload them once
+    dataset_points = S._dev(dataset_points, torch.float32)
+    dataset_mask = S._u8(dataset_mask)
     n = Tbm.shape[0]
     ident = torch.zeros((n, 8), dtype=torch.float32, device=Tbm.device)
     ident[:, 3] = 1.0

@@ -1,5 +1,6 @@
-// Host-buffer forms of rmg_simulate and rmg_simulate_scene: poses and results
-// in host memory, like the Embree simulators' RAM bundles
+// Host-buffer forms of rmg_simulate, rmg_simulate_scene and
+// rmg_simulate_statistics: poses, inputs and results in host memory, like the
+// Embree simulators' RAM bundles
 // (SphereSimulatorEmbree.hpp:130-155).  The poses are uploaded once; the rays
 // are cast in pose chunks into device staging slots, alternating between the
 // caller's stream and further compute streams so that one chunk's last warps
@@ -218,6 +219,138 @@ int host_pipeline(const char* what, uint64_t rays_per_pose, const rmg_transform*
 
 uint64_t rays_of(const rmg_sensor* sensor) { return (uint64_t)sensor->width * sensor->height; }
 
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Host form of the fused correction step.  Poses, pre-transforms and the small
+// per-pose results move in one copy each; per-pose scans (per_pose = 1) are
+// uploaded in pose chunks on an upload stream into device slots while earlier
+// chunks are reduced, the launches alternating between compute streams.  A
+// slot is refilled only after the launch that read it has finished (the
+// upload of chunk j waits for the launch of chunk j - slots, issued one
+// iteration earlier at least).
+int statistics_pipeline(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                        const rmg_transform* Tbm_h, uint32_t n, const rmg_scan& scan_h, const rmg_transform* pre_h,
+                        uint32_t pre_stride, const rmg_umeyama_constraints* params, int p2l,
+                        rmg_cross_stats* stats_h, rmg_transform* T_h, cudaStream_t st) {
+  const char* what = "rmg_simulate_statistics_host";
+  const uint64_t rays = rays_of(sensor);
+  const bool per_pose = scan_h.per_pose != 0;
+  const size_t in_per_ray = 12 + (scan_h.mask ? 1 : 0) + (scan_h.ids ? 4 : 0);
+  const size_t in_per_pose = in_per_ray * rays;
+  const uint32_t nc = (uint32_t)std::min(std::max(g_compute.load(), 1), kMaxCompute);
+  size_t chunk = n;
+  if (per_pose) {
+    chunk = std::max<size_t>(1, g_chunk_bytes.load() / std::max<size_t>(1, in_per_pose));
+    chunk = std::min<size_t>(chunk, std::max<uint32_t>(1u, (n + 1) / 2));
+  }
+  const uint32_t n_chunks = (uint32_t)((n + chunk - 1) / chunk);
+  const int slots = per_pose ? (int)std::min<uint32_t>(kSlots, n_chunks) : 1;
+  const size_t scan_poses = per_pose ? chunk : 1;  // poses' worth of scan per slot
+
+  cudaMemPool_t pool;
+  int s = staging_pool(&pool);
+  if (s != RMG_OK) return s;
+  Pipeline pl;  // copy = the upload stream here
+  RMG_CUDA_TRY(cudaStreamCreateWithFlags(&pl.copy, cudaStreamNonBlocking));
+  for (uint32_t k = 0; k + 1 < nc; ++k) {
+    RMG_CUDA_TRY(cudaStreamCreateWithFlags(&pl.side[k], cudaStreamNonBlocking));
+    RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.side_done[k], cudaEventDisableTiming));
+  }
+  for (int k = 0; k < slots; ++k) {
+    RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.cast[k], cudaEventDisableTiming));    // slot uploaded
+    RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.copied[k], cudaEventDisableTiming));  // slot consumed
+  }
+  RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.ready, cudaEventDisableTiming));
+  RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.done, cudaEventDisableTiming));
+  cudaStream_t compute[kMaxCompute] = {st};
+  for (uint32_t k = 0; k + 1 < nc; ++k) compute[k + 1] = pl.side[k];
+
+  // staging layout
+  const size_t n_pre = pre_h ? (pre_stride ? (size_t)n : 1) : 0;
+  size_t off = 0;
+  const size_t o_T = off;    off += align256((size_t)n * sizeof(rmg_transform));
+  const size_t o_pre = off;  off += align256(n_pre * sizeof(rmg_transform));
+  const size_t o_st = off;   off += align256(stats_h ? (size_t)n * sizeof(rmg_cross_stats) : 0);
+  const size_t o_Tout = off; off += align256(T_h ? (size_t)n * sizeof(rmg_transform) : 0);
+  const size_t sp_pts = align256(scan_poses * rays * 12);
+  const size_t sp_mask = scan_h.mask ? align256(scan_poses * rays) : 0;
+  const size_t sp_ids = scan_h.ids ? align256(scan_poses * rays * 4) : 0;
+  const size_t slot_bytes = sp_pts + sp_mask + sp_ids;
+  const size_t o_slots = off;
+  off += slots * slot_bytes;
+  char* stg = nullptr;
+  RMG_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&stg), off, pool, st));
+  auto* Tbm_d = reinterpret_cast<rmg_transform*>(stg + o_T);
+  auto* pre_d = pre_h ? reinterpret_cast<rmg_transform*>(stg + o_pre) : nullptr;
+  auto* stats_d = stats_h ? reinterpret_cast<rmg_cross_stats*>(stg + o_st) : nullptr;
+  auto* Tout_d = T_h ? reinterpret_cast<rmg_transform*>(stg + o_Tout) : nullptr;
+  s = cuda_status(cudaMemcpyAsync(Tbm_d, Tbm_h, (size_t)n * sizeof(rmg_transform), cudaMemcpyDefault, st), what);
+  if (s == RMG_OK && pre_d)
+    s = cuda_status(cudaMemcpyAsync(pre_d, pre_h, n_pre * sizeof(rmg_transform), cudaMemcpyDefault, st), what);
+  if (s == RMG_OK) s = cuda_status(cudaEventRecord(pl.ready, st), what);
+  if (s == RMG_OK) s = cuda_status(cudaStreamWaitEvent(pl.copy, pl.ready, 0), what);
+  for (uint32_t k = 0; s == RMG_OK && k + 1 < nc; ++k) s = cuda_status(cudaStreamWaitEvent(pl.side[k], pl.ready, 0), what);
+
+  auto upload = [&](uint32_t k) -> int {
+    const int slot = (int)(k % slots);
+    const uint64_t p0 = per_pose ? (uint64_t)k * chunk : 0;
+    const uint64_t np = per_pose ? std::min<uint64_t>(chunk, n - p0) : 1;
+    char* base = stg + o_slots + slot * slot_bytes;
+    if (k >= (uint32_t)slots) RMG_CUDA_TRY(cudaStreamWaitEvent(pl.copy, pl.copied[slot], 0));
+    RMG_CUDA_TRY(cudaMemcpyAsync(base, scan_h.points + p0 * rays, np * rays * 12, cudaMemcpyDefault, pl.copy));
+    if (scan_h.mask)
+      RMG_CUDA_TRY(cudaMemcpyAsync(base + sp_pts, scan_h.mask + p0 * rays, np * rays, cudaMemcpyDefault, pl.copy));
+    if (scan_h.ids)
+      RMG_CUDA_TRY(cudaMemcpyAsync(base + sp_pts + sp_mask, scan_h.ids + p0 * rays, np * rays * 4, cudaMemcpyDefault,
+                                   pl.copy));
+    RMG_CUDA_TRY(cudaEventRecord(pl.cast[slot], pl.copy));
+    return RMG_OK;
+  };
+  auto reduce = [&](uint32_t k) -> int {
+    const int slot = per_pose ? (int)(k % slots) : 0;
+    const cudaStream_t cs = compute[k % nc];
+    const uint32_t p0 = (uint32_t)(k * chunk), np = (uint32_t)std::min<size_t>(chunk, n - p0);
+    char* base = stg + o_slots + slot * slot_bytes;
+    if (per_pose || k == 0) RMG_CUDA_TRY(cudaStreamWaitEvent(cs, pl.cast[slot], 0));
+    rmg_scan sc;
+    sc.points = reinterpret_cast<const rmg_vec3*>(base);
+    sc.mask = scan_h.mask ? reinterpret_cast<const uint8_t*>(base + sp_pts) : nullptr;
+    sc.ids = scan_h.ids ? reinterpret_cast<const uint32_t*>(base + sp_pts + sp_mask) : nullptr;
+    sc.per_pose = scan_h.per_pose;
+    const int r = rmg_simulate_statistics(map, sensor, Tsb, Tbm_d + p0, np, &sc,
+                                          pre_d ? pre_d + (pre_stride ? p0 : 0) : nullptr, pre_stride, params, p2l,
+                                          stats_d ? stats_d + p0 : nullptr, Tout_d ? Tout_d + p0 : nullptr, cs);
+    if (r != RMG_OK) return r;
+    if (per_pose) RMG_CUDA_TRY(cudaEventRecord(pl.copied[slot], cs));
+    return RMG_OK;
+  };
+  if (per_pose) {
+    for (uint32_t k = 0; s == RMG_OK && k < n_chunks; ++k) {
+      s = upload(k);
+      if (s == RMG_OK) s = reduce(k);
+    }
+  } else {
+    s = upload(0);
+    for (uint32_t k = 0; s == RMG_OK && k < n_chunks; ++k) s = reduce(k);
+  }
+  // join, download the per-pose results, free in stream order
+  cudaEventRecord(pl.done, pl.copy);
+  cudaStreamWaitEvent(st, pl.done, 0);
+  for (uint32_t k = 0; k + 1 < nc; ++k) {
+    cudaEventRecord(pl.side_done[k], pl.side[k]);
+    cudaStreamWaitEvent(st, pl.side_done[k], 0);
+  }
+  if (s == RMG_OK && stats_h)
+    s = cuda_status(cudaMemcpyAsync(stats_h, stats_d, (size_t)n * sizeof(rmg_cross_stats), cudaMemcpyDefault, st),
+                    what);
+  if (s == RMG_OK && T_h)
+    s = cuda_status(cudaMemcpyAsync(T_h, Tout_d, (size_t)n * sizeof(rmg_transform), cudaMemcpyDefault, st), what);
+  cudaFreeAsync(stg, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (s != RMG_OK) return s;
+  return cuda_status(e, what);
+}
+
 }  // namespace
 }  // namespace rmg
 
@@ -247,6 +380,20 @@ extern "C" int rmg_simulate_scene_host(const rmg_scene* scene, const rmg_sensor*
                        [&](const rmg_transform* T, uint32_t n, const rmg_outputs* o, cudaStream_t st) {
                          return rmg_simulate_scene(scene, sensor, Tsb, T, n, o, st);
                        });
+}
+
+extern "C" int rmg_simulate_statistics_host(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                                            const rmg_transform* Tbm, uint32_t n_poses, const rmg_scan* dataset,
+                                            const rmg_transform* pre_transforms, uint32_t pre_transform_stride,
+                                            const rmg_umeyama_constraints* params, int point_to_plane,
+                                            rmg_cross_stats* stats, rmg_transform* transforms, void* stream) {
+  if (!map || !sensor || !Tsb || !dataset || !params)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics_host: NULL map, sensor, Tsb, dataset or params");
+  if (n_poses == 0) return RMG_OK;
+  if (!Tbm || !dataset->points) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics_host: Tbm or points NULL");
+  if (!stats && !transforms) return RMG_OK;
+  return statistics_pipeline(map, sensor, Tsb, Tbm, n_poses, *dataset, pre_transforms, pre_transform_stride ? 1u : 0u,
+                             params, point_to_plane, stats, transforms, as_stream(stream));
 }
 
 extern "C" int rmg_host_set_pipeline(uint64_t chunk_bytes, uint32_t compute_streams) {

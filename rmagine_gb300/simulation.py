@@ -461,17 +461,16 @@ class _Simulator:
         for every pose) or [n, W*H, 3] (one per pose), in the sensor frame and ray order of
         simulate(); dataset_mask (e.g. the scan's hits) and dataset_ids follow its shape.  pre is
         one transform or one per pose.  Returns (stats [n,16] or None, transforms [n,8] or None)
-        on the device, asynchronously on the current stream.  Per-pose scans in host memory are
-        uploaded in pose chunks on a copy stream while earlier chunks are computed, the launches
-        alternating between two compute streams (the same result as one call on device data: every
-        pose is reduced on its own)."""
+        on the device, asynchronously on the current stream.  A dataset in host memory goes
+        through rmg_simulate_statistics_host instead: per-pose scans are uploaded in pose chunks
+        while earlier chunks are reduced, and the results come back in host memory when the call
+        returns (the same values as one call on device data: every pose is reduced on its own)."""
         from . import statistics as S
 
         self._check_ready()
         if isinstance(self._map, Scene):
             raise L.RmgError(L.RMG_ERR_UNSUPPORTED, "simulate_statistics", "needs a single-mesh Map")
-        if (isinstance(dataset_points, torch.Tensor) and not dataset_points.is_cuda and dataset_points.dim() == 3
-                and dataset_points.shape[0] > 1):
+        if not (isinstance(dataset_points, torch.Tensor) and dataset_points.is_cuda):
             return self._simulate_statistics_host(Tbm, dataset_points, dataset_mask, dataset_ids, pre, params,
                                                   point_to_plane, want_stats, want_transforms)
         Tbm = S._dev(Tbm, torch.float32).reshape(-1, 8)
@@ -499,52 +498,43 @@ class _Simulator:
         return stats, T
 
     def _simulate_statistics_host(self, Tbm, dp_h, dm_h, di_h, pre, params, point_to_plane, want_stats,
-                                  want_transforms, chunks: int = 16):
+                                  want_transforms):
         from . import statistics as S
 
-        Tbm = S._dev(Tbm, torch.float32).reshape(-1, 8)
-        n = Tbm.shape[0]
+        T_in = (Tbm if isinstance(Tbm, torch.Tensor) else torch.as_tensor(np.asarray(Tbm, np.float32)))
+        T_in = T_in.reshape(-1, 8).to(torch.float32).contiguous()
+        n = T_in.shape[0]
         W, H = self.sensor.width, self.sensor.height
         per = W * H
-        if tuple(dp_h.shape) != (n, per, 3):
+        dp = torch.as_tensor(dp_h).to(torch.float32).contiguous()
+        per_pose = dp.dim() == 3
+        if dp.shape[-2:] != (per, 3) or (per_pose and dp.shape[0] != n):
             raise L.RmgError(L.RMG_ERR_INVALID_ARG, "simulate_statistics",
-                             f"dataset points {tuple(dp_h.shape)} do not match {n} poses x {per} rays")
-        host = {"points": dp_h.to(torch.float32).reshape(n, per, 3)}
-        if dm_h is not None:
-            host["mask"] = torch.as_tensor(dm_h).reshape(n, per).to(torch.uint8)
+                             f"dataset points {tuple(dp.shape)} do not match {n} poses x {per} rays")
+        dm = None if dm_h is None else torch.as_tensor(dm_h).to(torch.uint8).contiguous()
+        di = None
         if di_h is not None:
-            host["ids"] = (di_h if isinstance(di_h, torch.Tensor) else
-                           torch.as_tensor(np.asarray(di_h).astype(np.uint32).view(np.int32))).reshape(n, per).to(torch.int32)
-        dev = {k: torch.empty(v.shape, dtype=v.dtype, device="cuda") for k, v in host.items()}
-        pre_t, stride = S._pre(pre, n)
+            di = (di_h if isinstance(di_h, torch.Tensor) else
+                  torch.as_tensor(np.asarray(di_h).astype(np.uint32).view(np.int32))).to(torch.int32).contiguous()
+        for name, t in (("mask", dm), ("ids", di)):
+            if t is not None and t.numel() != dp.numel() // 3:
+                raise L.RmgError(L.RMG_ERR_INVALID_ARG, "simulate_statistics", f"dataset {name} size mismatch")
+        pre_t, stride = None, 0
+        if pre is not None:
+            pre_t = (pre if isinstance(pre, torch.Tensor) else torch.as_tensor(np.asarray(pre, np.float32)))
+            pre_t = pre_t.reshape(-1, 8).to(torch.float32).contiguous()
+            stride = 1 if pre_t.shape[0] > 1 else 0
+            if stride and pre_t.shape[0] != n:
+                raise L.RmgError(L.RMG_ERR_INVALID_ARG, "simulate_statistics", "pre: one transform or one per pose")
         params = params or S.UmeyamaReductionConstraints()
-        stats = torch.empty((n, 16), dtype=torch.float32, device="cuda") if want_stats else None
-        T = torch.empty((n, 8), dtype=torch.float32, device="cuda") if want_transforms else None
-        if self._copy_stream is None:
-            self._copy_stream = torch.cuda.Stream()
-        streams = self._compute_streams()
-        copy = self._copy_stream
-        copy.wait_stream(streams[0])
+        stats = torch.empty((n, 16), dtype=torch.float32) if want_stats else None
+        T = torch.empty((n, 8), dtype=torch.float32) if want_transforms else None
+        scan = L.ScanC(dp.data_ptr(), None if dm is None else dm.data_ptr(), None if di is None else di.data_ptr(),
+                       1 if per_pose else 0)
         pc = params.to_c()
-        step = max(1, -(-n // chunks))
-        for i, c0 in enumerate(range(0, n, step)):
-            c1 = min(n, c0 + step)
-            compute = streams[i % len(streams)]
-            with torch.cuda.stream(copy):
-                for k in dev:
-                    dev[k][c0:c1].copy_(host[k][c0:c1], non_blocking=True)
-            ev = torch.cuda.Event()
-            ev.record(copy)
-            compute.wait_event(ev)
-            scan = L.ScanC(dev["points"][c0].data_ptr(), dev["mask"][c0].data_ptr() if "mask" in dev else None,
-                           dev["ids"][c0].data_ptr() if "ids" in dev else None, 1)
-            L.call("rmg_simulate_statistics", self._map.handle, self.sensor.handle, C.byref(self._Tsb),
-                   C.c_void_p(Tbm[c0].data_ptr()), c1 - c0, C.byref(scan),
-                   None if pre_t is None else C.c_void_p(pre_t[c0 if stride else 0].data_ptr()), stride,
-                   C.byref(pc), 1 if point_to_plane else 0,
-                   None if stats is None else C.c_void_p(stats[c0].data_ptr()),
-                   None if T is None else C.c_void_p(T[c0].data_ptr()), C.c_void_p(compute.cuda_stream))
-        self._join_streams(streams)
+        L.call("rmg_simulate_statistics_host", self._map.handle, self.sensor.handle, C.byref(self._Tsb),
+               C.c_void_p(T_in.data_ptr()), n, C.byref(scan), _ptr(pre_t), stride, C.byref(pc),
+               1 if point_to_plane else 0, _ptr(stats), _ptr(T), _stream_ptr())
         return stats, T
 
     def _simulate_host(self, Tbm: torch.Tensor, bundle: Bundle, n: int) -> Bundle:

@@ -188,6 +188,14 @@ static void test_fused_step(const rm::MapPtr& map) {
   rm::Memory<rm::Transform, rm::RAM> o;
   o = out;
   fail_if(std::memcmp(&o[0], &t[0], 28) != 0, "compose");
+  // the host form on RAM copies of the same data gives the same statistics and transform
+  rm::Memory<rm::Vector3, rm::RAM> pts;
+  pts = data.points;
+  rm::Memory<rm::CrossStatistics, rm::RAM> s_h;
+  rm::Memory<rm::Transform, rm::RAM> t_h;
+  sim.simulateStatistics(identity_poses(1), pts, &h, false, nullptr, {1.0f, 0, 0}, true, &s_h, &t_h);
+  fail_if(std::memcmp(&s_h[0], &s[0], sizeof(rm::CrossStatistics)) != 0, "fused host form: statistics");
+  fail_if(std::memcmp(&t_h[0], &t[0], sizeof(rm::Transform)) != 0, "fused host form: transform");
 }
 
 // Noise: two objects with the same seed draw the same numbers; the next call differs.

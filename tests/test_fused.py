@@ -343,6 +343,7 @@ def test_host_scans_give_the_device_result_bitwise(built):
     device data bit for bit (pose counts that do and do not divide into the chunks)."""
     import torch
 
+    from rmagine_gb300 import _lib
     from rmagine_gb300 import statistics as rs
 
     torch.cuda.set_device(0)
@@ -357,5 +358,18 @@ def test_host_scans_give_the_device_result_bitwise(built):
         s1, T1 = sim.simulate_statistics(E, dp[:k].cpu().pin_memory(), dataset_mask=dm[:k].cpu().pin_memory(),
                                          pre=pre[:k], params=P)
         torch.cuda.synchronize()
-        assert torch.equal(s0, s1) and torch.equal(T0, T1), k
+        assert not s1.is_cuda and not T1.is_cuda  # the host form returns host results
+        assert torch.equal(s0.cpu(), s1) and torch.equal(T0.cpu(), T1), k
+        # host poses, a single host scan for every pose, pageable memory, a small chunk size
+        _lib.call("rmg_host_set_pipeline", 1, 3)
+        try:
+            s2, T2 = sim.simulate_statistics(torch.from_numpy(est[:k].copy()), dp[0].cpu(), dataset_mask=dm[0].cpu(),
+                                             params=P)
+            s3, T3 = sim.simulate_statistics(E, dp[0], dataset_mask=dm[0], params=P)
+            torch.cuda.synchronize()
+            assert torch.equal(s3.cpu(), s2) and torch.equal(T3.cpu(), T2), k
+            s4, T4 = sim.simulate_statistics(E, dp[:k].cpu(), dataset_mask=dm[:k].cpu(), pre=pre[:k], params=P)
+            assert torch.equal(s0.cpu(), s4) and torch.equal(T0.cpu(), T4), k
+        finally:
+            _lib.call("rmg_host_set_pipeline", 0, 0)
     assert m.status() == 0
