@@ -671,7 +671,7 @@ def gpu_posegrad(args, world):
     for _ in range(max(3, min(args.steps, 5))):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        g, l_ = rg.range_pose_grad(sim, host_est, host_obs, 0.2)
+        g, l_ = rg.range_pose_grad(sim, host_est, host_obs, 0.2)  # rmg_range_pose_grad_host: results in host memory
         g.cpu()
         l_.cpu()
         e2e_t.append(time.perf_counter() - t0)

@@ -334,6 +334,15 @@ int rmg_range_pose_grad(const rmg_map* map, const rmg_sensor* sensor,
                         const float* ranges_obs, float huber_delta,
                         float* grad, float* loss, float* ranges_sim, uint32_t* face_ids, void* stream);
 
+/* Host form of rmg_range_pose_grad: Tbm, ranges_obs and every output are HOST
+ * pointers (pinned or pageable).  Observations are uploaded and results
+ * downloaded in pose chunks that overlap the launches; any number of poses.
+ * Results are bit-identical to rmg_range_pose_grad.  Synchronous. */
+int rmg_range_pose_grad_host(const rmg_map* map, const rmg_sensor* sensor,
+                             const rmg_transform* Tsb, const rmg_transform* Tbm, uint32_t n_poses,
+                             const float* ranges_obs, float huber_delta,
+                             float* grad, float* loss, float* ranges_sim, uint32_t* face_ids, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Correspondence statistics and Umeyama.
  *

@@ -213,6 +213,8 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_batch_autotune": (C.c_int, [_P, _P, _U32, C.POINTER(BatchConfigC)]),
     "rmg_batch_destroy": (C.c_int, [_P]),
     "rmg_range_pose_grad": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, _P, C.c_float, _P, _P, _P, _P, _P]),
+    "rmg_range_pose_grad_host": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, _P, C.c_float, _P, _P, _P, _P,
+                                           _P]),
     "rmg_umeyama_backward": (C.c_int, [_P, _U32, _P, _P, _P, _P, _P, _P, C.POINTER(ConstraintsC), _U32, _U32,
                                        _P, _P, _P, _P, _P, _P]),
 }

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <functional>
 #include <mutex>
+#include <vector>
 
 #include "internal.h"
 
@@ -351,6 +352,141 @@ int statistics_pipeline(const rmg_map* map, const rmg_sensor* sensor, const rmg_
   return cuda_status(e, what);
 }
 
+// A three-stage pipeline over pose chunks: per-pose host inputs are uploaded
+// into a device slot (upload stream), the chunk is computed (alternating
+// compute streams) and its per-pose outputs are downloaded (download stream),
+// so the copies of neighbouring chunks overlap the computation.  A slot is
+// uploaded into again only after its previous chunk's downloads (which wait
+// for that chunk's computation) were issued, at least one iteration earlier.
+struct HostArray {
+  const void* src;  // input: host (or device) array of n * per_pose bytes, or NULL
+  void* dst;        // output: host (or device) array of n * per_pose bytes, or NULL
+  size_t per_pose;
+};
+using ChunkLaunch = std::function<int(uint32_t p0, uint32_t np, char* const* dev, cudaStream_t st)>;
+
+int io_pipeline(const char* what, uint32_t n, const std::vector<HostArray>& arrays, size_t max_chunk,
+                const ChunkLaunch& launch, cudaStream_t st) {
+  const size_t na = arrays.size();
+  size_t per_pose = 0;
+  for (const HostArray& a : arrays) per_pose += a.per_pose;
+  size_t chunk = std::max<size_t>(1, g_chunk_bytes.load() / std::max<size_t>(1, per_pose));
+  chunk = std::min<size_t>(chunk, std::max<uint32_t>(1u, (n + 1) / 2));
+  chunk = std::min<size_t>(chunk, std::max<size_t>(1, max_chunk));
+  const uint32_t n_chunks = (uint32_t)((n + chunk - 1) / chunk);
+  const int slots = (int)std::min<uint32_t>(kSlots, n_chunks);
+  const uint32_t nc = (uint32_t)std::min(std::max(g_compute.load(), 1), kMaxCompute);
+
+  cudaMemPool_t pool;
+  int s = staging_pool(&pool);
+  if (s != RMG_OK) return s;
+  Pipeline pl;  // copy = upload stream, down = the download stream below
+  cudaStream_t down = nullptr;
+  cudaEvent_t uploaded[kSlots] = {}, computed[kSlots] = {}, released[kSlots] = {};
+  struct Release {
+    cudaStream_t* s;
+    cudaEvent_t* ev[3];
+    int n;
+    ~Release() {
+      for (int k = 0; k < n; ++k)
+        for (cudaEvent_t* e : ev)
+          if (e[k]) cudaEventDestroy(e[k]);
+      if (*s) cudaStreamDestroy(*s);
+    }
+  } rel{&down, {uploaded, computed, released}, kSlots};
+  RMG_CUDA_TRY(cudaStreamCreateWithFlags(&pl.copy, cudaStreamNonBlocking));
+  RMG_CUDA_TRY(cudaStreamCreateWithFlags(&down, cudaStreamNonBlocking));
+  for (uint32_t k = 0; k + 1 < nc; ++k) {
+    RMG_CUDA_TRY(cudaStreamCreateWithFlags(&pl.side[k], cudaStreamNonBlocking));
+    RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.side_done[k], cudaEventDisableTiming));
+  }
+  for (int k = 0; k < slots; ++k) {
+    RMG_CUDA_TRY(cudaEventCreateWithFlags(&uploaded[k], cudaEventDisableTiming));
+    RMG_CUDA_TRY(cudaEventCreateWithFlags(&computed[k], cudaEventDisableTiming));
+    RMG_CUDA_TRY(cudaEventCreateWithFlags(&released[k], cudaEventDisableTiming));
+  }
+  RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.ready, cudaEventDisableTiming));
+  RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.done, cudaEventDisableTiming));
+  cudaStream_t compute[kMaxCompute] = {st};
+  for (uint32_t k = 0; k + 1 < nc; ++k) compute[k + 1] = pl.side[k];
+
+  std::vector<size_t> offset(na);
+  size_t slot_bytes = 0;
+  for (size_t a = 0; a < na; ++a) {
+    offset[a] = slot_bytes;
+    slot_bytes += align256(chunk * arrays[a].per_pose);
+  }
+  char* stg = nullptr;
+  RMG_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&stg), std::max<size_t>(256, slots * slot_bytes), pool,
+                                       st));
+  s = cuda_status(cudaEventRecord(pl.ready, st), what);
+  if (s == RMG_OK) s = cuda_status(cudaStreamWaitEvent(pl.copy, pl.ready, 0), what);
+  if (s == RMG_OK) s = cuda_status(cudaStreamWaitEvent(down, pl.ready, 0), what);
+  for (uint32_t k = 0; s == RMG_OK && k + 1 < nc; ++k) s = cuda_status(cudaStreamWaitEvent(pl.side[k], pl.ready, 0), what);
+
+  std::vector<char*> dev(na);
+  auto place = [&](int slot) {
+    for (size_t a = 0; a < na; ++a) dev[a] = stg + (size_t)slot * slot_bytes + offset[a];
+  };
+  auto upload = [&](uint32_t k) -> int {
+    const int slot = (int)(k % slots);
+    const uint64_t p0 = (uint64_t)k * chunk, np = std::min<uint64_t>(chunk, n - p0);
+    place(slot);
+    if (k >= (uint32_t)slots) RMG_CUDA_TRY(cudaStreamWaitEvent(pl.copy, released[slot], 0));
+    for (size_t a = 0; a < na; ++a) {
+      if (!arrays[a].src) continue;
+      const size_t b = arrays[a].per_pose;
+      RMG_CUDA_TRY(cudaMemcpyAsync(dev[a], static_cast<const char*>(arrays[a].src) + p0 * b, np * b, cudaMemcpyDefault,
+                                   pl.copy));
+    }
+    RMG_CUDA_TRY(cudaEventRecord(uploaded[slot], pl.copy));
+    return RMG_OK;
+  };
+  auto run = [&](uint32_t k) -> int {
+    const int slot = (int)(k % slots);
+    const cudaStream_t cs = compute[k % nc];
+    const uint32_t p0 = (uint32_t)(k * chunk), np = (uint32_t)std::min<size_t>(chunk, n - p0);
+    place(slot);
+    RMG_CUDA_TRY(cudaStreamWaitEvent(cs, uploaded[slot], 0));
+    const int r = launch(p0, np, dev.data(), cs);
+    if (r != RMG_OK) return r;
+    RMG_CUDA_TRY(cudaEventRecord(computed[slot], cs));
+    return RMG_OK;
+  };
+  auto download = [&](uint32_t k) -> int {
+    const int slot = (int)(k % slots);
+    const uint64_t p0 = (uint64_t)k * chunk, np = std::min<uint64_t>(chunk, n - p0);
+    place(slot);
+    RMG_CUDA_TRY(cudaStreamWaitEvent(down, computed[slot], 0));
+    for (size_t a = 0; a < na; ++a) {
+      if (!arrays[a].dst) continue;
+      const size_t b = arrays[a].per_pose;
+      RMG_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(arrays[a].dst) + p0 * b, dev[a], np * b, cudaMemcpyDefault, down));
+    }
+    RMG_CUDA_TRY(cudaEventRecord(released[slot], down));
+    return RMG_OK;
+  };
+  for (uint32_t k = 0; s == RMG_OK && k < n_chunks; ++k) {
+    s = upload(k);
+    if (s == RMG_OK) s = run(k);
+    if (s == RMG_OK && k > 0) s = download(k - 1);
+  }
+  if (s == RMG_OK) s = download(n_chunks - 1);
+  // join everything into the caller's stream, free in stream order
+  cudaEventRecord(pl.done, down);
+  cudaStreamWaitEvent(st, pl.done, 0);
+  cudaEventRecord(pl.done, pl.copy);
+  cudaStreamWaitEvent(st, pl.done, 0);
+  for (uint32_t k = 0; k + 1 < nc; ++k) {
+    cudaEventRecord(pl.side_done[k], pl.side[k]);
+    cudaStreamWaitEvent(st, pl.side_done[k], 0);
+  }
+  cudaFreeAsync(stg, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (s != RMG_OK) return s;
+  return cuda_status(e, what);
+}
+
 }  // namespace
 }  // namespace rmg
 
@@ -394,6 +530,33 @@ extern "C" int rmg_simulate_statistics_host(const rmg_map* map, const rmg_sensor
   if (!stats && !transforms) return RMG_OK;
   return statistics_pipeline(map, sensor, Tsb, Tbm, n_poses, *dataset, pre_transforms, pre_transform_stride ? 1u : 0u,
                              params, point_to_plane, stats, transforms, as_stream(stream));
+}
+
+extern "C" int rmg_range_pose_grad_host(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
+                                        const rmg_transform* Tbm, uint32_t n_poses, const float* ranges_obs,
+                                        float huber_delta, float* grad, float* loss, float* ranges_sim,
+                                        uint32_t* face_ids, void* stream) {
+  if (!map || !sensor || !Tsb)
+    return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad_host: NULL map, sensor or Tsb");
+  if (n_poses == 0) return RMG_OK;
+  if (!Tbm || !ranges_obs) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad_host: Tbm or ranges_obs NULL");
+  if (!grad && !loss) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad_host: grad and loss are both NULL");
+  const size_t rays = rays_of(sensor);
+  // device arrays of a chunk: Tbm, observed ranges (inputs); grad, loss, ranges, face ids (outputs)
+  const std::vector<HostArray> arrays = {
+      {Tbm, nullptr, sizeof(rmg_transform)}, {ranges_obs, nullptr, 4 * rays},
+      {nullptr, grad, grad ? 24 : 0}, {nullptr, loss, loss ? 4 : 0},
+      {nullptr, ranges_sim, ranges_sim ? 4 * rays : 0}, {nullptr, face_ids, face_ids ? 4 * rays : 0}};
+  return io_pipeline("rmg_range_pose_grad_host", n_poses, arrays, 65535,
+                     [&](uint32_t, uint32_t np, char* const* d, cudaStream_t cs) {
+                       return rmg_range_pose_grad(map, sensor, Tsb, reinterpret_cast<const rmg_transform*>(d[0]), np,
+                                                  reinterpret_cast<const float*>(d[1]), huber_delta,
+                                                  grad ? reinterpret_cast<float*>(d[2]) : nullptr,
+                                                  loss ? reinterpret_cast<float*>(d[3]) : nullptr,
+                                                  ranges_sim ? reinterpret_cast<float*>(d[4]) : nullptr,
+                                                  face_ids ? reinterpret_cast<uint32_t*>(d[5]) : nullptr, cs);
+                     },
+                     as_stream(stream));
 }
 
 extern "C" int rmg_host_set_pipeline(uint64_t chunk_bytes, uint32_t compute_streams) {

@@ -40,9 +40,9 @@ def perturb(Tbm: torch.Tensor, xi: torch.Tensor) -> torch.Tensor:
 def range_pose_grad(sim: _Simulator, Tbm: torch.Tensor, ranges_obs: torch.Tensor, delta: float = 0.2,
                     want_sim: bool = False):
     """Returns (grad [N,6], loss [N]) and, with want_sim, the simulated (ranges, face_ids), on the
-    device.  Observed ranges in host memory are uploaded in pose chunks on a copy stream while earlier
-    chunks are computed, the launches alternating between two compute streams (the result is the
-    same as one call on device data)."""
+    device.  Observed ranges in host memory go through rmg_range_pose_grad_host instead: uploads and
+    downloads in pose chunks overlap the launches, and the results come back in host memory (the
+    same values as one call on device data)."""
     sim._check_ready()
     if isinstance(ranges_obs, torch.Tensor) and not ranges_obs.is_cuda:
         return _range_pose_grad_host(sim, Tbm, ranges_obs, delta, want_sim)
@@ -64,41 +64,24 @@ def range_pose_grad(sim: _Simulator, Tbm: torch.Tensor, ranges_obs: torch.Tensor
     return grad, loss
 
 
-def _range_pose_grad_host(sim, Tbm, ranges_obs, delta, want_sim, chunks: int = 8):
-    Tbm_d = Tbm.reshape(-1, 8).to("cuda", non_blocking=True).contiguous()
-    n = Tbm_d.shape[0]
+def _range_pose_grad_host(sim, Tbm, ranges_obs, delta, want_sim):
+    """Observations in host memory: rmg_range_pose_grad_host uploads them in pose chunks and
+    downloads the results while other chunks are computed; the results come back in host memory
+    when the call returns."""
+    T = (Tbm if isinstance(Tbm, torch.Tensor) else torch.as_tensor(np.asarray(Tbm, np.float32)))
+    T = T.reshape(-1, 8).to(torch.float32).contiguous()
+    n = T.shape[0]
     W, H = sim.sensor.width, sim.sensor.height
-    per = W * H
-    obs_h = ranges_obs.reshape(-1)
-    if obs_h.dtype != torch.float32:
-        obs_h = obs_h.to(torch.float32)
-    if obs_h.numel() != n * per:
+    obs = torch.as_tensor(ranges_obs).reshape(-1).to(torch.float32).contiguous()
+    if obs.numel() != n * W * H:
         raise L.RmgError(L.RMG_ERR_INVALID_ARG, "range_pose_grad", "ranges_obs must hold n_poses*W*H values")
-    obs_d = torch.empty((n * per,), dtype=torch.float32, device="cuda")
-    grad = torch.empty((n, 6), dtype=torch.float32, device="cuda")
-    loss = torch.empty((n,), dtype=torch.float32, device="cuda")
-    rs = torch.empty((n * per,), dtype=torch.float32, device="cuda") if want_sim else None
-    fs = torch.empty((n * per,), dtype=torch.int32, device="cuda") if want_sim else None
-    if getattr(sim, "_copy_stream", None) is None:
-        sim._copy_stream = torch.cuda.Stream()
-    streams = sim._compute_streams()
-    copy = sim._copy_stream
-    copy.wait_stream(streams[0])
-    step = max(1, -(-n // chunks))
+    grad = torch.empty((n, 6), dtype=torch.float32)
+    loss = torch.empty((n,), dtype=torch.float32)
+    rs = torch.empty((n * W * H,), dtype=torch.float32) if want_sim else None
+    fs = torch.empty((n * W * H,), dtype=torch.int32) if want_sim else None
     p = lambda t: None if t is None else C.c_void_p(t.data_ptr())  # noqa: E731
-    for i, c0 in enumerate(range(0, n, step)):
-        c1 = min(n, c0 + step)
-        compute = streams[i % len(streams)]
-        with torch.cuda.stream(copy):
-            obs_d[c0 * per:c1 * per].copy_(obs_h[c0 * per:c1 * per], non_blocking=True)
-        ev = torch.cuda.Event()
-        ev.record(copy)
-        compute.wait_event(ev)
-        L.call("rmg_range_pose_grad", sim._map.handle, sim.sensor.handle, C.byref(sim._Tsb), p(Tbm_d[c0:c1]),
-               c1 - c0, p(obs_d[c0 * per:c1 * per]), float(delta), p(grad[c0:c1]), p(loss[c0:c1]),
-               None if rs is None else p(rs[c0 * per:c1 * per]), None if fs is None else p(fs[c0 * per:c1 * per]),
-               C.c_void_p(compute.cuda_stream))
-    sim._join_streams(streams)
+    L.call("rmg_range_pose_grad_host", sim._map.handle, sim.sensor.handle, C.byref(sim._Tsb), p(T), n, p(obs),
+           float(delta), p(grad), p(loss), p(rs), p(fs), C.c_void_p(torch.cuda.current_stream().cuda_stream))
     if want_sim:
         return grad, loss, rs, fs
     return grad, loss

@@ -121,8 +121,17 @@ def test_host_observations_give_the_device_result_bitwise(rm_mod):
         g1, l1, r1, f1 = rg.range_pose_grad(sim, torch.from_numpy(est[:n].copy()).pin_memory(), host, DELTA,
                                             want_sim=True)
         torch.cuda.synchronize()
+        assert not g1.is_cuda  # the host form returns host results
         for a, b in ((g0, g1), (l0, l1), (r0, r1), (f0, f1)):
-            assert torch.equal(a, b), n
+            assert torch.equal(a.cpu(), b), n
+        # pageable observations, device poses, one pose per chunk over three compute streams
+        from rmagine_gb300 import _lib
+        _lib.call("rmg_host_set_pipeline", 1, 3)
+        try:
+            g2, l2 = rg.range_pose_grad(sim, Td, obs[:n * per].cpu(), DELTA)
+            assert torch.equal(g0.cpu(), g2) and torch.equal(l0.cpu(), l2), n
+        finally:
+            _lib.call("rmg_host_set_pipeline", 0, 0)
     assert m.status() == 0
 
 
