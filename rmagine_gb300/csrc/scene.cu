@@ -125,11 +125,14 @@ __device__ __forceinline__ void trace_scene(const SceneParams& S, const V& o, co
     slab(rb, b.x, b.y, b.z, b.w, c.z, c.w, tminR, tmaxR);
     bool hitL = visit(tminL, tmaxL, best.t);
     bool hitR = visit(tminR, tmaxR, best.t);
-    if (hitL && ln.x < 0) { instance_hit(S, ~ln.x, o, d, best, over); hitL = false; }
-    if (hitR && ln.y < 0) { instance_hit(S, ~ln.y, o, d, best, over); hitR = false; }
-    if (over) break;
-    hitL = hitL && tminL <= best.t * kWiden;
-    hitR = hitR && tminR <= best.t * kWiden;
+    const bool leafL = hitL && ln.x < 0, leafR = hitR && ln.y < 0;
+    if (leafL || leafR) {  // only an instance walk can move the closest hit: re-cull on this path
+      if (leafL) instance_hit(S, ~ln.x, o, d, best, over);
+      if (leafR) instance_hit(S, ~ln.y, o, d, best, over);
+      if (over) break;
+      hitL = hitL && !leafL && tminL <= best.t * kWiden;
+      hitR = hitR && !leafR && tminR <= best.t * kWiden;
+    }
     if (hitL && hitR) {
       if (sp >= kFullStack) { over = true; break; }
       const bool lf = tminL <= tminR;
