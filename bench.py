@@ -908,12 +908,21 @@ def gpu_batched(args, world):
             setattr(hb, a, host_out[a][r0:r0 + nr])
         host_jobs.append(hb)
         r0 += nr
-    e2e_chunks = 16
-    cplan = batched.ChunkedBatchPlan(m, jobs, e2e_chunks, best)
+    # 16 ranges when the outputs are large (their copies then hide behind the casting); one plan and
+    # one copy per attribute of the whole contiguous output when they are small (the 1,024-sensor set:
+    # 3.9 MB, where per-job copies would cost more than they hide)
+    e2e_chunks = 16 if rays * 5 > (256 << 20) else 1
+    cplan = batched.ChunkedBatchPlan(m, jobs, e2e_chunks, best) if e2e_chunks > 1 else None
 
     def e2e_step():
         all_poses.copy_(host_poses, non_blocking=True)
-        cplan.run_to_host(host_jobs)
+        if cplan is not None:
+            cplan.run_to_host(host_jobs)
+        else:
+            plan.launch()
+            for a in attrs:
+                host_out[a].copy_(all_out[a], non_blocking=True)
+            torch.cuda.synchronize(dev)
 
     e2e_step()
     e2e_t = []
