@@ -57,7 +57,7 @@ WORK_PER_RAY = {
 # from one ncu capture of the workload (profiles/).
 TRAFFIC: dict = {
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
-    "terrain1m_spherical": 10 * (289994240 + 438243328),
+    "terrain1m_spherical": 10 * (292263680 + 442672640),
     "icp_stats_fwd": 6442640128 + 4728320,
     "icp_stats_bwd": 6444127744 + 6394882560,
     "pose_grad": 12633964800 + 681905664,
