@@ -64,7 +64,7 @@ TRAFFIC: dict = {
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
     "rcc_fused": 10 * (295375872 + 23611136),
     # full-size launch (131,072,000 ranges)
-    "noise": 524372992 + 463147776,
+    "noise": 524465664 + 463988224,
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
     "scene_terrain1m": 10 * (351828992 + 659708416),
 }

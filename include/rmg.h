@@ -460,6 +460,12 @@ typedef struct rmg_noise {
 } rmg_noise;
 
 int rmg_noise_apply(const rmg_noise* noise, float* ranges, uint64_t n, void* stream);
+/* Device error word of the noise kernels on the current device: 0, or
+ * RMG_ERR_TIMEOUT when a bulk copy into a kernel's shared-memory ring did not
+ * land within the kernel's wait limit (that chunk and the rest of its CTA's
+ * chunks were left unchanged).  Synchronises; `clear` != 0 resets it.  No
+ * counterpart in rmagine, whose noise kernels have no waits. */
+int rmg_noise_status(uint32_t* status, int clear);
 /* The generator itself (for tests): out[4*i .. 4*i+3] = Philox4x32-10 of
  * counter (i, call) and key seed, i < n_blocks; DEVICE out. */
 int rmg_noise_philox(const rmg_noise* noise, uint32_t* out, uint64_t n_blocks, void* stream);

@@ -198,6 +198,7 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_map_load": (C.c_int, [C.c_char_p, _P, C.POINTER(_P)]),
     "rmg_noise_apply": (C.c_int, [C.POINTER(NoiseC), _P, C.c_uint64, _P]),
     "rmg_noise_philox": (C.c_int, [C.POINTER(NoiseC), _P, C.c_uint64, _P]),
+    "rmg_noise_status": (C.c_int, [C.POINTER(C.c_uint32), C.c_int]),
     "rmg_scene_create": (C.c_int, [_P, _U32, _P, _U32, _P, C.POINTER(_P)]),
     "rmg_scene_update": (C.c_int, [_P, _P, _U32, C.c_int, _P]),
     "rmg_scene_destroy": (C.c_int, [_P]),

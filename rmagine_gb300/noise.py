@@ -55,6 +55,14 @@ class _Noise:
         return ranges
 
 
+def device_status(clear: bool = False) -> int:
+    """The noise kernels' device error word (0, or RMG_ERR_TIMEOUT after a lost bulk copy);
+    synchronises the device."""
+    v = C.c_uint32(0)
+    L.call("rmg_noise_status", C.byref(v), 1 if clear else 0)
+    return int(v.value)
+
+
 class GaussianNoise(_Noise):
     """GaussianNoiseCuda: r += N(0, 1) * stddev + mean for r <= max_range."""
     kind = L.RMG_NOISE_GAUSSIAN

@@ -128,3 +128,54 @@ def test_noise_is_deterministic_tail_safe_and_unaligned(built):
     n2.apply(c.clone())
     n2.apply(c)  # second call: different numbers
     assert not torch.equal(a, c)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["gaussian", "dust"])
+def test_bulk_copy_ring_equals_register_path(built, kind):
+    """A 16-byte aligned buffer streams through the bulk-copy (TMA) ring of k_noise_tma in chunks
+    of 4,096 ranges (the tail through k_noise); an unaligned view of the same values goes through
+    k_noise alone.  Both must give the same bits, over enough chunks that every CTA's ring wraps
+    several times, and the noise status word must stay clear."""
+    import torch
+
+    from rmagine_gb300 import noise
+
+    torch.cuda.set_device(0)
+    noise.device_status(clear=True)
+    n = 32 * 4096 * 1024 + 5
+    g = torch.Generator(device="cuda").manual_seed(11)
+    r = torch.rand(n, device="cuda", generator=g) * 120.0 + 0.5
+    aligned = r.clone()
+    assert aligned.data_ptr() % 16 == 0
+    base = torch.empty(n + 1, device="cuda")
+    base[1:] = r
+    view = base[1:]
+    assert view.data_ptr() % 16 != 0
+    opts = noise.NoiseOptions(seed=77, max_range=100.0)
+    make = (lambda: noise.GaussianNoise(0.01, 0.03, opts)) if kind == "gaussian" else \
+        (lambda: noise.UniformDustNoise(0.01, 0.9, opts))
+    make().apply(aligned)
+    make().apply(view)
+    torch.cuda.synchronize()
+    assert torch.equal(aligned.view(torch.int32), view.view(torch.int32))
+    assert not torch.equal(aligned, r)
+    assert noise.device_status() == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [4096, 3 * 4096, 4096 * 997, 4096 * 997 + 4, 4096 * 997 + 4095])
+def test_chunk_boundaries_match_the_oracle(built, n):
+    """Sizes at and around whole chunks of the bulk-copy ring, against the oracle."""
+    import torch
+
+    from rmagine_gb300 import noise
+
+    torch.cuda.set_device(0)
+    r = _ranges(n, seed=n % 1000)
+    t = torch.from_numpy(r).cuda()
+    noise.GaussianNoise(0.0, 0.05, noise.NoiseOptions(seed=4, max_range=100.0)).apply(t)
+    got = t.cpu().numpy().astype(np.float64)
+    want = on.apply(0, r, seed=4, call=0, mean=0.0, stddev=0.05, max_range=100.0)
+    assert np.abs(got - want).max() <= 4e-6 * (1.0 + np.abs(want).max())
+    assert noise.device_status() == 0
