@@ -507,7 +507,9 @@ typedef struct rmg_instance_desc {
 /* geometries: HOST array of n_geometries map handles (each built with
  * rmg_map_build, tree depth <= 32, alive as long as the scene);
  * instances: HOST array.  Builds the top-level tree on `stream` and
- * synchronises with it.  n_instances == 0 gives a scene where every ray misses. */
+ * synchronises with it.  n_instances == 0 gives a scene where every ray misses.
+ * The tree of a geometry of 32,768 triangles or more is opened into pieces
+ * that enter the top-level tree separately (same results, faster walks). */
 int rmg_scene_create(const rmg_map* const* geometries, uint32_t n_geometries,
                      const rmg_instance_desc* instances, uint32_t n_instances, void* stream, rmg_scene** out);
 /* New instance poses, scales or ids (same count).  rebuild == 0 refits the

@@ -10,15 +10,27 @@
 // is the box centre -- so rmg_map_refit of that tree is the dynamic-scene
 // update.  Leaf k of the top tree is the k-th live instance (face id k).
 //
+// Partial re-braiding (Benthin, Woop, Wald, Afra, "Improved Two-Level BVHs
+// using Partial Re-Braiding", HPG 2017): the tree of a large geometry (at
+// least 2 x RMG_SCENE_PIECE_TRIS triangles) is opened at scene creation into
+// pieces -- subtrees of about RMG_SCENE_PIECE_TRIS triangles, found by opening
+// the piece with the largest box first -- and every instance of it enters the
+// top tree once per piece, with that piece's box in the map frame.  A top-level
+// leaf is then (instance, start node): a ray enters only the pieces of a big
+// mesh that lie along it, and the top tree sorts them among the small
+// instances as a single tree of the baked geometry would.  Every triangle lies
+// under exactly one piece and the ray transform does not depend on the piece,
+// so the hits and the result are those of the unopened tree.
+//
 // Traversal (k_trace_scene): the top tree is walked with a full stack; at an
 // instance leaf the ray is taken into the instance's mesh frame,
 //     o_l = s^-1 (.) R^T (o - t),   d_l = s^-1 (.) R^T d   (R^T as conj(q) sandwich),
 // which keeps the ray parameter t, and the geometry's tree is walked by the
-// plain kernel's RayTrav with tfar = the best range so far.  A hit replaces
-// the best when its range is smaller, or equal with a smaller instance index;
-// within one mesh equal ranges already go to the smaller face index, so the
-// result is the lexicographic minimum (t, instance, face) over all hits,
-// independent of the visiting order.  Both trees must be at most 32 levels deep
+// plain kernel's RayTrav from the leaf's start node with tfar = the best range
+// so far.  A hit replaces the best when its range is smaller, or equal with a
+// smaller instance index, or equal in both with a smaller face index (two
+// pieces of one instance), so the result is the lexicographic minimum
+// (t, instance, face) over all hits, independent of the visiting order.  Both trees must be at most 32 levels deep
 // (checked at creation; the stack guards turn a corrupt tree into
 // RMG_ERR_TRAVERSAL_BUDGET in the scene's status word).
 #include <cmath>
@@ -52,6 +64,7 @@ struct SceneParams {
   TraceParams T;  // T.map: the top-level tree, status = the scene's word
   const InstDev* inst;
   const GeomDev* geoms;
+  const uint2* leaves;  // top-level leaf -> (instance record, start node in its geometry's tree)
 };
 
 struct Best {
@@ -64,7 +77,8 @@ struct Best {
 
 __device__ __forceinline__ void instance_hit(const SceneParams& S, int k, const V& o, const V& d, Best& best,
                                              bool& over) {
-  const uint32_t slot = __float_as_uint(__ldg(&S.T.map.tris[k].v0.w));
+  const uint2 leaf = __ldg(&S.leaves[__float_as_uint(__ldg(&S.T.map.tris[k].v0.w))]);
+  const uint32_t slot = leaf.x;
   const InstDev* ip = S.inst + slot;
   const float4 qi = __ldg(&ip->qinv), tt = __ldg(&ip->t), is = __ldg(&ip->inv_s);
   const uint4 ids = __ldg(&ip->ids);
@@ -77,7 +91,7 @@ __device__ __forceinline__ void instance_hit(const SceneParams& S, int k, const 
   DeviceMap bm;
   bm.nodes = reinterpret_cast<const Node*>(__ldg(reinterpret_cast<const unsigned long long*>(&gp->nodes)));
   bm.tris = reinterpret_cast<const Tri*>(__ldg(reinterpret_cast<const unsigned long long*>(&gp->tris)));
-  bm.root = __ldg(&gp->root);
+  bm.root = (int)leaf.y;
   bm.n_nodes = 0;
   bm.n_tris = 0;
   bm.status = S.T.map.status;
@@ -89,7 +103,9 @@ __device__ __forceinline__ void instance_hit(const SceneParams& S, int k, const 
   }
   if (r.over) { over = true; return; }
   if (r.h.tri < 0) return;
-  if (r.h.t < best.t || best.inst < 0 || ids.w < best.order) {
+  // r.h.t <= best.t here (the walk's tfar); at equal range the smaller instance,
+  // then the smaller face (another piece of the same instance) wins
+  if (r.h.t < best.t || best.inst < 0 || ids.w < best.order || (ids.w == best.order && r.h.face < best.face)) {
     best.t = r.h.t;
     best.tri = r.h.tri;
     best.face = r.h.face;
@@ -237,6 +253,27 @@ __global__ void __launch_bounds__(256, RMG_SCENE_MIN_BLOCKS) k_trace_scene(const
   }
 }
 
+// Request of k_piece_boxes: the box of one piece, read from its parent node.
+struct PieceReq {
+  const Node* nodes;
+  int parent, side;
+};
+
+// Current boxes of the pieces (after any refit of their geometries).
+__global__ void k_piece_boxes(const PieceReq* req, uint32_t n, float* out) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const PieceReq q = req[i];
+  const Node* p = q.nodes + q.parent;
+  const float4 a = p->a, b = p->b, c = p->c;
+  float* o = out + 6 * (size_t)i;
+  if (q.side == 0) {
+    o[0] = a.x; o[1] = a.z; o[2] = c.x; o[3] = a.y; o[4] = a.w; o[5] = c.y;
+  } else {
+    o[0] = b.x; o[1] = b.z; o[2] = c.z; o[3] = b.y; o[4] = b.w; o[5] = c.w;
+  }
+}
+
 }  // namespace
 
 int default_config(const rmg_sensor* s, rmg_launch_config* cfg);
@@ -249,14 +286,27 @@ DeviceMap device_view(const rmg_map* m);
 
 using namespace rmg;
 
+// A piece of an opened geometry tree: subtree root `node`, the box of which
+// sits in child slot `side` of node `parent`.
+struct ScenePiece {
+  int node, parent, side;
+};
+
 struct rmg_scene {
   int device = 0;
   std::vector<const rmg_map*> geoms;
+  std::vector<std::vector<ScenePiece>> pieces;  // per geometry; empty = not opened
+  std::vector<uint32_t> piece_base;             // per geometry: first request in d_piece_req
+  uint32_t n_pieces = 0;
   uint32_t n_instances = 0;
-  std::vector<uint32_t> live;   // instance index of each top-level leaf
+  std::vector<uint32_t> live;   // instance index of each live instance record
+  uint32_t n_leaves = 0;        // top-level leaves: (instance, piece) pairs
   rmg_map* tlas = nullptr;      // NULL when no instance is live
   InstDev* d_inst = nullptr;
+  uint2* d_leaves = nullptr;
   GeomDev* d_geoms = nullptr;
+  PieceReq* d_piece_req = nullptr;
+  float* d_piece_box = nullptr;  // 6 per piece: lo, hi
   unsigned int* d_status = nullptr;
 };
 
@@ -265,10 +315,64 @@ namespace {
 void free_scene(rmg_scene* s) {
   if (s->tlas) rmg_map_destroy(s->tlas);
   cudaFree(s->d_inst);
+  cudaFree(s->d_leaves);
   cudaFree(s->d_geoms);
+  cudaFree(s->d_piece_req);
+  cudaFree(s->d_piece_box);
   cudaFree(s->d_status);
   delete s;
 }
+
+// Triangles per piece of an opened geometry tree; 0 opens none.  Measured on
+// the 1M-triangle terrain under 2,000 box instances (the terrain cut into
+// K x K separate meshes as a stand-in): 3,864 Mrays/s unopened, 4,525 / 4,620 /
+// 4,613 / 4,548 for 16 / 64 / 256 / 1,024 pieces of 62k / 16k / 4k / 1k.
+#ifndef RMG_SCENE_PIECE_TRIS
+#define RMG_SCENE_PIECE_TRIS 16384
+#endif
+constexpr uint32_t kMaxPieces = 256;
+
+double box_area(const float lo[3], const float hi[3]) {
+  const double dx = (double)hi[0] - lo[0], dy = (double)hi[1] - lo[1], dz = (double)hi[2] - lo[2];
+  return dx * dy + dy * dz + dz * dx;
+}
+
+// Opens the tree of a geometry with at least 2 x RMG_SCENE_PIECE_TRIS
+// triangles into about n_faces / RMG_SCENE_PIECE_TRIS pieces (at most
+// kMaxPieces): the piece with the largest box surface is replaced by its two
+// children until there are enough, or until every piece has a leaf child.
+int open_geometry(const rmg_map* g, cudaStream_t st, std::vector<ScenePiece>& out) {
+  out.clear();
+  const uint32_t per = RMG_SCENE_PIECE_TRIS;
+  if (per == 0 || g->n_faces < 2u * per) return RMG_OK;
+  const uint32_t want = std::min<uint32_t>(kMaxPieces, g->n_faces / per);
+  struct Cand {
+    ScenePiece p;
+    float lo[3], hi[3];
+    bool closed;  // has a leaf child: stays whole
+  };
+  std::vector<Cand> c;
+  c.push_back(Cand{ScenePiece{0, -1, 0}, {g->lo[0], g->lo[1], g->lo[2]}, {g->hi[0], g->hi[1], g->hi[2]}, false});
+  RMG_CUDA_TRY(cudaStreamSynchronize(st));
+  while (c.size() < want) {
+    int pick = -1;
+    double area = -1.0;
+    for (size_t i = 0; i < c.size(); ++i)
+      if (!c[i].closed && box_area(c[i].lo, c[i].hi) > area) { area = box_area(c[i].lo, c[i].hi); pick = (int)i; }
+    if (pick < 0) break;
+    Node nd;
+    RMG_CUDA_TRY(cudaMemcpyAsync(&nd, g->d_nodes + c[pick].p.node, sizeof nd, cudaMemcpyDeviceToHost, st));
+    RMG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (nd.d.x < 0 || nd.d.y < 0) { c[pick].closed = true; continue; }
+    const int parent = c[pick].p.node;
+    c[pick] = Cand{ScenePiece{nd.d.x, parent, 0}, {nd.a.x, nd.a.z, nd.c.x}, {nd.a.y, nd.a.w, nd.c.y}, false};
+    c.push_back(Cand{ScenePiece{nd.d.y, parent, 1}, {nd.b.x, nd.b.z, nd.c.z}, {nd.b.y, nd.b.w, nd.c.w}, false});
+  }
+  if (c.size() < 2) return RMG_OK;
+  for (const Cand& x : c) out.push_back(x.p);
+  return RMG_OK;
+}
+
 
 // q (x) p (x) conj(q) in binary64 with the binary32 q as given.
 void qrot_d(const rmg_quat& q, const double p[3], double out[3]) {
@@ -302,49 +406,80 @@ int check_instances(const rmg_scene* s, const rmg_instance_desc* inst, uint32_t 
   return RMG_OK;
 }
 
-// Map-frame box of every live instance as the top-level "triangles"
-// (lo, hi, centre), padded by 1e-5 of the coordinates' magnitude so that the
-// binary32 ray transform of a hit near the mesh's bounds can never fall outside.
-void instance_boxes(const rmg_scene* s, const rmg_instance_desc* inst, uint32_t n, std::vector<uint32_t>& live,
-                    std::vector<rmg_vec3>& verts, std::vector<rmg_face>& faces, std::vector<InstDev>& rec) {
+// Map-frame box of a mesh-frame box [lo, hi] under an instance, padded by 1e-5
+// of the coordinates' magnitude so that the binary32 ray transform of a hit
+// near the box's faces can never fall outside: the top-level "triangle"
+// (lo, hi, centre).
+void world_box(const rmg_instance_desc& I, const float lo_m[3], const float hi_m[3], std::vector<rmg_vec3>& verts,
+               std::vector<rmg_face>& faces) {
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  double mag = 1.0;
+  for (int c = 0; c < 8; ++c) {
+    const double p[3] = {(double)I.scale.x * ((c & 1) ? hi_m[0] : lo_m[0]),
+                         (double)I.scale.y * ((c & 2) ? hi_m[1] : lo_m[1]),
+                         (double)I.scale.z * ((c & 4) ? hi_m[2] : lo_m[2])};
+    double w[3];
+    qrot_d(I.T.R, p, w);
+    w[0] += I.T.t.x; w[1] += I.T.t.y; w[2] += I.T.t.z;
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = std::min(lo[k], w[k]);
+      hi[k] = std::max(hi[k], w[k]);
+      mag = std::max(mag, std::fabs(w[k]));
+    }
+  }
+  const double pad = 1e-5 * mag;
+  rmg_vec3 vlo, vhi, vc;
+  float* fl = &vlo.x;
+  float* fh = &vhi.x;
+  float* fc = &vc.x;
+  for (int k = 0; k < 3; ++k) {
+    fl[k] = std::nextafter((float)(lo[k] - pad), -INFINITY);
+    fh[k] = std::nextafter((float)(hi[k] + pad), INFINITY);
+    fc[k] = (float)(0.5 * ((double)fl[k] + (double)fh[k]));
+  }
+  const uint32_t b = (uint32_t)verts.size();
+  verts.push_back(vlo);
+  verts.push_back(vhi);
+  verts.push_back(vc);
+  faces.push_back(rmg_face{b, b + 1, b + 2});
+}
+
+// The top-level leaves: one per (live instance, piece of its geometry's tree),
+// or per live instance where the tree is not opened, with their boxes, and the
+// record of every live instance.
+int instance_leaves(const rmg_scene* s, const rmg_instance_desc* inst, uint32_t n, cudaStream_t st,
+                    std::vector<uint32_t>& live, std::vector<rmg_vec3>& verts, std::vector<rmg_face>& faces,
+                    std::vector<InstDev>& rec, std::vector<uint2>& leaves) {
   live.clear();
   verts.clear();
   faces.clear();
   rec.clear();
+  leaves.clear();
+  std::vector<float> pbox;
+  if (s->n_pieces > 0) {
+    const unsigned grid = (s->n_pieces + 127) / 128;
+    k_piece_boxes<<<grid, 128, 0, st>>>(s->d_piece_req, s->n_pieces, s->d_piece_box);
+    RMG_CUDA_TRY(cudaGetLastError());
+    pbox.resize(6 * (size_t)s->n_pieces);
+    RMG_CUDA_TRY(cudaMemcpyAsync(pbox.data(), s->d_piece_box, sizeof(float) * pbox.size(), cudaMemcpyDeviceToHost, st));
+    RMG_CUDA_TRY(cudaStreamSynchronize(st));
+  }
   for (uint32_t i = 0; i < n; ++i) {
     const rmg_instance_desc& I = inst[i];
     const rmg_map* g = s->geoms[I.geometry];
     if (g->n_faces == 0) continue;
-    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    double mag = 1.0;
-    for (int c = 0; c < 8; ++c) {
-      const double p[3] = {(double)I.scale.x * ((c & 1) ? g->hi[0] : g->lo[0]),
-                           (double)I.scale.y * ((c & 2) ? g->hi[1] : g->lo[1]),
-                           (double)I.scale.z * ((c & 4) ? g->hi[2] : g->lo[2])};
-      double w[3];
-      qrot_d(I.T.R, p, w);
-      w[0] += I.T.t.x; w[1] += I.T.t.y; w[2] += I.T.t.z;
-      for (int k = 0; k < 3; ++k) {
-        lo[k] = std::min(lo[k], w[k]);
-        hi[k] = std::max(hi[k], w[k]);
-        mag = std::max(mag, std::fabs(w[k]));
+    const uint32_t slot = (uint32_t)rec.size();
+    const std::vector<ScenePiece>& pc = s->pieces[I.geometry];
+    if (pc.empty()) {
+      world_box(I, g->lo, g->hi, verts, faces);
+      leaves.push_back(make_uint2(slot, 0u));
+    } else {
+      for (size_t j = 0; j < pc.size(); ++j) {
+        const float* b = &pbox[6 * ((size_t)s->piece_base[I.geometry] + j)];
+        world_box(I, b, b + 3, verts, faces);
+        leaves.push_back(make_uint2(slot, (uint32_t)pc[j].node));
       }
     }
-    const double pad = 1e-5 * mag;
-    rmg_vec3 vlo, vhi, vc;
-    float* fl = &vlo.x;
-    float* fh = &vhi.x;
-    float* fc = &vc.x;
-    for (int k = 0; k < 3; ++k) {
-      fl[k] = std::nextafter((float)(lo[k] - pad), -INFINITY);
-      fh[k] = std::nextafter((float)(hi[k] + pad), INFINITY);
-      fc[k] = (float)(0.5 * ((double)fl[k] + (double)fh[k]));
-    }
-    const uint32_t b = (uint32_t)verts.size();
-    verts.push_back(vlo);
-    verts.push_back(vhi);
-    verts.push_back(vc);
-    faces.push_back(rmg_face{b, b + 1, b + 2});
     InstDev r;
     r.qinv = make_float4(-I.T.R.x, -I.T.R.y, -I.T.R.z, I.T.R.w);
     r.t = make_float4(I.T.t.x, I.T.t.y, I.T.t.z, 0.0f);
@@ -354,15 +489,21 @@ void instance_boxes(const rmg_scene* s, const rmg_instance_desc* inst, uint32_t 
     rec.push_back(r);
     live.push_back(i);
   }
+  return RMG_OK;
 }
 
-int upload_instances(rmg_scene* s, const std::vector<InstDev>& rec, cudaStream_t st) {
+int upload_instances(rmg_scene* s, const std::vector<InstDev>& rec, const std::vector<uint2>& leaves,
+                     cudaStream_t st) {
   cudaFree(s->d_inst);
   s->d_inst = nullptr;
+  cudaFree(s->d_leaves);
+  s->d_leaves = nullptr;
   if (rec.empty()) return RMG_OK;
   int r = dev_alloc(&s->d_inst, rec.size(), "scene instances");
+  if (r == RMG_OK) r = dev_alloc(&s->d_leaves, leaves.size(), "scene leaves");
   if (r != RMG_OK) return r;
   RMG_CUDA_TRY(cudaMemcpyAsync(s->d_inst, rec.data(), sizeof(InstDev) * rec.size(), cudaMemcpyHostToDevice, st));
+  RMG_CUDA_TRY(cudaMemcpyAsync(s->d_leaves, leaves.data(), sizeof(uint2) * leaves.size(), cudaMemcpyHostToDevice, st));
   return RMG_OK;
 }
 
@@ -371,9 +512,10 @@ int build_top(rmg_scene* s, const rmg_instance_desc* inst, uint32_t n, bool rebu
   std::vector<rmg_vec3> verts;
   std::vector<rmg_face> faces;
   std::vector<InstDev> rec;
-  instance_boxes(s, inst, n, live, verts, faces, rec);
-  int r = RMG_OK;
-  const bool same = s->tlas && live.size() == s->live.size() && !live.empty();
+  std::vector<uint2> leaves;
+  int r = instance_leaves(s, inst, n, st, live, verts, faces, rec, leaves);
+  if (r != RMG_OK) return r;
+  const bool same = s->tlas && live.size() == s->live.size() && leaves.size() == s->n_leaves && !live.empty();
   if (!rebuild && same) {
     r = rmg_map_refit(s->tlas, verts.data(), (uint32_t)verts.size(), st);
   } else {
@@ -385,10 +527,11 @@ int build_top(rmg_scene* s, const rmg_instance_desc* inst, uint32_t n, bool rebu
     }
   }
   if (r != RMG_OK) return r;
-  r = upload_instances(s, rec, st);
+  r = upload_instances(s, rec, leaves, st);
   if (r != RMG_OK) return r;
   RMG_CUDA_TRY(cudaStreamSynchronize(st));
   s->live = live;
+  s->n_leaves = (uint32_t)leaves.size();
   s->n_instances = n;
   return RMG_OK;
 }
@@ -427,6 +570,33 @@ extern "C" int rmg_scene_create(const rmg_map* const* geometries, uint32_t n_geo
     if (r == RMG_OK)
       r = cuda_status(cudaMemcpyAsync(s->d_geoms, g.data(), sizeof(GeomDev) * n_geometries, cudaMemcpyHostToDevice, st),
                       "copy geometries");
+  }
+  // Open the trees of large geometries into pieces (only those some instance places).
+  s->pieces.assign(n_geometries, {});
+  s->piece_base.assign(n_geometries, 0);
+  std::vector<bool> used(n_geometries, false);
+  for (uint32_t i = 0; i < n_instances; ++i) used[instances[i].geometry] = true;
+  std::vector<PieceReq> req;
+  for (uint32_t gi = 0; r == RMG_OK && gi < n_geometries; ++gi) {
+    if (!used[gi]) continue;
+    r = open_geometry(geometries[gi], st, s->pieces[gi]);
+    s->piece_base[gi] = (uint32_t)req.size();
+    for (const ScenePiece& p : s->pieces[gi]) req.push_back(PieceReq{geometries[gi]->d_nodes, p.parent, p.side});
+  }
+  // Bound the top tree: with more than 2^22 leaves from opened trees, open none.
+  uint64_t n_leaves = 0;
+  for (uint32_t i = 0; i < n_instances; ++i) n_leaves += std::max<size_t>(1, s->pieces[instances[i].geometry].size());
+  if (n_leaves > (1ull << 22)) {
+    for (auto& pc : s->pieces) pc.clear();
+    req.clear();
+  }
+  s->n_pieces = (uint32_t)req.size();
+  if (r == RMG_OK && !req.empty()) {
+    r = dev_alloc(&s->d_piece_req, req.size(), "scene pieces");
+    if (r == RMG_OK) r = dev_alloc(&s->d_piece_box, 6 * req.size(), "scene piece boxes");
+    if (r == RMG_OK)
+      r = cuda_status(cudaMemcpyAsync(s->d_piece_req, req.data(), sizeof(PieceReq) * req.size(), cudaMemcpyHostToDevice,
+                                      st), "copy pieces");
   }
   if (r == RMG_OK) r = build_top(s, instances, n_instances, true, st);
   if (r != RMG_OK) { free_scene(s); return r; }
@@ -481,6 +651,7 @@ extern "C" int rmg_simulate_scene(const rmg_scene* s, const rmg_sensor* sensor, 
   S.T.map.status = s->d_status;
   S.inst = s->d_inst;
   S.geoms = s->d_geoms;
+  S.leaves = s->d_leaves;
   const uint64_t blocks = (S.T.n_tiles + cfg.block_warps - 1) / cfg.block_warps;
   if (blocks > 0x7fffffffull) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene: too many rays for one launch");
   const unsigned block = 32u * cfg.block_warps;

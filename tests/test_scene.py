@@ -304,3 +304,99 @@ def test_oracle_instanced_terrain_equals_the_baked_terrain():
     box_of_face = (b["face_ids"][on_box] - n_terrain) // 12
     agree = a["object_ids"][on_box] == 1 + box_of_face
     assert on_box.sum() > 20 and agree.mean() > 0.99
+
+
+# ---- opened trees (partial re-braiding) ----------------------------------------------------
+# A geometry of at least 2 x 16,384 triangles enters the top tree as pieces of its own tree; the
+# results must be those of the unopened tree: bit-equal to the single-mesh path for an identity
+# instance, and the oracle's (which tries every instance whole) under rotated, scaled instances.
+def _opened_terrain(grid=256, size=120.0, n_boxes=0, seed=21):
+    sc = scenes.terrain(grid=grid, size=size, n_boxes=n_boxes, seed=seed)
+    assert sc.faces.shape[0] >= 4 * 16384  # opened into several pieces
+    return sc
+
+
+@pytest.mark.gpu
+def test_opened_tree_identity_instance_equals_the_map_bitwise(built):
+    import torch
+
+    import rmagine_gb300 as rm
+
+    torch.cuda.set_device(0)
+    sc = _opened_terrain()
+    model = sensors.ouster_like(rows=32, cols=512)
+    poses = scenes.terrain_poses(sc, 6, seed=22, size=120.0)
+    scene = _gpu_scene([(sc.vertices, sc.faces)], [dict(geometry=0, T=IDENT, geom_id=2, object_id=5)])
+    a = _run(scene, model, poses)
+    b = _run(rm.Map(sc.vertices, sc.faces), model, poses)
+    hit = b["face_ids"] != 0xFFFFFFFF
+    assert hit.mean() > 0.5
+    for k in ("hits", "ranges", "points", "normals", "face_ids"):
+        assert np.array_equal(a[k], b[k], equal_nan=True), k
+    assert np.all(a["object_ids"][hit] == 5) and np.all(a["object_ids"][~hit] == 0xFFFFFFFF)
+    assert scene.status() == 0
+
+
+def _opened_scene_instances(sc):
+    cube_v, cube_f = scenes.gen_cube()
+    insts = [dict(geometry=0, T=pose(quat([0, 0, 1], 0.5), [3.0, -2.0, 0.5]), scale=np.array([1.0, 1.2, 0.8], np.float32),
+                  geom_id=0, object_id=1),
+             dict(geometry=0, T=pose(quat([0.2, 1, 0], 3.0), [0.0, 0.0, 14.0]), scale=np.array([0.5, 0.5, 0.5], np.float32),
+                  geom_id=0, object_id=2)]
+    rng = np.random.default_rng(23)
+    for i in range(40):
+        t = np.array([*rng.uniform(-40, 40, 2), rng.uniform(0.0, 6.0)], np.float32)
+        insts.append(dict(geometry=1, T=pose(quat(rng.standard_normal(3), rng.uniform(0, 6)), t),
+                          scale=rng.uniform(0.5, 3.0, 3).astype(np.float32), geom_id=1, object_id=10 + i))
+    return [(sc.vertices, sc.faces), (cube_v, cube_f)], insts
+
+
+@pytest.mark.gpu
+def test_opened_tree_under_rotated_scaled_instances_matches_the_oracle(built):
+    import torch
+
+    torch.cuda.set_device(0)
+    sc = _opened_terrain()
+    meshes, insts = _opened_scene_instances(sc)
+    scene = _gpu_scene(meshes, insts)
+    model = sensors.ouster_like(rows=32, cols=512)
+    poses = np.stack([pose(quat([0, 0, 1], a), [np.cos(a) * 20, np.sin(a) * 20, 8.0])
+                      for a in np.linspace(0, 2 * np.pi, 5, endpoint=False)])
+    got = _run(scene, model, poses)
+    osc = InstancedScene(meshes, insts)
+    want = osc.simulate(model, IDENT, poses)
+    assert got["hits"].mean() > 0.3
+    assert len(np.unique(got["object_ids"])) >= 10
+    rep = osc.certify(model, IDENT, poses, got, want)
+    _agree(got, {k: want[k] for k in got}, rep)
+    assert scene.status() == 0
+
+
+@pytest.mark.gpu
+def test_opened_tree_follows_a_geometry_refit(built):
+    """The pieces keep their nodes after a refit of the geometry; the scene update takes their new
+    boxes from the refitted tree."""
+    import torch
+
+    import rmagine_gb300 as rm
+
+    torch.cuda.set_device(0)
+    sc = _opened_terrain()
+    meshes, insts = _opened_scene_instances(sc)
+    geoms = [rm.Map(v, f) for v, f in meshes]
+    objs = [rm.Instance(i["geometry"], i["T"], i["scale"], i["geom_id"], i["object_id"]) for i in insts]
+    scene = rm.Scene(geoms, objs)
+    v2 = sc.vertices.copy()
+    v2[:, 2] = v2[:, 2] * np.float32(1.7) + np.float32(1.0)  # heights change: every piece's box moves
+    geoms[0].refit(v2)
+    scene.update(objs)
+    model = sensors.ouster_like(rows=32, cols=512)
+    poses = np.stack([pose(quat([0, 0, 1], a), [np.cos(a) * 15, np.sin(a) * 15, 20.0])
+                      for a in np.linspace(0, 2 * np.pi, 4, endpoint=False)])
+    got = _run(scene, model, poses)
+    meshes2 = [(v2, sc.faces), meshes[1]]
+    osc = InstancedScene(meshes2, insts)
+    want = osc.simulate(model, IDENT, poses)
+    assert got["hits"].mean() > 0.3
+    _agree(got, {k: want[k] for k in got}, osc.certify(model, IDENT, poses, got, want))
+    assert scene.status() == 0
