@@ -66,7 +66,7 @@ TRAFFIC: dict = {
     # full-size launch (131,072,000 ranges)
     "noise": 524465664 + 463988224,
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
-    "scene_terrain1m": 10 * (351828992 + 659708416),
+    "scene_terrain1m": 10 * (357533440 + 682603008),
 }
 
 RAYCAST = ("terrain1m_spherical", "terrain1m_pinhole", "terrain2m_spherical", "terrain33m_spherical", "room_vlp16")
