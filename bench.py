@@ -67,6 +67,9 @@ TRAFFIC: dict = {
     "noise": 524465664 + 463988224,
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
     "scene_terrain1m": 10 * (357533440 + 682603008),
+    # captured with every sensor cut to 16 poses (143,238,688 rays) and scaled by the ray count to the
+    # full 64-sensor launch (9,025,081,856 rays)
+    "batched": round(9025081856 / 143238688 * (1247344000 + 448487168)),
 }
 
 RAYCAST = ("terrain1m_spherical", "terrain1m_pinhole", "terrain2m_spherical", "terrain33m_spherical", "room_vlp16")
@@ -935,7 +938,7 @@ def gpu_batched(args, world):
     wk = WORK_PER_RAY.get("terrain2m_spherical")
     rl = roofline(5 + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
                   "per ray: Hits+Ranges 5 B + 64 B per node visit + 48 B per triangle test (work per ray of the "
-                  "2.1M-triangle terrain's spherical workload used as the estimate)", TRAFFIC.get("batched"))
+                  "2.1M-triangle terrain's spherical workload used as the estimate)", None if small else TRAFFIC.get("batched"))
     config = {"workload": ("batched small sensors: terrain 1024x1024 + 2000 boxes (2,117,058 tris), 1024 sensors "
                            "(O1Dn 256 dirs / pinhole 32x8, alternating), poses log-uniform [1,8], Hits+Ranges") if small
               else ("batched: terrain 1024x1024 + 2000 boxes (2,117,058 tris), 64 sensors from {VLP-16 16x900, "
