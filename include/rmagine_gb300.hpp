@@ -668,6 +668,13 @@ class NoiseGB300 {
     check(rmg_noise_apply(&p, ranges.raw(), ranges.size(), s), "rmg_noise_apply");
   }
 
+  // throws when a noise kernel on the current device recorded a lost bulk copy; synchronises
+  static void check_device(bool clear = true) {
+    uint32_t word = 0;
+    check(rmg_noise_status(&word, clear ? 1 : 0), "rmg_noise_status");
+    check((int)word, "noise kernel");
+  }
+
  protected:
   NoiseGB300(uint32_t kind, const NoiseOptions& o) {
     p_.kind = kind;

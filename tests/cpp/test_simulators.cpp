@@ -198,9 +198,10 @@ static void test_fused_step(const rm::MapPtr& map) {
   fail_if(std::memcmp(&t_h[0], &t[0], sizeof(rm::Transform)) != 0, "fused host form: transform");
 }
 
-// Noise: two objects with the same seed draw the same numbers; the next call differs.
+// Noise: two objects with the same seed draw the same numbers; the next call differs.  The size
+// takes both the bulk-copy ring (whole chunks of 4,096 ranges) and the register path (the tail).
 static void test_noise() {
-  rm::Memory<float, rm::RAM> r(1001);
+  rm::Memory<float, rm::RAM> r(3 * 4096 + 1001);
   for (size_t i = 0; i < r.size(); ++i) r[i] = 1.0f + 0.01f * (float)i;
   rm::Memory<float, rm::VRAM_CUDA> a, b;
   a = r;
@@ -221,6 +222,7 @@ static void test_noise() {
   rm::UniformDustNoiseGB300 dust(0.01f, 0.9f);
   dust.apply(b);
   rm::cuda_check(cudaDeviceSynchronize(), "sync");
+  rm::NoiseGB300::check_device();
 }
 
 // Mesh and map files round trip.
