@@ -247,8 +247,12 @@ def tree_count(export: dict, o, d, tfar: float, nthreads: int = 0):
     return visits, tests, t, f
 
 
-def certify(scene: Scene, model, Tsb, Tbm, got: dict, want: dict, band: float = 1e-6, tol: float = 1e-4):
+def certify(scene: Scene, model, Tsb, Tbm, got: dict, want: dict, band: float = 1e-6, tol: float = 1e-4,
+            gids=None):
     """Compares two simulation results ray by ray (hits, face ids, ranges).
+
+    `gids`, when given, holds the global ray id of every entry of the arrays (a
+    sample of a larger simulation); otherwise entry i is ray i.
 
     A ray is disputed when the hit flag or face id differ, or |dr| > tol.
     It is excused when binary64 re-intersection puts the relevant hit within
@@ -269,7 +273,8 @@ def certify(scene: Scene, model, Tsb, Tbm, got: dict, want: dict, band: float = 
     rep = {"rays": int(f_got.size), "disputed": int(idx.size), "excused": 0, "unexcused": 0, "examples": []}
     if idx.size == 0:
         return rep
-    o, d = scene.rays(model, Tsb, Tbm, idx.astype(np.uint64))
+    ray_ids = idx if gids is None else np.asarray(gids, np.uint64)[idx]
+    o, d = scene.rays(model, Tsb, Tbm, np.ascontiguousarray(ray_ids, np.uint64))
     for j, gid in enumerate(idx):
         reasons = []
         faces = {int(x) for x in (f_got[gid], f_want[gid]) if int(x) != 0xFFFFFFFF}
@@ -288,7 +293,7 @@ def certify(scene: Scene, model, Tsb, Tbm, got: dict, want: dict, band: float = 
         else:
             rep["unexcused"] += 1
             if len(rep["examples"]) < 10:
-                rep["examples"].append({"gid": int(gid), "face_got": int(f_got[gid]), "face_want": int(f_want[gid]),
+                rep["examples"].append({"gid": int(ray_ids[j]), "face_got": int(f_got[gid]), "face_want": int(f_want[gid]),
                                         "r_got": float(r_got[gid]), "r_want": float(r_want[gid]),
                                         "f64": {k: v for k, v in res.items()}})
     return rep
