@@ -118,3 +118,76 @@ def test_full_size_workload(name):
     for k in bench.ALL:
         assert torch.equal(getattr(hb, k).view(torch.uint8), getattr(ref, k).cpu().view(torch.uint8)), ("host", k)
     assert m.status() == 0
+
+
+def test_full_size_pose_gradient():
+    """4,096 poses of a 64 x 1024 sensor on the 2.1M-triangle terrain (268 M rays): the fused forward
+    equals plain simulate, each half of the poses gives the same rows, the host form gives the device
+    result, the true poses give zero loss and gradient, and four sampled poses match the binary64
+    analytic gradient of the oracle's ray set."""
+    from test_pose_grad import rayset
+
+    from rmagine_gb300 import grad as rg
+
+    sc, model, true, est = bench.posegrad_workload(4096)
+    W, H = oracle.model_size(model)
+    n = true.shape[0]
+    m = rm.Map(sc.vertices, sc.faces)
+    sim = rm.SphereSimulator(m)
+    sim.setModel(model)
+    obs = sim.simulate(torch.from_numpy(true).cuda(), attrs=("ranges",)).ranges
+    E = torch.from_numpy(est).cuda()
+    g, loss, rs, fs = rg.range_pose_grad(sim, E, obs, 0.2, want_sim=True)
+    plain = sim.simulate(E, attrs=("ranges", "face_ids"))
+    torch.cuda.synchronize()
+    assert torch.equal(plain.ranges, rs) and torch.equal(plain.face_ids, fs)
+    assert float(loss.sum()) > 0
+    half = n // 2
+    for lo, hi in ((0, half), (half, n)):
+        gh, lh = rg.range_pose_grad(sim, E[lo:hi], obs[lo * W * H:hi * W * H], 0.2)
+        assert torch.equal(gh, g[lo:hi]) and torch.equal(lh, loss[lo:hi])
+    gh, lh = rg.range_pose_grad(sim, torch.from_numpy(est).pin_memory(), obs.cpu().pin_memory(), 0.2)
+    assert torch.equal(gh, g.cpu()) and torch.equal(lh, loss.cpu())
+    g0, l0 = rg.range_pose_grad(sim, torch.from_numpy(true).cuda(), obs, 0.2)
+    assert float(g0.abs().max()) == 0.0 and float(l0.abs().max()) == 0.0
+    pick = np.array([0, 1234, 2900, 4095])
+    sl = np.concatenate([np.arange(p * W * H, (p + 1) * W * H) for p in pick])
+    rset, nn = rayset(sc, model, est[pick], fs.cpu().numpy().view(np.uint32)[sl], rs.cpu().numpy()[sl],
+                      obs.cpu().numpy()[sl])
+    an, an_loss = rset.analytic(nn, 0.2)
+    got = g.cpu().numpy()[pick]
+    assert np.abs(got - an).max() / np.abs(an).max() < 1e-3
+    assert m.status() == 0
+
+
+def test_full_size_fused_correction_step():
+    """The fused simulate -> statistics_p2l -> Umeyama step for 1,000 estimates on the 1M-triangle
+    terrain (131 M rays): each half of the estimates gives the same rows, the host form gives the
+    device result, and at the true poses the correction is the identity."""
+    from rmagine_gb300 import statistics as rs_
+
+    sc, model, true, est = bench.rcc_workload(1000)
+    W, H = oracle.model_size(model)
+    n = true.shape[0]
+    m = rm.Map(sc.vertices, sc.faces)
+    sim = rm.SphereSimulator(m)
+    sim.setModel(model)
+    data = sim.simulate(torch.from_numpy(true).cuda(), attrs=("hits", "points"))
+    dp, dm = data.points.reshape(n, W * H, 3), data.hits.reshape(n, W * H)
+    P = rs_.UmeyamaReductionConstraints(max_dist=0.5)
+    E = torch.from_numpy(est).cuda()
+    st, T = sim.simulate_statistics(E, dp, dataset_mask=dm, params=P)
+    torch.cuda.synchronize()
+    counts = rs_.decode_stats(st)["n"]
+    assert (counts > 0).mean() > 0.99 and counts.mean() > 1000, (int((counts == 0).sum()), float(counts.mean()))
+    half = n // 2
+    for lo, hi in ((0, half), (half, n)):
+        sh, Th = sim.simulate_statistics(E[lo:hi], dp[lo:hi], dataset_mask=dm[lo:hi], params=P)
+        assert torch.equal(sh, st[lo:hi]) and torch.equal(Th, T[lo:hi])
+    sh, Th = sim.simulate_statistics(torch.from_numpy(est), dp.cpu(), dataset_mask=dm.cpu(), params=P)
+    assert torch.equal(sh.cpu(), st.cpu()) and torch.equal(Th.cpu(), T.cpu())
+    _, T0 = sim.simulate_statistics(torch.from_numpy(true).cuda(), dp, dataset_mask=dm, params=P)
+    T0 = T0.cpu().numpy()
+    assert np.abs(T0[:, :3]).max() < 1e-5 and np.abs(np.abs(T0[:, 3]) - 1).max() < 1e-6
+    assert np.abs(T0[:, 4:7]).max() < 1e-4
+    assert m.status() == 0
