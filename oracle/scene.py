@@ -155,11 +155,12 @@ class InstancedScene:
             out["object_ids"] = oi[inst]
         return out
 
-    def certify(self, model, Tsb, Tbm, got: dict, want: dict, band: float = 1e-6, tol: float = 1e-4):
+    def certify(self, model, Tsb, Tbm, got: dict, want: dict, band: float = 1e-6, tol: float = 1e-4, gids=None):
         """Rays on which two results differ (hit, face, object id or |dr| > tol) are excused when a
         binary64 re-intersection of the involved (instance, face) pairs puts a hit within `band`
         barycentric of an edge, or two candidate hits tie within `band` relative.  got / want
-        must carry face_ids, ranges and object_ids (object ids unique per instance)."""
+        must carry face_ids, ranges and object_ids (object ids unique per instance).  `gids`, when
+        given, holds the global ray id of every entry (a sample of a larger simulation)."""
         f_got, f_want = got["face_ids"], want["face_ids"]
         bad = (f_got != f_want) | (got["object_ids"] != want["object_ids"]) | \
             (np.abs(got["ranges"].astype(np.float64) - want["ranges"].astype(np.float64)) > tol)
@@ -168,7 +169,8 @@ class InstancedScene:
         if idx.size == 0:
             return rep
         by_obj = {I["object_id"]: i for i, I in enumerate(self.instances)}
-        o, d = self._ray_scene.rays(model, Tsb, Tbm, idx.astype(np.uint64))
+        ray_ids = idx if gids is None else np.asarray(gids, np.uint64)[idx]
+        o, d = self._ray_scene.rays(model, Tsb, Tbm, np.ascontiguousarray(ray_ids, np.uint64))
         for j, gid in enumerate(idx):
             cands = []
             for res in (got, want):

@@ -191,3 +191,87 @@ def test_full_size_fused_correction_step():
     assert np.abs(T0[:, :3]).max() < 1e-5 and np.abs(np.abs(T0[:, 3]) - 1).max() < 1e-6
     assert np.abs(T0[:, 4:7]).max() < 1e-4
     assert m.status() == 0
+
+
+def test_full_size_batched_sensors():
+    """The 64-sensor mix of the batched benchmark (9.0 G rays on the 2.1M-triangle terrain,
+    Hits + Ranges): one batched launch gives every sensor the bytes of its own plain launch."""
+    from rmagine_gb300 import batched, scenes
+
+    sc = scenes.terrain(grid=1024, n_boxes=2000, seed=0)
+    m = rm.Map(sc.vertices, sc.faces)
+    spec = batched.mixed_sensor_set(64, seed=0)
+    attrs = ("hits", "ranges")
+    jobs, total = [], 0
+    for i, (mod, c) in enumerate(spec):
+        sim = rm.make_simulator(mod, m)
+        poses = torch.from_numpy(scenes.terrain_poses(sc, c, seed=100 + i)).cuda()
+        b = rm.resize_memory_bundle(rm.Bundle(*attrs), sim.sensor.width, sim.sensor.height, c, device="cuda")
+        jobs.append((sim, poses, b))
+        total += sim.sensor.width * sim.sensor.height * c
+    assert total > 8e9
+    plan = batched.BatchPlan(m, jobs)
+    plan.launch()
+    torch.cuda.synchronize()
+    for sim, poses, b in jobs:
+        p = sim.simulate(poses, attrs=attrs)
+        for a in attrs:
+            assert torch.equal(getattr(b, a).view(torch.uint8), getattr(p, a).view(torch.uint8)), a
+        del p
+    assert m.status() == 0
+
+
+def test_full_size_instanced_scene():
+    """The instanced benchmark scene (1M-triangle terrain with its tree opened into pieces + 2,000
+    box instances, 1,000 poses, 131 M rays, all seven attributes): two launches over the halves of the
+    poses give the bytes of one, the host form the device result, and a seeded sample of 20,000 rays
+    matches the scene oracle (which tries every instance whole)."""
+    from oracle.scene import InstancedScene
+    from rmagine_gb300 import scenes, sensors
+
+    meshes, insts, baked = scenes.instanced_terrain(grid=708, n_boxes=2000, seed=0)
+    model = sensors.ouster_like(128, 1024, 45.0, 0.5, 130.0)
+    poses = scenes.terrain_poses(baked, 1000, seed=2)
+    W, H = oracle.model_size(model)
+    n = poses.shape[0]
+    geoms = [rm.Map(v, f) for v, f in meshes]
+    scene = rm.Scene(geoms, [rm.Instance(i["geometry"], i["T"], i["scale"], i["geom_id"], i["object_id"])
+                             for i in insts])
+    sim = rm.make_simulator(model, scene)
+    A = rm.ATTRIBUTES
+    P = torch.from_numpy(poses).cuda()
+    ref = rm.resize_memory_bundle(rm.Bundle(*A), W, H, n, device="cuda")
+    sim.simulate(P, ref)
+    halves = rm.resize_memory_bundle(rm.Bundle(*A), W, H, n, device="cuda")
+    for lo, hi in ((0, n // 2), (n // 2, n)):
+        part = rm.Bundle(*A)
+        for k in A:
+            full = getattr(halves, k)
+            per = full.shape[0] // n
+            setattr(part, k, full[lo * per:hi * per])
+        sim.simulate(P[lo:hi], part)
+    torch.cuda.synchronize()
+    for k in A:
+        assert torch.equal(getattr(ref, k).view(torch.uint8), getattr(halves, k).view(torch.uint8)), k
+    del halves
+    hb = rm.resize_memory_bundle(rm.Bundle(*A), W, H, n, device="cpu", pin_memory=True)
+    sim.simulate(torch.from_numpy(poses), hb)
+    for k in A:
+        assert torch.equal(getattr(hb, k).view(torch.uint8), getattr(ref, k).cpu().view(torch.uint8)), ("host", k)
+    # oracle on a sample of rays: every instance tried whole, disputed rays certified in binary64
+    rng = np.random.default_rng(5)
+    gids = np.sort(rng.choice(n * W * H, 20000, replace=False)).astype(np.uint64)
+    osc = InstancedScene(meshes, insts)
+    o, d = osc._ray_scene.rays(model, IDENT, poses, gids)
+    t, inst, f = osc.trace(o, d, float(model.range.max))
+    rmin, rmax = np.float32(model.range.min), np.float32(model.range.max)
+    obj = np.array([I["object_id"] for I in osc.instances], np.uint32)
+    want = {"face_ids": f, "ranges": np.where(f != MISS, t, rmax + np.float32(1)).astype(np.float32),
+            "object_ids": np.where(inst >= 0, obj[np.maximum(inst, 0)], MISS).astype(np.uint32)}
+    idx = torch.from_numpy(gids.astype(np.int64)).cuda()
+    got = {"face_ids": ref.face_ids[idx].cpu().numpy().view(np.uint32), "ranges": ref.ranges[idx].cpu().numpy(),
+           "object_ids": ref.object_ids[idx].cpu().numpy().view(np.uint32)}
+    rep = osc.certify(model, IDENT, poses, got, want, gids=gids)
+    assert rep["unexcused"] == 0, rep
+    assert (got["face_ids"] != MISS).mean() > 0.2
+    assert scene.status() == 0
