@@ -275,3 +275,37 @@ def test_full_size_instanced_scene():
     assert rep["unexcused"] == 0, rep
     assert (got["face_ids"] != MISS).mean() > 0.2
     assert scene.status() == 0
+
+
+def test_full_size_icp_statistics():
+    """The ICP workload (8,192 batches x 32,768 correspondences, 6.4 GB of points): statistics,
+    Umeyama and the backward of each half of the batches give the rows of one call, and four sampled
+    batches match the binary64 two-pass statistics of the oracle."""
+    from oracle import stats as ost
+
+    from rmagine_gb300 import statistics as rs_
+
+    src, tgt = bench.icp_data(8192, 32768, torch.device("cuda", 0))
+    B = src.shape[0]
+    st, T = rs_.statistics(src, tgt)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(3)
+    gR = torch.randn((B, 9), generator=g, device="cuda")
+    gt = torch.randn((B, 3), generator=g, device="cuda")
+    gd, gm = rs_.umeyama_backward(src, tgt, st, gR, gt)
+    torch.cuda.synchronize()
+    h = B // 2
+    for lo, hi in ((0, h), (h, B)):
+        sh, Th = rs_.statistics(src[lo:hi], tgt[lo:hi])
+        assert torch.equal(sh, st[lo:hi]) and torch.equal(Th, T[lo:hi])
+        dh, mh = rs_.umeyama_backward(src[lo:hi], tgt[lo:hi], sh, gR[lo:hi], gt[lo:hi])
+        assert torch.equal(dh, gd[lo:hi]) and torch.equal(mh, gm[lo:hi])
+    pick = [0, 2047, 5000, 8191]
+    got = rs_.decode_stats(st[pick])
+    want = ost.stats(*ost.correspondences(src[pick].cpu().numpy(), tgt[pick].cpu().numpy()))
+    assert np.array_equal(got["n"], want["n"])
+    assert np.abs(got["dataset_mean"] - want["dataset_mean"]).max() <= 2e-5 * (1 + np.abs(want["dataset_mean"]).max())
+    assert np.abs(got["model_mean"] - want["model_mean"]).max() <= 2e-5 * (1 + np.abs(want["model_mean"]).max())
+    scale = np.abs(want["covariance"]).max(axis=(1, 2), keepdims=True)
+    assert (np.abs(got["covariance"] - want["covariance"]) / scale).max() <= 2e-6
+    assert bool(torch.isfinite(gd).all()) and bool(torch.isfinite(gm).all())
