@@ -383,6 +383,23 @@ int rmg_statistics_p2l(const rmg_transform* pre_transforms, uint32_t pre_transfo
  * optimization.cpp:51-55): DEVICE stats[n] -> DEVICE out[n]. */
 int rmg_umeyama_transform(const rmg_cross_stats* stats, uint32_t n, rmg_transform* out, void* stream);
 
+/* Batched 3x3 singular value decomposition A = U W V^T.  Replaces rmagine's
+ * svd(MemoryView<Matrix3x3,VRAM_CUDA> As, Us, Ws, Vs) and the ws-vector form
+ * (src/rmagine_cuda/include/rmagine/math/memory_math.cuh:561-578, kernels
+ * memory_math.cu:1564-1622) and the per-matrix svd (math/linalg.h:164-175,
+ * linalg.cpp:101, 645).  A, U, W, V: n column-major 3x3 float matrices
+ * (rmagine::Matrix3x3) in DEVICE memory; w: n Vector3 (the diagonal of W);
+ * any output may be NULL.  Computed in binary64 (Jacobi on A^T A), returned in
+ * binary32.  rotations == 0: the usual form, W >= 0 sorted descending, U and V
+ * orthogonal.  rotations != 0: U and V both
+ * rotations and the last singular value signed (sign det A), the form of the
+ * Kabsch/Umeyama step (R = U V^T).  Singular values are unique; U and V are
+ * unique only up to the usual sign and subspace freedom, so parity with
+ * rmagine's Numerical-Recipes svdcmp is on the reconstruction, the
+ * orthonormality and the singular values, as in its own tests
+ * (tests/core/math_svd.cpp:161-237, tests/cuda/math_svd.cpp:38-109). */
+int rmg_svd3(const float* A, float* U, float* W, float* w, float* V, uint32_t n, int rotations, void* stream);
+
 /* Backward of statistics_p2p + Umeyama (no counterpart in the reference):
  * given the forward's stats and upstream gradients grad_R (DEVICE, 9 floats
  * per batch, row-major dL/dR of the rotation matrix; NULL = 0) and grad_t
@@ -591,18 +608,19 @@ int rmg_transforms_compose(const rmg_transform* a, uint32_t a_stride, const rmg_
 /* ---------------------------------------------------------------------------
  * LBVH build without device allocation.
  * No counterpart in the reference: rmagine's maps always allocate their own
- * memory.  This is for callers that cannot call cudaMalloc -- code running
- * while a CUDA graph is being captured (an allocation would break the
- * capture), real-time loops that forbid allocator calls, hosts that give the
- * library one fixed device arena.  The caller passes the mesh in DEVICE
+ * memory.  This is for callers that cannot call cudaMalloc -- real-time loops
+ * that forbid allocator calls once they run, and hosts that hand the library
+ * one fixed device arena and own every other byte of device memory.  The
+ * caller passes the mesh in DEVICE
  * memory and receives the tree in its own DEVICE buffers, in the same record
  * layouts rmg_map_export returns; the build's temporary data (Morton keys,
  * sort buffers, bounds) lives in a fixed 4 MiB device array inside the
  * library, which limits the mesh to RMG_NOALLOC_MAX_FACES faces (larger
  * meshes return RMG_ERR_INVALID_ARG).  The first call on a device looks up
  * that array's address; make it before any stream capture.  Calls share the
- * array: calls that overlap on the GPU race.  Synchronises with `stream` once
- * (face-index check).
+ * array and it keeps the last call's contents (each call clears what must
+ * start at zero): calls that overlap on the GPU race.  Synchronises with
+ * `stream` once (face-index check).
  * ------------------------------------------------------------------------- */
 #define RMG_NOALLOC_MAX_FACES 65536u
 

@@ -812,11 +812,10 @@ extern "C" int rmg_map_debug_set_child(rmg_map* m, uint32_t node, uint32_t which
 // rmg_lbvh_build_noalloc: the LBVH build into caller-owned device memory,
 // with no device allocation.  No counterpart in the reference.
 //
-// Callers that cannot allocate device memory (code running while a CUDA graph
-// is being captured, real-time loops whose allocator calls are forbidden,
-// hosts that give the library one fixed device arena) still need temporary
-// space for the Morton keys, their sorted copy, the sort's own temporary
-// storage and the partial bounds.  That space is the file-scope array below:
+// Callers that cannot allocate device memory (real-time loops whose allocator
+// calls are forbidden, hosts that give the library one fixed device arena and
+// own every other byte) still need temporary space for the Morton keys, their
+// sorted copy, the sort's own temporary storage and the partial bounds.  That space is the file-scope array below:
 // kNoAllocScratchBytes bytes that every GPU which loads this library holds
 // until the process exits.  It bounds the mesh to RMG_NOALLOC_MAX_FACES.
 //
@@ -849,6 +848,30 @@ __global__ void k_check_faces(const uint32_t* f, uint32_t n_faces, uint32_t n_ve
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * n_faces) return;
   if (f[i] >= n_vertices) atomicExch(bad, 1u);
+}
+
+// The single-triangle tree of single_node(), on the device: the same min/max
+// order (std::min / std::max semantics), leaf 0 under no parent, cleared flag.
+__device__ __forceinline__ float min_like_std(float a, float b) { return b < a ? b : a; }
+__device__ __forceinline__ float max_like_std(float a, float b) { return a < b ? b : a; }
+
+__global__ void k_single_node(const float* v, const uint32_t* f, Node* node, uint32_t* leaf_order,
+                              int32_t* leaf_parent, uint32_t* flags) {
+  if (threadIdx.x != 0) return;
+  float lo[3], hi[3];
+  for (int k = 0; k < 3; ++k) {
+    const float a = v[3ull * f[0] + k], b = v[3ull * f[1] + k], c = v[3ull * f[2] + k];
+    lo[k] = min_like_std(min_like_std(a, b), c);
+    hi[k] = max_like_std(max_like_std(a, b), c);
+  }
+  const float far = 1e30f;
+  node->a = make_float4(lo[0], hi[0], lo[1], hi[1]);
+  node->b = make_float4(far, far, far, far);
+  node->c = make_float4(lo[2], hi[2], far, far);
+  node->d = make_int4(-1, -1, -1, 0);
+  leaf_order[0] = 0u;
+  leaf_parent[0] = -1;
+  flags[0] = 0u;
 }
 
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -927,24 +950,10 @@ extern "C" int rmg_lbvh_build_noalloc(const rmg_vec3* vertices, uint32_t n_verti
   RMG_CUDA_TRY(cudaStreamSynchronize(st));
   if (bad_h) return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: face index out of range");
 
-  if (n == 1) {
-    uint32_t fi[3];
-    RMG_CUDA_TRY(cudaMemcpy(fi, f, sizeof(fi), cudaMemcpyDeviceToHost));
-    float vv[9];
-    for (int k = 0; k < 3; ++k)
-      RMG_CUDA_TRY(cudaMemcpy(vv + 3 * k, v + 3ull * fi[k], 12, cudaMemcpyDeviceToHost));
-    const uint32_t local[3] = {0, 1, 2};
-    Node node;
-    single_node(vv, local, &node);
-    const uint32_t zero = 0;
-    const int minus1 = -1;
-    RMG_CUDA_TRY(cudaMemcpyAsync(nodes, &node, sizeof(Node), cudaMemcpyHostToDevice, st));
-    RMG_CUDA_TRY(cudaMemcpyAsync(out->leaf_order, &zero, 4, cudaMemcpyHostToDevice, st));
-    RMG_CUDA_TRY(cudaMemcpyAsync(out->leaf_parent, &minus1, 4, cudaMemcpyHostToDevice, st));
-    RMG_CUDA_TRY(cudaMemsetAsync(out->flags, 0, 4, st));
+  if (n == 1) {  // one node with a phantom far-away right child, built on `stream` like the rest
+    k_single_node<<<1, 32, 0, st>>>(v, f, nodes, out->leaf_order, out->leaf_parent, out->flags);
     k_pack<<<1, 32, 0, st>>>(v, f, out->leaf_order, 1, tris, nullptr);
     RMG_CUDA_TRY(cudaGetLastError());
-    RMG_CUDA_TRY(cudaStreamSynchronize(st));
     return RMG_OK;
   }
 

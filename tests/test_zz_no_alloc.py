@@ -1,9 +1,9 @@
 """rmg_lbvh_build_noalloc: the LBVH build for callers that cannot allocate device memory.
 
-Such callers (code running under CUDA graph capture, real-time loops that
-forbid allocator calls, hosts with one fixed device arena) pass the mesh and
-the output buffers in device memory; the build's temporary data lives in a
-fixed array inside the library.  Its trees must equal, bit for bit, the trees
+Such callers (real-time loops that forbid allocator calls once they run,
+hosts that hand the library one fixed device arena and own the rest) pass the
+mesh and the output buffers in device memory; the build's temporary data lives
+in a fixed array inside the library.  Its trees must equal, bit for bit, the trees
 of the allocating rmg_map_build -- on consecutive calls, since the calls
 share (and do not reset) that array.
 
@@ -26,8 +26,9 @@ def _built(built):
     torch.cuda.set_device(0)
 
 
-def build_noalloc(v: np.ndarray, f: np.ndarray):
-    """Calls the C entry point with torch-owned device buffers (the test plays the caller)."""
+def build_noalloc(v: np.ndarray, f: np.ndarray, stream=None):
+    """Calls the C entry point with torch-owned device buffers (the test plays the caller), on
+    `stream` (a torch.cuda.Stream) or torch's current stream."""
     n = f.shape[0]
     nn = max(n - 1, 1)
     vd = torch.from_numpy(np.ascontiguousarray(v, np.float32)).cuda()
@@ -39,9 +40,10 @@ def build_noalloc(v: np.ndarray, f: np.ndarray):
     flags = torch.full((nn,), 7, dtype=torch.int32, device="cuda")  # the call must clear these
     bufs = _lib.LbvhBuffersC(nodes.data_ptr(), tris.data_ptr(), order.data_ptr(), parent.data_ptr(),
                              flags.data_ptr())
-    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    s_ = stream or torch.cuda.current_stream()
+    s_.wait_stream(torch.cuda.current_stream())  # the buffers' fills come first
     st = _lib.load().rmg_lbvh_build_noalloc(C.c_void_p(vd.data_ptr()), v.shape[0], C.c_void_p(fd.data_ptr()), n,
-                                            C.byref(bufs), stream)
+                                            C.byref(bufs), C.c_void_p(s_.cuda_stream))
     torch.cuda.synchronize()
     nodes_h = nodes.cpu().numpy()
     return st, {"boxes": nodes_h[:, :12], "links": nodes_h.view(np.int32)[:, 12:], "tris": tris.cpu().numpy(),
@@ -91,3 +93,28 @@ def test_noalloc_rejects_out_of_range_face_indices():
     st, got = build_noalloc(v, f)
     assert st == _lib.RMG_OK
     assert same(got["links"], rm.Map(v, f, builder="lbvh").export()["links"])
+
+
+def heightfield(nx: int, ny: int, seed: int = 0):
+    """A (nx-1) x (ny-1) grid of quads, two triangles each, with random heights."""
+    rng = np.random.default_rng(seed)
+    xs, ys = np.meshgrid(np.arange(nx, dtype=np.float32), np.arange(ny, dtype=np.float32), indexing="xy")
+    v = np.stack([xs.ravel() * 0.5, ys.ravel() * 0.5, rng.uniform(0, 2, nx * ny).astype(np.float32)], 1)
+    i = np.arange(ny - 1)[:, None] * nx + np.arange(nx - 1)[None, :]
+    i = i.ravel().astype(np.uint32)
+    f = np.concatenate([np.stack([i, i + 1, i + nx], 1), np.stack([i + 1, i + nx + 1, i + nx], 1)])
+    return v.astype(np.float32), f.astype(np.uint32)
+
+
+def test_noalloc_at_the_face_limit_and_on_a_side_stream():
+    # 128 x 256 quads = exactly RMG_NOALLOC_MAX_FACES triangles: keys, values, bounds and the sort's
+    # temporary storage must all fit the fixed array
+    v, f = heightfield(129, 257)
+    assert f.shape[0] == _lib.RMG_NOALLOC_MAX_FACES
+    want = rm.Map(v, f, builder="lbvh").export()
+    side = torch.cuda.Stream()
+    for stream in (None, side, side):
+        st, got = build_noalloc(v, f, stream)
+        assert st == _lib.RMG_OK, _lib.load().rmg_last_error()
+        for k in ("leaf_order", "links", "boxes", "tris"):
+            assert same(got[k], want[k]), k
