@@ -57,10 +57,12 @@ WORK_PER_RAY = {
 # from one ncu capture of the workload (profiles/).
 TRAFFIC: dict = {
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
-    "terrain1m_spherical": 10 * (292263680 + 442672640),
-    "icp_stats_fwd": 6442640128 + 4728320,
-    "icp_stats_bwd": 6444127744 + 6394882560,
-    "pose_grad": 12633964800 + 681905664,
+    "terrain1m_spherical": 10 * (292245504 + 441846016),
+    # captured on 512 batches (16.8 M correspondences) and scaled by 16 to the 8,192-batch launch
+    "icp_stats_fwd": 16 * (402915328 + 3088384),
+    "icp_stats_bwd": 16 * (403369216 + 357416960),
+    # captured on 64 poses (4.19 M rays) and scaled by 64 to the 4,096-pose launch
+    "pose_grad": 64 * (226699264 + 14085632),
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
     "rcc_fused": 10 * (295375872 + 23611136),
     # full-size launch (131,072,000 ranges)
@@ -69,7 +71,18 @@ TRAFFIC: dict = {
     "scene_terrain1m": 10 * (357533440 + 682603008),
     # captured with every sensor cut to 16 poses (143,238,688 rays) and scaled by the ray count to the
     # full 64-sensor launch (9,025,081,856 rays)
-    "batched": round(9025081856 / 143238688 * (1247344000 + 448487168)),
+    "batched": round(9025081856 / 143238688 * (2200136960 + 877252864)),
+}
+
+# Warp instructions per unit (ray) of the dominant kernel, `smsp__inst_executed.sum` of one ncu
+# capture on the small case of the workload divided by its rays (profiles/), keyed by kernel walk.
+ISSUE: dict = {
+    "terrain1m_spherical/full_stack": {"warp_inst_per_unit": 1598561620 / 13107200, "source":
+                                       "profiles/k_trace_terrain1m_spherical.md (100 poses, 13,107,200 rays)"},
+    "pose_grad/k_range_grad": {"warp_inst_per_unit": 591522244 / 4194304, "source":
+                               "profiles/k_range_grad_terrain2m_posegrad.md (64 poses, 4,194,304 rays)"},
+    "batched/k_trace_batched": {"warp_inst_per_unit": 14765923075 / 143238688, "source":
+                                "profiles/k_trace_batched_mixed64.md (16 poses per sensor, 143,238,688 rays)"},
 }
 
 RAYCAST = ("terrain1m_spherical", "terrain1m_pinhole", "terrain2m_spherical", "terrain33m_spherical", "room_vlp16")
@@ -106,9 +119,7 @@ def raycast_workload(name: str):
 
 
 def model_size(model):
-    import oracle
-
-    return oracle.model_size(model)
+    return int(model.getWidth()), int(model.getHeight())
 
 
 # ---- clocks ------------------------------------------------------------------------------
@@ -170,6 +181,42 @@ def measured_hbm():
     return 6800.0, "fallback"
 
 
+def sm_count():
+    import ctypes as C
+
+    from rmagine_gb300 import _lib
+
+    n, a, b = C.c_int(0), C.c_int(0), C.c_int(0)
+    _lib.check(_lib.load().rmg_device_info(C.byref(n), C.byref(a), C.byref(b)), "rmg_device_info")
+    return int(n.value)
+
+
+def issue_roofline(kernel, units_per_launch, launch_s, clocks, traffic, note):
+    """The traversal kernels are bound by instruction issue (ALU pipe, divergence, dependent node
+    fetches), not by DRAM: `achieved` = warp instructions per ray (ncu, `ISSUE` below) x rays per
+    launch / the launch's CUDA-event time, `peak` = SMs x 4 schedulers x the SM clock sampled during
+    the timed region (one warp instruction per scheduler per cycle).  `hbm` beside it is the measured
+    DRAM traffic per launch over the same time against the measured copy peak."""
+    inst = ISSUE.get(kernel)
+    if inst is None:
+        return None
+    sms = sm_count()
+    mhz = (clocks or {}).get("sm_mhz") or float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["sm_max_mhz"]
+                                                if (ROOT / "MEASURED_PEAKS.json").exists() else 2070.0)
+    achieved = inst["warp_inst_per_unit"] * units_per_launch / launch_s / 1e9
+    peak = sms * 4 * mhz * 1e6 / 1e9
+    hbm_peak, kind = measured_hbm()
+    out = {"bound": "issue", "achieved": round(achieved, 1), "peak": round(peak, 1), "unit": "Gwarp-inst/s",
+           "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": "SMs x 4 x sampled SM clock",
+           "sm_count": sms, "sm_mhz": mhz, "warp_inst_per_unit": inst["warp_inst_per_unit"],
+           "inst_source": inst["source"], "units_per_launch": int(units_per_launch), "note": note}
+    if traffic:
+        hb = traffic / launch_s / 1e9
+        out["hbm"] = {"achieved": round(hb, 1), "peak": hbm_peak, "unit": "GB/s", "frac": round(hb / hbm_peak, 4),
+                      "peak_kind": kind}
+    return out
+
+
 def roofline(bytes_per_unit, units_per_launch, launch_s, note, traffic=None):
     peak, kind = measured_hbm()
     achieved = bytes_per_unit * units_per_launch / launch_s / 1e9
@@ -223,6 +270,29 @@ def barrier(world):
 
 
 # ---- ray casting -------------------------------------------------------------------------
+def raycast_config(desc, n_poses, rays, n_faces, world):
+    """The `config` of a ray-cast line; both arms print this same dict for the same workload."""
+    config = dict(desc)
+    config.update({"poses": int(n_poses), "rays_per_step": int(rays), "triangles": int(n_faces),
+                   "l2": "flushed between timed steps (256 MB write)",
+                   "parallelism": f"replicas{world}" if world > 1 else "single"})
+    return config
+
+
+def walk_name(cfg, depth):
+    """Which traversal the launch configuration selects on a tree of `depth` levels (the rules of
+    make_trace_params in csrc/simulate.cu)."""
+    if cfg.refill:
+        return "refill"
+    if cfg.bvh_width == 4:
+        return "wide4"
+    if cfg.packet == 1 and depth <= 32:
+        return "packet"
+    if cfg.stack_depth > 0 and depth <= 32:
+        return "full_stack"
+    return "trail"
+
+
 def cpu_raycast(sc, model, poses, attrs, target_s=15.0):
     """The oracle's OpenMP restatement of rmagine's Embree path on all host cores over a bounded
     pose sample (map build excluded, as in the reference's benchmark loop)."""
@@ -242,6 +312,34 @@ def cpu_raycast(sc, model, poses, attrs, target_s=15.0):
     return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": int(threads), "kind": "port",
             "sample": f"{n} of {len(poses)} poses ({rays} rays), all host threads, oracle SAH-BVH restatement "
                       f"of the Embree path (Embree itself is not buildable here)", "seconds": dt}
+
+
+def cpu_batched(sc, spec, pose_seed=100, target_s=10.0):
+    """The oracle's OpenMP ray cast over every sensor of a batched set, each with its first k poses
+    (k the same for all sensors, sized to about target_s): rays per second over the whole sample."""
+    import oracle
+    from rmagine_gb300 import scenes
+
+    ocs = oracle.Scene(sc.vertices, sc.faces)
+    threads = oracle.lib().orc_max_threads()
+    poses = [scenes.terrain_poses(sc, c, seed=pose_seed + i) for i, (_, c) in enumerate(spec)]
+
+    def run(k):
+        rays = 0
+        t0 = time.perf_counter()
+        for (mod, c), p in zip(spec, poses):
+            kk = min(k, c)
+            ocs.simulate(mod, IDENT, p[:kk], attrs=("hits", "ranges"), nthreads=threads)
+            W, H = model_size(mod)
+            rays += kk * W * H
+        return rays, time.perf_counter() - t0
+
+    r1, t1 = run(1)
+    k = int(max(1, min(64, target_s / max(t1, 1e-3))))
+    rays, dt = run(k)
+    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": int(threads), "kind": "port",
+            "sample": f"the first {k} poses of each of the {len(spec)} sensors ({rays} rays), all host threads, "
+                      f"oracle SAH-BVH restatement of the Embree path", "seconds": dt}
 
 
 def gpu_raycast(args, world):
@@ -293,21 +391,24 @@ def gpu_raycast(args, world):
     e2e = rays / float(np.median(e2e_t)) / 1e6
     out_b = sum(OUT_BYTES[a] for a in attrs)
     wk = WORK_PER_RAY.get(args.workload)
-    rl = None
-    if wk:
-        rl = roofline(out_b + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
+    walk = walk_name(tuned, int(m.info()["depth"]))
+    launch_s = total_ms / args.steps / 1e3
+    rl = issue_roofline(f"{args.workload}/{walk}", rays, launch_s, clocks, TRAFFIC.get(args.workload),
+                        f"{walk} walk of k_trace: issue-bound (ALU pipe, SIMD divergence, dependent node fetches); "
+                        f"DRAM carries the outputs and tree re-reads")
+    if rl is None and wk:
+        rl = roofline(out_b + 64 * wk["nodes"] + 48 * wk["tris"], rays, launch_s,
                       "algorithmic bytes per ray = outputs + 64 B per node visit + 48 B per triangle test, with the "
-                      "canonical LBVH's visit counts (the default SAH tree visits about 17% fewer nodes for the same "
-                      "rays); node and triangle fetches are served mostly from L1/L2, so this exceeds the HBM roof",
+                      "canonical LBVH's visit counts; node and triangle fetches are served mostly from L1/L2, so "
+                      "this exceeds the HBM roof (no instruction count is recorded for this walk)",
                       TRAFFIC.get(args.workload))
-    config = dict(desc)
-    config.update({"launch": {k: int(getattr(tuned, k)) for k, _ in tuned._fields_},
-                   "poses": int(n), "rays_per_step": int(rays), "triangles": int(sc.n_faces),
-                   "tree": {"builder": m.builder, "depth": int(m.info()["depth"]), "build_ms": round(build_ms, 1)},
-                   "l2": "flushed between timed steps (256 MB write)",
-                   "parallelism": f"replicas{world}" if world > 1 else "single"})
+    if rl is not None and wk:
+        rl["algorithmic_bytes_per_unit"] = round(out_b + 64 * wk["nodes"] + 48 * wk["tris"], 2)
+    config = raycast_config(desc, n, rays, sc.n_faces, world)
     line = {"metric": "Mrays/s", "unit": "Mrays/s", "value": round(value, 2), "ms_per_step": round(total_ms / args.steps, 3),
             "dtype": "f32", "config": config, "gpu_launches": args.steps,
+            "run": {"launch": {k: int(getattr(tuned, k)) for k, _ in tuned._fields_}, "walk": walk,
+                    "tree": {"builder": m.builder, "depth": int(m.info()["depth"]), "build_ms": round(build_ms, 1)}},
             "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": int(poses.nbytes),
                     "d2h_bytes_per_step": int(rays * out_b), "step_ms": [round(1e3 * x, 3) for x in e2e_t]},
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms],
@@ -640,7 +741,7 @@ def cpu_posegrad(sc, model, true, est, obs_h, target_s=10.0):
     t0 = time.perf_counter()
     run(n)
     dt = time.perf_counter() - t0
-    return {"value": n / dt, "unit": "pose-grad evals/s", "cores": int(threads), "kind": "port",
+    return {"value": n / dt, "unit": "poses/s", "cores": int(threads), "kind": "port",
             "sample": f"{n} of {len(est)} poses: oracle OpenMP ray cast + numpy binary64 adjoint", "seconds": dt}
 
 
@@ -680,7 +781,10 @@ def gpu_posegrad(args, world):
         e2e_t.append(time.perf_counter() - t0)
     e2e = n_poses / float(np.median(e2e_t))
     wk = WORK_PER_RAY["pose_grad"]
-    rl = roofline(4 + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
+    rl = issue_roofline("pose_grad/k_range_grad", rays, total_ms / args.steps / 1e3, clocks, TRAFFIC.get("pose_grad"),
+                        "k_range_grad (ray cast fused with the range adjoint and the per-pose reduction): "
+                        "issue-bound like k_trace")
+    rl = rl or roofline(4 + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
                   "per ray: observed range 4 B + 64 B per node visit + 48 B per triangle test (the adjoint re-reads "
                   "the hit triangle from L1); node/triangle fetches are served mostly from L1/L2",
                   TRAFFIC.get("pose_grad"))
@@ -860,7 +964,10 @@ def gpu_batched(args, world):
             setattr(sb, a, getattr(b, a)[:n])
         sample.append((sim, poses[:k], sb))
     t0 = time.perf_counter()
-    best = batched.BatchPlan(m, sample).autotune(reps=3, use_cache=False)
+    if args.no_autotune:  # the plan's default launch options
+        best = batched.BatchPlan(m, sample).config()
+    else:
+        best = batched.BatchPlan(m, sample).autotune(reps=3, use_cache=False)
     tune_s = time.perf_counter() - t0
     plan = batched.BatchPlan(m, jobs, best)
     for _ in range(args.warmup):
@@ -936,7 +1043,10 @@ def gpu_batched(args, world):
         e2e_t.append(time.perf_counter() - t0)
     e2e = rays / float(np.median(e2e_t)) / 1e6
     wk = WORK_PER_RAY.get("terrain2m_spherical")
-    rl = roofline(5 + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
+    rl = None if small else issue_roofline(
+        "batched/k_trace_batched", rays, total_ms / args.steps / 1e3, clocks, TRAFFIC.get("batched"),
+        "k_trace_batched (persistent warps over all sensors' tiles, per-ray walk of k_trace): issue-bound")
+    rl = rl or roofline(5 + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
                   "per ray: Hits+Ranges 5 B + 64 B per node visit + 48 B per triangle test (work per ray of the "
                   "2.1M-triangle terrain's spherical workload used as the estimate)", None if small else TRAFFIC.get("batched"))
     config = {"workload": ("batched small sensors: terrain 1024x1024 + 2000 boxes (2,117,058 tris), 1024 sensors "
@@ -964,8 +1074,7 @@ def gpu_batched(args, world):
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
 
     def cpu():
-        mod, c = spec[0]
-        return cpu_raycast(sc, mod, scenes.terrain_poses(sc, max(c, 64), seed=100), attrs, target_s=10.0)
+        return cpu_batched(sc, spec, target_s=10.0)
 
     return line, cpu, config
 
@@ -980,6 +1089,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="ray-cast workloads: the default launch configuration")
     ap.add_argument("--poses", type=int, default=0, help="use only the first N poses / batches (profiling case)")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="default workload: skip the batched and pose-gradient parts of the line")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -1013,6 +1124,19 @@ def main():
         line, cpu, _ = gpu_noise(args, world)
     else:
         raise SystemExit(f"unknown workload {args.workload}")
+    subs = {}
+    if args.workload == "terrain1m_spherical" and not args.headline_only and not args.poses:
+        # the other two parts of the headline metric ("plain vs batched", "pose-grad evals/s"), each
+        # timed on its own workload with its own clocks, e2e, roofline and CPU baseline
+        import torch
+
+        for key, fn, steps in (("batched", gpu_batched, min(args.steps, 5)), ("pose_grad", gpu_posegrad, args.steps)):
+            torch.cuda.empty_cache()
+            sub_args = argparse.Namespace(**vars(args))
+            sub_args.workload, sub_args.steps, sub_args.warmup = key, steps, max(3, min(args.warmup, 3))
+            sline, scpu, _ = fn(sub_args, world)
+            sline.update({"steps": steps, "warmup": sub_args.warmup})
+            subs[key] = (sline, scpu)
     if rank != 0:
         return
     out = dict(base)
@@ -1021,9 +1145,17 @@ def main():
         from oracle import build as ob
 
         ob.build()
-        c = cpu()
-        out["cpu_baseline"] = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in c.items() if k != "seconds"}
+    for key, (sline, scpu) in subs.items():
+        if not args.no_cpu_baseline:
+            sline["cpu_baseline"] = rounded(scpu())
+        out[key] = sline
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = rounded(cpu())
     print(json.dumps(out))
+
+
+def rounded(c):
+    return {k: (round(v, 4) if isinstance(v, float) else v) for k, v in c.items() if k != "seconds"}
 
 
 def reference_arm(args, base):
@@ -1034,8 +1166,13 @@ def reference_arm(args, base):
     ob.build()
     if args.workload in RAYCAST:
         sc, model, poses, attrs, desc = raycast_workload(args.workload)
+        if args.poses:
+            poses = poses[:args.poses]
         run = lambda: cpu_raycast(sc, model, poses, attrs, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
-        metric, unit, config = "Mrays/s", "Mrays/s", desc
+        W, H = model_size(model)
+        metric, unit = "Mrays/s", "Mrays/s"
+        config = raycast_config(desc, poses.shape[0], poses.shape[0] * W * H, sc.n_faces,
+                                int(os.environ.get("WORLD_SIZE", "1")))
     elif args.workload == "icp_stats":
         rng = np.random.default_rng(0)
         src = rng.uniform(-25, 25, (64, 32768, 3)).astype(np.float32)
@@ -1066,6 +1203,17 @@ def reference_arm(args, base):
         metric, unit, config = "Mrays/s", "Mrays/s", {"workload": "fused simulate -> statistics_p2l (CPU sample)"}
     else:
         raise SystemExit(f"unknown workload {args.workload}")
+    extras = {}
+    if args.workload == "terrain1m_spherical" and not args.headline_only and not args.poses:
+        # the CPU legs of the line's batched and pose-gradient parts, one bounded sample each
+        import oracle
+        from rmagine_gb300 import batched, scenes
+
+        sc2 = scenes.terrain(grid=1024, n_boxes=2000, seed=0)
+        extras["batched"] = cpu_batched(sc2, batched.mixed_sensor_set(64, seed=0), target_s=8.0)
+        psc, pmodel, ptrue, pest = posegrad_workload(16)
+        pobs = oracle.Scene(psc.vertices, psc.faces).simulate(pmodel, IDENT, ptrue, attrs=("ranges",))["ranges"]
+        extras["pose_grad"] = cpu_posegrad(psc, pmodel, ptrue, pest, pobs, target_s=8.0)
     vals, leg = [], None
     for _ in range(args.warmup + args.steps):
         leg = run()
@@ -1077,6 +1225,9 @@ def reference_arm(args, base):
                 "cpu_baseline": {"value": round(v, 4), "unit": unit, "cores": leg["cores"], "kind": leg["kind"],
                                  "sample": leg["sample"]},
                 "e2e": {"value": round(v, 4), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+    for key, leg2 in extras.items():
+        out[key] = {"metric": "Mrays/s" if key == "batched" else "pose-grad evals/s", "unit": leg2["unit"],
+                    "value": round(leg2["value"], 4), "cpu_baseline": rounded(leg2)}
     return out
 
 

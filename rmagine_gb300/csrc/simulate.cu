@@ -99,12 +99,12 @@ int launch_refill(const TraceParams& P, const rmg_sensor* sensor, const rmg_laun
     switch (sensor->model.kind) {
       case RMG_MODEL_SPHERICAL:
       case RMG_MODEL_PINHOLE:
-        e = launch_trace_refill_pose(P, (int)cfg.stack_depth, block, counter, cfg.chunk, cfg.refill, st);
+        e = launch_trace_refill<ORIGIN_POSE>(P, (int)cfg.stack_depth, block, counter, cfg.chunk, cfg.refill, st);
         break;
       case RMG_MODEL_O1DN:
-        e = launch_trace_refill_single(P, (int)cfg.stack_depth, block, counter, cfg.chunk, cfg.refill, st);
+        e = launch_trace_refill<ORIGIN_SINGLE>(P, (int)cfg.stack_depth, block, counter, cfg.chunk, cfg.refill, st);
         break;
-      default: e = launch_trace_refill_table(P, (int)cfg.stack_depth, block, counter, cfg.chunk, cfg.refill, st); break;
+      default: e = launch_trace_refill<ORIGIN_TABLE>(P, (int)cfg.stack_depth, block, counter, cfg.chunk, cfg.refill, st); break;
     }
   }
   const int s = cuda_status(e, "trace refill launch");
@@ -121,9 +121,9 @@ int launch_plain(const TraceParams& P, const rmg_sensor* sensor, const rmg_launc
   cudaError_t e;
   switch (sensor->model.kind) {
     case RMG_MODEL_SPHERICAL:
-    case RMG_MODEL_PINHOLE: e = launch_trace_pose(P, (int)cfg.stack_depth, (unsigned)blocks, block, st); break;
-    case RMG_MODEL_O1DN: e = launch_trace_single(P, (int)cfg.stack_depth, (unsigned)blocks, block, st); break;
-    default: e = launch_trace_table(P, (int)cfg.stack_depth, (unsigned)blocks, block, st); break;
+    case RMG_MODEL_PINHOLE: e = launch_trace<ORIGIN_POSE>(P, (int)cfg.stack_depth, (unsigned)blocks, block, st); break;
+    case RMG_MODEL_O1DN: e = launch_trace<ORIGIN_SINGLE>(P, (int)cfg.stack_depth, (unsigned)blocks, block, st); break;
+    default: e = launch_trace<ORIGIN_TABLE>(P, (int)cfg.stack_depth, (unsigned)blocks, block, st); break;
   }
   return cuda_status(e, "trace launch");
 }
