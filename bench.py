@@ -71,7 +71,7 @@ TRAFFIC: dict = {
     "scene_terrain1m": 10 * (357533440 + 682603008),
     # captured with every sensor cut to 16 poses (143,238,688 rays) and scaled by the ray count to the
     # full 64-sensor launch (9,025,081,856 rays)
-    "batched": round(9025081856 / 143238688 * (2200136960 + 877252864)),
+    "batched": round(9025081856 / 143238688 * (2129916160 + 849543424)),
 }
 
 # Warp instructions per unit (ray) of the dominant kernel, `smsp__inst_executed.sum` of one ncu
@@ -81,8 +81,9 @@ ISSUE: dict = {
                                        "profiles/k_trace_terrain1m_spherical.md (100 poses, 13,107,200 rays)"},
     "pose_grad/k_range_grad": {"warp_inst_per_unit": 591522244 / 4194304, "source":
                                "profiles/k_range_grad_terrain2m_posegrad.md (64 poses, 4,194,304 rays)"},
-    "batched/k_trace_batched": {"warp_inst_per_unit": 14765923075 / 143238688, "source":
-                                "profiles/k_trace_batched_mixed64.md (16 poses per sensor, 143,238,688 rays)"},
+    "batched/k_trace_batched": {"warp_inst_per_unit": 14537272107 / 143238688, "source":
+                                "profiles/k_trace_batched_mixed64.md (16 poses per sensor, 143,238,688 rays, "
+                                "autotuned launch options)"},
 }
 
 RAYCAST = ("terrain1m_spherical", "terrain1m_pinhole", "terrain2m_spherical", "terrain33m_spherical", "room_vlp16")
@@ -226,6 +227,17 @@ def roofline(bytes_per_unit, units_per_launch, launch_s, note, traffic=None):
             "note": note}
 
 
+def nvtx_range(name):
+    """Pushes an NVTX range; returns the function that pops it (a no-op where NVTX is missing)."""
+    try:
+        import torch
+
+        torch.cuda.nvtx.range_push(name)
+        return torch.cuda.nvtx.range_pop
+    except Exception:
+        return lambda: None
+
+
 class Timer:
     """Per-step CUDA events on the launching stream with an L2 flush between steps."""
 
@@ -244,11 +256,13 @@ class Timer:
         barrier(world)
         torch.cuda.synchronize(self.dev)
         with ClockSampler(self.dev.index) as clk:
+            nvtx = nvtx_range("timed")  # lets a profiler select the timed launches (ncu --nvtx-include timed/)
             for s, e in self.ev:
                 self.flush.zero_()  # evict L2 between timed steps (outside the events)
                 s.record(stream)
                 fn()
                 e.record(stream)
+            nvtx()
             torch.cuda.synchronize(self.dev)
         barrier(world)
         ms = [s.elapsed_time(e) for s, e in self.ev]

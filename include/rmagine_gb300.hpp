@@ -4,7 +4,12 @@
 // siblings) switches by changing the simulator type.
 //
 // Mirrors (uos/rmagine v2.4.2):
-//   Memory<T, RAM | VRAM_CUDA>       types/Memory.hpp:59-266, types/MemoryCuda.hpp:66-100
+//   Memory<T, RAM | VRAM_CUDA |
+//          RAM_CUDA | UNIFIED_CUDA>  types/Memory.hpp:59-266, types/MemoryCuda.hpp:66-100
+//   MemoryView<T, MemT>, slice,
+//     operator()(a, b)               types/Memory.hpp:60-173
+//   SimulatorType / Simulator /
+//     make_simulator<ModelT, CompT>  simulation/Simulator.hpp:52-78 (CompT = GB300)
 //   Bundle / Hits / Ranges / ...     types/Bundle.hpp:72-131, simulation/SimulationResults.hpp:56-215
 //   resize_memory_bundle             SimulationResults.hpp:176-215
 //   SphericalModel / PinholeModel /
@@ -14,6 +19,9 @@
 //     setModel/simulate              SimulatorEmbree.hpp:52-72, SphereSimulatorEmbree.hpp:107-159,
 //                                    SphereSimulatorOptix.hpp:122-190
 //   statistics_p2p / _p2l / umeyama  math/statistics.h:72-157, math/optimization.h:61-75
+//   svd (batched 3x3)                 rmagine_cuda math/memory_math.cuh:561-578, math/linalg.h:164-175
+//   rangePoseGrad / umeyama_backward  no counterpart (the differentiable forms of simulate and
+//                                     of statistics_p2p + umeyama_transform)
 //   InstancedScene / Instance        EmbreeScene / EmbreeInstance (map/embree/EmbreeScene.hpp,
 //                                    EmbreeInstance.hpp), OptixScene instances
 //   GaussianNoiseGB300 / ...         noise/GaussianNoiseCuda.hpp, RelGaussianNoiseCuda.hpp,
@@ -82,14 +90,65 @@ struct DiscreteInterval {
 };
 
 // ---- memory -----------------------------------------------------------------------
+// Memory kinds (rmagine's memory tags): RAM (pageable host), VRAM_CUDA (device), RAM_CUDA
+// (pinned host, MemoryCuda.hpp:78), UNIFIED_CUDA (managed, MemoryCuda.hpp:89).
 struct RAM {};
 struct VRAM_CUDA {};
+struct RAM_CUDA {};
+struct UNIFIED_CUDA {};
+
+// Host-side memory kinds take the host forms of the calls; device-side ones the device forms.
+template <typename MemT> struct host_memory : std::false_type {};
+template <> struct host_memory<RAM> : std::true_type {};
+template <> struct host_memory<RAM_CUDA> : std::true_type {};
+
+// A non-owning window of n elements (MemoryView, types/Memory.hpp:60-173): what rmagine's
+// simulate / setTsb / setModel overloads take.  A view of const T binds to a view of T.
+template <typename T, typename MemT = RAM>
+class MemoryView {
+ public:
+  using DataType = T;
+  using MemType = MemT;
+  MemoryView(T* mem, size_t n) : p_(mem), n_(n) {}
+  template <typename U, typename = std::enable_if_t<std::is_same<const U, T>::value>>
+  MemoryView(const MemoryView<U, MemT>& o) : p_(o.raw()), n_(o.size()) {}
+  static MemoryView Empty() { return MemoryView(nullptr, 0); }
+  bool empty() const { return p_ == nullptr; }
+  T* raw() const { return p_; }
+  size_t size() const { return n_; }
+  T& operator[](size_t i) const { return p_[i]; }  // host-accessible kinds only
+  MemoryView slice(size_t a, size_t b) const { return MemoryView(p_ + a, b - a); }
+  MemoryView operator()(size_t a, size_t b) const { return slice(a, b); }
+
+ private:
+  T* p_ = nullptr;
+  size_t n_ = 0;
+};
 
 template <typename T, typename MemT>
 class Memory;
 
+// Views, slices and conversions shared by every owning Memory kind.
+template <typename T, typename MemT, typename Derived>
+struct MemoryViews {
+  operator MemoryView<T, MemT>() { return MemoryView<T, MemT>(self().raw(), self().size()); }
+  operator MemoryView<const T, MemT>() const { return MemoryView<const T, MemT>(self().raw(), self().size()); }
+  MemoryView<T, MemT> view() { return *this; }
+  MemoryView<const T, MemT> view() const { return *this; }
+  MemoryView<T, MemT> slice(size_t a, size_t b) { return MemoryView<T, MemT>(self().raw() + a, b - a); }
+  MemoryView<const T, MemT> slice(size_t a, size_t b) const {
+    return MemoryView<const T, MemT>(self().raw() + a, b - a);
+  }
+  MemoryView<T, MemT> operator()(size_t a, size_t b) { return slice(a, b); }
+  MemoryView<const T, MemT> operator()(size_t a, size_t b) const { return slice(a, b); }
+
+ private:
+  Derived& self() { return static_cast<Derived&>(*this); }
+  const Derived& self() const { return static_cast<const Derived&>(*this); }
+};
+
 template <typename T>
-class Memory<T, RAM> {
+class Memory<T, RAM> : public MemoryViews<T, RAM, Memory<T, RAM>> {
  public:
   Memory() = default;
   explicit Memory(size_t n) : v_(n) {}
@@ -99,50 +158,107 @@ class Memory<T, RAM> {
   const T* raw() const { return v_.data(); }
   T& operator[](size_t i) { return v_[i]; }
   const T& operator[](size_t i) const { return v_[i]; }
-  Memory& operator=(const Memory<T, VRAM_CUDA>& o);
+  template <typename MemT2>
+  Memory& operator=(const Memory<T, MemT2>& o);
 
  private:
   std::vector<T> v_;
 };
 
-template <typename T>
-class Memory<T, VRAM_CUDA> {
+// cudaMalloc'd (VRAM_CUDA), cudaMallocHost'd (RAM_CUDA) or cudaMallocManaged (UNIFIED_CUDA) storage.
+template <typename T, typename MemT>
+class CudaMemory : public MemoryViews<T, MemT, Memory<T, MemT>> {
  public:
-  Memory() = default;
-  explicit Memory(size_t n) { resize(n); }
-  Memory(const Memory&) = delete;
-  Memory& operator=(const Memory&) = delete;
-  Memory(Memory&& o) noexcept : p_(o.p_), n_(o.n_) { o.p_ = nullptr; o.n_ = 0; }
-  ~Memory() { cudaFree(p_); }
+  CudaMemory() = default;
+  explicit CudaMemory(size_t n) { resize(n); }
+  CudaMemory(const CudaMemory&) = delete;
+  CudaMemory& operator=(const CudaMemory&) = delete;
+  CudaMemory(CudaMemory&& o) noexcept : p_(o.p_), n_(o.n_) { o.p_ = nullptr; o.n_ = 0; }
+  ~CudaMemory() { release(); }
   void resize(size_t n) {
     if (n == n_) return;
-    cudaFree(p_);
-    p_ = nullptr;
-    n_ = 0;
-    if (n) cuda_check(cudaMalloc(reinterpret_cast<void**>(&p_), n * sizeof(T)), "cudaMalloc");
+    release();
+    if (n) {
+      void* p = nullptr;
+      if constexpr (std::is_same<MemT, RAM_CUDA>::value) cuda_check(cudaMallocHost(&p, n * sizeof(T)), "cudaMallocHost");
+      else if constexpr (std::is_same<MemT, UNIFIED_CUDA>::value)
+        cuda_check(cudaMallocManaged(&p, n * sizeof(T)), "cudaMallocManaged");
+      else cuda_check(cudaMalloc(&p, n * sizeof(T)), "cudaMalloc");
+      p_ = static_cast<T*>(p);
+    }
     n_ = n;
   }
   size_t size() const { return n_; }
   T* raw() { return p_; }
   const T* raw() const { return p_; }
-  // RAM -> VRAM assignment copies (MemoryCuda.cu:10-90 semantics)
-  Memory& operator=(const Memory<T, RAM>& o) {
-    resize(o.size());
-    if (n_) cuda_check(cudaMemcpy(p_, o.raw(), n_ * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy");
-    return *this;
-  }
 
- private:
+ protected:
+  void release() {
+    if (p_) {
+      if constexpr (std::is_same<MemT, RAM_CUDA>::value) cudaFreeHost(p_);
+      else cudaFree(p_);
+    }
+    p_ = nullptr;
+    n_ = 0;
+  }
   T* p_ = nullptr;
   size_t n_ = 0;
 };
 
+// Assignment between any two kinds copies (MemoryCuda.cu:10-90 semantics).
+template <typename T, typename MemT, typename MemT2, typename Dst, typename Src>
+void copy_memory(Dst& dst, const Src& src) {
+  dst.resize(src.size());
+  if (src.size())
+    cuda_check(cudaMemcpy(dst.raw(), src.raw(), src.size() * sizeof(T), cudaMemcpyDefault), "cudaMemcpy");
+}
+
 template <typename T>
-Memory<T, RAM>& Memory<T, RAM>::operator=(const Memory<T, VRAM_CUDA>& o) {
-  resize(o.size());
-  if (o.size()) cuda_check(cudaMemcpy(raw(), o.raw(), o.size() * sizeof(T), cudaMemcpyDeviceToHost), "cudaMemcpy");
+class Memory<T, VRAM_CUDA> : public CudaMemory<T, VRAM_CUDA> {
+ public:
+  using CudaMemory<T, VRAM_CUDA>::CudaMemory;
+  Memory() = default;
+  Memory(Memory&&) noexcept = default;
+  template <typename MemT2>
+  Memory& operator=(const Memory<T, MemT2>& o) { copy_memory<T, VRAM_CUDA, MemT2>(*this, o); return *this; }
+};
+
+template <typename T>
+class Memory<T, RAM_CUDA> : public CudaMemory<T, RAM_CUDA> {
+ public:
+  using CudaMemory<T, RAM_CUDA>::CudaMemory;
+  Memory() = default;
+  Memory(Memory&&) noexcept = default;
+  T& operator[](size_t i) { return this->p_[i]; }
+  const T& operator[](size_t i) const { return this->p_[i]; }
+  template <typename MemT2>
+  Memory& operator=(const Memory<T, MemT2>& o) { copy_memory<T, RAM_CUDA, MemT2>(*this, o); return *this; }
+};
+
+template <typename T>
+class Memory<T, UNIFIED_CUDA> : public CudaMemory<T, UNIFIED_CUDA> {
+ public:
+  using CudaMemory<T, UNIFIED_CUDA>::CudaMemory;
+  Memory() = default;
+  Memory(Memory&&) noexcept = default;
+  T& operator[](size_t i) { return this->p_[i]; }  // after a device synchronisation
+  const T& operator[](size_t i) const { return this->p_[i]; }
+  template <typename MemT2>
+  Memory& operator=(const Memory<T, MemT2>& o) { copy_memory<T, UNIFIED_CUDA, MemT2>(*this, o); return *this; }
+};
+
+template <typename T>
+template <typename MemT2>
+Memory<T, RAM>& Memory<T, RAM>::operator=(const Memory<T, MemT2>& o) {
+  copy_memory<T, RAM, MemT2>(*this, o);
   return *this;
 }
+
+// Element type and memory kind of a pose buffer (Memory or MemoryView of Transform).
+template <typename P> struct pose_buffer : std::false_type {};
+template <typename MemT> struct pose_buffer<MemoryView<Transform, MemT>> : std::true_type { using Mem = MemT; };
+template <typename MemT> struct pose_buffer<MemoryView<const Transform, MemT>> : std::true_type { using Mem = MemT; };
+template <typename MemT> struct pose_buffer<Memory<Transform, MemT>> : std::true_type { using Mem = MemT; };
 
 // ---- result attributes and bundles ---------------------------------------------------
 template <typename MemT> struct Hits { Memory<uint8_t, MemT> hits; };
@@ -193,6 +309,25 @@ rmg_outputs outputs_of(BundleT& b) {
     o.geom_ids = b.GeomIds<M>::geom_ids.size() ? b.GeomIds<M>::geom_ids.raw() : nullptr;
   if constexpr (BundleT::template has<ObjectIds<M>>())
     o.object_ids = b.ObjectIds<M>::object_ids.size() ? b.ObjectIds<M>::object_ids.raw() : nullptr;
+  return o;
+}
+
+inline void merge_outputs(rmg_outputs& o, const rmg_outputs& b) {
+  if (!o.hits) o.hits = b.hits;
+  if (!o.ranges) o.ranges = b.ranges;
+  if (!o.points) o.points = b.points;
+  if (!o.normals) o.normals = b.normals;
+  if (!o.face_ids) o.face_ids = b.face_ids;
+  if (!o.geom_ids) o.geom_ids = b.geom_ids;
+  if (!o.object_ids) o.object_ids = b.object_ids;
+}
+
+// The bundle's buffers that the host forms fill (RAM and RAM_CUDA attributes) and those the device
+// forms fill (VRAM_CUDA and UNIFIED_CUDA attributes).
+template <bool Host, typename BundleT>
+rmg_outputs outputs_for(BundleT& b) {
+  rmg_outputs o = outputs_of<std::conditional_t<Host, RAM, VRAM_CUDA>>(b);
+  merge_outputs(o, outputs_of<std::conditional_t<Host, RAM_CUDA, UNIFIED_CUDA>>(b));
   return o;
 }
 
@@ -490,11 +625,21 @@ class SimulatorGB300 {
           "rmg_simulate_statistics_host");
   }
   void setTsb(const Transform& T) { Tsb_ = T; }
+  // setTsb(MemoryView<Transform, RAM>) (SimulatorEmbree.hpp:60): the first transform.
+  void setTsb(const MemoryView<const Transform, RAM>& T) {
+    if (T.size() == 0) throw Exception(RMG_ERR_INVALID_ARG, "setTsb: no transform");
+    Tsb_ = T[0];
+  }
+  void setTsb(const MemoryView<Transform, RAM>& T) { setTsb(MemoryView<const Transform, RAM>(T)); }
+  void setTsb(const Memory<Transform, RAM>& T) { setTsb(T.view()); }
+  const Transform& Tsb() const { return Tsb_; }
   // setModel(MemoryView<ModelT, RAM>) (SphereSimulatorEmbree.hpp:115): the first model.
-  void setModel(const Memory<ModelT, RAM>& models) {
+  void setModel(const MemoryView<const ModelT, RAM>& models) {
     if (models.size() == 0) throw Exception(RMG_ERR_INVALID_ARG, "setModel: no model");
     setModel(models[0]);
   }
+  void setModel(const MemoryView<ModelT, RAM>& models) { setModel(MemoryView<const ModelT, RAM>(models)); }
+  void setModel(const Memory<ModelT, RAM>& models) { setModel(models.view()); }
   void setModel(const ModelT& model) {
     const rmg_model c = model.to_c();
     rmg_sensor* s = nullptr;
@@ -504,78 +649,122 @@ class SimulatorGB300 {
     rmg_sensor_size(sensor_, &W_, &H_);
   }
 
-  // Device form (SphereSimulatorOptix.hpp:141-160): asynchronous on `stream`.
-  template <typename BundleT>
-  void simulate(const Memory<Transform, VRAM_CUDA>& Tbm, BundleT& ret, cudaStream_t stream = 0) const {
-    ready();
-    const rmg_outputs o = outputs_of(ret);
-    const auto* T = reinterpret_cast<const rmg_transform*>(Tbm.raw());
-    const auto* Tsb = reinterpret_cast<const rmg_transform*>(&Tsb_);
-    if (scene_)
-      check(rmg_simulate_scene(scene_->handle(), sensor_, Tsb, T, (uint32_t)Tbm.size(), &o, stream),
-            "rmg_simulate_scene");
-    else if (tuned_)
-      check(rmg_simulate_ex(map_->handle(), sensor_, Tsb, T, (uint32_t)Tbm.size(), &o, &cfg_, stream),
-            "rmg_simulate_ex");
-    else
-      check(rmg_simulate(map_->handle(), sensor_, Tsb, T, (uint32_t)Tbm.size(), &o, stream), "rmg_simulate");
+  // Poses in any Memory / MemoryView of Transform (const or not; RAM, RAM_CUDA, VRAM_CUDA,
+  // UNIFIED_CUDA): a caller's slice Tbm(a, b) binds as in SphereSimulatorEmbree.hpp:140-155.
+  //  * device kinds (VRAM_CUDA, UNIFIED_CUDA) -- the OptiX-style device form
+  //    (SphereSimulatorOptix.hpp:141-160): fills the bundle's device buffers, asynchronous on `stream`;
+  //  * host kinds (RAM, RAM_CUDA) -- the Embree-style host form (SphereSimulatorEmbree.hpp:130-155):
+  //    fills the bundle's host buffers through rmg_simulate_host (pose chunks cast on `stream`
+  //    while earlier chunks are copied back; the requested buffers are resized); synchronises.
+  template <typename PosesT, typename BundleT, typename = std::enable_if_t<pose_buffer<PosesT>::value>>
+  void simulate(const PosesT& Tbm, BundleT& ret, cudaStream_t stream = 0) const {
+    using MemT = typename pose_buffer<PosesT>::Mem;
+    const MemoryView<const Transform, MemT> T = view_of(Tbm);
+    if constexpr (host_memory<MemT>::value) simulate_host(T.raw(), T.size(), ret, stream);
+    else simulate_device(T.raw(), T.size(), ret, stream);
   }
 
-  // Allocating device form: simulate<BundleT>(Tbm).
-  template <typename BundleT>
-  BundleT simulate(const Memory<Transform, VRAM_CUDA>& Tbm, cudaStream_t stream = 0) const {
+  // Allocating forms: simulate<BundleT>(Tbm) returns a bundle of the poses' memory side, sized
+  // width x height x poses.
+  template <typename BundleT, typename PosesT, typename = std::enable_if_t<pose_buffer<PosesT>::value>>
+  BundleT simulate(const PosesT& Tbm, cudaStream_t stream = 0) const {
+    using MemT = typename pose_buffer<PosesT>::Mem;
     BundleT res;
-    resize_memory_bundle<VRAM_CUDA>(res, W_, H_, (unsigned)Tbm.size());
+    resize_memory_bundle<std::conditional_t<host_memory<MemT>::value, RAM, VRAM_CUDA>>(res, W_, H_,
+                                                                                      (unsigned)Tbm.size());
     simulate(Tbm, res, stream);
-    return res;
-  }
-
-  // Host form (SphereSimulatorEmbree.hpp:130-155): poses and results in RAM; the non-empty
-  // buffers are filled through rmg_simulate_host (pose chunks cast on `stream` while earlier
-  // chunks are copied back).  Synchronises.
-  template <typename BundleRAM>
-  void simulate(const Memory<Transform, RAM>& Tbm, BundleRAM& ret, cudaStream_t stream = 0) const {
-    ready();
-    resize_requested<RAM>(ret, (size_t)W_ * H_ * Tbm.size());
-    const rmg_outputs o = outputs_of<RAM>(ret);
-    const auto* T = reinterpret_cast<const rmg_transform*>(Tbm.raw());
-    const auto* Tsb = reinterpret_cast<const rmg_transform*>(&Tsb_);
-    if (scene_)
-      check(rmg_simulate_scene_host(scene_->handle(), sensor_, Tsb, T, (uint32_t)Tbm.size(), &o, stream),
-            "rmg_simulate_scene_host");
-    else
-      check(rmg_simulate_host(map_->handle(), sensor_, Tsb, T, (uint32_t)Tbm.size(), &o, tuned_ ? &cfg_ : nullptr,
-                              stream),
-            "rmg_simulate_host");
-  }
-
-  template <typename BundleRAM>
-  BundleRAM simulate(const Memory<Transform, RAM>& Tbm) const {
-    BundleRAM res;
-    resize_memory_bundle<RAM>(res, W_, H_, (unsigned)Tbm.size());
-    simulate(Tbm, res);
     return res;
   }
 
   // One pose (SphereSimulatorEmbree.hpp:128-135): results in RAM; synchronises.
   template <typename BundleRAM>
   void simulate(const Transform& Tbm, BundleRAM& ret) const {
-    Memory<Transform, RAM> T(1);
-    T[0] = Tbm;
-    simulate(T, ret);
+    simulate(MemoryView<const Transform, RAM>(&Tbm, 1), ret);
   }
 
   template <typename BundleRAM>
   BundleRAM simulate(const Transform& Tbm) const {
-    Memory<Transform, RAM> T(1);
-    T[0] = Tbm;
-    return simulate<BundleRAM>(T);
+    return simulate<BundleRAM>(MemoryView<const Transform, RAM>(&Tbm, 1));
+  }
+
+  // d(loss)/d(pose) of the range residuals (rmg_range_pose_grad; no counterpart in rmagine, whose
+  // simulators are not differentiable).  For every pose: loss = sum over rays with a simulated hit
+  // and an observation in [range.min, range.max] of Huber_delta(r_sim - r_obs), and grad = dloss/dxi
+  // (6 floats, translation first) for the right perturbation Tbm * exp(xi^).  ranges_obs holds
+  // width x height ranges per pose; grad / loss are resized to 6 / 1 per pose, ranges_sim /
+  // face_ids (optional) to width x height per pose.  Device kinds: asynchronous, at most 65,535
+  // poses per call; host kinds (rmg_range_pose_grad_host): any number of poses, synchronises.
+  template <typename PosesT, typename ObsT, typename MemT = typename pose_buffer<PosesT>::Mem>
+  void rangePoseGrad(const PosesT& Tbm, const ObsT& ranges_obs, float huber_delta, Memory<float, MemT>& grad,
+                     Memory<float, MemT>* loss = nullptr, Memory<float, MemT>* ranges_sim = nullptr,
+                     Memory<uint32_t, MemT>* face_ids = nullptr, cudaStream_t stream = 0) const {
+    ready();
+    if (!map_) throw Exception(RMG_ERR_UNSUPPORTED, "rangePoseGrad: needs a single-mesh map");
+    const MemoryView<const Transform, MemT> T = view_of(Tbm);
+    const MemoryView<const float, MemT> obs = ranges_obs;
+    const size_t n = T.size();
+    if (obs.size() != n * W_ * H_)
+      throw Exception(RMG_ERR_INVALID_ARG, "rangePoseGrad: ranges_obs must hold width*height ranges per pose");
+    grad.resize(6 * n);
+    if (loss) loss->resize(n);
+    if (ranges_sim) ranges_sim->resize(n * W_ * H_);
+    if (face_ids) face_ids->resize(n * W_ * H_);
+    const auto* Tp = reinterpret_cast<const rmg_transform*>(T.raw());
+    const auto* Tsb = reinterpret_cast<const rmg_transform*>(&Tsb_);
+    float* lp = loss ? loss->raw() : nullptr;
+    float* rp = ranges_sim ? ranges_sim->raw() : nullptr;
+    uint32_t* fp = face_ids ? face_ids->raw() : nullptr;
+    if constexpr (host_memory<MemT>::value)
+      check(rmg_range_pose_grad_host(map_->handle(), sensor_, Tsb, Tp, (uint32_t)n, obs.raw(), huber_delta,
+                                     grad.raw(), lp, rp, fp, stream),
+            "rmg_range_pose_grad_host");
+    else
+      check(rmg_range_pose_grad(map_->handle(), sensor_, Tsb, Tp, (uint32_t)n, obs.raw(), huber_delta, grad.raw(),
+                                lp, rp, fp, stream),
+            "rmg_range_pose_grad");
   }
 
   uint32_t width() const { return W_; }
   uint32_t height() const { return H_; }
 
  private:
+  template <typename MemT>
+  static MemoryView<const Transform, MemT> view_of(const MemoryView<const Transform, MemT>& v) { return v; }
+  template <typename MemT>
+  static MemoryView<const Transform, MemT> view_of(const MemoryView<Transform, MemT>& v) { return v; }
+  template <typename MemT>
+  static MemoryView<const Transform, MemT> view_of(const Memory<Transform, MemT>& m) { return m.view(); }
+
+  template <typename BundleT>
+  void simulate_device(const Transform* Tbm, size_t n, BundleT& ret, cudaStream_t stream) const {
+    ready();
+    const rmg_outputs o = outputs_for<false>(ret);
+    const auto* T = reinterpret_cast<const rmg_transform*>(Tbm);
+    const auto* Tsb = reinterpret_cast<const rmg_transform*>(&Tsb_);
+    if (scene_)
+      check(rmg_simulate_scene(scene_->handle(), sensor_, Tsb, T, (uint32_t)n, &o, stream), "rmg_simulate_scene");
+    else if (tuned_)
+      check(rmg_simulate_ex(map_->handle(), sensor_, Tsb, T, (uint32_t)n, &o, &cfg_, stream), "rmg_simulate_ex");
+    else
+      check(rmg_simulate(map_->handle(), sensor_, Tsb, T, (uint32_t)n, &o, stream), "rmg_simulate");
+  }
+
+  template <typename BundleT>
+  void simulate_host(const Transform* Tbm, size_t n, BundleT& ret, cudaStream_t stream) const {
+    ready();
+    resize_requested<RAM>(ret, (size_t)W_ * H_ * n);
+    resize_requested<RAM_CUDA>(ret, (size_t)W_ * H_ * n);
+    const rmg_outputs o = outputs_for<true>(ret);
+    const auto* T = reinterpret_cast<const rmg_transform*>(Tbm);
+    const auto* Tsb = reinterpret_cast<const rmg_transform*>(&Tsb_);
+    if (scene_)
+      check(rmg_simulate_scene_host(scene_->handle(), sensor_, Tsb, T, (uint32_t)n, &o, stream),
+            "rmg_simulate_scene_host");
+    else
+      check(rmg_simulate_host(map_->handle(), sensor_, Tsb, T, (uint32_t)n, &o, tuned_ ? &cfg_ : nullptr, stream),
+            "rmg_simulate_host");
+  }
+
   void ready() const {
     if (!map_ && !scene_) throw Exception(RMG_ERR_INVALID_ARG, "simulate: no map set");
     if (!sensor_) throw Exception(RMG_ERR_INVALID_ARG, "simulate: no model set");
@@ -593,6 +782,50 @@ using SphereSimulatorGB300 = SimulatorGB300<SphericalModel>;
 using PinholeSimulatorGB300 = SimulatorGB300<PinholeModel>;
 using O1DnSimulatorGB300 = SimulatorGB300<O1DnModel>;
 using OnDnSimulatorGB300 = SimulatorGB300<OnDnModel>;
+using SphereSimulatorGB300Ptr = std::shared_ptr<SphereSimulatorGB300>;
+using PinholeSimulatorGB300Ptr = std::shared_ptr<PinholeSimulatorGB300>;
+using O1DnSimulatorGB300Ptr = std::shared_ptr<O1DnSimulatorGB300>;
+using OnDnSimulatorGB300Ptr = std::shared_ptr<OnDnSimulatorGB300>;
+
+// ---- simulator factory (simulation/Simulator.hpp:52-78) ------------------------------------
+// The computing backend tag of this library, beside rmagine's Embree / Optix / Vulkan tags.
+struct GB300 {};
+struct NoneType {};
+
+template <typename ModelT, typename CompT>
+struct SimulatorType {
+  using Class = NoneType;
+  using Ptr = NoneType;
+};
+template <typename ModelT>
+struct SimulatorType<ModelT, GB300> {
+  using Class = SimulatorGB300<ModelT>;
+  using Ptr = std::shared_ptr<Class>;
+};
+template <typename ModelT, typename CompT>
+using Simulator = typename SimulatorType<ModelT, CompT>::Class;
+template <typename ModelT, typename CompT>
+using SimulatorPtr = typename SimulatorType<ModelT, CompT>::Ptr;
+
+// make_simulator<SphericalModel, GB300>() -> SphereSimulatorGB300Ptr (false for an unknown pair,
+// as rmagine's factory returns)
+template <typename ModelT, typename CompT>
+auto make_simulator() {
+  using SimT = SimulatorType<ModelT, CompT>;
+  if constexpr (std::is_same<typename SimT::Class, NoneType>::value) {
+    return false;
+  } else {
+    return typename SimT::Ptr(new typename SimT::Class);
+  }
+}
+
+// The same with the map set.
+template <typename ModelT, typename CompT>
+auto make_simulator(MapPtr map) {
+  auto sim = make_simulator<ModelT, CompT>();
+  if constexpr (!std::is_same<decltype(sim), bool>::value) sim->setMap(std::move(map));
+  return sim;
+}
 
 // ---- statistics / Umeyama -----------------------------------------------------------------
 
@@ -640,6 +873,43 @@ inline void statistics_p2l(const Memory<Vector3, VRAM_CUDA>& dataset, const Memo
                            reinterpret_cast<rmg_cross_stats*>(stats.raw()),
                            Ts ? reinterpret_cast<rmg_transform*>(Ts->raw()) : nullptr, s),
         "rmg_statistics_p2l");
+}
+
+// Backward of statistics_p2p + umeyama_transform (rmg_umeyama_backward; no counterpart in
+// rmagine): given the forward's stats and upstream gradients dL/dR (9 floats per batch,
+// row-major) and dL/dt (3 per batch) -- either may be null, meaning zero -- writes dL/d(dataset
+// point) and dL/d(model point) for every correspondence; filtered-out correspondences get 0.
+// Same DEVICE inputs and filter as statistics_p2p.
+inline void umeyama_backward(const Memory<Vector3, VRAM_CUDA>& dataset, const Memory<Vector3, VRAM_CUDA>& model,
+                             const UmeyamaReductionConstraints& params, uint32_t n_batches,
+                             const Memory<CrossStatistics, VRAM_CUDA>& stats, const Memory<float, VRAM_CUDA>* grad_R,
+                             const Memory<float, VRAM_CUDA>* grad_t, Memory<Vector3, VRAM_CUDA>* grad_dataset,
+                             Memory<Vector3, VRAM_CUDA>* grad_model,
+                             const Memory<uint8_t, VRAM_CUDA>* dataset_mask = nullptr, cudaStream_t s = 0) {
+  const uint32_t n_per = n_batches ? (uint32_t)(dataset.size() / n_batches) : 0;
+  if (grad_dataset) grad_dataset->resize(dataset.size());
+  if (grad_model) grad_model->resize(model.size());
+  const rmg_umeyama_constraints c{params.max_dist, params.dataset_id, params.model_id};
+  check(rmg_umeyama_backward(nullptr, 0, reinterpret_cast<const rmg_vec3*>(dataset.raw()),
+                             dataset_mask ? dataset_mask->raw() : nullptr, nullptr,
+                             reinterpret_cast<const rmg_vec3*>(model.raw()), nullptr, nullptr, &c, n_batches, n_per,
+                             reinterpret_cast<const rmg_cross_stats*>(stats.raw()), grad_R ? grad_R->raw() : nullptr,
+                             grad_t ? grad_t->raw() : nullptr,
+                             grad_dataset ? reinterpret_cast<rmg_vec3*>(grad_dataset->raw()) : nullptr,
+                             grad_model ? reinterpret_cast<rmg_vec3*>(grad_model->raw()) : nullptr, s),
+        "rmg_umeyama_backward");
+}
+
+// Batched 3x3 SVD A = U W V^T (svd(As, Us, Ws, Vs), memory_math.cuh:561-578) of column-major
+// DEVICE matrices (9 floats each, rmagine's Matrix3x3 layout): W >= 0 on the diagonal, sorted
+// descending; with rotations = true, U and V are rotations and the last value carries det A's sign.
+inline void svd(const Memory<float, VRAM_CUDA>& As, Memory<float, VRAM_CUDA>& Us, Memory<float, VRAM_CUDA>& Ws,
+                Memory<float, VRAM_CUDA>& Vs, bool rotations = false, cudaStream_t s = 0) {
+  const size_t n = As.size() / 9;
+  Us.resize(9 * n);
+  Ws.resize(9 * n);
+  Vs.resize(9 * n);
+  check(rmg_svd3(As.raw(), Us.raw(), Ws.raw(), nullptr, Vs.raw(), (uint32_t)n, rotations ? 1 : 0, s), "rmg_svd3");
 }
 
 // out[i] = a[i] * b[i] on the device (Transform::mult); a one-element operand is repeated.

@@ -198,20 +198,29 @@ __host__ __device__ inline void umeyama_d(const M3d& C, const double d[3], const
   for (int i = 0; i < 3; ++i) t[i] = m[i] - (R.a[i][0] * d[0] + R.a[i][1] * d[1] + R.a[i][2] * d[2]);
 }
 
+// Relative size below which s_i + s_j counts as zero in rotation_backward.
+// The covariance reaches the backward in binary32 (rmagine's CrossStatistics),
+// so singular values carry an absolute error of about 1e-7 s0: a smaller sum
+// is rounding noise, and dividing by it would only amplify that noise.
+constexpr double kRotGradGap = 1e-6;
+
 // Gradient of L through R = U V^T (C = U diag(s) V^T, rotations U, V):
 // dL/dC = U K V^T with K_ij = (G_ij - G_ji) / (s_i + s_j) for i != j, K_ii = 0,
-// G = U^T (dL/dR) V.  Denominators below eps * s0 are clamped (the rotation
-// is ill-conditioned there).
+// G = U^T (dL/dR) V.  Where s_i + s_j <= kRotGradGap * s0 the optimal rotation
+// about the axis u_i x u_j is not unique (collinear correspondences: s2 = s3 = 0;
+// a reflection with two equal singular values: s2 = -s3) and R is not
+// differentiable there: that pair contributes no gradient (K_ij = K_ji = 0).
+// The rest of the gradient is exact; close to the boundary it grows like
+// 1 / (s_i + s_j), as the rotation's true derivative does.
 __host__ __device__ inline M3d rotation_backward(const M3d& U, const double s[3], const M3d& V, const M3d& gR) {
   const M3d G = m3_mul(m3_mul_tn(U, gR), V);
   M3d K = m3_zero();
-  const double eps = 1e-12 * fmax(fabs(s[0]), 1e-300);
+  const double gap = kRotGradGap * fabs(s[0]);
   for (int i = 0; i < 3; ++i) {
     for (int j = 0; j < 3; ++j) {
       if (i == j) continue;
-      double den = s[i] + s[j];
-      if (fabs(den) < eps) den = den < 0.0 ? -eps : eps;
-      K.a[i][j] = (G.a[i][j] - G.a[j][i]) / den;
+      const double den = s[i] + s[j];
+      K.a[i][j] = den > gap ? (G.a[i][j] - G.a[j][i]) / den : 0.0;
     }
   }
   return m3_mul_nt(m3_mul(U, K), V);

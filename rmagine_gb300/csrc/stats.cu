@@ -481,6 +481,56 @@ extern "C" int rmg_statistics_p2l(const rmg_transform* pre_transforms, uint32_t 
                      true);
 }
 
+// One 3x3 SVD per thread (binary64 inside, binary32 in and out; column-major
+// matrices as in rmagine's Matrix3x3).  rotations == 0 gives the usual form
+// (W >= 0 on the diagonal, sorted descending; U, V orthogonal); rotations != 0
+// gives U and V both rotations with the last singular value carrying the sign
+// of det A, the form the Umeyama step uses.
+__global__ void k_svd3(const float* A, float* U, float* W, float* w, float* V, uint32_t n, int rotations) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  M3d C, u, v;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) C.a[r][c] = A[9ull * b + 3 * c + r];
+  double sv[3];
+  svd3_rot(C, u, sv, v);
+  if (!rotations) {
+    if (sv[2] < 0.0) {  // move the sign into U's third column
+      sv[2] = -sv[2];
+      for (int k = 0; k < 3; ++k) u.a[k][2] = -u.a[k][2];
+    }
+    // W >= 0 in descending order (rank-deficient inputs can leave the two
+    // smallest values swapped at rounding level): swap columns of U and V alike
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2 - i; ++j)
+        if (sv[j] < sv[j + 1]) {
+          const double t = sv[j]; sv[j] = sv[j + 1]; sv[j + 1] = t;
+          for (int k = 0; k < 3; ++k) {
+            double x = u.a[k][j]; u.a[k][j] = u.a[k][j + 1]; u.a[k][j + 1] = x;
+            x = v.a[k][j]; v.a[k][j] = v.a[k][j + 1]; v.a[k][j + 1] = x;
+          }
+        }
+  }
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 3; ++c) {
+      if (U) U[9ull * b + 3 * c + r] = (float)u.a[r][c];
+      if (V) V[9ull * b + 3 * c + r] = (float)v.a[r][c];
+      if (W) W[9ull * b + 3 * c + r] = r == c ? (float)sv[r] : 0.0f;
+    }
+    if (w) w[3ull * b + r] = (float)sv[r];
+  }
+}
+
+extern "C" int rmg_svd3(const float* A, float* U, float* W, float* w, float* V, uint32_t n, int rotations,
+                        void* stream) {
+  if (n == 0) return RMG_OK;
+  if (!A) return fail(RMG_ERR_INVALID_ARG, "rmg_svd3: A is NULL");
+  if (!U && !W && !w && !V) return RMG_OK;
+  const uint64_t grid = (n + 127ull) / 128ull;
+  k_svd3<<<(unsigned)grid, 128, 0, as_stream(stream)>>>(A, U, W, w, V, n, rotations);
+  return cuda_status(cudaGetLastError(), "k_svd3");
+}
+
 extern "C" int rmg_umeyama_transform(const rmg_cross_stats* stats, uint32_t n, rmg_transform* out, void* stream) {
   if (n == 0) return RMG_OK;
   if (!stats || !out) return fail(RMG_ERR_INVALID_ARG, "rmg_umeyama_transform: NULL argument");

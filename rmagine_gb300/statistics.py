@@ -116,6 +116,23 @@ def umeyama_transform(stats: torch.Tensor) -> torch.Tensor:
     return out
 
 
+def svd(A, rotations: bool = False):
+    """Batched 3x3 SVD A = U W V^T (rmagine's svd(As, Us, Ws, Vs), memory_math.cuh:561-578).
+    A: [..., 3, 3] (row-major here; the library takes rmagine's column-major Matrix3x3).  Returns
+    (U, w, V) as [..., 3, 3], [..., 3], [..., 3, 3] float32 CUDA tensors.  rotations=False: w >= 0
+    sorted descending, U, V orthogonal; rotations=True: U, V rotations, w[..., 2] carries the sign of
+    det A."""
+    A = _dev(A, torch.float32)
+    shape = A.shape[:-2]
+    Acm = A.reshape(-1, 3, 3).transpose(1, 2).contiguous()  # column-major records
+    n = Acm.shape[0]
+    U = torch.empty((n, 3, 3), dtype=torch.float32, device="cuda")
+    V = torch.empty((n, 3, 3), dtype=torch.float32, device="cuda")
+    w = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    L.call("rmg_svd3", _ptr(Acm), _ptr(U), None, _ptr(w), _ptr(V), n, 1 if rotations else 0, _stream())
+    return (U.transpose(1, 2).reshape(*shape, 3, 3), w.reshape(*shape, 3), V.transpose(1, 2).reshape(*shape, 3, 3))
+
+
 def umeyama_backward(dataset, model, stats, grad_R=None, grad_t=None, pre=None, params=None, dataset_mask=None,
                      model_mask=None, dataset_ids=None, model_ids=None):
     """dL/d(dataset points), dL/d(model points) of L(R, t) with the given upstream gradients."""

@@ -10,6 +10,7 @@
 #include <memory>
 #include <vector>
 #include <sstream>
+#include <type_traits>
 
 #include "rmagine_gb300.hpp"
 
@@ -327,6 +328,172 @@ static void test_builders_and_host_form() {
           "single-pose simulate differs from the batch");
 }
 
+
+// MemoryView slices, the const-view overloads, setTsb(MemoryView), the pinned / managed memory
+// kinds and the factory (SphereSimulatorEmbree.hpp:140-155, SimulatorEmbree.hpp:60,
+// MemoryCuda.hpp:78-89, Simulator.hpp:52-78).
+static void test_views_kinds_and_factory(const rm::MapPtr& map) {
+  rm::SphericalModel model;
+  model.theta = {(float)-M_PI, (float)(0.4 * M_PI / 180.0), 900};
+  model.phi = {(float)(-15.0 * M_PI / 180.0), (float)(2.0 * M_PI / 180.0), 16};
+  model.range = {0.0f, 100.0f};
+  auto sim = rm::make_simulator<rm::SphericalModel, rm::GB300>(map);
+  static_assert(std::is_same<decltype(sim), rm::SimulatorPtr<rm::SphericalModel, rm::GB300>>::value, "factory type");
+  static_assert(std::is_same<decltype(rm::make_simulator<rm::SphericalModel, rm::NoneType>()), bool>::value,
+                "unknown backend");
+  sim->setModel(model);
+  rm::Memory<rm::Transform, rm::RAM> T(20);
+  for (int i = 0; i < 20; ++i) {
+    T[i] = rm::Transform::Identity();
+    T[i].t = {0.01f * i, -0.005f * i, 0.002f * i};
+    T[i].R = {0.0f, 0.0f, std::sin(0.05f * i), std::cos(0.05f * i)};
+  }
+  const size_t n = model.size();
+  auto full = sim->simulate<rm::Bundle<rm::Ranges<rm::RAM>, rm::FaceIds<rm::RAM>>>(T);
+  // a slice of the poses gives the matching slice of the results
+  rm::Bundle<rm::Ranges<rm::RAM>, rm::FaceIds<rm::RAM>> part;
+  rm::resize_memory_bundle<rm::RAM>(part, model.getWidth(), model.getHeight(), 5);
+  sim->simulate(T(10, 15), part);
+  fail_if(std::memcmp(part.ranges.raw(), full.ranges.raw() + 10 * n, 5 * n * sizeof(float)) != 0, "slice ranges");
+  fail_if(std::memcmp(part.face_ids.raw(), full.face_ids.raw() + 10 * n, 5 * n * 4) != 0, "slice face ids");
+  // a view of const poses
+  const rm::Memory<rm::Transform, rm::RAM>& Tc = T;
+  rm::MemoryView<const rm::Transform, rm::RAM> cv = Tc(3, 4);
+  auto one = sim->simulate<rm::Bundle<rm::Ranges<rm::RAM>>>(cv);
+  fail_if(std::memcmp(one.ranges.raw(), full.ranges.raw() + 3 * n, n * sizeof(float)) != 0, "const view");
+  // pinned poses and a pinned bundle take the host form; managed poses the device form
+  rm::Memory<rm::Transform, rm::RAM_CUDA> Tp;
+  Tp = T;
+  rm::Bundle<rm::Ranges<rm::RAM_CUDA>> pinned;
+  rm::resize_memory_bundle<rm::RAM_CUDA>(pinned, model.getWidth(), model.getHeight(), 20);
+  sim->simulate(Tp, pinned);
+  fail_if(std::memcmp(pinned.ranges.raw(), full.ranges.raw(), 20 * n * sizeof(float)) != 0, "pinned kinds");
+  rm::Memory<rm::Transform, rm::UNIFIED_CUDA> Tu;
+  Tu = T;
+  rm::Bundle<rm::Ranges<rm::UNIFIED_CUDA>> managed;
+  rm::resize_memory_bundle<rm::UNIFIED_CUDA>(managed, model.getWidth(), model.getHeight(), 20);
+  sim->simulate(Tu, managed);
+  rm::cuda_check(cudaDeviceSynchronize(), "sync");
+  fail_if(std::memcmp(managed.ranges.raw(), full.ranges.raw(), 20 * n * sizeof(float)) != 0, "managed kinds");
+  // setTsb from a view: the first transform
+  rm::Memory<rm::Transform, rm::RAM> Tsb(2);
+  Tsb[0] = rm::Transform::Identity();
+  Tsb[0].t = {0.1f, 0.0f, 0.0f};
+  Tsb[1] = rm::Transform::Identity();
+  sim->setTsb(Tsb(0, 1));
+  fail_if(sim->Tsb().t.x != 0.1f, "setTsb(MemoryView)");
+  auto shifted = sim->simulate<rm::Bundle<rm::Ranges<rm::RAM>>>(rm::Transform::Identity());
+  // the ray at theta = 0 (1 degree up) meets the cube's x = 0.5 wall: 0.1 m closer, range x 0.4 / 0.5
+  const uint32_t fwd = model.getBufferId(model.phi.size / 2, model.theta.size / 2);
+  fail_if(std::fabs(shifted.ranges[fwd] - 0.8f * full.ranges[fwd]) > 1e-5f, "setTsb moves the sensor");
+}
+
+// The differentiable forms: the range adjoint (device and host forms agree; a step against the
+// gradient lowers the loss) and the Umeyama backward (exact translation identities).
+static void test_gradients(const rm::MapPtr& map) {
+  rm::SphericalModel model;
+  model.theta = {(float)-M_PI, (float)(2.0 * M_PI / 256.0), 256};
+  model.phi = {(float)(-60.0 * M_PI / 180.0), (float)(120.0 * M_PI / 180.0 / 31.0), 32};
+  model.range = {0.0f, 100.0f};
+  rm::SphereSimulatorGB300 sim(map);
+  sim.setModel(model);
+  rm::Memory<rm::Transform, rm::RAM> truth(4), est(4);
+  for (int i = 0; i < 4; ++i) {
+    truth[i] = rm::Transform::Identity();
+    truth[i].t = {0.05f * i - 0.1f, 0.02f, -0.03f};
+    est[i] = truth[i];
+    est[i].t.x += 0.04f;
+    est[i].t.z -= 0.03f;
+  }
+  auto obs = sim.simulate<rm::Bundle<rm::Ranges<rm::RAM>>>(truth);
+  rm::Memory<float, rm::RAM> grad_h, loss_h;
+  sim.rangePoseGrad(est, obs.ranges, 0.2f, grad_h, &loss_h);
+  rm::Memory<rm::Transform, rm::VRAM_CUDA> est_d;
+  est_d = est;
+  rm::Memory<float, rm::VRAM_CUDA> obs_d, grad_d, loss_d;
+  obs_d = obs.ranges;
+  sim.rangePoseGrad(est_d, obs_d, 0.2f, grad_d, &loss_d);
+  rm::Memory<float, rm::RAM> grad_b, loss_b;
+  grad_b = grad_d;
+  loss_b = loss_d;
+  fail_if(std::memcmp(grad_b.raw(), grad_h.raw(), 24 * 4) != 0, "rangePoseGrad: host and device forms differ");
+  fail_if(std::memcmp(loss_b.raw(), loss_h.raw(), 4 * 4) != 0, "rangePoseGrad: host and device losses differ");
+  for (int i = 0; i < 4; ++i) {
+    fail_if(!(loss_h[i] > 0.0f), "rangePoseGrad: loss");
+    // the translation error is (+0.04, 0, -0.03): the gradient points along it
+    fail_if(!(grad_h[6 * i + 0] > 0.0f && grad_h[6 * i + 2] < 0.0f), "rangePoseGrad: gradient direction");
+  }
+  // Umeyama backward: shifting all model points by d moves t by d (sum of model gradients = dL/dt);
+  // shifting all dataset points by d moves t by -R d (sum of dataset gradients = -R^T dL/dt)
+  const uint32_t N = 64;
+  rm::Memory<rm::Vector3, rm::RAM> d(N), m(N);
+  for (uint32_t i = 0; i < N; ++i) {
+    const float a = 0.37f * i, b = 0.11f * i * i;
+    d[i] = {std::cos(a) * 3.0f, std::sin(b) * 2.0f, 0.05f * i};
+    m[i] = {-d[i].y + 1.0f, d[i].x - 0.5f, d[i].z + 0.25f};  // 90 degrees about z, shifted
+  }
+  rm::Memory<rm::Vector3, rm::VRAM_CUDA> dd, md, gd, gm;
+  dd = d;
+  md = m;
+  rm::Memory<rm::CrossStatistics, rm::VRAM_CUDA> st;
+  rm::Memory<rm::Transform, rm::VRAM_CUDA> Td;
+  const rm::UmeyamaReductionConstraints params{1e30f, 0, 0};
+  rm::statistics_p2p(dd, md, params, 1, st, &Td);
+  rm::Memory<float, rm::RAM> gR_h(9), gt_h(3);
+  for (int k = 0; k < 9; ++k) gR_h[k] = 0.1f * (k - 4);
+  gt_h[0] = 1.0f; gt_h[1] = -2.0f; gt_h[2] = 0.5f;
+  rm::Memory<float, rm::VRAM_CUDA> gR, gt;
+  gR = gR_h;
+  gt = gt_h;
+  rm::umeyama_backward(dd, md, params, 1, st, &gR, &gt, &gd, &gm);
+  rm::Memory<rm::Vector3, rm::RAM> gd_h, gm_h;
+  gd_h = gd;
+  gm_h = gm;
+  double sm[3] = {0, 0, 0}, sd[3] = {0, 0, 0};
+  for (uint32_t i = 0; i < N; ++i) {
+    sm[0] += gm_h[i].x; sm[1] += gm_h[i].y; sm[2] += gm_h[i].z;
+    sd[0] += gd_h[i].x; sd[1] += gd_h[i].y; sd[2] += gd_h[i].z;
+  }
+  // R = 90 degrees about z: R^T gt = (gt.y, -gt.x, gt.z)
+  const double want_d[3] = {-gt_h[1], gt_h[0], -gt_h[2]};
+  for (int k = 0; k < 3; ++k) {
+    fail_if(std::fabs(sm[k] - gt_h[k]) > 1e-4, "umeyama_backward: sum of model gradients");
+    fail_if(std::fabs(sd[k] - want_d[k]) > 1e-4, "umeyama_backward: sum of dataset gradients");
+  }
+}
+
+// Batched SVD of rmagine's column-major Matrix3x3 records (tests/cuda/math_svd.cpp:38-109).
+static void test_svd() {
+  const size_t n = 1000;
+  rm::Memory<float, rm::RAM> A(9 * n);
+  uint32_t x = 12345u;
+  for (size_t i = 0; i < 9 * n; ++i) {
+    x = x * 1664525u + 1013904223u;
+    A[i] = (float)((x >> 8) * (1.0 / 16777216.0) * 2.0 - 1.0);
+  }
+  rm::Memory<float, rm::VRAM_CUDA> Ad, Ud, Wd, Vd;
+  Ad = A;
+  rm::svd(Ad, Ud, Wd, Vd);
+  rm::Memory<float, rm::RAM> U, W, V;
+  U = Ud;
+  W = Wd;
+  V = Vd;
+  double err = 0.0;
+  for (size_t b = 0; b < n; ++b) {
+    const float* u = U.raw() + 9 * b;  // column-major: element (r, c) at 3 c + r
+    const float* w = W.raw() + 9 * b;
+    const float* v = V.raw() + 9 * b;
+    fail_if(w[0] < w[4] || w[4] < w[8] || w[8] < 0.0f, "svd: W sorted, non-negative");
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) {
+        double acc = 0.0;
+        for (int k = 0; k < 3; ++k) acc += (double)u[3 * k + r] * w[4 * k] * v[3 * k + c];
+        err = std::fmax(err, std::fabs(acc - A[9 * b + 3 * c + r]));
+      }
+  }
+  fail_if(err > 2e-6, "svd: U W V^T != A");
+}
+
 int main() {
   try {
     auto map = make_cube_map();
@@ -341,6 +508,9 @@ int main() {
     test_files(map);
     test_autotune(map);
     test_builders_and_host_form();
+    test_views_kinds_and_factory(map);
+    test_gradients(map);
+    test_svd();
     fail_if(map->status() != 0, "device status");
   } catch (const std::exception& e) {
     std::fprintf(stderr, "FAILED: %s\n", e.what());
