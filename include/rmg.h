@@ -123,8 +123,9 @@ typedef struct rmg_launch_config {
   uint32_t refill;        /* 0: one tile per warp.  1..32: persistent warps that hand new rays to
                              idle lanes whenever fewer than `refill` lanes are busy (stack_depth 8 or 16) */
   uint32_t chunk;         /* refill mode: tiles a warp takes from the work counter at a time (>= 1) */
-  uint32_t bvh_width;     /* 2: walk the binary tree; 4: the 4-wide tree collapsed from it (when the map
-                             has one and refill == 0); 0: the default.  Results are identical. */
+  uint32_t bvh_width;     /* 2: walk the binary tree; 4: the 4-wide tree collapsed from it; 8: the 8-wide
+                             tree with quantized boxes collapsed from it (4 and 8 when the map has the tree
+                             and refill == 0); 0: the default.  Results are identical. */
   uint32_t packet;        /* 1: the warp walks the binary tree together (a node is visited when any of
                              its 32 rays needs it; refill == 0, bvh_width != 4); 0: each ray walks alone;
                              2: the default.  Results are identical. */
@@ -135,7 +136,8 @@ typedef struct rmg_map_info {
   uint32_t n_faces;
   uint32_t n_nodes;       /* internal BVH nodes */
   uint32_t depth;         /* longest root-to-leaf path (edges) */
-  uint64_t device_bytes;  /* BVH nodes (binary and 4-wide) + packed triangles + vertices + faces */
+  uint64_t device_bytes;  /* BVH nodes (binary, 4-wide, 8-wide) + packed triangles (and their 8-wide copy)
+                             + vertices + faces */
   float bounds_lo[3];
   float bounds_hi[3];
 } rmg_map_info;
@@ -186,6 +188,16 @@ int rmg_map_build_ex(const rmg_vec3* vertices, uint32_t n_vertices,
  * existing tree bottom-up without re-sorting.  Needs exclusive use of the
  * map (no simulate in flight).  Synchronises with `stream`. */
 int rmg_map_refit(rmg_map* map, const rmg_vec3* vertices, uint32_t n_vertices, void* stream);
+
+/* Adds the 8-wide tree with quantized child boxes (80-byte nodes after Ylitie,
+ * Karras and Laine, HPG 2017) collapsed from the map's binary tree, for
+ * rmg_launch_config.bvh_width = 8; refits refresh it.  Opt-in, as Embree's
+ * scene build options choose its BVH (EmbreeScene.hpp:61-83): on the
+ * workloads measured here the binary walk is faster, so maps do not build it
+ * by default.  Not concurrent with simulate calls on the same map; synchronises
+ * with `stream`.  A map whose boxes cannot be quantized (extents beyond
+ * 255 * 2^60) keeps no 8-wide tree. */
+int rmg_map_build_wide8(rmg_map* map, void* stream);
 int rmg_map_destroy(rmg_map* map);
 int rmg_map_info_get(const rmg_map* map, rmg_map_info* out);
 /* Copies the tree to host memory (tests): nodes = n_nodes*16 floats/ints

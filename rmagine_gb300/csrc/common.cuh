@@ -53,13 +53,30 @@ struct __align__(16) Node4 {
   int4 meta;
 };
 
+// 8-wide node with quantized child boxes, 80 B (wide8.cu):
+//   h0 = (p.x, p.y, p.z, e.x + 127 | (e.y + 127) << 8 | (e.z + 127) << 16 | imask << 24 as bits)
+//   h1 = (child_base, tri_base, valid, 0)
+//   qx = (lo.x slots 0-3, lo.x slots 4-7, hi.x slots 0-3, hi.x slots 4-7), one byte per slot; qy, qz alike
+// Slot k's box is [p + 2^e * q_lo, p + 2^e * q_hi] per axis, containing the
+// child's exact box.  valid / imask: bit k set when slot k holds a child / an
+// internal child.  Internal children are nodes child_base + (internal slots
+// below k), leaf children triangles tri_base + (leaf slots below k) of tris8.
+struct __align__(16) Node8 {
+  float4 h0;
+  uint4 h1;
+  uint4 qx, qy, qz;
+};
+
 static_assert(sizeof(Node) == 64, "node record is 64 B");
+static_assert(sizeof(Node8) == 80, "8-wide node record is 80 B");
 static_assert(sizeof(Node4) == 128, "wide node record is 128 B");
 static_assert(sizeof(Tri) == 48, "triangle record is 48 B");
 
 // Device error word values are rmg_status codes.
 struct DeviceMap {
   const Node4* nodes4;  // the 4-wide tree, or NULL
+  const Node8* nodes8;  // the 8-wide tree, or NULL
+  const Tri* tris8;     // its triangles (a permutation of tris), or NULL
   const Node* nodes;
   const Tri* tris;
   int n_nodes;

@@ -30,6 +30,13 @@ struct rmg_map {
   int* d_src4;                // 4*n_nodes4: binary record (2*parent + side) of each slot, -1 empty
   uint32_t n_nodes4;
   uint32_t depth4;            // levels of the wide tree
+  // 8-wide tree with quantized boxes (wide8.cu)
+  rmg::Node8* d_nodes8;       // n_nodes8
+  int* d_src8;                // 8*n_nodes8: binary record of each slot, -1 empty
+  rmg::Tri* d_tris8;          // n_faces: the triangles in 8-wide leaf order
+  int* d_tri8_src;            // n_faces: packed triangle of each d_tris8 entry
+  uint32_t n_nodes8;
+  uint32_t depth8;            // levels of the 8-wide tree
 };
 
 struct rmg_sensor {
@@ -76,6 +83,9 @@ int wide_build(rmg_map* m, cudaStream_t st);
 int sah_build_topology(rmg_map* m, cudaStream_t st, uint32_t* d_order);
 int wide_refit(rmg_map* m, cudaStream_t st);
 void wide_free(rmg_map* m);
+int wide8_build(rmg_map* m, cudaStream_t st);
+int wide8_refit(rmg_map* m, cudaStream_t st);
+void wide8_free(rmg_map* m);
 SensorDev device_view(const rmg_sensor* s);
 
 int device_sm_count();

@@ -325,6 +325,8 @@ void update_info(rmg_map* m, cudaStream_t st) {
 DeviceMap device_view(const rmg_map* m) {
   DeviceMap d;
   d.nodes4 = m->d_nodes4;
+  d.nodes8 = m->d_nodes8;
+  d.tris8 = m->d_tris8;
   d.nodes = m->d_nodes;
   d.tris = m->d_tris;
   d.n_nodes = (int)m->n_nodes;
@@ -337,6 +339,12 @@ DeviceMap device_view(const rmg_map* m) {
 }  // namespace rmg
 
 using namespace rmg;
+
+extern "C" int rmg_map_build_wide8(rmg_map* m, void* stream) {
+  if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_build_wide8: map is NULL");
+  if (m->n_faces == 0 || m->d_nodes8) return RMG_OK;
+  return wide8_build(m, as_stream(stream));
+}
 
 extern "C" int rmg_map_build(const rmg_vec3* vertices, uint32_t n_vertices, const rmg_face* faces,
                              uint32_t n_faces, void* stream, rmg_map** out) {
@@ -537,7 +545,9 @@ extern "C" int rmg_map_info_get(const rmg_map* m, rmg_map_info* out) {
   out->depth = m->depth;
   out->device_bytes = (uint64_t)m->n_nodes * sizeof(Node) + (uint64_t)m->n_faces * sizeof(Tri) +
                       12ull * m->n_vertices + 12ull * m->n_faces +
-                      (uint64_t)m->n_nodes4 * (sizeof(Node4) + 4 * sizeof(int));
+                      (uint64_t)m->n_nodes4 * (sizeof(Node4) + 4 * sizeof(int)) +
+                      (uint64_t)m->n_nodes8 * (sizeof(Node8) + 8 * sizeof(int)) +
+                      (m->d_tris8 ? (uint64_t)m->n_faces * sizeof(Tri) : 0ull);
   for (int k = 0; k < 3; ++k) { out->bounds_lo[k] = m->lo[k]; out->bounds_hi[k] = m->hi[k]; }
   return RMG_OK;
 }

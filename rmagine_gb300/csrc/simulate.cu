@@ -15,6 +15,11 @@
 #define RMG_DEFAULT_WIDE 0
 #endif
 
+// 8-wide quantized walk when the launch config leaves the width open.
+#ifndef RMG_DEFAULT_WIDE8
+#define RMG_DEFAULT_WIDE8 0
+#endif
+
 // Warp-synchronous packet walk when the launch config leaves the choice open.
 #ifndef RMG_DEFAULT_PACKET
 #define RMG_DEFAULT_PACKET 0
@@ -48,8 +53,8 @@ int check_config(const rmg_launch_config& c) {
   if (c.refill && c.stack_depth == 0)
     return fail(RMG_ERR_UNSUPPORTED, "launch config: refill mode needs stack_depth 8 or 16");
   if (c.refill && (c.chunk < 1 || c.chunk > 1024)) return fail(RMG_ERR_UNSUPPORTED, "launch config: chunk 1..1024");
-  if (c.bvh_width != 0 && c.bvh_width != 2 && c.bvh_width != 4)
-    return fail(RMG_ERR_UNSUPPORTED, "launch config: bvh_width must be 0, 2 or 4");
+  if (c.bvh_width != 0 && c.bvh_width != 2 && c.bvh_width != 4 && c.bvh_width != 8)
+    return fail(RMG_ERR_UNSUPPORTED, "launch config: bvh_width must be 0, 2, 4 or 8");
   if (c.packet > 2) return fail(RMG_ERR_UNSUPPORTED, "launch config: packet must be 0, 1 or 2");
   return RMG_OK;
 }
@@ -84,9 +89,16 @@ int make_trace_params(const rmg_map* map, const rmg_sensor* sensor, const rmg_tr
   P.wide = (cfg.bvh_width != 2 && cfg.refill == 0 && map->d_nodes4 && 3 * map->depth4 <= (unsigned)kStack4 &&
             RMG_DEFAULT_WIDE) ? 1 : 0;
   if (cfg.bvh_width == 4 && cfg.refill == 0 && map->d_nodes4 && 3 * map->depth4 <= (unsigned)kStack4) P.wide = 1;
+  // 8-wide quantized walk: a pending-children stack of kStack8 entries holds trees of kStack8 + 1 levels
+  const bool have8 = map->d_nodes8 && map->depth8 <= (unsigned)kStack8 + 1u;
+  P.wide8 = (have8 && cfg.refill == 0 && (cfg.bvh_width == 8 || (cfg.bvh_width == 0 && RMG_DEFAULT_WIDE8))) ? 1 : 0;
+  if (P.wide8) {
+    P.wide = 0;
+    P.map.tris = map->d_tris8;  // h.tri of this walk indexes the 8-wide triangle copy
+  }
   // warp-synchronous packet walk: binary tree, full stack
   const bool want_packet = cfg.packet == 1 || (cfg.packet == 2 && RMG_DEFAULT_PACKET);
-  P.packet = (want_packet && !P.wide && cfg.refill == 0 && P.full_stack) ? 1 : 0;
+  P.packet = (want_packet && !P.wide && !P.wide8 && cfg.refill == 0 && P.full_stack) ? 1 : 0;
   return RMG_OK;
 }
 
@@ -180,7 +192,7 @@ extern "C" int rmg_autotune_launch_config(const rmg_map* map, const rmg_sensor* 
   rmg_launch_config base;
   default_config(sensor, &base);
   struct Walk { uint32_t bvh_width, packet; };
-  const Walk walks[3] = {{2, 0}, {2, 1}, {4, 0}};
+  const Walk walks[4] = {{2, 0}, {2, 1}, {4, 0}, {8, 0}};
   const uint32_t tiles[3][2] = {{8, 4}, {16, 2}, {4, 8}};
   const uint32_t warps[2] = {4, 2};
   cudaEvent_t e0, e1;
@@ -202,7 +214,8 @@ extern "C" int rmg_autotune_launch_config(const rmg_map* map, const rmg_sensor* 
         if (check_config(c) != RMG_OK) continue;
         TraceParams P;
         make_trace_params(map, sensor, Tsb, Tbm, n_poses, out, c, P);
-        if ((w.bvh_width == 4 && !P.wide) || (w.packet == 1 && !P.packet)) continue;  // not available here
+        if ((w.bvh_width == 4 && !P.wide) || (w.bvh_width == 8 && !P.wide8) || (w.packet == 1 && !P.packet))
+          continue;  // not available here
         s = launch_plain(P, sensor, c, st);
         if (s != RMG_OK) break;
         std::vector<float> ms;

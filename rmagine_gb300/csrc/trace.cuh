@@ -80,13 +80,14 @@ __device__ __forceinline__ RayBox make_raybox(const V& o, const V& d) {
   r.ix = fabsf(d.x) > 1e-20f ? __frcp_rn(d.x) : copysignf(1e20f, d.x);
   r.iy = fabsf(d.y) > 1e-20f ? __frcp_rn(d.y) : copysignf(1e20f, d.y);
   r.iz = fabsf(d.z) > 1e-20f ? __frcp_rn(d.z) : copysignf(1e20f, d.z);
-  const float oix = o.x * r.ix, oiy = o.y * r.iy, oiz = o.z * r.iz;
+  // explicit roundings: the 8-wide walk's leaf test (leaf_exact) repeats these operations
+  const float oix = __fmul_rn(o.x, r.ix), oiy = __fmul_rn(o.y, r.iy), oiz = __fmul_rn(o.z, r.iz);
   const float kE = 4.76837158e-7f;  // 2^-21
   const float ex = copysignf(fabsf(oix) * kE, r.ix), ey = copysignf(fabsf(oiy) * kE, r.iy),
               ez = copysignf(fabsf(oiz) * kE, r.iz);
-  r.clx = -oix - ex; r.chx = -oix + ex;
-  r.cly = -oiy - ey; r.chy = -oiy + ey;
-  r.clz = -oiz - ez; r.chz = -oiz + ez;
+  r.clx = __fsub_rn(-oix, ex); r.chx = __fadd_rn(-oix, ex);
+  r.cly = __fsub_rn(-oiy, ey); r.chy = __fadd_rn(-oiy, ey);
+  r.clz = __fsub_rn(-oiz, ez); r.chz = __fadd_rn(-oiz, ez);
 #if RMG_SLAB_F32X2
   r.pix = pack2(r.ix, r.ix);
   r.piy = pack2(r.iy, r.iy);
@@ -438,6 +439,175 @@ __device__ __forceinline__ void trace_ray4(const DeviceMap& map, const V& o, con
   }
 }
 
+// Trail tag of the 8-wide walk (trace_ray8).
+constexpr int kWide8TB = 8;
+// Stack of the 8-wide walk: one entry (a node's pending children) per level,
+// so trees of up to kStack8 + 1 levels (the launcher checks the built depth);
+// a deeper push (a corrupt tree) ends in the budget error.
+constexpr int kStack8 = 24;
+
+// One quantized plane offset as a float: 2^23 + q exactly (the byte q = byte
+// k of w in the mantissa of 2^23), one byte permute instead of a conversion.
+__device__ __forceinline__ float q_magic(uint32_t w, uint32_t k) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | k));
+}
+
+// Slot order -> key order: bit s of m moves to bit s ^ oct.
+__device__ __forceinline__ uint32_t octant_order(uint32_t m, uint32_t oct) {
+  if (oct & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+  if (oct & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+  if (oct & 4u) m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
+  return m;
+}
+
+// Near and far plane addends of one axis of an 8-wide node, for the plane
+// distance t = fma(2^23 + q, s, addend) with s = 2^e / d:
+//   c = fma(p, 1/d, -o/d) is the distance of the grid origin plane, and the
+//   addend is c -+ eps - 2^23 s.  eps bounds every rounding outward: -o/d and
+//   c carry |o/d| 2^-24 and |c| 2^-24, forming the addend another |c| 2^-24 +
+//   |s| / 2 (the 2^23 s term), the fma one relative rounding of t; eps =
+//   (|o/d| + 3|c|) 2^-21 + 2.0625 |s| covers them with the relative widening
+//   kWiden of the far plane (|t| <= |c| + 256 |s|) folded in.
+__device__ __forceinline__ void wide8_axis(float p, uint32_t ebyte, float inv, float noi, float eo,
+                                           float& s, float& an, float& af) {
+  s = __int_as_float(__float_as_int(inv) + (((int)ebyte - 127) << 23));  // inv * 2^e, exact
+  const float c = fmaf(p, inv, noi);
+  const float as = fabsf(s);
+  const float eps = fmaf(as, 2.0625f, fmaf(fabsf(c), 1.430511474609375e-6f, eo));  // 3 * 2^-21
+  an = fmaf(-8388608.0f, s, c - eps);
+  af = fmaf(-8388608.0f, s, c + eps);
+}
+
+// A leaf of the 8-wide tree: the triangle's exact box (the min / max of its
+// vertices, as the binary builders store it) tested with the binary walk's
+// slab arithmetic (make_raybox / slab / visit, operation for operation), then
+// the triangle.  The quantized boxes alone would be conservative, but the
+// binary walk is not conservative everywhere: a ray lying exactly in a box
+// face (a zero direction component with the origin on that plane) enters the
+// box or not by the sign of the zero (1/d = +-1e20), as in Embree.  Testing a
+// leaf only when the binary walk's own test admits it keeps the closest hit of
+// both walks identical in that case too.
+__device__ __forceinline__ void leaf_exact(const DeviceMap& map, const RayW& rw, int k, float ix, float iy, float iz,
+                                           float nx, float ny, float nz, float ex, float ey, float ez, Hit& h) {
+  const Tri* tp = map.tris + k;
+  const float4 p0 = __ldg(&tp->v0), p1 = __ldg(&tp->v1), p2 = __ldg(&tp->v2);
+  const float sx = copysignf(ex, ix), sy = copysignf(ey, iy), sz = copysignf(ez, iz);
+  const float x0 = __fmaf_rn(fminf(fminf(p0.x, p1.x), p2.x), ix, __fsub_rn(nx, sx));
+  const float x1 = __fmaf_rn(fmaxf(fmaxf(p0.x, p1.x), p2.x), ix, __fadd_rn(nx, sx));
+  const float y0 = __fmaf_rn(fminf(fminf(p0.y, p1.y), p2.y), iy, __fsub_rn(ny, sy));
+  const float y1 = __fmaf_rn(fmaxf(fmaxf(p0.y, p1.y), p2.y), iy, __fadd_rn(ny, sy));
+  const float z0 = __fmaf_rn(fminf(fminf(p0.z, p1.z), p2.z), iz, __fsub_rn(nz, sz));
+  const float z1 = __fmaf_rn(fmaxf(fmaxf(p0.z, p1.z), p2.z), iz, __fadd_rn(nz, sz));
+  const float tmin = fmax3f(fminf(x0, x1), fminf(y0, y1), fmaxf(fminf(z0, z1), 0.0f));
+  const float tmax = fmin3f(fmaxf(x0, x1), fmaxf(y0, y1), fmaxf(z0, z1));
+  if (!visit(tmin, tmax, h.t)) return;
+  float t;
+  if (tri_hit(rw, p0, p1, p2, h.t, t)) {
+    const uint32_t f = __float_as_uint(p0.w);
+    if (t < h.t || f < h.face) { h.t = t; h.tri = k; h.face = f; }
+  }
+}
+
+// Closest hit through the 8-wide quantized tree (wide8.cu).  Every child box
+// of a visited node is tested (uniform work for the warp), leaf children's
+// triangles are intersected at once, and the internal children that the ray
+// enters are visited in the order of the ray's octant (nearest slots first);
+// a node's pending children wait on the stack as one entry (node base,
+// remaining children, internal-slot mask).  The boxes are conservative and
+// the triangle test and tie rule are those of the binary walk, so the hit
+// (t, face) is identical; h.tri indexes map.tris, which the launcher points
+// at the 8-wide tree's triangle copy.
+__device__ __forceinline__ void trace_ray8(const DeviceMap& map, const V& o, const V& d, float tfar,
+                                           unsigned budget, Hit& h, bool& over_budget) {
+  h.t = tfar;
+  h.tri = -1;
+  h.face = 0xffffffffu;
+  if (map.root < 0) return;
+  const RayW rw = make_rayw(o, d);
+  const float ix = fabsf(d.x) > 1e-20f ? __frcp_rn(d.x) : copysignf(1e20f, d.x);
+  const float iy = fabsf(d.y) > 1e-20f ? __frcp_rn(d.y) : copysignf(1e20f, d.y);
+  const float iz = fabsf(d.z) > 1e-20f ? __frcp_rn(d.z) : copysignf(1e20f, d.z);
+  const float nx = -__fmul_rn(o.x, ix), ny = -__fmul_rn(o.y, iy), nz = -__fmul_rn(o.z, iz);
+  const float kE = 4.76837158e-7f;  // 2^-21
+  const float ex = fabsf(nx) * kE, ey = fabsf(ny) * kE, ez = fabsf(nz) * kE;
+  const uint32_t oct = (ix < 0.f ? 1u : 0u) | (iy < 0.f ? 2u : 0u) | (iz < 0.f ? 4u : 0u);
+  uint2 stack[kStack8];
+  int sp = 0;
+  uint32_t cur_base = 0, cur_bits = 0;  // pending children in key order (bits 0-7) | internal slots << 8
+  int node = 0;
+  unsigned steps = 0;
+  for (;;) {
+    if (++steps > budget) { over_budget = true; break; }
+    const Node8* np = map.nodes8 + node;
+    const float4 h0 = __ldg(&np->h0);
+    const uint4 h1 = __ldg(&np->h1);
+    const uint4 qx = __ldg(&np->qx), qy = __ldg(&np->qy), qz = __ldg(&np->qz);
+    const uint32_t meta = __float_as_uint(h0.w);
+    float sx, sy, sz, anx, afx, any, afy, anz, afz;
+    wide8_axis(h0.x, meta & 0xffu, ix, nx, ex, sx, anx, afx);
+    wide8_axis(h0.y, (meta >> 8) & 0xffu, iy, ny, ey, sy, any, afy);
+    wide8_axis(h0.z, (meta >> 16) & 0xffu, iz, nz, ez, sz, anz, afz);
+    // near / far plane bytes of each axis by the ray's direction
+    const uint32_t nx0 = ix >= 0.f ? qx.x : qx.z, nx1 = ix >= 0.f ? qx.y : qx.w;
+    const uint32_t fx0 = ix >= 0.f ? qx.z : qx.x, fx1 = ix >= 0.f ? qx.w : qx.y;
+    const uint32_t ny0 = iy >= 0.f ? qy.x : qy.z, ny1 = iy >= 0.f ? qy.y : qy.w;
+    const uint32_t fy0 = iy >= 0.f ? qy.z : qy.x, fy1 = iy >= 0.f ? qy.w : qy.y;
+    const uint32_t nz0 = iz >= 0.f ? qz.x : qz.z, nz1 = iz >= 0.f ? qz.y : qz.w;
+    const uint32_t fz0 = iz >= 0.f ? qz.z : qz.x, fz1 = iz >= 0.f ? qz.w : qz.y;
+    const float cull = h.t * kWiden;
+    uint32_t hit = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const uint32_t b = (uint32_t)(k & 3);
+      const float tnx = fmaf(q_magic(k < 4 ? nx0 : nx1, b), sx, anx);
+      const float tfx = fmaf(q_magic(k < 4 ? fx0 : fx1, b), sx, afx);
+      const float tny = fmaf(q_magic(k < 4 ? ny0 : ny1, b), sy, any);
+      const float tfy = fmaf(q_magic(k < 4 ? fy0 : fy1, b), sy, afy);
+      const float tnz = fmaf(q_magic(k < 4 ? nz0 : nz1, b), sz, anz);
+      const float tfz = fmaf(q_magic(k < 4 ? fz0 : fz1, b), sz, afz);
+      const float tmin = fmax3f(tnx, tny, fmaxf(tnz, 0.0f));
+      const float tmax = fmin3f(tfx, tfy, fminf(tfz, cull));
+      if (tmin <= tmax) hit |= 1u << k;
+    }
+    const uint32_t valid = h1.z, imask = meta >> 24;
+    hit &= valid;
+    // leaf children: the binary walk's own box test on the triangle's exact
+    // bounds, then the triangle (see leaf_exact)
+    const uint32_t leaves = valid & ~imask;
+    uint32_t lh = hit & ~imask;
+    while (lh) {
+      const uint32_t s = (uint32_t)(__ffs((int)lh) - 1);
+      lh &= lh - 1u;
+      leaf_exact(map, rw, (int)(h1.y + __popc(leaves & ((1u << s) - 1u))), ix, iy, iz, nx, ny, nz, ex, ey, ez, h);
+    }
+    // internal children: nearest-octant slots first
+    const uint32_t km = octant_order(hit & imask, oct);
+    if (km) {
+      if (cur_bits & 0xffu) {
+        if (sp >= kStack8) { over_budget = true; break; }  // only a corrupt tree gets this deep
+        stack[sp++] = make_uint2(cur_base, cur_bits);
+      }
+      cur_base = h1.x;
+      cur_bits = km | (imask << 8);
+    }
+    while (!(cur_bits & 0xffu) && sp > 0) {
+      const uint2 e = stack[--sp];
+      cur_base = e.x;
+      cur_bits = e.y;
+    }
+    if (!(cur_bits & 0xffu)) break;
+    const uint32_t k = (uint32_t)(__ffs((int)(cur_bits & 0xffu)) - 1);
+    cur_bits &= ~(1u << k);
+    const uint32_t s = k ^ oct;
+    node = (int)(cur_base + __popc((cur_bits >> 8) & ((1u << s) - 1u)));
+  }
+  if (over_budget) {
+    h.tri = -1;
+    h.t = tfar;
+    h.face = 0xffffffffu;
+  }
+}
+
 // Trail tag of the warp-synchronous packet walk (trace_ray_packet).
 constexpr int kPacketTB = 1;
 
@@ -535,6 +705,8 @@ __device__ __forceinline__ void trace_ray(const DeviceMap& map, const V& o, cons
                                           unsigned budget, Hit& h, bool& over_budget) {
   if constexpr (TB == kWideTB) {
     trace_ray4(map, o, d, tfar, budget, h, over_budget);
+  } else if constexpr (TB == kWide8TB) {
+    trace_ray8(map, o, d, tfar, budget, h, over_budget);
   } else {
     RayTrav<SS, TB> r;
     ShortStack<SS> stack;
@@ -563,6 +735,7 @@ struct TraceParams {
   int trail_bits;
   int full_stack;  // internal depth < kFullStack: the traversal may keep every pending child on a stack
   int wide;        // walk the 4-wide tree (map.nodes4)
+  int wide8;       // walk the 8-wide quantized tree (map.nodes8; map.tris is then its triangle copy)
   int packet;      // warp-synchronous packet walk of the binary tree
 };
 
@@ -673,8 +846,17 @@ __device__ __forceinline__ void setup_ray(const SensorDev& sen, const Tf& Tsm, u
 #define RMG_TRACE_MIN_BLOCKS 5
 #endif
 
+// The 8-wide walk holds a node's twenty words and three axes of plane
+// addends at once: it gets 64 registers (4 CTAs of 256 threads per SM).
+#ifndef RMG_TRACE8_MIN_BLOCKS
+#define RMG_TRACE8_MIN_BLOCKS 4
+#endif
+
+template <int TB>
+constexpr int trace_min_blocks() { return TB == kWide8TB ? RMG_TRACE8_MIN_BLOCKS : RMG_TRACE_MIN_BLOCKS; }
+
 template <int OK, int SS, int TB>
-__global__ void __launch_bounds__(256, RMG_TRACE_MIN_BLOCKS) k_trace(const TraceParams P) {
+__global__ void __launch_bounds__(256, trace_min_blocks<TB>()) k_trace(const TraceParams P) {
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp >= P.n_tiles) return;
   const uint32_t lane = threadIdx.x & 31;

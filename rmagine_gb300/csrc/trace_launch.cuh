@@ -15,6 +15,10 @@ namespace trace_detail {
 
 template <int OK, int SS>
 cudaError_t by_trail(const TraceParams& P, unsigned grid, unsigned block, cudaStream_t st) {
+  if (P.wide8) {  // the 8-wide quantized tree: same results
+    k_trace<OK, 0, kWide8TB><<<grid, block, 0, st>>>(P);
+    return cudaGetLastError();
+  }
   if (P.wide) {  // the 4-wide tree: same results, fewer and wider visits
     k_trace<OK, 0, kWideTB><<<grid, block, 0, st>>>(P);
     return cudaGetLastError();

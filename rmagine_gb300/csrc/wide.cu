@@ -121,6 +121,7 @@ __global__ void k_wide_refit(const Node* __restrict__ bn, const int* __restrict_
 }  // namespace
 
 void wide_free(rmg_map* m) {
+  wide8_free(m);
   cudaFree(m->d_nodes4);
   cudaFree(m->d_src4);
   m->d_nodes4 = nullptr;
@@ -175,7 +176,8 @@ int wide_refit(rmg_map* m, cudaStream_t st) {
   if (!m->d_nodes4 || m->n_nodes4 == 0) return RMG_OK;
   k_wide_refit<<<(m->n_nodes4 + kBlock4 - 1) / kBlock4, kBlock4, 0, st>>>(m->d_nodes, m->d_src4, m->n_nodes4,
                                                                         m->d_nodes4);
-  return cuda_status(cudaGetLastError(), "k_wide_refit");
+  const int s = cuda_status(cudaGetLastError(), "k_wide_refit");
+  return s == RMG_OK ? wide8_refit(m, st) : s;
 }
 
 }  // namespace rmg

@@ -127,6 +127,11 @@ class Map:
         return {"boxes": nodes[:, :12].copy(), "links": nodes.view(np.int32)[:, 12:].copy(),
                 "tris": tris, "leaf_order": order}
 
+    def build_wide8(self) -> "Map":
+        """Adds the 8-wide tree with quantized boxes (rmg_map_build_wide8) for launch_config(bvh_width=8)."""
+        L.call("rmg_map_build_wide8", self.handle, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        return self
+
     def status(self, clear: bool = True) -> int:
         return int(L.load().rmg_map_status(self.handle, 1 if clear else 0))
 

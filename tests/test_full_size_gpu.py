@@ -90,7 +90,8 @@ def test_full_size_workload(name):
     ref = _simulate(sim, P, n, W, H, dict(packet=0, bvh_width=2))
     _consistent(ref, model, oracle.directions(model), W, H)
     _oracle_sample(sc, model, poses, ref, n_rays)
-    for cfg in (dict(packet=1), dict(bvh_width=4, packet=0)):
+    m.build_wide8()
+    for cfg in (dict(packet=1), dict(bvh_width=4, packet=0), dict(bvh_width=8, packet=0)):
         b = _simulate(sim, P, n, W, H, cfg)
         _same(ref, b, cfg)
         del b

@@ -14,7 +14,8 @@ from rmagine_gb300 import scenes, sensors
 
 pytestmark = pytest.mark.gpu
 IDENT = np.array([0, 0, 0, 1, 0, 0, 0, 0], np.float32)
-WALKS = [dict(packet=0), dict(packet=1), dict(bvh_width=4, packet=0), dict(stack_depth=0, packet=0)]
+WALKS = [dict(packet=0), dict(packet=1), dict(bvh_width=4, packet=0), dict(bvh_width=8, packet=0),
+         dict(stack_depth=0, packet=0)]
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -69,7 +70,7 @@ def same(a, b):
 def check_everything(v, f, model, poses):
     """Parity with the oracle (certified) on the SAH map, and bit-identical results on the LBVH map
     and for every walk."""
-    sah, lbvh = rm.Map(v, f), rm.Map(v, f, builder="lbvh")
+    sah, lbvh = rm.Map(v, f).build_wide8(), rm.Map(v, f, builder="lbvh").build_wide8()
     got = run(sah, model, poses)
     sc = oracle.Scene(v, f)
     want = sc.simulate(model, IDENT, poses)

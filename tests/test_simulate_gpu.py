@@ -168,7 +168,7 @@ def test_parity_o1dn_ondn_with_sensor_offset():
 def test_stack_depths_and_tiles_bitwise_identical():
     sc = scenes.terrain(grid=128, n_boxes=200, seed=12)
     poses = scenes.terrain_poses(sc, 4, seed=13)
-    m = rm.Map(sc.vertices, sc.faces)
+    m = rm.Map(sc.vertices, sc.faces).build_wide8()
     model = sensors.ouster_like(64, 512)
     base = gpu_sim(m, model, poses, cfg=rm.launch_config(8, 4, 8, 4, bvh_width=2))
     assert m.info()["depth"] <= 32
@@ -177,6 +177,7 @@ def test_stack_depths_and_tiles_bitwise_identical():
                 (16, 4, 8, 4, 0, 4, 4), (16, 2, 16, 2, 0, 4, 4), (16, 8, 32, 1, 0, 4, 4), (16, 4, 8, 4),
                 (16, 4, 8, 4, 0, 4, 2, 1), (16, 2, 16, 2, 0, 4, 2, 1), (16, 8, 32, 1, 0, 4, 2, 1),
                 (16, 4, 4, 8, 0, 4, 0, 1),
+                (16, 4, 8, 4, 0, 4, 8), (16, 2, 16, 2, 0, 4, 8), (16, 8, 4, 8, 0, 4, 8),
                 (8, 4, 8, 4, 16, 4), (16, 2, 8, 4, 32, 1), (8, 8, 16, 2, 1, 7), (16, 4, 4, 8, 24, 64)]:
         other = gpu_sim(m, model, poses, cfg=rm.launch_config(*cfg))
         for a in ALL:
@@ -300,13 +301,17 @@ def test_host_bundle_matches_device_bundle():
 @pytest.mark.parametrize("builder", ["lbvh", "sah"])
 def test_refit_moves_geometry(builder):
     sc = scenes.box_room(seed=6, n_boxes=60)
-    m = rm.Map(sc.vertices, sc.faces, builder=builder)
+    m = rm.Map(sc.vertices, sc.faces, builder=builder).build_wide8()
     links = m.export()["links"]
     moved = sc.vertices + np.array([0.3, -0.2, 0.1], np.float32)
     m.refit(moved)
     model = sensors.vlp16_900()
     poses = scenes.room_poses(4, seed=7)
     got = gpu_sim(m, model, poses)
+    # the 8-wide tree (boxes and triangle copy) follows the refit
+    wide8 = gpu_sim(m, model, poses, cfg=rm.launch_config(bvh_width=8, packet=0))
+    for a in ALL:
+        assert np.array_equal(wide8[a].view(np.uint8), got[a].view(np.uint8)), a
     sc2 = oracle.Scene(moved, sc.faces)
     want = sc2.simulate(model, IDENT, poses)
     rep = oracle.certify(sc2, model, IDENT, poses, got, want)
@@ -360,7 +365,7 @@ def test_autotune_returns_a_config_with_identical_results():
     want = gpu_sim(m, model, poses)
     sim = rm.make_simulator(model, m)
     cfg = sim.autotune(torch.from_numpy(poses).cuda(), attrs=ALL, reps=2)
-    assert cfg.tile_w * cfg.tile_h == 32 and cfg.bvh_width in (2, 4) and cfg.packet in (0, 1)
+    assert cfg.tile_w * cfg.tile_h == 32 and cfg.bvh_width in (2, 4, 8) and cfg.packet in (0, 1)
     got = gpu_sim(m, model, poses, cfg=cfg)
     for a in ALL:
         assert np.array_equal(got[a].view(np.uint8), want[a].view(np.uint8)), a

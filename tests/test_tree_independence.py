@@ -14,6 +14,7 @@ from rmagine_gb300 import scenes, sensors
 pytestmark = pytest.mark.gpu
 
 WALKS = {"per_ray": dict(packet=0), "packet": dict(packet=1), "wide": dict(bvh_width=4, packet=0),
+         "wide8": dict(bvh_width=8, packet=0),
          "short_stack": dict(stack_depth=8, packet=0)}
 
 
@@ -38,7 +39,7 @@ def _poses_translated(poses, dx, dy, dz=0.0):
 def _both_maps(v, f, tmp_path):
     path = tmp_path / "sah.rmg"
     depth = oracle.Scene(v, f, max_leaf=1).save_map(path)
-    return rm.Map(v, f), rm.Map.load(path), depth
+    return rm.Map(v, f).build_wide8(), rm.Map.load(path).build_wide8(), depth
 
 
 def _run(m, model, poses, cfg):
