@@ -39,6 +39,14 @@ IDENT = np.array([0, 0, 0, 1, 0, 0, 0, 0], np.float32)
 ALL = ("hits", "ranges", "points", "normals", "face_ids")
 OUT_BYTES = {"hits": 1, "ranges": 4, "points": 12, "normals": 12, "face_ids": 4, "geom_ids": 4, "object_ids": 4}
 
+
+def host_link_bytes(attrs, rays):
+    """Bytes per ray the host-buffer forms move device -> host: with Ranges requested and at least
+    64 MB of Points, the points are formed on the host from the ranges (csrc/host.cu, HostDerive)
+    and not copied."""
+    derived = {"points"} if "ranges" in attrs and "points" in attrs and rays * 12 >= (64 << 20) else set()
+    return sum(OUT_BYTES[a] for a in attrs if a not in derived)
+
 # Mean internal-node visits and triangle tests per ray of the canonical LBVH in the kernel's
 # traversal order, measured by the oracle's instrumented traversal (oracle.CanonicalLbvh.count)
 # on a fixed 0.1% ray sample (rng seed 0) of each workload; tests/test_work_constants.py
@@ -404,6 +412,7 @@ def gpu_raycast(args, world):
         e2e_t.append(time.perf_counter() - t0)
     e2e = rays / float(np.median(e2e_t)) / 1e6
     out_b = sum(OUT_BYTES[a] for a in attrs)
+    attrs_e2e = attrs
     wk = WORK_PER_RAY.get(args.workload)
     walk = walk_name(tuned, int(m.info()["depth"]))
     launch_s = total_ms / args.steps / 1e3
@@ -424,7 +433,8 @@ def gpu_raycast(args, world):
             "run": {"launch": {k: int(getattr(tuned, k)) for k, _ in tuned._fields_}, "walk": walk,
                     "tree": {"builder": m.builder, "depth": int(m.info()["depth"]), "build_ms": round(build_ms, 1)}},
             "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": int(poses.nbytes),
-                    "d2h_bytes_per_step": int(rays * out_b), "step_ms": [round(1e3 * x, 3) for x in e2e_t]},
+                    "d2h_bytes_per_step": int(rays * host_link_bytes(attrs_e2e, rays)),
+                    "step_ms": [round(1e3 * x, 3) for x in e2e_t]},
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms],
             "map": {k: m.info()[k] for k in ("n_faces", "n_nodes", "depth", "device_bytes")}}
     return line, lambda: cpu_raycast(sc, model, poses, attrs), config
@@ -487,6 +497,7 @@ def gpu_scene(args, world):
         e2e_t.append(time.perf_counter() - t0)
     e2e = rays / float(np.median(e2e_t)) / 1e6
     out_b = sum(OUT_BYTES[a] for a in SCENE_ATTRS)
+    attrs_e2e = SCENE_ATTRS
     wk = WORK_PER_RAY["terrain1m_spherical"]
     rl = roofline(out_b + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
                   "algorithmic bytes per ray of the same geometry as one mesh (canonical LBVH counts of the "
@@ -503,7 +514,8 @@ def gpu_scene(args, world):
             "baked_single_mesh": {"value": round(rays / (baked_ms / 1e3) / 1e6, 2), "unit": "Mrays/s",
                                   "ms_per_step": round(baked_ms, 3)},
             "e2e": {"value": round(e2e, 2), "unit": "Mrays/s", "h2d_bytes_per_step": int(poses.nbytes),
-                    "d2h_bytes_per_step": int(rays * out_b), "step_ms": [round(1e3 * x, 3) for x in e2e_t]},
+                    "d2h_bytes_per_step": int(rays * host_link_bytes(attrs_e2e, rays)),
+                    "step_ms": [round(1e3 * x, 3) for x in e2e_t]},
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
     return line, lambda: cpu_raycast(baked, model, poses, SCENE_ATTRS), config
 

@@ -12,8 +12,10 @@
 // with the casting.
 #include <atomic>
 #include <algorithm>
+#include <cstring>
 #include <functional>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "internal.h"
@@ -88,6 +90,113 @@ rmg_outputs outputs_at(const AttrList& a) {
 
 using Launch = std::function<int(const rmg_transform* Tbm, uint32_t n, const rmg_outputs* out, cudaStream_t st)>;
 
+// Points follow from the range of a ray (the attribute rules of
+// SphereSimulatorEmbree.tcc:104-249, as the traversal kernels write them): a
+// ray hit iff its range is at most range.max (a miss writes range.max + 1), and
+// points = dir_s * range (+ orig_s for O1Dn / OnDn) for a hit, NaN for a miss.
+// When the caller wants Ranges and Points of many rays, the host forms copy the
+// ranges over the host link (which bounds these calls) but not the 12-byte
+// points, and form the points on host threads from the ranges as each chunk
+// lands, in the same binary32 operations as the kernel (one product, one sum,
+// no contraction): the same bytes in the results, 12 fewer per ray on the
+// link.  Hits (1 byte per ray) are cheaper to copy than to form.  Not used
+// when range.max + 1 rounds to range.max (a hit at range.max would look like a
+// miss), nor below kDeriveMinBytes of points (threads cost more than they save).
+constexpr uint64_t kDeriveMinBytes = uint64_t(64) << 20;
+struct HostDerive {
+  bool points = false;
+  float rmax = 0.f;
+  int kind = 0;                    // rmg_model_kind
+  std::vector<float> dirs, origs;  // sensor frame, 3 per ray of one pose
+  float orig[3] = {0.f, 0.f, 0.f};
+  uint64_t rays_per_pose = 0;
+  const float* ranges_h = nullptr;
+  float* points_h = nullptr;
+
+  bool active() const { return points; }
+
+  // rays [r0, r1) of the whole output, pose segment by pose segment (contiguous
+  // ranges, directions and points: loops the compiler vectorizes)
+  void run(uint64_t r0, uint64_t r1) const {
+    while (r0 < r1) {
+      const uint64_t loc0 = r0 % rays_per_pose;
+      const uint64_t len = std::min<uint64_t>(r1 - r0, rays_per_pose - loc0);
+      segment(r0, loc0, len);
+      r0 += len;
+    }
+  }
+
+  void segment(uint64_t i0, uint64_t loc0, uint64_t len) const {
+    const float* __restrict__ rr = ranges_h + i0;
+    const float hi = rmax;
+    uint32_t nan_bits = 0x7fc00000u;
+    float nan_;
+    std::memcpy(&nan_, &nan_bits, 4);
+    const float* __restrict__ dd = dirs.data() + 3 * loc0;
+    float* __restrict__ pp = points_h + 3 * i0;
+    if (kind == RMG_MODEL_O1DN) {
+      const float ox = orig[0], oy = orig[1], oz = orig[2];
+      for (uint64_t j = 0; j < len; ++j) {
+        const float r = rr[j];
+        const bool hit = r <= hi;
+        const float x = dd[3 * j] * r + ox, y = dd[3 * j + 1] * r + oy, z = dd[3 * j + 2] * r + oz;
+        pp[3 * j] = hit ? x : nan_;
+        pp[3 * j + 1] = hit ? y : nan_;
+        pp[3 * j + 2] = hit ? z : nan_;
+      }
+    } else if (kind == RMG_MODEL_ONDN) {
+      const float* __restrict__ oo = origs.data() + 3 * loc0;
+      for (uint64_t j = 0; j < len; ++j) {
+        const float r = rr[j];
+        const bool hit = r <= hi;
+        const float x = dd[3 * j] * r + oo[3 * j], y = dd[3 * j + 1] * r + oo[3 * j + 1],
+                    z = dd[3 * j + 2] * r + oo[3 * j + 2];
+        pp[3 * j] = hit ? x : nan_;
+        pp[3 * j + 1] = hit ? y : nan_;
+        pp[3 * j + 2] = hit ? z : nan_;
+      }
+    } else {
+      for (uint64_t j = 0; j < len; ++j) {
+        const float r = rr[j];
+        const bool hit = r <= hi;
+        const float x = dd[3 * j] * r, y = dd[3 * j + 1] * r, z = dd[3 * j + 2] * r;
+        pp[3 * j] = hit ? x : nan_;
+        pp[3 * j + 1] = hit ? y : nan_;
+        pp[3 * j + 2] = hit ? z : nan_;
+      }
+    }
+  }
+};
+
+// Sets up the host-side derivation of Points for `out` (and removes them from
+// the device outputs) when the caller wants Ranges and Points of n_poses poses.
+int host_derive_setup(const rmg_sensor* sensor, uint32_t n_poses, rmg_outputs& out, HostDerive& d) {
+  if (!out.ranges || !out.points) return RMG_OK;
+  if ((uint64_t)n_poses * sensor->width * sensor->height * 12 < kDeriveMinBytes) return RMG_OK;
+  const float rmax = sensor->model.range.max;
+  const float miss = rmax + 1.0f;  // the kernels' miss range, binary32
+  if (!(miss > rmax)) return RMG_OK;
+  d.rmax = rmax;
+  d.kind = (int)sensor->model.kind;
+  d.rays_per_pose = (uint64_t)sensor->width * sensor->height;
+  {
+    d.dirs.resize(3 * d.rays_per_pose);
+    RMG_CUDA_TRY(cudaMemcpy(d.dirs.data(), sensor->d_dirs, d.dirs.size() * 4, cudaMemcpyDeviceToHost));
+    if (d.kind == RMG_MODEL_ONDN) {
+      d.origs.resize(3 * d.rays_per_pose);
+      RMG_CUDA_TRY(cudaMemcpy(d.origs.data(), sensor->d_origs, d.origs.size() * 4, cudaMemcpyDeviceToHost));
+    }
+    d.orig[0] = sensor->model.orig.x;
+    d.orig[1] = sensor->model.orig.y;
+    d.orig[2] = sensor->model.orig.z;
+  }
+  d.points = true;
+  d.ranges_h = out.ranges;
+  d.points_h = reinterpret_cast<float*>(out.points);
+  out.points = nullptr;
+  return RMG_OK;
+}
+
 // Streams and events of one call; released in every exit path.
 struct Pipeline {
   cudaStream_t side[kMaxCompute - 1] = {};  // compute streams besides the caller's
@@ -117,12 +226,17 @@ struct Pipeline {
 // chunk k+nc and issues chunk k's copies.  The launch of chunk j waits for the
 // copy of chunk j-kSlots (same slot), which was issued at iteration j-kSlots <
 // j-nc, i.e. before the wait is enqueued, because kSlots > nc.
-int host_pipeline(const char* what, uint64_t rays_per_pose, const rmg_transform* Tbm_host, uint32_t n_poses,
-                  const rmg_outputs& out_host, cudaStream_t st, const Launch& launch) {
+int host_pipeline(const char* what, const rmg_sensor* sensor, const rmg_transform* Tbm_host, uint32_t n_poses,
+                  const rmg_outputs& out_caller, cudaStream_t st, const Launch& launch) {
   static_assert(kSlots > kMaxCompute, "a slot is reused only after its copy was issued");
+  const uint64_t rays_per_pose = (uint64_t)sensor->width * sensor->height;
   const uint32_t nc = (uint32_t)std::min(std::max(g_compute.load(), 1), kMaxCompute);
+  rmg_outputs out_host = out_caller;
+  HostDerive derive;
+  const int r = host_derive_setup(sensor, n_poses, out_host, derive);
+  if (r != RMG_OK) return r;
   const AttrList host = attrs_of(out_host);
-  size_t bytes_per_ray = 0;
+  size_t bytes_per_ray = derive.points ? 12 : 0;  // chunks sized by the results, derived ones included
   for (int a = 0; a < 7; ++a)
     if (host.ptr[a]) bytes_per_ray += host.size[a];
   if (bytes_per_ray == 0 || rays_per_pose == 0) return RMG_OK;
@@ -160,6 +274,16 @@ int host_pipeline(const char* what, uint64_t rays_per_pose, const rmg_transform*
     offset[a] = slot_bytes;
     slot_bytes += (chunk * rays_per_pose * host.size[a] + 255) & ~size_t(255);
   }
+  std::vector<cudaEvent_t> chunk_copied;  // per chunk: its outputs are in host memory (host derivation)
+  struct EventsGuard {
+    std::vector<cudaEvent_t>& v;
+    ~EventsGuard() { for (cudaEvent_t e : v) if (e) cudaEventDestroy(e); }
+  } events_guard{chunk_copied};
+  if (derive.active()) {
+    chunk_copied.assign(n_chunks, nullptr);
+    for (uint32_t k = 0; k < n_chunks; ++k)
+      RMG_CUDA_TRY(cudaEventCreateWithFlags(&chunk_copied[k], cudaEventDisableTiming | cudaEventBlockingSync));
+  }
   char* staging = nullptr;
   RMG_CUDA_TRY(cudaMallocFromPoolAsync(reinterpret_cast<void**>(&staging), pose_bytes + slots * slot_bytes, pool, st));
   const auto* Tbm_dev = reinterpret_cast<const rmg_transform*>(staging);
@@ -196,6 +320,7 @@ int host_pipeline(const char* what, uint64_t rays_per_pose, const rmg_transform*
       RMG_CUDA_TRY(cudaMemcpyAsync(host.ptr[a] + p0 * row, d.ptr[a], np * row, cudaMemcpyDefault, pl.copy));
     }
     RMG_CUDA_TRY(cudaEventRecord(pl.copied[slot], pl.copy));
+    if (!chunk_copied.empty()) RMG_CUDA_TRY(cudaEventRecord(chunk_copied[k], pl.copy));
     return RMG_OK;
   };
 
@@ -203,6 +328,28 @@ int host_pipeline(const char* what, uint64_t rays_per_pose, const rmg_transform*
   for (uint32_t k = 0; s == RMG_OK && k < n_chunks; ++k) {
     if (k + nc < n_chunks) s = cast_chunk(k + nc);
     if (s == RMG_OK) s = copy_chunk(k);
+  }
+  // Hits / Points on host threads, chunk by chunk as each chunk's ranges land,
+  // while the later chunks are still cast and copied
+  if (s == RMG_OK && derive.active()) {
+    const uint64_t total = (uint64_t)n_poses * rays_per_pose;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned T = (unsigned)std::min<uint64_t>(std::min(hw, 32u), std::max<uint64_t>(1, total >> 20));
+    std::atomic<int> err{RMG_OK};
+    auto worker = [&](unsigned w) {
+      for (uint32_t k = 0; k < n_chunks; ++k) {
+        if (cudaEventSynchronize(chunk_copied[k]) != cudaSuccess) { err.store(RMG_ERR_CUDA); return; }
+        const uint64_t c0 = (uint64_t)k * chunk * rays_per_pose;
+        const uint64_t c1 = std::min<uint64_t>((uint64_t)(k + 1) * chunk, n_poses) * rays_per_pose;
+        const uint64_t len = c1 - c0;
+        derive.run(c0 + len * w / T, c0 + len * (w + 1) / T);
+      }
+    };
+    std::vector<std::thread> pool_threads;
+    for (unsigned w = 1; w < T; ++w) pool_threads.emplace_back(worker, w);
+    worker(0);
+    for (auto& t : pool_threads) t.join();
+    if (err.load() != RMG_OK) s = fail(RMG_ERR_CUDA, std::string(what) + ": waiting for a chunk's copy failed");
   }
   // the staging is freed in stream order after the last copy and the side
   // streams' last launches, whatever happened
@@ -499,7 +646,7 @@ extern "C" int rmg_simulate_host(const rmg_map* map, const rmg_sensor* sensor, c
     return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_host: NULL map, sensor, Tsb or outputs");
   if (n_poses == 0) return RMG_OK;
   if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_host: Tbm is NULL");
-  return host_pipeline("rmg_simulate_host", rays_of(sensor), Tbm, n_poses, *out, as_stream(stream),
+  return host_pipeline("rmg_simulate_host", sensor, Tbm, n_poses, *out, as_stream(stream),
                        [&](const rmg_transform* T, uint32_t n, const rmg_outputs* o, cudaStream_t st) {
                          return rmg_simulate_ex(map, sensor, Tsb, T, n, o, cfg, st);
                        });
@@ -512,7 +659,7 @@ extern "C" int rmg_simulate_scene_host(const rmg_scene* scene, const rmg_sensor*
     return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene_host: NULL scene, sensor, Tsb or outputs");
   if (n_poses == 0) return RMG_OK;
   if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene_host: Tbm is NULL");
-  return host_pipeline("rmg_simulate_scene_host", rays_of(sensor), Tbm, n_poses, *out, as_stream(stream),
+  return host_pipeline("rmg_simulate_scene_host", sensor, Tbm, n_poses, *out, as_stream(stream),
                        [&](const rmg_transform* T, uint32_t n, const rmg_outputs* o, cudaStream_t st) {
                          return rmg_simulate_scene(scene, sensor, Tsb, T, n, o, st);
                        });

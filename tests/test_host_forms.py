@@ -115,3 +115,33 @@ def test_scene_host_form_equals_device_form(built, chunk_bytes):
         chunk_bytes(chunk, streams)
         for pin in (True, False):
             _same(_host(sim, poses, ALL, pin), want)
+
+
+
+@pytest.mark.gpu
+def test_host_form_o1dn_ondn_and_a_huge_range_max(built, chunk_bytes):
+    """Points of large host-form calls are formed on the host from the ranges (with the sensor origin
+    for O1Dn / OnDn, above 64 MB of points); they must equal the device form bit for bit, with a
+    sensor offset, every chunking, pinned and pageable, and for a range.max so large that
+    range.max + 1 rounds to range.max (then the points are copied from the device instead)."""
+    sc = scenes.terrain(grid=80, size=50.0, n_boxes=30, seed=13)
+    m = rm.Map(sc.vertices, sc.faces)
+    rng = np.random.default_rng(14)
+    models = [sensors.O1DnModel(width=5000, height=20, range=sensors.Interval(0.5, 40.0), orig=(0.1, -0.2, 0.3),
+                                dirs=sensors.sphere_directions(100000, seed=15)),
+              sensors.OnDnModel(width=400, height=250, range=sensors.Interval(0.0, 130.0),
+                                origs=rng.uniform(-0.5, 0.5, (100000, 3)).astype(np.float32),
+                                dirs=sensors.sphere_directions(100000, seed=16)),
+              sensors.ouster_like(128, 800, 45.0, 0.5, 3.0e7)]
+    poses = scenes.terrain_poses(sc, 60, seed=17, size=50.0)  # 6 M rays, 72 MB of points
+    for model in models:
+        sim = rm.make_simulator(model, m)
+        sim.setTsb(np.array([0, 0, np.sin(0.2), np.cos(0.2), 0.05, 0.0, 0.1, 0], np.float32))
+        want = _device(sim, poses, ALL)
+        for chunk, streams in ((8 << 20, 2), (0, 0)):
+            chunk_bytes(chunk, streams)
+            for pin in (True, False):
+                _same(_host(sim, poses, ALL, pin), want)
+                sub = ("ranges", "points")
+                _same(_host(sim, poses, sub, pin), {a: want[a] for a in sub})
+        del want
