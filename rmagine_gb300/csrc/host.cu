@@ -90,6 +90,27 @@ rmg_outputs outputs_at(const AttrList& a) {
 
 using Launch = std::function<int(const rmg_transform* Tbm, uint32_t n, const rmg_outputs* out, cudaStream_t st)>;
 
+// Pose chunks of the simulate host forms: full chunks of `chunk` poses, then
+// the last two chunks' worth split in halving sizes (at least chunk / 8 poses),
+// so that the work left after the final launch -- its copy, and forming its
+// points -- is a small chunk's.  Returns the first pose of every chunk and n.
+std::vector<uint32_t> chunk_schedule(uint32_t n, size_t chunk) {
+  std::vector<uint32_t> first{0};
+  uint64_t p = 0;
+  while (n - p > 2 * chunk) {
+    p += chunk;
+    first.push_back((uint32_t)p);
+  }
+  const uint64_t min_tail = std::max<uint64_t>(1, chunk / 8);
+  while (p < n) {
+    const uint64_t rem = n - p;
+    const uint64_t take = rem <= min_tail ? rem : std::max<uint64_t>(min_tail, std::min<uint64_t>(chunk, (rem + 1) / 2));
+    p += take;
+    first.push_back((uint32_t)p);
+  }
+  return first;
+}
+
 // Points follow from the range of a ray (the attribute rules of
 // SphereSimulatorEmbree.tcc:104-249, as the traversal kernels write them): a
 // ray hit iff its range is at most range.max (a miss writes range.max + 1), and
@@ -244,7 +265,8 @@ int host_pipeline(const char* what, const rmg_sensor* sensor, const rmg_transfor
   // at least one pose, at most ceil(n/2) so that two chunks overlap
   size_t chunk = std::max<size_t>(1, g_chunk_bytes.load() / bytes_per_pose);
   chunk = std::min<size_t>(chunk, std::max<uint32_t>(1u, (n_poses + 1) / 2));
-  const uint32_t n_chunks = (uint32_t)((n_poses + chunk - 1) / chunk);
+  const std::vector<uint32_t> first = chunk_schedule(n_poses, chunk);  // chunk k: poses [first[k], first[k+1])
+  const uint32_t n_chunks = (uint32_t)first.size() - 1;
   const int slots = (int)std::min<uint32_t>(kSlots, n_chunks);
 
   cudaMemPool_t pool;
@@ -301,7 +323,7 @@ int host_pipeline(const char* what, const rmg_sensor* sensor, const rmg_transfor
   auto cast_chunk = [&](uint32_t k) -> int {
     const int slot = (int)(k % slots);
     const cudaStream_t cs = compute[k % nc];
-    const uint32_t p0 = (uint32_t)(k * chunk), np = (uint32_t)std::min<size_t>(chunk, n_poses - p0);
+    const uint32_t p0 = first[k], np = first[k + 1] - first[k];
     if (k >= (uint32_t)slots) RMG_CUDA_TRY(cudaStreamWaitEvent(cs, pl.copied[slot], 0));
     const rmg_outputs o = outputs_at(slot_outputs(slot));
     const int r = launch(Tbm_dev + p0, np, &o, cs);
@@ -311,7 +333,7 @@ int host_pipeline(const char* what, const rmg_sensor* sensor, const rmg_transfor
   };
   auto copy_chunk = [&](uint32_t k) -> int {
     const int slot = (int)(k % slots);
-    const uint64_t p0 = (uint64_t)k * chunk, np = std::min<uint64_t>(chunk, n_poses - p0);
+    const uint64_t p0 = first[k], np = first[k + 1] - first[k];
     RMG_CUDA_TRY(cudaStreamWaitEvent(pl.copy, pl.cast[slot], 0));
     const AttrList d = slot_outputs(slot);
     for (int a = 0; a < 7; ++a) {
@@ -339,8 +361,8 @@ int host_pipeline(const char* what, const rmg_sensor* sensor, const rmg_transfor
     auto worker = [&](unsigned w) {
       for (uint32_t k = 0; k < n_chunks; ++k) {
         if (cudaEventSynchronize(chunk_copied[k]) != cudaSuccess) { err.store(RMG_ERR_CUDA); return; }
-        const uint64_t c0 = (uint64_t)k * chunk * rays_per_pose;
-        const uint64_t c1 = std::min<uint64_t>((uint64_t)(k + 1) * chunk, n_poses) * rays_per_pose;
+        const uint64_t c0 = (uint64_t)first[k] * rays_per_pose;
+        const uint64_t c1 = (uint64_t)first[k + 1] * rays_per_pose;
         const uint64_t len = c1 - c0;
         derive.run(c0 + len * w / T, c0 + len * (w + 1) / T);
       }
