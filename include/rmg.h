@@ -275,6 +275,14 @@ int rmg_simulate_host(const rmg_map* map, const rmg_sensor* sensor, const rmg_tr
  * one chunk's last warps overlap the next chunk's first ones.  Results do not
  * depend on either. */
 int rmg_host_set_pipeline(uint64_t chunk_bytes, uint32_t compute_streams);
+/* Points in the host forms of simulate (process-wide; no counterpart in the
+ * reference).  A point is dir_s * range (+ orig_s) for a hit and NaN for a
+ * miss, so when Ranges and at least 64 MB of Points are wanted, host threads
+ * form the points from the copied ranges instead of moving 12 bytes per ray
+ * over the host link (policy 0, the default); policy 1 copies them like the
+ * other attributes and keeps the host threads free.  The results are the same
+ * bytes under both. */
+int rmg_host_set_points_policy(uint32_t policy);
 /* Returns the host forms' cached staging memory to the driver. */
 int rmg_host_staging_trim(void);
 

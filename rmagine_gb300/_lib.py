@@ -188,6 +188,7 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_umeyama_transform": (C.c_int, [_P, _U32, _P, _P]),
     "rmg_svd3": (C.c_int, [_P, _P, _P, _P, _P, _U32, C.c_int, _P]),
     "rmg_map_build_wide8": (C.c_int, [_P, _P]),
+    "rmg_host_set_points_policy": (C.c_int, [_U32]),
     "rmg_simulate_statistics": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(ScanC), _P, _U32,
                                           C.POINTER(ConstraintsC), C.c_int, _P, _P, _P]),
     "rmg_simulate_statistics_host": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(ScanC), _P, _U32,

@@ -124,6 +124,8 @@ std::vector<uint32_t> chunk_schedule(uint32_t n, size_t chunk) {
 // when range.max + 1 rounds to range.max (a hit at range.max would look like a
 // miss), nor below kDeriveMinBytes of points (threads cost more than they save).
 constexpr uint64_t kDeriveMinBytes = uint64_t(64) << 20;
+// rmg_host_set_points_policy: 0 form points on the host threads, 1 copy them over the link
+std::atomic<uint32_t> g_points_policy{0};
 struct HostDerive {
   bool points = false;
   float rmax = 0.f;
@@ -192,7 +194,7 @@ struct HostDerive {
 // Sets up the host-side derivation of Points for `out` (and removes them from
 // the device outputs) when the caller wants Ranges and Points of n_poses poses.
 int host_derive_setup(const rmg_sensor* sensor, uint32_t n_poses, rmg_outputs& out, HostDerive& d) {
-  if (!out.ranges || !out.points) return RMG_OK;
+  if (!out.ranges || !out.points || g_points_policy.load() == 1) return RMG_OK;
   if ((uint64_t)n_poses * sensor->width * sensor->height * 12 < kDeriveMinBytes) return RMG_OK;
   const float rmax = sensor->model.range.max;
   const float miss = rmax + 1.0f;  // the kernels' miss range, binary32
@@ -733,6 +735,12 @@ extern "C" int rmg_host_set_pipeline(uint64_t chunk_bytes, uint32_t compute_stre
     return fail(RMG_ERR_UNSUPPORTED, "rmg_host_set_pipeline: compute_streams must be 0..3");
   g_chunk_bytes.store(chunk_bytes ? (size_t)chunk_bytes : kDefaultChunkBytes);
   g_compute.store(compute_streams ? (int)compute_streams : kDefaultCompute);
+  return RMG_OK;
+}
+
+extern "C" int rmg_host_set_points_policy(uint32_t policy) {
+  if (policy > 1) return fail(RMG_ERR_UNSUPPORTED, "rmg_host_set_points_policy: policy must be 0 or 1");
+  g_points_policy.store(policy);
   return RMG_OK;
 }
 

@@ -140,8 +140,11 @@ def test_host_form_o1dn_ondn_and_a_huge_range_max(built, chunk_bytes):
         want = _device(sim, poses, ALL)
         for chunk, streams in ((8 << 20, 2), (0, 0)):
             chunk_bytes(chunk, streams)
-            for pin in (True, False):
-                _same(_host(sim, poses, ALL, pin), want)
-                sub = ("ranges", "points")
-                _same(_host(sim, poses, sub, pin), {a: want[a] for a in sub})
+            for policy in (0, 1):  # points formed on the host, points copied
+                _lib.call("rmg_host_set_points_policy", policy)
+                for pin in (True, False):
+                    _same(_host(sim, poses, ALL, pin), want)
+                    sub = ("ranges", "points")
+                    _same(_host(sim, poses, sub, pin), {a: want[a] for a in sub})
+        _lib.call("rmg_host_set_points_policy", 0)
         del want
