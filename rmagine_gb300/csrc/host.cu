@@ -370,8 +370,16 @@ int host_pipeline(const char* what, const rmg_sensor* sensor, const rmg_transfor
       }
     };
     std::vector<std::thread> pool_threads;
-    for (unsigned w = 1; w < T; ++w) pool_threads.emplace_back(worker, w);
+    unsigned started = 1;
+    try {  // no exception may leave the C entry points: slices whose thread did not start run here
+      for (unsigned w = 1; w < T; ++w) {
+        pool_threads.emplace_back(worker, w);
+        started = w + 1;
+      }
+    } catch (...) {
+    }
     worker(0);
+    for (unsigned w = started; w < T; ++w) worker(w);
     for (auto& t : pool_threads) t.join();
     if (err.load() != RMG_OK) s = fail(RMG_ERR_CUDA, std::string(what) + ": waiting for a chunk's copy failed");
   }
