@@ -287,72 +287,84 @@ int capture(rmg_batch* b) {
 using namespace rmg;
 
 extern "C" int rmg_batch_default_config(rmg_batch_config* cfg) {
-  if (!cfg) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_default_config: NULL");
-  cfg->stack_depth = 8;
-  cfg->block_warps = 4;
-  cfg->tile_w = 8;
-  cfg->tile_h = 4;
-  cfg->grab = 2;
-  cfg->ctas_per_sm = 0;
-  cfg->use_graph = 1;
-  return RMG_OK;
+  return guarded("rmg_batch_default_config", [&]() -> int {
+    if (!cfg) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_default_config: NULL");
+    cfg->stack_depth = 8;
+    cfg->block_warps = 4;
+    cfg->tile_w = 8;
+    cfg->tile_h = 4;
+    cfg->grab = 2;
+    cfg->ctas_per_sm = 0;
+    cfg->use_graph = 1;
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_batch_create(const rmg_map* map, const rmg_batch_entry* entries, uint32_t n_entries,
                                 rmg_batch** out) {
-  if (!map || !out || (n_entries && !entries)) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_create: NULL argument");
-  *out = nullptr;
-  for (uint32_t i = 0; i < n_entries; ++i) {
-    const rmg_batch_entry& e = entries[i];
-    if (!e.sensor) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_create: entry without sensor");
-    if (e.n_poses && !e.Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_create: entry without poses");
-  }
-  rmg_batch* b = new (std::nothrow) rmg_batch;
-  if (!b) return fail(RMG_ERR_OOM, "rmg_batch_create: host allocation");
-  cudaGetDevice(&b->device);
-  b->map = map;
-  b->entries.assign(entries, entries + n_entries);
-  rmg_batch_default_config(&b->cfg);
-  int s = dev_alloc(&b->counter, 1, "batch counter");
-  if (s == RMG_OK) s = build_jobs(b);
-  if (s != RMG_OK) { cudaFree(b->jobs); cudaFree(b->counter); delete b; return s; }
-  *out = b;
-  return RMG_OK;
+  return guarded("rmg_batch_create", [&]() -> int {
+    if (!map || !out || (n_entries && !entries)) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_create: NULL argument");
+    *out = nullptr;
+    for (uint32_t i = 0; i < n_entries; ++i) {
+      const rmg_batch_entry& e = entries[i];
+      if (!e.sensor) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_create: entry without sensor");
+      if (e.n_poses && !e.Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_create: entry without poses");
+    }
+    rmg_batch* b = new (std::nothrow) rmg_batch;
+    if (!b) return fail(RMG_ERR_OOM, "rmg_batch_create: host allocation");
+    cudaGetDevice(&b->device);
+    b->map = map;
+    b->entries.assign(entries, entries + n_entries);
+    rmg_batch_default_config(&b->cfg);
+    int s = dev_alloc(&b->counter, 1, "batch counter");
+    if (s == RMG_OK) s = build_jobs(b);
+    if (s != RMG_OK) { cudaFree(b->jobs); cudaFree(b->counter); delete b; return s; }
+    *out = b;
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_batch_set_config(rmg_batch* b, const rmg_batch_config* cfg) {
-  if (!b || !cfg) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_set_config: NULL argument");
-  int s = check_batch_config(*cfg);
-  if (s != RMG_OK) return s;
-  b->cfg = *cfg;
-  drop_graph(b);
-  return build_jobs(b);
+  return guarded("rmg_batch_set_config", [&]() -> int {
+    if (!b || !cfg) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_set_config: NULL argument");
+    int s = check_batch_config(*cfg);
+    if (s != RMG_OK) return s;
+    b->cfg = *cfg;
+    drop_graph(b);
+    return build_jobs(b);
+  });
 }
 
 extern "C" int rmg_batch_get_config(const rmg_batch* b, rmg_batch_config* cfg) {
-  if (!b || !cfg) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_get_config: NULL argument");
-  *cfg = b->cfg;
-  return RMG_OK;
+  return guarded("rmg_batch_get_config", [&]() -> int {
+    if (!b || !cfg) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_get_config: NULL argument");
+    *cfg = b->cfg;
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_batch_info(const rmg_batch* b, uint64_t* total_rays, uint64_t* total_tiles) {
-  if (!b) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_info: NULL batch");
-  if (total_rays) *total_rays = b->total_rays;
-  if (total_tiles) *total_tiles = b->total_tiles;
-  return RMG_OK;
+  return guarded("rmg_batch_info", [&]() -> int {
+    if (!b) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_info: NULL batch");
+    if (total_rays) *total_rays = b->total_rays;
+    if (total_tiles) *total_tiles = b->total_tiles;
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_batch_launch(rmg_batch* b, void* stream) {
-  if (!b) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_launch: NULL batch");
-  cudaStream_t st = as_stream(stream);
-  if (!b->cfg.use_graph) return launch_direct(b, st);
-  if (!b->exec) {
-    const int s = capture(b);
-    if (s != RMG_OK) return s;
-  }
-  if (b->total_tiles == 0) return RMG_OK;
-  RMG_CUDA_TRY(cudaGraphLaunch(b->exec, st));
-  return RMG_OK;
+  return guarded("rmg_batch_launch", [&]() -> int {
+    if (!b) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_launch: NULL batch");
+    cudaStream_t st = as_stream(stream);
+    if (!b->cfg.use_graph) return launch_direct(b, st);
+    if (!b->exec) {
+      const int s = capture(b);
+      if (s != RMG_OK) return s;
+    }
+    if (b->total_tiles == 0) return RMG_OK;
+    RMG_CUDA_TRY(cudaGraphLaunch(b->exec, st));
+    return RMG_OK;
+  });
 }
 
 // Times candidate launch options on the plan itself (direct launches, CUDA
@@ -361,73 +373,77 @@ extern "C" int rmg_batch_launch(rmg_batch* b, void* stream) {
 // per CTA {2, 4, 8} x tile {8x4, 4x8, 16x2} x grab {1, 4}, searched one
 // coordinate at a time from the default.
 extern "C" int rmg_batch_autotune(rmg_batch* b, void* stream, uint32_t reps, rmg_batch_config* best_out) {
-  if (!b) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_autotune: NULL batch");
-  cudaStream_t st = as_stream(stream);
-  reps = std::max<uint32_t>(reps, 1);
-  cudaEvent_t e0, e1;
-  RMG_CUDA_TRY(cudaEventCreate(&e0));
-  RMG_CUDA_TRY(cudaEventCreate(&e1));
-  auto time_cfg = [&](const rmg_batch_config& c, float& ms) -> int {
-    b->cfg = c;
-    int s = build_jobs(b);
-    if (s != RMG_OK) return s;
-    s = launch_direct(b, st);  // warm-up
-    if (s != RMG_OK) return s;
-    std::vector<float> t;
-    for (uint32_t r = 0; r < reps; ++r) {
-      RMG_CUDA_TRY(cudaEventRecord(e0, st));
-      s = launch_direct(b, st);
+  return guarded("rmg_batch_autotune", [&]() -> int {
+    if (!b) return fail(RMG_ERR_INVALID_ARG, "rmg_batch_autotune: NULL batch");
+    cudaStream_t st = as_stream(stream);
+    reps = std::max<uint32_t>(reps, 1);
+    cudaEvent_t e0, e1;
+    RMG_CUDA_TRY(cudaEventCreate(&e0));
+    RMG_CUDA_TRY(cudaEventCreate(&e1));
+    auto time_cfg = [&](const rmg_batch_config& c, float& ms) -> int {
+      b->cfg = c;
+      int s = build_jobs(b);
       if (s != RMG_OK) return s;
-      RMG_CUDA_TRY(cudaEventRecord(e1, st));
-      RMG_CUDA_TRY(cudaEventSynchronize(e1));
-      float x = 0;
-      RMG_CUDA_TRY(cudaEventElapsedTime(&x, e0, e1));
-      t.push_back(x);
+      s = launch_direct(b, st);  // warm-up
+      if (s != RMG_OK) return s;
+      std::vector<float> t;
+      for (uint32_t r = 0; r < reps; ++r) {
+        RMG_CUDA_TRY(cudaEventRecord(e0, st));
+        s = launch_direct(b, st);
+        if (s != RMG_OK) return s;
+        RMG_CUDA_TRY(cudaEventRecord(e1, st));
+        RMG_CUDA_TRY(cudaEventSynchronize(e1));
+        float x = 0;
+        RMG_CUDA_TRY(cudaEventElapsedTime(&x, e0, e1));
+        t.push_back(x);
+      }
+      std::sort(t.begin(), t.end());
+      ms = t[t.size() / 2];
+      return RMG_OK;
+    };
+    rmg_batch_config best = b->cfg;
+    best.use_graph = b->cfg.use_graph;
+    float best_ms = 0;
+    int s = time_cfg(best, best_ms);
+    const uint32_t stacks[] = {0, 8, 16};
+    const uint32_t warps[] = {2, 4, 8};
+    const uint32_t tiles[][2] = {{8, 4}, {4, 8}, {16, 2}};
+    const uint32_t grabs[] = {1, 4};
+    for (int coord = 0; coord < 4 && s == RMG_OK; ++coord) {
+      const int n = coord == 0 ? 3 : coord == 1 ? 3 : coord == 2 ? 3 : 2;
+      rmg_batch_config round_best = best;
+      for (int i = 0; i < n && s == RMG_OK; ++i) {
+        rmg_batch_config c = best;
+        if (coord == 0) c.stack_depth = stacks[i];
+        if (coord == 1) c.block_warps = warps[i];
+        if (coord == 2) { c.tile_w = tiles[i][0]; c.tile_h = tiles[i][1]; }
+        if (coord == 3) c.grab = grabs[i];
+        if (std::memcmp(&c, &best, sizeof(c)) == 0) continue;
+        float ms = 0;
+        s = time_cfg(c, ms);
+        if (s == RMG_OK && ms < best_ms) { best_ms = ms; round_best = c; }
+      }
+      best = round_best;
     }
-    std::sort(t.begin(), t.end());
-    ms = t[t.size() / 2];
-    return RMG_OK;
-  };
-  rmg_batch_config best = b->cfg;
-  best.use_graph = b->cfg.use_graph;
-  float best_ms = 0;
-  int s = time_cfg(best, best_ms);
-  const uint32_t stacks[] = {0, 8, 16};
-  const uint32_t warps[] = {2, 4, 8};
-  const uint32_t tiles[][2] = {{8, 4}, {4, 8}, {16, 2}};
-  const uint32_t grabs[] = {1, 4};
-  for (int coord = 0; coord < 4 && s == RMG_OK; ++coord) {
-    const int n = coord == 0 ? 3 : coord == 1 ? 3 : coord == 2 ? 3 : 2;
-    rmg_batch_config round_best = best;
-    for (int i = 0; i < n && s == RMG_OK; ++i) {
-      rmg_batch_config c = best;
-      if (coord == 0) c.stack_depth = stacks[i];
-      if (coord == 1) c.block_warps = warps[i];
-      if (coord == 2) { c.tile_w = tiles[i][0]; c.tile_h = tiles[i][1]; }
-      if (coord == 3) c.grab = grabs[i];
-      if (std::memcmp(&c, &best, sizeof(c)) == 0) continue;
-      float ms = 0;
-      s = time_cfg(c, ms);
-      if (s == RMG_OK && ms < best_ms) { best_ms = ms; round_best = c; }
-    }
-    best = round_best;
-  }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  b->cfg = best;
-  drop_graph(b);
-  int s2 = build_jobs(b);
-  if (s == RMG_OK) s = s2;
-  if (s == RMG_OK && best_out) *best_out = best;
-  return s;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->cfg = best;
+    drop_graph(b);
+    int s2 = build_jobs(b);
+    if (s == RMG_OK) s = s2;
+    if (s == RMG_OK && best_out) *best_out = best;
+    return s;
+  });
 }
 
 extern "C" int rmg_batch_destroy(rmg_batch* b) {
-  if (!b) return RMG_OK;
-  drop_graph(b);
-  if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
-  cudaFree(b->jobs);
-  cudaFree(b->counter);
-  delete b;
-  return RMG_OK;
+  return guarded("rmg_batch_destroy", [&]() -> int {
+    if (!b) return RMG_OK;
+    drop_graph(b);
+    if (b->capture_stream) cudaStreamDestroy(b->capture_stream);
+    cudaFree(b->jobs);
+    cudaFree(b->counter);
+    delete b;
+    return RMG_OK;
+  });
 }

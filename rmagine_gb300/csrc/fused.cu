@@ -239,50 +239,54 @@ extern "C" int rmg_simulate_statistics(const rmg_map* map, const rmg_sensor* sen
                                        const rmg_transform* pre_transforms, uint32_t pre_transform_stride,
                                        const rmg_umeyama_constraints* params, int point_to_plane,
                                        rmg_cross_stats* stats, rmg_transform* transforms, void* stream) {
-  if (!map || !sensor || !Tsb || !dataset || !params)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics: NULL map, sensor, Tsb, dataset or params");
-  if (n_poses == 0) return RMG_OK;
-  if (!Tbm || !dataset->points) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics: NULL Tbm or dataset points");
-  if (!stats && !transforms) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics: no output requested");
-  rmg_launch_config cfg;
-  default_config(sensor, &cfg);
-  rmg_outputs out{};
-  FusedParams F;
-  make_trace_params(map, sensor, Tsb, Tbm, n_poses, &out, cfg, F.T);
-  F.dp = reinterpret_cast<const float*>(dataset->points);
-  F.dmask = dataset->mask;
-  F.dids = dataset->ids;
-  F.d_stride = dataset->per_pose ? (uint64_t)sensor->width * sensor->height : 0ull;
-  F.pre = pre_transforms;
-  F.pre_stride = pre_transform_stride ? 1u : 0u;
-  F.max_dist = params->max_dist;
-  F.dataset_id = params->dataset_id;
-  F.tiles_per_cta = cfg.block_warps * RMG_FUSED_TILES_PER_WARP;
-  F.ctas_per_pose = (F.T.tiles_per_pose + F.tiles_per_cta - 1) / F.tiles_per_cta;
-  const uint64_t grid = (uint64_t)F.ctas_per_pose * n_poses;
-  if (grid > 0x7fffffffull) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics: too many rays for one launch");
-  cudaStream_t st = as_stream(stream);
-  double* partial = nullptr;
-  RMG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&partial), 16 * sizeof(double) * (size_t)grid, st));
-  F.partial = partial;
-  const unsigned block = 32u * cfg.block_warps;
-  const cudaError_t e = point_to_plane ? launch_fused<true>(F, sensor->model.kind, (unsigned)grid, block, st)
-                                       : launch_fused<false>(F, sensor->model.kind, (unsigned)grid, block, st);
-  int s = cuda_status(e, "k_trace_stats");
-  if (s == RMG_OK) {
-    const uint64_t threads = 32ull * n_poses;
-    k_fused_final<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(partial, n_poses, F.ctas_per_pose, stats,
-                                                                     transforms);
-    s = cuda_status(cudaGetLastError(), "k_fused_final");
-  }
-  cudaFreeAsync(partial, st);
-  return s;
+  return guarded("rmg_simulate_statistics", [&]() -> int {
+    if (!map || !sensor || !Tsb || !dataset || !params)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics: NULL map, sensor, Tsb, dataset or params");
+    if (n_poses == 0) return RMG_OK;
+    if (!Tbm || !dataset->points) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics: NULL Tbm or dataset points");
+    if (!stats && !transforms) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics: no output requested");
+    rmg_launch_config cfg;
+    default_config(sensor, &cfg);
+    rmg_outputs out{};
+    FusedParams F;
+    make_trace_params(map, sensor, Tsb, Tbm, n_poses, &out, cfg, F.T);
+    F.dp = reinterpret_cast<const float*>(dataset->points);
+    F.dmask = dataset->mask;
+    F.dids = dataset->ids;
+    F.d_stride = dataset->per_pose ? (uint64_t)sensor->width * sensor->height : 0ull;
+    F.pre = pre_transforms;
+    F.pre_stride = pre_transform_stride ? 1u : 0u;
+    F.max_dist = params->max_dist;
+    F.dataset_id = params->dataset_id;
+    F.tiles_per_cta = cfg.block_warps * RMG_FUSED_TILES_PER_WARP;
+    F.ctas_per_pose = (F.T.tiles_per_pose + F.tiles_per_cta - 1) / F.tiles_per_cta;
+    const uint64_t grid = (uint64_t)F.ctas_per_pose * n_poses;
+    if (grid > 0x7fffffffull) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics: too many rays for one launch");
+    cudaStream_t st = as_stream(stream);
+    double* partial = nullptr;
+    RMG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&partial), 16 * sizeof(double) * (size_t)grid, st));
+    F.partial = partial;
+    const unsigned block = 32u * cfg.block_warps;
+    const cudaError_t e = point_to_plane ? launch_fused<true>(F, sensor->model.kind, (unsigned)grid, block, st)
+                                         : launch_fused<false>(F, sensor->model.kind, (unsigned)grid, block, st);
+    int s = cuda_status(e, "k_trace_stats");
+    if (s == RMG_OK) {
+      const uint64_t threads = 32ull * n_poses;
+      k_fused_final<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(partial, n_poses, F.ctas_per_pose, stats,
+                                                                       transforms);
+      s = cuda_status(cudaGetLastError(), "k_fused_final");
+    }
+    cudaFreeAsync(partial, st);
+    return s;
+  });
 }
 
 extern "C" int rmg_transforms_compose(const rmg_transform* a, uint32_t a_stride, const rmg_transform* b,
                                       uint32_t b_stride, rmg_transform* out, uint32_t n, void* stream) {
-  if (n == 0) return RMG_OK;
-  if (!a || !b || !out) return fail(RMG_ERR_INVALID_ARG, "rmg_transforms_compose: NULL argument");
-  k_compose<<<(n + 255) / 256, 256, 0, as_stream(stream)>>>(a, a_stride, b, b_stride, out, n);
-  return cuda_status(cudaGetLastError(), "k_compose");
+  return guarded("rmg_transforms_compose", [&]() -> int {
+    if (n == 0) return RMG_OK;
+    if (!a || !b || !out) return fail(RMG_ERR_INVALID_ARG, "rmg_transforms_compose: NULL argument");
+    k_compose<<<(n + 255) / 256, 256, 0, as_stream(stream)>>>(a, a_stride, b, b_stride, out, n);
+    return cuda_status(cudaGetLastError(), "k_compose");
+  });
 }

@@ -163,41 +163,43 @@ extern "C" int rmg_range_pose_grad(const rmg_map* map, const rmg_sensor* sensor,
                                    const rmg_transform* Tbm, uint32_t n_poses, const float* ranges_obs,
                                    float huber_delta, float* grad, float* loss, float* ranges_sim,
                                    uint32_t* face_ids, void* stream) {
-  if (!map || !sensor || !Tsb) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad: NULL map, sensor or Tsb");
-  if (n_poses == 0) return RMG_OK;
-  if (!Tbm || !ranges_obs) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad: NULL Tbm or ranges_obs");
-  if (!grad && !loss) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad: no output requested");
-  if (!(huber_delta > 0.0f)) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad: huber_delta must be > 0");
-  if (n_poses > 65535u) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad: at most 65535 poses per call");
-  rmg_launch_config cfg;
-  default_config(sensor, &cfg);
-  rmg_outputs out{};
-  out.ranges = ranges_sim;
-  out.face_ids = face_ids;
-  GradParams G;
-  make_trace_params(map, sensor, Tsb, Tbm, n_poses, &out, cfg, G.T);
-  G.r_obs = ranges_obs;
-  G.delta = huber_delta;
-  G.ctas_per_pose = (G.T.tiles_per_pose + cfg.block_warps - 1) / cfg.block_warps;
-  cudaStream_t st = as_stream(stream);
-  float* partial = nullptr;
-  RMG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&partial),
-                               8 * sizeof(float) * (size_t)n_poses * G.ctas_per_pose, st));
-  G.partial = partial;
-  const dim3 grid(G.ctas_per_pose, n_poses);
-  const unsigned block = 32u * cfg.block_warps;
-  cudaError_t e;
-  switch (sensor->model.kind) {
-    case RMG_MODEL_SPHERICAL:
-    case RMG_MODEL_PINHOLE: e = launch_grad<ORIGIN_POSE>(G, (int)cfg.stack_depth, grid, block, st); break;
-    case RMG_MODEL_O1DN: e = launch_grad<ORIGIN_SINGLE>(G, (int)cfg.stack_depth, grid, block, st); break;
-    default: e = launch_grad<ORIGIN_TABLE>(G, (int)cfg.stack_depth, grid, block, st); break;
-  }
-  int s = cuda_status(e, "k_range_grad");
-  if (s == RMG_OK) {
-    k_grad_final<<<(7 * n_poses + 255) / 256, 256, 0, st>>>(partial, n_poses, G.ctas_per_pose, grad, loss);
-    s = cuda_status(cudaGetLastError(), "k_grad_final");
-  }
-  cudaFreeAsync(partial, st);
-  return s;
+  return guarded("rmg_range_pose_grad", [&]() -> int {
+    if (!map || !sensor || !Tsb) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad: NULL map, sensor or Tsb");
+    if (n_poses == 0) return RMG_OK;
+    if (!Tbm || !ranges_obs) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad: NULL Tbm or ranges_obs");
+    if (!grad && !loss) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad: no output requested");
+    if (!(huber_delta > 0.0f)) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad: huber_delta must be > 0");
+    if (n_poses > 65535u) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad: at most 65535 poses per call");
+    rmg_launch_config cfg;
+    default_config(sensor, &cfg);
+    rmg_outputs out{};
+    out.ranges = ranges_sim;
+    out.face_ids = face_ids;
+    GradParams G;
+    make_trace_params(map, sensor, Tsb, Tbm, n_poses, &out, cfg, G.T);
+    G.r_obs = ranges_obs;
+    G.delta = huber_delta;
+    G.ctas_per_pose = (G.T.tiles_per_pose + cfg.block_warps - 1) / cfg.block_warps;
+    cudaStream_t st = as_stream(stream);
+    float* partial = nullptr;
+    RMG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&partial),
+                                 8 * sizeof(float) * (size_t)n_poses * G.ctas_per_pose, st));
+    G.partial = partial;
+    const dim3 grid(G.ctas_per_pose, n_poses);
+    const unsigned block = 32u * cfg.block_warps;
+    cudaError_t e;
+    switch (sensor->model.kind) {
+      case RMG_MODEL_SPHERICAL:
+      case RMG_MODEL_PINHOLE: e = launch_grad<ORIGIN_POSE>(G, (int)cfg.stack_depth, grid, block, st); break;
+      case RMG_MODEL_O1DN: e = launch_grad<ORIGIN_SINGLE>(G, (int)cfg.stack_depth, grid, block, st); break;
+      default: e = launch_grad<ORIGIN_TABLE>(G, (int)cfg.stack_depth, grid, block, st); break;
+    }
+    int s = cuda_status(e, "k_range_grad");
+    if (s == RMG_OK) {
+      k_grad_final<<<(7 * n_poses + 255) / 256, 256, 0, st>>>(partial, n_poses, G.ctas_per_pose, grad, loss);
+      s = cuda_status(cudaGetLastError(), "k_grad_final");
+    }
+    cudaFreeAsync(partial, st);
+    return s;
+  });
 }

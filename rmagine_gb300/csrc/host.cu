@@ -674,27 +674,31 @@ using namespace rmg;
 extern "C" int rmg_simulate_host(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
                                  const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
                                  const rmg_launch_config* cfg, void* stream) {
-  if (!map || !sensor || !Tsb || !out)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_host: NULL map, sensor, Tsb or outputs");
-  if (n_poses == 0) return RMG_OK;
-  if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_host: Tbm is NULL");
-  return host_pipeline("rmg_simulate_host", sensor, Tbm, n_poses, *out, as_stream(stream),
-                       [&](const rmg_transform* T, uint32_t n, const rmg_outputs* o, cudaStream_t st) {
-                         return rmg_simulate_ex(map, sensor, Tsb, T, n, o, cfg, st);
-                       });
+  return guarded("rmg_simulate_host", [&]() -> int {
+    if (!map || !sensor || !Tsb || !out)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_host: NULL map, sensor, Tsb or outputs");
+    if (n_poses == 0) return RMG_OK;
+    if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_host: Tbm is NULL");
+    return host_pipeline("rmg_simulate_host", sensor, Tbm, n_poses, *out, as_stream(stream),
+                         [&](const rmg_transform* T, uint32_t n, const rmg_outputs* o, cudaStream_t st) {
+                           return rmg_simulate_ex(map, sensor, Tsb, T, n, o, cfg, st);
+                         });
+  });
 }
 
 extern "C" int rmg_simulate_scene_host(const rmg_scene* scene, const rmg_sensor* sensor, const rmg_transform* Tsb,
                                        const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
                                        void* stream) {
-  if (!scene || !sensor || !Tsb || !out)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene_host: NULL scene, sensor, Tsb or outputs");
-  if (n_poses == 0) return RMG_OK;
-  if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene_host: Tbm is NULL");
-  return host_pipeline("rmg_simulate_scene_host", sensor, Tbm, n_poses, *out, as_stream(stream),
-                       [&](const rmg_transform* T, uint32_t n, const rmg_outputs* o, cudaStream_t st) {
-                         return rmg_simulate_scene(scene, sensor, Tsb, T, n, o, st);
-                       });
+  return guarded("rmg_simulate_scene_host", [&]() -> int {
+    if (!scene || !sensor || !Tsb || !out)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene_host: NULL scene, sensor, Tsb or outputs");
+    if (n_poses == 0) return RMG_OK;
+    if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene_host: Tbm is NULL");
+    return host_pipeline("rmg_simulate_scene_host", sensor, Tbm, n_poses, *out, as_stream(stream),
+                         [&](const rmg_transform* T, uint32_t n, const rmg_outputs* o, cudaStream_t st) {
+                           return rmg_simulate_scene(scene, sensor, Tsb, T, n, o, st);
+                         });
+  });
 }
 
 extern "C" int rmg_simulate_statistics_host(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
@@ -702,59 +706,69 @@ extern "C" int rmg_simulate_statistics_host(const rmg_map* map, const rmg_sensor
                                             const rmg_transform* pre_transforms, uint32_t pre_transform_stride,
                                             const rmg_umeyama_constraints* params, int point_to_plane,
                                             rmg_cross_stats* stats, rmg_transform* transforms, void* stream) {
-  if (!map || !sensor || !Tsb || !dataset || !params)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics_host: NULL map, sensor, Tsb, dataset or params");
-  if (n_poses == 0) return RMG_OK;
-  if (!Tbm || !dataset->points) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics_host: Tbm or points NULL");
-  if (!stats && !transforms) return RMG_OK;
-  return statistics_pipeline(map, sensor, Tsb, Tbm, n_poses, *dataset, pre_transforms, pre_transform_stride ? 1u : 0u,
-                             params, point_to_plane, stats, transforms, as_stream(stream));
+  return guarded("rmg_simulate_statistics_host", [&]() -> int {
+    if (!map || !sensor || !Tsb || !dataset || !params)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics_host: NULL map, sensor, Tsb, dataset or params");
+    if (n_poses == 0) return RMG_OK;
+    if (!Tbm || !dataset->points) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_statistics_host: Tbm or points NULL");
+    if (!stats && !transforms) return RMG_OK;
+    return statistics_pipeline(map, sensor, Tsb, Tbm, n_poses, *dataset, pre_transforms, pre_transform_stride ? 1u : 0u,
+                               params, point_to_plane, stats, transforms, as_stream(stream));
+  });
 }
 
 extern "C" int rmg_range_pose_grad_host(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
                                         const rmg_transform* Tbm, uint32_t n_poses, const float* ranges_obs,
                                         float huber_delta, float* grad, float* loss, float* ranges_sim,
                                         uint32_t* face_ids, void* stream) {
-  if (!map || !sensor || !Tsb)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad_host: NULL map, sensor or Tsb");
-  if (n_poses == 0) return RMG_OK;
-  if (!Tbm || !ranges_obs) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad_host: Tbm or ranges_obs NULL");
-  if (!grad && !loss) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad_host: grad and loss are both NULL");
-  const size_t rays = rays_of(sensor);
-  // device arrays of a chunk: Tbm, observed ranges (inputs); grad, loss, ranges, face ids (outputs)
-  const std::vector<HostArray> arrays = {
-      {Tbm, nullptr, sizeof(rmg_transform)}, {ranges_obs, nullptr, 4 * rays},
-      {nullptr, grad, grad ? 24 : 0}, {nullptr, loss, loss ? 4 : 0},
-      {nullptr, ranges_sim, ranges_sim ? 4 * rays : 0}, {nullptr, face_ids, face_ids ? 4 * rays : 0}};
-  return io_pipeline("rmg_range_pose_grad_host", n_poses, arrays, 65535,
-                     [&](uint32_t, uint32_t np, char* const* d, cudaStream_t cs) {
-                       return rmg_range_pose_grad(map, sensor, Tsb, reinterpret_cast<const rmg_transform*>(d[0]), np,
-                                                  reinterpret_cast<const float*>(d[1]), huber_delta,
-                                                  grad ? reinterpret_cast<float*>(d[2]) : nullptr,
-                                                  loss ? reinterpret_cast<float*>(d[3]) : nullptr,
-                                                  ranges_sim ? reinterpret_cast<float*>(d[4]) : nullptr,
-                                                  face_ids ? reinterpret_cast<uint32_t*>(d[5]) : nullptr, cs);
-                     },
-                     as_stream(stream));
+  return guarded("rmg_range_pose_grad_host", [&]() -> int {
+    if (!map || !sensor || !Tsb)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad_host: NULL map, sensor or Tsb");
+    if (n_poses == 0) return RMG_OK;
+    if (!Tbm || !ranges_obs) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad_host: Tbm or ranges_obs NULL");
+    if (!grad && !loss) return fail(RMG_ERR_INVALID_ARG, "rmg_range_pose_grad_host: grad and loss are both NULL");
+    const size_t rays = rays_of(sensor);
+    // device arrays of a chunk: Tbm, observed ranges (inputs); grad, loss, ranges, face ids (outputs)
+    const std::vector<HostArray> arrays = {
+        {Tbm, nullptr, sizeof(rmg_transform)}, {ranges_obs, nullptr, 4 * rays},
+        {nullptr, grad, grad ? 24 : 0}, {nullptr, loss, loss ? 4 : 0},
+        {nullptr, ranges_sim, ranges_sim ? 4 * rays : 0}, {nullptr, face_ids, face_ids ? 4 * rays : 0}};
+    return io_pipeline("rmg_range_pose_grad_host", n_poses, arrays, 65535,
+                       [&](uint32_t, uint32_t np, char* const* d, cudaStream_t cs) {
+                         return rmg_range_pose_grad(map, sensor, Tsb, reinterpret_cast<const rmg_transform*>(d[0]), np,
+                                                    reinterpret_cast<const float*>(d[1]), huber_delta,
+                                                    grad ? reinterpret_cast<float*>(d[2]) : nullptr,
+                                                    loss ? reinterpret_cast<float*>(d[3]) : nullptr,
+                                                    ranges_sim ? reinterpret_cast<float*>(d[4]) : nullptr,
+                                                    face_ids ? reinterpret_cast<uint32_t*>(d[5]) : nullptr, cs);
+                       },
+                       as_stream(stream));
+  });
 }
 
 extern "C" int rmg_host_set_pipeline(uint64_t chunk_bytes, uint32_t compute_streams) {
-  if (compute_streams > (uint32_t)kMaxCompute)
-    return fail(RMG_ERR_UNSUPPORTED, "rmg_host_set_pipeline: compute_streams must be 0..3");
-  g_chunk_bytes.store(chunk_bytes ? (size_t)chunk_bytes : kDefaultChunkBytes);
-  g_compute.store(compute_streams ? (int)compute_streams : kDefaultCompute);
-  return RMG_OK;
+  return guarded("rmg_host_set_pipeline", [&]() -> int {
+    if (compute_streams > (uint32_t)kMaxCompute)
+      return fail(RMG_ERR_UNSUPPORTED, "rmg_host_set_pipeline: compute_streams must be 0..3");
+    g_chunk_bytes.store(chunk_bytes ? (size_t)chunk_bytes : kDefaultChunkBytes);
+    g_compute.store(compute_streams ? (int)compute_streams : kDefaultCompute);
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_host_set_points_policy(uint32_t policy) {
-  if (policy > 1) return fail(RMG_ERR_UNSUPPORTED, "rmg_host_set_points_policy: policy must be 0 or 1");
-  g_points_policy.store(policy);
-  return RMG_OK;
+  return guarded("rmg_host_set_points_policy", [&]() -> int {
+    if (policy > 1) return fail(RMG_ERR_UNSUPPORTED, "rmg_host_set_points_policy: policy must be 0 or 1");
+    g_points_policy.store(policy);
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_host_staging_trim(void) {
-  std::lock_guard<std::mutex> lock(g_pool_mu);
-  for (int d = 0; d < kMaxDevices; ++d)
-    if (g_pool[d]) RMG_CUDA_TRY(cudaMemPoolTrimTo(g_pool[d], 0));
-  return RMG_OK;
+  return guarded("rmg_host_staging_trim", [&]() -> int {
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    for (int d = 0; d < kMaxDevices; ++d)
+      if (g_pool[d]) RMG_CUDA_TRY(cudaMemPoolTrimTo(g_pool[d], 0));
+    return RMG_OK;
+  });
 }

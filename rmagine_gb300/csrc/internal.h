@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "guard.h"
 
 struct rmg_map {
   int device;

@@ -341,100 +341,165 @@ DeviceMap device_view(const rmg_map* m) {
 using namespace rmg;
 
 extern "C" int rmg_map_build_wide8(rmg_map* m, void* stream) {
-  if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_build_wide8: map is NULL");
-  if (m->n_faces == 0 || m->d_nodes8) return RMG_OK;
-  return wide8_build(m, as_stream(stream));
+  return guarded("rmg_map_build_wide8", [&]() -> int {
+    if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_build_wide8: map is NULL");
+    if (m->n_faces == 0 || m->d_nodes8) return RMG_OK;
+    return wide8_build(m, as_stream(stream));
+  });
 }
 
 extern "C" int rmg_map_build(const rmg_vec3* vertices, uint32_t n_vertices, const rmg_face* faces,
                              uint32_t n_faces, void* stream, rmg_map** out) {
-  return rmg_map_build_ex(vertices, n_vertices, faces, n_faces, RMG_BUILD_SAH, stream, out);
+  return guarded("rmg_map_build", [&]() -> int {
+    return rmg_map_build_ex(vertices, n_vertices, faces, n_faces, RMG_BUILD_SAH, stream, out);
+  });
 }
 
 extern "C" int rmg_map_build_ex(const rmg_vec3* vertices, uint32_t n_vertices, const rmg_face* faces,
                                 uint32_t n_faces, uint32_t builder, void* stream, rmg_map** out) {
-  if (!out) return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: out is NULL");
-  *out = nullptr;
-  if (builder != RMG_BUILD_SAH && builder != RMG_BUILD_LBVH)
-    return fail(RMG_ERR_UNSUPPORTED, "rmg_map_build_ex: builder must be RMG_BUILD_SAH or RMG_BUILD_LBVH");
-  *out = nullptr;
-  if (n_faces > 0 && (!vertices || !faces))
-    return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: vertices/faces are NULL");
-  if (n_faces > (1u << 30)) return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: too many faces");
-  for (uint32_t i = 0; i < n_faces; ++i) {
-    if (faces[i].v0 >= n_vertices || faces[i].v1 >= n_vertices || faces[i].v2 >= n_vertices)
-      return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: face index out of range");
-  }
-  cudaStream_t st = as_stream(stream);
-  rmg_map* m = new (std::nothrow) rmg_map;
-  if (!m) return fail(RMG_ERR_OOM, "rmg_map_build: host allocation");
-  std::memset(m, 0, sizeof(*m));
-  cudaGetDevice(&m->device);
-  m->n_vertices = n_vertices;
-  m->n_faces = n_faces;
-  m->n_nodes = n_faces >= 2 ? n_faces - 1 : (n_faces == 1 ? 1 : 0);
-
-  int s = RMG_OK;
-  auto check = [&](int r) { if (s == RMG_OK) s = r; return s == RMG_OK; };
-
-  check(dev_alloc(&m->d_status, 1, "status"));
-  if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(m->d_status, 0, sizeof(unsigned int), st), "memset");
-  if (s == RMG_OK && n_faces == 0) {
-    s = cuda_status(cudaStreamSynchronize(st), "sync");
-    if (s != RMG_OK) { free_map(m); return s; }
-    update_info(m, st);
-    *out = m;
-    return RMG_OK;
-  }
-  check(dev_alloc(&m->d_vertices, 3 * (size_t)n_vertices, "vertices"));
-  check(dev_alloc(&m->d_faces, 3 * (size_t)n_faces, "faces"));
-  check(dev_alloc(&m->d_nodes, m->n_nodes, "nodes"));
-  check(dev_alloc(&m->d_tris, n_faces, "tris"));
-  check(dev_alloc(&m->d_leaf_order, n_faces, "leaf order"));
-  check(dev_alloc(&m->d_leaf_parent, n_faces, "leaf parent"));
-  check(dev_alloc(&m->d_flags, m->n_nodes, "flags"));
-  if (s != RMG_OK) { free_map(m); return s; }
-  s = cuda_status(cudaMemcpyAsync(m->d_vertices, vertices, 12 * (size_t)n_vertices,
-                                  cudaMemcpyHostToDevice, st), "copy vertices");
-  if (s == RMG_OK)
-    s = cuda_status(cudaMemcpyAsync(m->d_faces, faces, 12 * (size_t)n_faces,
-                                    cudaMemcpyHostToDevice, st), "copy faces");
-  if (s != RMG_OK) { free_map(m); return s; }
-
-  if (n_faces == 1) {
-    Node node;
-    const uint32_t local[3] = {0, 1, 2};
-    float v[9];
-    for (int k = 0; k < 3; ++k) {
-      const uint32_t vi = k == 0 ? faces[0].v0 : (k == 1 ? faces[0].v1 : faces[0].v2);
-      v[3 * k + 0] = vertices[vi].x; v[3 * k + 1] = vertices[vi].y; v[3 * k + 2] = vertices[vi].z;
+  return guarded("rmg_map_build_ex", [&]() -> int {
+    if (!out) return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: out is NULL");
+    *out = nullptr;
+    if (builder != RMG_BUILD_SAH && builder != RMG_BUILD_LBVH)
+      return fail(RMG_ERR_UNSUPPORTED, "rmg_map_build_ex: builder must be RMG_BUILD_SAH or RMG_BUILD_LBVH");
+    *out = nullptr;
+    if (n_faces > 0 && (!vertices || !faces))
+      return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: vertices/faces are NULL");
+    if (n_faces > (1u << 30)) return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: too many faces");
+    for (uint32_t i = 0; i < n_faces; ++i) {
+      if (faces[i].v0 >= n_vertices || faces[i].v1 >= n_vertices || faces[i].v2 >= n_vertices)
+        return fail(RMG_ERR_INVALID_ARG, "rmg_map_build: face index out of range");
     }
-    single_node(v, local, &node);
-    const uint32_t zero = 0;
-    const int minus1 = -1;
-    s = cuda_status(cudaMemcpyAsync(m->d_nodes, &node, sizeof(Node), cudaMemcpyHostToDevice, st), "node");
-    if (s == RMG_OK) s = cuda_status(cudaMemcpyAsync(m->d_leaf_order, &zero, 4, cudaMemcpyHostToDevice, st), "order");
-    if (s == RMG_OK) s = cuda_status(cudaMemcpyAsync(m->d_leaf_parent, &minus1, 4, cudaMemcpyHostToDevice, st), "parent");
-    if (s == RMG_OK) {
-      k_pack<<<1, 32, 0, st>>>(m->d_vertices, m->d_faces, m->d_leaf_order, 1, m->d_tris, nullptr);
-      s = cuda_status(cudaGetLastError(), "k_pack");
+    cudaStream_t st = as_stream(stream);
+    rmg_map* m = new (std::nothrow) rmg_map;
+    if (!m) return fail(RMG_ERR_OOM, "rmg_map_build: host allocation");
+    std::memset(m, 0, sizeof(*m));
+    cudaGetDevice(&m->device);
+    m->n_vertices = n_vertices;
+    m->n_faces = n_faces;
+    m->n_nodes = n_faces >= 2 ? n_faces - 1 : (n_faces == 1 ? 1 : 0);
+  
+    int s = RMG_OK;
+    auto check = [&](int r) { if (s == RMG_OK) s = r; return s == RMG_OK; };
+  
+    check(dev_alloc(&m->d_status, 1, "status"));
+    if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(m->d_status, 0, sizeof(unsigned int), st), "memset");
+    if (s == RMG_OK && n_faces == 0) {
+      s = cuda_status(cudaStreamSynchronize(st), "sync");
+      if (s != RMG_OK) { free_map(m); return s; }
+      update_info(m, st);
+      *out = m;
+      return RMG_OK;
     }
-    if (s == RMG_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
+    check(dev_alloc(&m->d_vertices, 3 * (size_t)n_vertices, "vertices"));
+    check(dev_alloc(&m->d_faces, 3 * (size_t)n_faces, "faces"));
+    check(dev_alloc(&m->d_nodes, m->n_nodes, "nodes"));
+    check(dev_alloc(&m->d_tris, n_faces, "tris"));
+    check(dev_alloc(&m->d_leaf_order, n_faces, "leaf order"));
+    check(dev_alloc(&m->d_leaf_parent, n_faces, "leaf parent"));
+    check(dev_alloc(&m->d_flags, m->n_nodes, "flags"));
     if (s != RMG_OK) { free_map(m); return s; }
-    m->depth = 1;
-    s = wide_build(m, st);
+    s = cuda_status(cudaMemcpyAsync(m->d_vertices, vertices, 12 * (size_t)n_vertices,
+                                    cudaMemcpyHostToDevice, st), "copy vertices");
+    if (s == RMG_OK)
+      s = cuda_status(cudaMemcpyAsync(m->d_faces, faces, 12 * (size_t)n_faces,
+                                      cudaMemcpyHostToDevice, st), "copy faces");
     if (s != RMG_OK) { free_map(m); return s; }
-    update_info(m, st);
-    *out = m;
-    return RMG_OK;
-  }
-
-  const uint32_t n = n_faces;
-  if (builder == RMG_BUILD_SAH) {
-    s = sah_build_topology(m, st, m->d_leaf_order);
-    if (s == RMG_OK) s = repack_and_refit(m, st, m->d_leaf_order);
+  
+    if (n_faces == 1) {
+      Node node;
+      const uint32_t local[3] = {0, 1, 2};
+      float v[9];
+      for (int k = 0; k < 3; ++k) {
+        const uint32_t vi = k == 0 ? faces[0].v0 : (k == 1 ? faces[0].v1 : faces[0].v2);
+        v[3 * k + 0] = vertices[vi].x; v[3 * k + 1] = vertices[vi].y; v[3 * k + 2] = vertices[vi].z;
+      }
+      single_node(v, local, &node);
+      const uint32_t zero = 0;
+      const int minus1 = -1;
+      s = cuda_status(cudaMemcpyAsync(m->d_nodes, &node, sizeof(Node), cudaMemcpyHostToDevice, st), "node");
+      if (s == RMG_OK) s = cuda_status(cudaMemcpyAsync(m->d_leaf_order, &zero, 4, cudaMemcpyHostToDevice, st), "order");
+      if (s == RMG_OK) s = cuda_status(cudaMemcpyAsync(m->d_leaf_parent, &minus1, 4, cudaMemcpyHostToDevice, st), "parent");
+      if (s == RMG_OK) {
+        k_pack<<<1, 32, 0, st>>>(m->d_vertices, m->d_faces, m->d_leaf_order, 1, m->d_tris, nullptr);
+        s = cuda_status(cudaGetLastError(), "k_pack");
+      }
+      if (s == RMG_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
+      if (s != RMG_OK) { free_map(m); return s; }
+      m->depth = 1;
+      s = wide_build(m, st);
+      if (s != RMG_OK) { free_map(m); return s; }
+      update_info(m, st);
+      *out = m;
+      return RMG_OK;
+    }
+  
+    const uint32_t n = n_faces;
+    if (builder == RMG_BUILD_SAH) {
+      s = sah_build_topology(m, st, m->d_leaf_order);
+      if (s == RMG_OK) s = repack_and_refit(m, st, m->d_leaf_order);
+      unsigned int* d_depth = nullptr;
+      if (s == RMG_OK) s = dev_alloc(&d_depth, 1, "depth");
+      if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(d_depth, 0, 4, st), "memset");
+      if (s == RMG_OK) {
+        k_depth<<<grid_for(n), kBlock, 0, st>>>(m->d_nodes, m->d_leaf_parent, n, d_depth);
+        s = cuda_status(cudaGetLastError(), "depth");
+      }
+      unsigned int depth = 0;
+      if (s == RMG_OK) s = cuda_status(cudaMemcpyAsync(&depth, d_depth, 4, cudaMemcpyDeviceToHost, st), "depth copy");
+      if (s == RMG_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
+      cudaFree(d_depth);
+      if (s != RMG_OK) { free_map(m); return s; }
+      m->depth = depth;
+      s = wide_build(m, st);
+      if (s != RMG_OK) { free_map(m); return s; }
+      update_info(m, st);
+      *out = m;
+      return RMG_OK;
+    }
+  
+    // ---- LBVH scratch -----------------------------------------------------
+    const int nb = std::min<int>((int)grid_for(n), 4 * device_sm_count());
+    float* d_partial = nullptr;
+    float* d_bounds = nullptr;
+    uint64_t *d_keys = nullptr, *d_keys2 = nullptr;
+    uint32_t *d_vals = nullptr, *d_vals2 = nullptr;
     unsigned int* d_depth = nullptr;
-    if (s == RMG_OK) s = dev_alloc(&d_depth, 1, "depth");
+    void* d_temp = nullptr;
+    size_t temp_bytes = 0;
+    check(dev_alloc(&d_partial, 6 * (size_t)nb, "partial bounds"));
+    check(dev_alloc(&d_bounds, 6, "bounds"));
+    check(dev_alloc(&d_keys, n, "keys"));
+    check(dev_alloc(&d_keys2, n, "keys2"));
+    check(dev_alloc(&d_vals, n, "vals"));
+    check(dev_alloc(&d_vals2, n, "vals2"));
+    check(dev_alloc(&d_depth, 1, "depth"));
+    if (s == RMG_OK) {
+      s = cuda_status(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, d_keys, d_keys2, d_vals,
+                                                       d_vals2, (int)n, 0, 63, st), "sort size");
+    }
+    if (s == RMG_OK) {
+      char* tmp = nullptr;
+      s = dev_alloc(&tmp, temp_bytes, "sort temp");
+      d_temp = tmp;
+    }
+    if (s == RMG_OK) {
+      k_centroid_bounds<<<nb, kBlock, 0, st>>>(m->d_vertices, m->d_faces, n, d_partial);
+      k_bounds_final<<<1, 32, 0, st>>>(d_partial, nb, d_bounds);
+      k_morton<<<grid_for(n), kBlock, 0, st>>>(m->d_vertices, m->d_faces, n, d_bounds, d_keys, d_vals);
+      s = cuda_status(cudaGetLastError(), "morton");
+    }
+    if (s == RMG_OK)
+      s = cuda_status(cub::DeviceRadixSort::SortPairs(d_temp, temp_bytes, d_keys, d_keys2, d_vals,
+                                                       d_vals2, (int)n, 0, 63, st), "sort");
+    if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(m->d_nodes, 0, sizeof(Node) * m->n_nodes, st), "memset");
+    if (s == RMG_OK) {
+      k_karras<<<grid_for(n - 1), kBlock, 0, st>>>(d_keys2, (int)n, m->d_nodes, m->d_leaf_parent);
+      k_pack<<<grid_for(n), kBlock, 0, st>>>(m->d_vertices, m->d_faces, d_vals2, n, m->d_tris,
+                                            m->d_leaf_order);
+      s = cuda_status(cudaGetLastError(), "karras");
+    }
+    if (s == RMG_OK) s = repack_and_refit(m, st, m->d_leaf_order);
     if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(d_depth, 0, 4, st), "memset");
     if (s == RMG_OK) {
       k_depth<<<grid_for(n), kBlock, 0, st>>>(m->d_nodes, m->d_leaf_parent, n, d_depth);
@@ -443,7 +508,8 @@ extern "C" int rmg_map_build_ex(const rmg_vec3* vertices, uint32_t n_vertices, c
     unsigned int depth = 0;
     if (s == RMG_OK) s = cuda_status(cudaMemcpyAsync(&depth, d_depth, 4, cudaMemcpyDeviceToHost, st), "depth copy");
     if (s == RMG_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
-    cudaFree(d_depth);
+    cudaFree(d_partial); cudaFree(d_bounds); cudaFree(d_keys); cudaFree(d_keys2);
+    cudaFree(d_vals); cudaFree(d_vals2); cudaFree(d_depth); cudaFree(d_temp);
     if (s != RMG_OK) { free_map(m); return s; }
     m->depth = depth;
     s = wide_build(m, st);
@@ -451,116 +517,64 @@ extern "C" int rmg_map_build_ex(const rmg_vec3* vertices, uint32_t n_vertices, c
     update_info(m, st);
     *out = m;
     return RMG_OK;
-  }
-
-  // ---- LBVH scratch -----------------------------------------------------
-  const int nb = std::min<int>((int)grid_for(n), 4 * device_sm_count());
-  float* d_partial = nullptr;
-  float* d_bounds = nullptr;
-  uint64_t *d_keys = nullptr, *d_keys2 = nullptr;
-  uint32_t *d_vals = nullptr, *d_vals2 = nullptr;
-  unsigned int* d_depth = nullptr;
-  void* d_temp = nullptr;
-  size_t temp_bytes = 0;
-  check(dev_alloc(&d_partial, 6 * (size_t)nb, "partial bounds"));
-  check(dev_alloc(&d_bounds, 6, "bounds"));
-  check(dev_alloc(&d_keys, n, "keys"));
-  check(dev_alloc(&d_keys2, n, "keys2"));
-  check(dev_alloc(&d_vals, n, "vals"));
-  check(dev_alloc(&d_vals2, n, "vals2"));
-  check(dev_alloc(&d_depth, 1, "depth"));
-  if (s == RMG_OK) {
-    s = cuda_status(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, d_keys, d_keys2, d_vals,
-                                                     d_vals2, (int)n, 0, 63, st), "sort size");
-  }
-  if (s == RMG_OK) {
-    char* tmp = nullptr;
-    s = dev_alloc(&tmp, temp_bytes, "sort temp");
-    d_temp = tmp;
-  }
-  if (s == RMG_OK) {
-    k_centroid_bounds<<<nb, kBlock, 0, st>>>(m->d_vertices, m->d_faces, n, d_partial);
-    k_bounds_final<<<1, 32, 0, st>>>(d_partial, nb, d_bounds);
-    k_morton<<<grid_for(n), kBlock, 0, st>>>(m->d_vertices, m->d_faces, n, d_bounds, d_keys, d_vals);
-    s = cuda_status(cudaGetLastError(), "morton");
-  }
-  if (s == RMG_OK)
-    s = cuda_status(cub::DeviceRadixSort::SortPairs(d_temp, temp_bytes, d_keys, d_keys2, d_vals,
-                                                     d_vals2, (int)n, 0, 63, st), "sort");
-  if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(m->d_nodes, 0, sizeof(Node) * m->n_nodes, st), "memset");
-  if (s == RMG_OK) {
-    k_karras<<<grid_for(n - 1), kBlock, 0, st>>>(d_keys2, (int)n, m->d_nodes, m->d_leaf_parent);
-    k_pack<<<grid_for(n), kBlock, 0, st>>>(m->d_vertices, m->d_faces, d_vals2, n, m->d_tris,
-                                          m->d_leaf_order);
-    s = cuda_status(cudaGetLastError(), "karras");
-  }
-  if (s == RMG_OK) s = repack_and_refit(m, st, m->d_leaf_order);
-  if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(d_depth, 0, 4, st), "memset");
-  if (s == RMG_OK) {
-    k_depth<<<grid_for(n), kBlock, 0, st>>>(m->d_nodes, m->d_leaf_parent, n, d_depth);
-    s = cuda_status(cudaGetLastError(), "depth");
-  }
-  unsigned int depth = 0;
-  if (s == RMG_OK) s = cuda_status(cudaMemcpyAsync(&depth, d_depth, 4, cudaMemcpyDeviceToHost, st), "depth copy");
-  if (s == RMG_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
-  cudaFree(d_partial); cudaFree(d_bounds); cudaFree(d_keys); cudaFree(d_keys2);
-  cudaFree(d_vals); cudaFree(d_vals2); cudaFree(d_depth); cudaFree(d_temp);
-  if (s != RMG_OK) { free_map(m); return s; }
-  m->depth = depth;
-  s = wide_build(m, st);
-  if (s != RMG_OK) { free_map(m); return s; }
-  update_info(m, st);
-  *out = m;
-  return RMG_OK;
+  });
 }
 
 extern "C" int rmg_map_refit(rmg_map* m, const rmg_vec3* vertices, uint32_t n_vertices, void* stream) {
-  if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_refit: map is NULL");
-  if (n_vertices != m->n_vertices)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_map_refit: vertex count differs from the build");
-  if (m->n_faces == 0) return RMG_OK;
-  if (!vertices) return fail(RMG_ERR_INVALID_ARG, "rmg_map_refit: vertices is NULL");
-  cudaStream_t st = as_stream(stream);
-  RMG_CUDA_TRY(cudaMemcpyAsync(m->d_vertices, vertices, 12 * (size_t)n_vertices,
-                               cudaMemcpyHostToDevice, st));
-  int s = repack_and_refit(m, st, m->d_leaf_order);
-  if (s == RMG_OK) s = wide_refit(m, st);
-  if (s != RMG_OK) return s;
-  RMG_CUDA_TRY(cudaStreamSynchronize(st));
-  update_info(m, st);
-  return RMG_OK;
+  return guarded("rmg_map_refit", [&]() -> int {
+    if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_refit: map is NULL");
+    if (n_vertices != m->n_vertices)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_map_refit: vertex count differs from the build");
+    if (m->n_faces == 0) return RMG_OK;
+    if (!vertices) return fail(RMG_ERR_INVALID_ARG, "rmg_map_refit: vertices is NULL");
+    cudaStream_t st = as_stream(stream);
+    RMG_CUDA_TRY(cudaMemcpyAsync(m->d_vertices, vertices, 12 * (size_t)n_vertices,
+                                 cudaMemcpyHostToDevice, st));
+    int s = repack_and_refit(m, st, m->d_leaf_order);
+    if (s == RMG_OK) s = wide_refit(m, st);
+    if (s != RMG_OK) return s;
+    RMG_CUDA_TRY(cudaStreamSynchronize(st));
+    update_info(m, st);
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_map_destroy(rmg_map* m) {
-  if (!m) return RMG_OK;
-  free_map(m);
-  return RMG_OK;
+  return guarded("rmg_map_destroy", [&]() -> int {
+    if (!m) return RMG_OK;
+    free_map(m);
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_map_info_get(const rmg_map* m, rmg_map_info* out) {
-  if (!m || !out) return fail(RMG_ERR_INVALID_ARG, "rmg_map_info_get: NULL argument");
-  out->n_vertices = m->n_vertices;
-  out->n_faces = m->n_faces;
-  out->n_nodes = m->n_nodes;
-  out->depth = m->depth;
-  out->device_bytes = (uint64_t)m->n_nodes * sizeof(Node) + (uint64_t)m->n_faces * sizeof(Tri) +
-                      12ull * m->n_vertices + 12ull * m->n_faces +
-                      (uint64_t)m->n_nodes4 * (sizeof(Node4) + 4 * sizeof(int)) +
-                      (uint64_t)m->n_nodes8 * (sizeof(Node8) + 8 * sizeof(int)) +
-                      (m->d_tris8 ? (uint64_t)m->n_faces * sizeof(Tri) : 0ull);
-  for (int k = 0; k < 3; ++k) { out->bounds_lo[k] = m->lo[k]; out->bounds_hi[k] = m->hi[k]; }
-  return RMG_OK;
+  return guarded("rmg_map_info_get", [&]() -> int {
+    if (!m || !out) return fail(RMG_ERR_INVALID_ARG, "rmg_map_info_get: NULL argument");
+    out->n_vertices = m->n_vertices;
+    out->n_faces = m->n_faces;
+    out->n_nodes = m->n_nodes;
+    out->depth = m->depth;
+    out->device_bytes = (uint64_t)m->n_nodes * sizeof(Node) + (uint64_t)m->n_faces * sizeof(Tri) +
+                        12ull * m->n_vertices + 12ull * m->n_faces +
+                        (uint64_t)m->n_nodes4 * (sizeof(Node4) + 4 * sizeof(int)) +
+                        (uint64_t)m->n_nodes8 * (sizeof(Node8) + 8 * sizeof(int)) +
+                        (m->d_tris8 ? (uint64_t)m->n_faces * sizeof(Tri) : 0ull);
+    for (int k = 0; k < 3; ++k) { out->bounds_lo[k] = m->lo[k]; out->bounds_hi[k] = m->hi[k]; }
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_map_export(const rmg_map* m, void* nodes, void* tris, uint32_t* leaf_order) {
-  if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_export: map is NULL");
-  if (nodes && m->n_nodes)
-    RMG_CUDA_TRY(cudaMemcpy(nodes, m->d_nodes, sizeof(Node) * m->n_nodes, cudaMemcpyDeviceToHost));
-  if (tris && m->n_faces)
-    RMG_CUDA_TRY(cudaMemcpy(tris, m->d_tris, sizeof(Tri) * m->n_faces, cudaMemcpyDeviceToHost));
-  if (leaf_order && m->n_faces)
-    RMG_CUDA_TRY(cudaMemcpy(leaf_order, m->d_leaf_order, 4ull * m->n_faces, cudaMemcpyDeviceToHost));
-  return RMG_OK;
+  return guarded("rmg_map_export", [&]() -> int {
+    if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_export: map is NULL");
+    if (nodes && m->n_nodes)
+      RMG_CUDA_TRY(cudaMemcpy(nodes, m->d_nodes, sizeof(Node) * m->n_nodes, cudaMemcpyDeviceToHost));
+    if (tris && m->n_faces)
+      RMG_CUDA_TRY(cudaMemcpy(tris, m->d_tris, sizeof(Tri) * m->n_faces, cudaMemcpyDeviceToHost));
+    if (leaf_order && m->n_faces)
+      RMG_CUDA_TRY(cudaMemcpy(leaf_order, m->d_leaf_order, 4ull * m->n_faces, cudaMemcpyDeviceToHost));
+    return RMG_OK;
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -667,155 +681,163 @@ int check_tree(const MapFileHeader& h, const uint32_t* faces, const Node* nodes,
 }  // namespace
 
 extern "C" int rmg_map_save(const rmg_map* m, const char* path) {
-  if (!m || !path) return fail(RMG_ERR_INVALID_ARG, "rmg_map_save: NULL argument");
-  const uint64_t nv = m->n_vertices, nf = m->n_faces, nn = m->n_nodes;
-  std::vector<unsigned char> payload(payload_size(nv, nf, nn));
-  unsigned char* p = payload.data();
-  auto dl = [&](const void* src, size_t bytes) -> int {
-    if (bytes) RMG_CUDA_TRY(cudaMemcpy(p, src, bytes, cudaMemcpyDeviceToHost));
-    p += bytes;
-    return RMG_OK;
-  };
-  int s = RMG_OK;
-  if (s == RMG_OK) s = dl(m->d_vertices, 12 * nv);
-  if (s == RMG_OK) s = dl(m->d_faces, 12 * nf);
-  if (s == RMG_OK) s = dl(m->d_nodes, sizeof(Node) * nn);
-  if (s == RMG_OK) s = dl(m->d_tris, sizeof(Tri) * nf);
-  if (s == RMG_OK) s = dl(m->d_leaf_order, 4 * nf);
-  if (s == RMG_OK) s = dl(m->d_leaf_parent, 4 * nf);
-  if (s != RMG_OK) return s;
-  MapFileHeader h;
-  std::memset(&h, 0, sizeof(h));
-  std::memcpy(h.magic, kMapMagic, 8);
-  h.version = 1;
-  h.n_vertices = m->n_vertices;
-  h.n_faces = m->n_faces;
-  h.n_nodes = m->n_nodes;
-  h.depth = m->depth;
-  h.payload_bytes = payload.size();
-  h.checksum = fnv1a64(payload.data(), payload.size());
-  FILE* fp = std::fopen(path, "wb");
-  if (!fp) return fail(RMG_ERR_INVALID_ARG, std::string("rmg_map_save: cannot write ") + path);
-  bool ok = std::fwrite(&h, sizeof(h), 1, fp) == 1;
-  ok = ok && (payload.empty() || std::fwrite(payload.data(), 1, payload.size(), fp) == payload.size());
-  ok = (std::fclose(fp) == 0) && ok;
-  return ok ? RMG_OK : fail(RMG_ERR_INVALID_ARG, "rmg_map_save: write failed");
+  return guarded("rmg_map_save", [&]() -> int {
+    if (!m || !path) return fail(RMG_ERR_INVALID_ARG, "rmg_map_save: NULL argument");
+    const uint64_t nv = m->n_vertices, nf = m->n_faces, nn = m->n_nodes;
+    std::vector<unsigned char> payload(payload_size(nv, nf, nn));
+    unsigned char* p = payload.data();
+    auto dl = [&](const void* src, size_t bytes) -> int {
+      if (bytes) RMG_CUDA_TRY(cudaMemcpy(p, src, bytes, cudaMemcpyDeviceToHost));
+      p += bytes;
+      return RMG_OK;
+    };
+    int s = RMG_OK;
+    if (s == RMG_OK) s = dl(m->d_vertices, 12 * nv);
+    if (s == RMG_OK) s = dl(m->d_faces, 12 * nf);
+    if (s == RMG_OK) s = dl(m->d_nodes, sizeof(Node) * nn);
+    if (s == RMG_OK) s = dl(m->d_tris, sizeof(Tri) * nf);
+    if (s == RMG_OK) s = dl(m->d_leaf_order, 4 * nf);
+    if (s == RMG_OK) s = dl(m->d_leaf_parent, 4 * nf);
+    if (s != RMG_OK) return s;
+    MapFileHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, kMapMagic, 8);
+    h.version = 1;
+    h.n_vertices = m->n_vertices;
+    h.n_faces = m->n_faces;
+    h.n_nodes = m->n_nodes;
+    h.depth = m->depth;
+    h.payload_bytes = payload.size();
+    h.checksum = fnv1a64(payload.data(), payload.size());
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return fail(RMG_ERR_INVALID_ARG, std::string("rmg_map_save: cannot write ") + path);
+    bool ok = std::fwrite(&h, sizeof(h), 1, fp) == 1;
+    ok = ok && (payload.empty() || std::fwrite(payload.data(), 1, payload.size(), fp) == payload.size());
+    ok = (std::fclose(fp) == 0) && ok;
+    return ok ? RMG_OK : fail(RMG_ERR_INVALID_ARG, "rmg_map_save: write failed");
+  });
 }
 
 extern "C" int rmg_map_load(const char* path, void* stream, rmg_map** out) {
-  if (!path || !out) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: NULL argument");
-  *out = nullptr;
-  FILE* fp = std::fopen(path, "rb");
-  if (!fp) return fail(RMG_ERR_INVALID_ARG, std::string("rmg_map_load: cannot read ") + path);
-  MapFileHeader h;
-  bool ok = std::fread(&h, sizeof(h), 1, fp) == 1;
-  if (!ok || std::memcmp(h.magic, kMapMagic, 8) != 0 || h.version != 1) {
+  return guarded("rmg_map_load", [&]() -> int {
+    if (!path || !out) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: NULL argument");
+    *out = nullptr;
+    FILE* fp = std::fopen(path, "rb");
+    if (!fp) return fail(RMG_ERR_INVALID_ARG, std::string("rmg_map_load: cannot read ") + path);
+    MapFileHeader h;
+    bool ok = std::fread(&h, sizeof(h), 1, fp) == 1;
+    if (!ok || std::memcmp(h.magic, kMapMagic, 8) != 0 || h.version != 1) {
+      std::fclose(fp);
+      return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: not a map file of this version");
+    }
+    if (h.n_faces > (1u << 30) || h.payload_bytes != payload_size(h.n_vertices, h.n_faces, h.n_nodes)) {
+      std::fclose(fp);
+      return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: sizes in the header do not agree");
+    }
+    std::vector<unsigned char> payload(h.payload_bytes);
+    ok = payload.empty() || std::fread(payload.data(), 1, payload.size(), fp) == payload.size();
+    const bool trailing = std::fgetc(fp) != EOF;
     std::fclose(fp);
-    return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: not a map file of this version");
-  }
-  if (h.n_faces > (1u << 30) || h.payload_bytes != payload_size(h.n_vertices, h.n_faces, h.n_nodes)) {
-    std::fclose(fp);
-    return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: sizes in the header do not agree");
-  }
-  std::vector<unsigned char> payload(h.payload_bytes);
-  ok = payload.empty() || std::fread(payload.data(), 1, payload.size(), fp) == payload.size();
-  const bool trailing = std::fgetc(fp) != EOF;
-  std::fclose(fp);
-  if (!ok || trailing) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: file size does not match the header");
-  if (fnv1a64(payload.data(), payload.size()) != h.checksum)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: checksum mismatch (damaged file)");
-  const uint64_t nv = h.n_vertices, nf = h.n_faces, nn = h.n_nodes;
-  const unsigned char* p = payload.data();
-  const unsigned char* pv = p;
-  const unsigned char* pf = pv + 12 * nv;
-  const unsigned char* pn = pf + 12 * nf;
-  const unsigned char* pt = pn + sizeof(Node) * nn;
-  const unsigned char* po = pt + sizeof(Tri) * nf;
-  const unsigned char* pp = po + 4 * nf;
-  // aligned host copies for the checks
-  std::vector<uint32_t> faces(3 * nf), order(nf);
-  std::vector<Node> nodes(nn);
-  std::vector<Tri> tris(nf);
-  std::vector<int> parents(nf);
-  if (nf) std::memcpy(faces.data(), pf, 12 * nf);
-  if (nn) std::memcpy(nodes.data(), pn, sizeof(Node) * nn);
-  if (nf) {
-    std::memcpy(tris.data(), pt, sizeof(Tri) * nf);
-    std::memcpy(order.data(), po, 4 * nf);
-    std::memcpy(parents.data(), pp, 4 * nf);
-  }
-  uint32_t depth = 0;
-  int s = check_tree(h, faces.data(), nodes.data(), tris.data(), order.data(), parents.data(), &depth);
-  if (s != RMG_OK) return s;
-  cudaStream_t st = as_stream(stream);
-  rmg_map* m = new (std::nothrow) rmg_map;
-  if (!m) return fail(RMG_ERR_OOM, "rmg_map_load: host allocation");
-  std::memset(m, 0, sizeof(*m));
-  cudaGetDevice(&m->device);
-  m->n_vertices = h.n_vertices;
-  m->n_faces = h.n_faces;
-  m->n_nodes = h.n_nodes;
-  m->depth = depth;
-  auto check = [&](int r) { if (s == RMG_OK) s = r; };
-  check(dev_alloc(&m->d_status, 1, "status"));
-  check(dev_alloc(&m->d_vertices, 3 * nv, "vertices"));
-  check(dev_alloc(&m->d_faces, 3 * nf, "faces"));
-  check(dev_alloc(&m->d_nodes, nn, "nodes"));
-  check(dev_alloc(&m->d_tris, nf, "tris"));
-  check(dev_alloc(&m->d_leaf_order, nf, "leaf order"));
-  check(dev_alloc(&m->d_leaf_parent, nf, "leaf parent"));
-  check(dev_alloc(&m->d_flags, nn, "flags"));
-  auto up = [&](void* dst, const void* src, size_t bytes) {
-    if (s == RMG_OK && bytes) s = cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st), "upload");
-  };
-  if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(m->d_status, 0, 4, st), "memset");
-  up(m->d_vertices, pv, 12 * nv);
-  up(m->d_faces, faces.data(), 12 * nf);
-  up(m->d_nodes, nodes.data(), sizeof(Node) * nn);
-  up(m->d_tris, tris.data(), sizeof(Tri) * nf);
-  up(m->d_leaf_order, order.data(), 4 * nf);
-  up(m->d_leaf_parent, parents.data(), 4 * nf);
-  if (s == RMG_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
-  if (s == RMG_OK) s = wide_build(m, st);
-  if (s != RMG_OK) { free_map(m); return s; }
-  update_info(m, st);
-  *out = m;
-  return RMG_OK;
+    if (!ok || trailing) return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: file size does not match the header");
+    if (fnv1a64(payload.data(), payload.size()) != h.checksum)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_map_load: checksum mismatch (damaged file)");
+    const uint64_t nv = h.n_vertices, nf = h.n_faces, nn = h.n_nodes;
+    const unsigned char* p = payload.data();
+    const unsigned char* pv = p;
+    const unsigned char* pf = pv + 12 * nv;
+    const unsigned char* pn = pf + 12 * nf;
+    const unsigned char* pt = pn + sizeof(Node) * nn;
+    const unsigned char* po = pt + sizeof(Tri) * nf;
+    const unsigned char* pp = po + 4 * nf;
+    // aligned host copies for the checks
+    std::vector<uint32_t> faces(3 * nf), order(nf);
+    std::vector<Node> nodes(nn);
+    std::vector<Tri> tris(nf);
+    std::vector<int> parents(nf);
+    if (nf) std::memcpy(faces.data(), pf, 12 * nf);
+    if (nn) std::memcpy(nodes.data(), pn, sizeof(Node) * nn);
+    if (nf) {
+      std::memcpy(tris.data(), pt, sizeof(Tri) * nf);
+      std::memcpy(order.data(), po, 4 * nf);
+      std::memcpy(parents.data(), pp, 4 * nf);
+    }
+    uint32_t depth = 0;
+    int s = check_tree(h, faces.data(), nodes.data(), tris.data(), order.data(), parents.data(), &depth);
+    if (s != RMG_OK) return s;
+    cudaStream_t st = as_stream(stream);
+    rmg_map* m = new (std::nothrow) rmg_map;
+    if (!m) return fail(RMG_ERR_OOM, "rmg_map_load: host allocation");
+    std::memset(m, 0, sizeof(*m));
+    cudaGetDevice(&m->device);
+    m->n_vertices = h.n_vertices;
+    m->n_faces = h.n_faces;
+    m->n_nodes = h.n_nodes;
+    m->depth = depth;
+    auto check = [&](int r) { if (s == RMG_OK) s = r; };
+    check(dev_alloc(&m->d_status, 1, "status"));
+    check(dev_alloc(&m->d_vertices, 3 * nv, "vertices"));
+    check(dev_alloc(&m->d_faces, 3 * nf, "faces"));
+    check(dev_alloc(&m->d_nodes, nn, "nodes"));
+    check(dev_alloc(&m->d_tris, nf, "tris"));
+    check(dev_alloc(&m->d_leaf_order, nf, "leaf order"));
+    check(dev_alloc(&m->d_leaf_parent, nf, "leaf parent"));
+    check(dev_alloc(&m->d_flags, nn, "flags"));
+    auto up = [&](void* dst, const void* src, size_t bytes) {
+      if (s == RMG_OK && bytes) s = cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st), "upload");
+    };
+    if (s == RMG_OK) s = cuda_status(cudaMemsetAsync(m->d_status, 0, 4, st), "memset");
+    up(m->d_vertices, pv, 12 * nv);
+    up(m->d_faces, faces.data(), 12 * nf);
+    up(m->d_nodes, nodes.data(), sizeof(Node) * nn);
+    up(m->d_tris, tris.data(), sizeof(Tri) * nf);
+    up(m->d_leaf_order, order.data(), 4 * nf);
+    up(m->d_leaf_parent, parents.data(), 4 * nf);
+    if (s == RMG_OK) s = cuda_status(cudaStreamSynchronize(st), "sync");
+    if (s == RMG_OK) s = wide_build(m, st);
+    if (s != RMG_OK) { free_map(m); return s; }
+    update_info(m, st);
+    *out = m;
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_map_status(rmg_map* m, int clear) {
-  if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_status: map is NULL");
-  unsigned int word = 0;
-  RMG_CUDA_TRY(cudaMemcpy(&word, m->d_status, 4, cudaMemcpyDeviceToHost));
-  if (clear) RMG_CUDA_TRY(cudaMemset(m->d_status, 0, 4));
-  if (word != 0) {
-    set_error("a kernel recorded a device error on this map");
-    return (int)word;
-  }
-  return RMG_OK;
+  return guarded("rmg_map_status", [&]() -> int {
+    if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_status: map is NULL");
+    unsigned int word = 0;
+    RMG_CUDA_TRY(cudaMemcpy(&word, m->d_status, 4, cudaMemcpyDeviceToHost));
+    if (clear) RMG_CUDA_TRY(cudaMemset(m->d_status, 0, 4));
+    if (word != 0) {
+      set_error("a kernel recorded a device error on this map");
+      return (int)word;
+    }
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_map_debug_set_child(rmg_map* m, uint32_t node, uint32_t which, int32_t child) {
-  if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: map is NULL");
-  if (which >= 2) {  // a slot of the 4-wide tree
-    if (!m->d_nodes4 || node >= m->n_nodes4 || which > 5)
-      return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: wide node/slot out of range");
-    if (child >= 0 ? (uint32_t)child >= m->n_nodes4 : (uint32_t)(~child) >= m->n_faces)
+  return guarded("rmg_map_debug_set_child", [&]() -> int {
+    if (!m) return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: map is NULL");
+    if (which >= 2) {  // a slot of the 4-wide tree
+      if (!m->d_nodes4 || node >= m->n_nodes4 || which > 5)
+        return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: wide node/slot out of range");
+      if (child >= 0 ? (uint32_t)child >= m->n_nodes4 : (uint32_t)(~child) >= m->n_faces)
+        return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: child out of range");
+      const size_t off = offsetof(Node4, child) + sizeof(int) * (which - 2);
+      RMG_CUDA_TRY(cudaMemcpy(reinterpret_cast<char*>(m->d_nodes4 + node) + off, &child, sizeof(int),
+                              cudaMemcpyHostToDevice));
+      return RMG_OK;
+    }
+    if (node >= m->n_nodes)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: node/which out of range");
+    if (child >= 0 ? (uint32_t)child >= m->n_nodes : (uint32_t)(~child) >= m->n_faces)
       return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: child out of range");
-    const size_t off = offsetof(Node4, child) + sizeof(int) * (which - 2);
-    RMG_CUDA_TRY(cudaMemcpy(reinterpret_cast<char*>(m->d_nodes4 + node) + off, &child, sizeof(int),
+    const size_t off = offsetof(Node, d) + (which ? sizeof(int) : 0);
+    RMG_CUDA_TRY(cudaMemcpy(reinterpret_cast<char*>(m->d_nodes + node) + off, &child, sizeof(int),
                             cudaMemcpyHostToDevice));
+    wide_free(m);  // the binary tree is the one damaged: walk it from now on
     return RMG_OK;
-  }
-  if (node >= m->n_nodes)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: node/which out of range");
-  if (child >= 0 ? (uint32_t)child >= m->n_nodes : (uint32_t)(~child) >= m->n_faces)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_map_debug_set_child: child out of range");
-  const size_t off = offsetof(Node, d) + (which ? sizeof(int) : 0);
-  RMG_CUDA_TRY(cudaMemcpy(reinterpret_cast<char*>(m->d_nodes + node) + off, &child, sizeof(int),
-                          cudaMemcpyHostToDevice));
-  wide_free(m);  // the binary tree is the one damaged: walk it from now on
-  return RMG_OK;
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -912,72 +934,74 @@ int noalloc_setup(int dev, NoAllocSetup** out) {
 
 extern "C" int rmg_lbvh_build_noalloc(const rmg_vec3* vertices, uint32_t n_vertices, const rmg_face* faces,
                                       uint32_t n_faces, const rmg_lbvh_buffers* out, void* stream) {
-  if (!out) return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: out is NULL");
-  if (n_faces > RMG_NOALLOC_MAX_FACES)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: n_faces exceeds RMG_NOALLOC_MAX_FACES (65536)");
-  if (n_faces == 0) return RMG_OK;
-  if (!vertices || !faces || !out->nodes || !out->tris || !out->leaf_order || !out->leaf_parent || !out->flags)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: NULL input or output buffer");
-  if ((reinterpret_cast<uintptr_t>(out->nodes) | reinterpret_cast<uintptr_t>(out->tris)) & 15u)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: nodes/tris must be 16-byte aligned");
-  int dev = 0;
-  RMG_CUDA_TRY(cudaGetDevice(&dev));
-  NoAllocSetup* su = nullptr;
-  int s = noalloc_setup(dev, &su);
-  if (s != RMG_OK) return s;
-
-  cudaStream_t st = as_stream(stream);
-  const uint32_t n = n_faces;
-  const int nb = std::min<int>((int)grid_for(n), 4 * device_sm_count());
-  // carve the scratch array
-  unsigned char* p = su->base;
-  size_t off = 0;
-  auto take = [&](size_t bytes) { unsigned char* q = p + off; off = align256(off + bytes); return q; };
-  uint64_t* keys = reinterpret_cast<uint64_t*>(take(8ull * n));
-  uint64_t* keys2 = reinterpret_cast<uint64_t*>(take(8ull * n));
-  uint32_t* vals = reinterpret_cast<uint32_t*>(take(4ull * n));
-  uint32_t* vals2 = reinterpret_cast<uint32_t*>(take(4ull * n));
-  float* partial = reinterpret_cast<float*>(take(24ull * nb));
-  float* bounds = reinterpret_cast<float*>(take(24));
-  unsigned int* bad = reinterpret_cast<unsigned int*>(take(4));
-  void* temp = take(su->sort_temp_bytes);
-  size_t temp_bytes = 0;
-  RMG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, keys, keys2, vals, vals2, (int)n, 0, 63, st));
-  if (off > kNoAllocScratchBytes || temp_bytes > su->sort_temp_bytes)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: scratch array too small for this mesh");
-
-  const float* v = reinterpret_cast<const float*>(vertices);
-  const uint32_t* f = reinterpret_cast<const uint32_t*>(faces);
-  Node* nodes = static_cast<Node*>(out->nodes);
-  Tri* tris = static_cast<Tri*>(out->tris);
-
-  // face indices are checked on the device before any kernel dereferences them
-  RMG_CUDA_TRY(cudaMemsetAsync(bad, 0, 4, st));
-  k_check_faces<<<grid_for(3ull * n), kBlock, 0, st>>>(f, n, n_vertices, bad);
-  RMG_CUDA_TRY(cudaGetLastError());
-  unsigned int bad_h = 0;
-  RMG_CUDA_TRY(cudaMemcpyAsync(&bad_h, bad, 4, cudaMemcpyDeviceToHost, st));
-  RMG_CUDA_TRY(cudaStreamSynchronize(st));
-  if (bad_h) return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: face index out of range");
-
-  if (n == 1) {  // one node with a phantom far-away right child, built on `stream` like the rest
-    k_single_node<<<1, 32, 0, st>>>(v, f, nodes, out->leaf_order, out->leaf_parent, out->flags);
-    k_pack<<<1, 32, 0, st>>>(v, f, out->leaf_order, 1, tris, nullptr);
+  return guarded("rmg_lbvh_build_noalloc", [&]() -> int {
+    if (!out) return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: out is NULL");
+    if (n_faces > RMG_NOALLOC_MAX_FACES)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: n_faces exceeds RMG_NOALLOC_MAX_FACES (65536)");
+    if (n_faces == 0) return RMG_OK;
+    if (!vertices || !faces || !out->nodes || !out->tris || !out->leaf_order || !out->leaf_parent || !out->flags)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: NULL input or output buffer");
+    if ((reinterpret_cast<uintptr_t>(out->nodes) | reinterpret_cast<uintptr_t>(out->tris)) & 15u)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: nodes/tris must be 16-byte aligned");
+    int dev = 0;
+    RMG_CUDA_TRY(cudaGetDevice(&dev));
+    NoAllocSetup* su = nullptr;
+    int s = noalloc_setup(dev, &su);
+    if (s != RMG_OK) return s;
+  
+    cudaStream_t st = as_stream(stream);
+    const uint32_t n = n_faces;
+    const int nb = std::min<int>((int)grid_for(n), 4 * device_sm_count());
+    // carve the scratch array
+    unsigned char* p = su->base;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { unsigned char* q = p + off; off = align256(off + bytes); return q; };
+    uint64_t* keys = reinterpret_cast<uint64_t*>(take(8ull * n));
+    uint64_t* keys2 = reinterpret_cast<uint64_t*>(take(8ull * n));
+    uint32_t* vals = reinterpret_cast<uint32_t*>(take(4ull * n));
+    uint32_t* vals2 = reinterpret_cast<uint32_t*>(take(4ull * n));
+    float* partial = reinterpret_cast<float*>(take(24ull * nb));
+    float* bounds = reinterpret_cast<float*>(take(24));
+    unsigned int* bad = reinterpret_cast<unsigned int*>(take(4));
+    void* temp = take(su->sort_temp_bytes);
+    size_t temp_bytes = 0;
+    RMG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, keys, keys2, vals, vals2, (int)n, 0, 63, st));
+    if (off > kNoAllocScratchBytes || temp_bytes > su->sort_temp_bytes)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: scratch array too small for this mesh");
+  
+    const float* v = reinterpret_cast<const float*>(vertices);
+    const uint32_t* f = reinterpret_cast<const uint32_t*>(faces);
+    Node* nodes = static_cast<Node*>(out->nodes);
+    Tri* tris = static_cast<Tri*>(out->tris);
+  
+    // face indices are checked on the device before any kernel dereferences them
+    RMG_CUDA_TRY(cudaMemsetAsync(bad, 0, 4, st));
+    k_check_faces<<<grid_for(3ull * n), kBlock, 0, st>>>(f, n, n_vertices, bad);
+    RMG_CUDA_TRY(cudaGetLastError());
+    unsigned int bad_h = 0;
+    RMG_CUDA_TRY(cudaMemcpyAsync(&bad_h, bad, 4, cudaMemcpyDeviceToHost, st));
+    RMG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (bad_h) return fail(RMG_ERR_INVALID_ARG, "rmg_lbvh_build_noalloc: face index out of range");
+  
+    if (n == 1) {  // one node with a phantom far-away right child, built on `stream` like the rest
+      k_single_node<<<1, 32, 0, st>>>(v, f, nodes, out->leaf_order, out->leaf_parent, out->flags);
+      k_pack<<<1, 32, 0, st>>>(v, f, out->leaf_order, 1, tris, nullptr);
+      RMG_CUDA_TRY(cudaGetLastError());
+      return RMG_OK;
+    }
+  
+    k_centroid_bounds<<<nb, kBlock, 0, st>>>(v, f, n, partial);
+    k_bounds_final<<<1, 32, 0, st>>>(partial, nb, bounds);
+    k_morton<<<grid_for(n), kBlock, 0, st>>>(v, f, n, bounds, keys, vals);
+    RMG_CUDA_TRY(cudaGetLastError());
+    RMG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(temp, temp_bytes, keys, keys2, vals, vals2, (int)n, 0, 63, st));
+    RMG_CUDA_TRY(cudaMemsetAsync(nodes, 0, sizeof(Node) * (n - 1), st));
+    k_karras<<<grid_for(n - 1), kBlock, 0, st>>>(keys2, (int)n, nodes, out->leaf_parent);
+    k_pack<<<grid_for(n), kBlock, 0, st>>>(v, f, vals2, n, tris, out->leaf_order);
+    RMG_CUDA_TRY(cudaGetLastError());
+    RMG_CUDA_TRY(cudaMemsetAsync(out->flags, 0, 4ull * (n - 1), st));
+    k_refit<<<grid_for(n), kBlock, 0, st>>>(nodes, tris, out->leaf_parent, out->flags, n);
     RMG_CUDA_TRY(cudaGetLastError());
     return RMG_OK;
-  }
-
-  k_centroid_bounds<<<nb, kBlock, 0, st>>>(v, f, n, partial);
-  k_bounds_final<<<1, 32, 0, st>>>(partial, nb, bounds);
-  k_morton<<<grid_for(n), kBlock, 0, st>>>(v, f, n, bounds, keys, vals);
-  RMG_CUDA_TRY(cudaGetLastError());
-  RMG_CUDA_TRY(cub::DeviceRadixSort::SortPairs(temp, temp_bytes, keys, keys2, vals, vals2, (int)n, 0, 63, st));
-  RMG_CUDA_TRY(cudaMemsetAsync(nodes, 0, sizeof(Node) * (n - 1), st));
-  k_karras<<<grid_for(n - 1), kBlock, 0, st>>>(keys2, (int)n, nodes, out->leaf_parent);
-  k_pack<<<grid_for(n), kBlock, 0, st>>>(v, f, vals2, n, tris, out->leaf_order);
-  RMG_CUDA_TRY(cudaGetLastError());
-  RMG_CUDA_TRY(cudaMemsetAsync(out->flags, 0, 4ull * (n - 1), st));
-  k_refit<<<grid_for(n), kBlock, 0, st>>>(nodes, tris, out->leaf_parent, out->flags, n);
-  RMG_CUDA_TRY(cudaGetLastError());
-  return RMG_OK;
+  });
 }

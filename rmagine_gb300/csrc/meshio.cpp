@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "../../include/rmg.h"
+#include "guard.h"
 
 namespace rmg {
 int fail(int status, const std::string& msg);
@@ -365,35 +366,37 @@ T* copy_out(const std::vector<T>& v) {
 }  // namespace
 
 extern "C" int rmg_mesh_read(const char* path, rmg_mesh* out) {
-  if (!path || !out) return rmg::fail(RMG_ERR_INVALID_ARG, "rmg_mesh_read: NULL argument");
-  std::memset(out, 0, sizeof(*out));
-  std::string data;
-  if (!read_file(path, data)) return rmg::fail(RMG_ERR_INVALID_ARG, std::string("rmg_mesh_read: cannot read ") + path);
-  const std::string p = lower(path);
-  auto ends = [&](const char* ext) {
-    const size_t n = std::strlen(ext);
-    return p.size() >= n && p.compare(p.size() - n, n, ext) == 0;
-  };
-  MeshBuf m;
-  int s;
-  if (ends(".ply")) s = read_ply(data, m);
-  else if (ends(".obj")) s = read_obj(data, m);
-  else if (ends(".stl")) s = read_stl(data, m);
-  else return rmg::fail(RMG_ERR_UNSUPPORTED, "rmg_mesh_read: file type not supported (.ply, .obj, .stl)");
-  if (s != RMG_OK) return s;
-  for (const rmg_face& f : m.f)
-    if (f.v0 >= m.v.size() || f.v1 >= m.v.size() || f.v2 >= m.v.size()) return bad("face index out of range");
-  out->vertices = copy_out(m.v);
-  out->faces = copy_out(m.f);
-  out->face_group = copy_out(m.g);
-  if ((!m.v.empty() && !out->vertices) || (!m.f.empty() && (!out->faces || !out->face_group))) {
-    rmg_mesh_free(out);
-    return rmg::fail(RMG_ERR_OOM, "rmg_mesh_read: host allocation");
-  }
-  out->n_vertices = (uint32_t)m.v.size();
-  out->n_faces = (uint32_t)m.f.size();
-  out->n_groups = m.f.empty() ? 0 : m.groups;
-  return RMG_OK;
+  return rmg::guarded("rmg_mesh_read", [&]() -> int {
+    if (!path || !out) return rmg::fail(RMG_ERR_INVALID_ARG, "rmg_mesh_read: NULL argument");
+    std::memset(out, 0, sizeof(*out));
+    std::string data;
+    if (!read_file(path, data)) return rmg::fail(RMG_ERR_INVALID_ARG, std::string("rmg_mesh_read: cannot read ") + path);
+    const std::string p = lower(path);
+    auto ends = [&](const char* ext) {
+      const size_t n = std::strlen(ext);
+      return p.size() >= n && p.compare(p.size() - n, n, ext) == 0;
+    };
+    MeshBuf m;
+    int s;
+    if (ends(".ply")) s = read_ply(data, m);
+    else if (ends(".obj")) s = read_obj(data, m);
+    else if (ends(".stl")) s = read_stl(data, m);
+    else return rmg::fail(RMG_ERR_UNSUPPORTED, "rmg_mesh_read: file type not supported (.ply, .obj, .stl)");
+    if (s != RMG_OK) return s;
+    for (const rmg_face& f : m.f)
+      if (f.v0 >= m.v.size() || f.v1 >= m.v.size() || f.v2 >= m.v.size()) return bad("face index out of range");
+    out->vertices = copy_out(m.v);
+    out->faces = copy_out(m.f);
+    out->face_group = copy_out(m.g);
+    if ((!m.v.empty() && !out->vertices) || (!m.f.empty() && (!out->faces || !out->face_group))) {
+      rmg_mesh_free(out);
+      return rmg::fail(RMG_ERR_OOM, "rmg_mesh_read: host allocation");
+    }
+    out->n_vertices = (uint32_t)m.v.size();
+    out->n_faces = (uint32_t)m.f.size();
+    out->n_groups = m.f.empty() ? 0 : m.groups;
+    return RMG_OK;
+  });
 }
 
 extern "C" void rmg_mesh_free(rmg_mesh* m) {
@@ -406,23 +409,25 @@ extern "C" void rmg_mesh_free(rmg_mesh* m) {
 
 extern "C" int rmg_mesh_write_ply(const char* path, const rmg_vec3* vertices, uint32_t n_vertices,
                                   const rmg_face* faces, uint32_t n_faces) {
-  if (!path || (n_vertices && !vertices) || (n_faces && !faces))
-    return rmg::fail(RMG_ERR_INVALID_ARG, "rmg_mesh_write_ply: NULL argument");
-  for (uint32_t i = 0; i < n_faces; ++i)
-    if (faces[i].v0 >= n_vertices || faces[i].v1 >= n_vertices || faces[i].v2 >= n_vertices)
-      return rmg::fail(RMG_ERR_INVALID_ARG, "rmg_mesh_write_ply: face index out of range");
-  FILE* fp = std::fopen(path, "wb");
-  if (!fp) return rmg::fail(RMG_ERR_INVALID_ARG, std::string("rmg_mesh_write_ply: cannot write ") + path);
-  const uint16_t probe = 1;
-  const bool little = *reinterpret_cast<const unsigned char*>(&probe) == 1;
-  std::fprintf(fp, "ply\nformat %s 1.0\nelement vertex %u\nproperty float x\nproperty float y\nproperty float z\n"
-               "element face %u\nproperty list uchar uint vertex_indices\nend_header\n",
-               little ? "binary_little_endian" : "binary_big_endian", n_vertices, n_faces);
-  bool ok = n_vertices == 0 || std::fwrite(vertices, sizeof(rmg_vec3), n_vertices, fp) == n_vertices;
-  for (uint32_t i = 0; ok && i < n_faces; ++i) {
-    const unsigned char c = 3;
-    ok = std::fwrite(&c, 1, 1, fp) == 1 && std::fwrite(&faces[i], sizeof(rmg_face), 1, fp) == 1;
-  }
-  ok = (std::fclose(fp) == 0) && ok;
-  return ok ? RMG_OK : rmg::fail(RMG_ERR_INVALID_ARG, "rmg_mesh_write_ply: write failed");
+  return rmg::guarded("rmg_mesh_write_ply", [&]() -> int {
+    if (!path || (n_vertices && !vertices) || (n_faces && !faces))
+      return rmg::fail(RMG_ERR_INVALID_ARG, "rmg_mesh_write_ply: NULL argument");
+    for (uint32_t i = 0; i < n_faces; ++i)
+      if (faces[i].v0 >= n_vertices || faces[i].v1 >= n_vertices || faces[i].v2 >= n_vertices)
+        return rmg::fail(RMG_ERR_INVALID_ARG, "rmg_mesh_write_ply: face index out of range");
+    FILE* fp = std::fopen(path, "wb");
+    if (!fp) return rmg::fail(RMG_ERR_INVALID_ARG, std::string("rmg_mesh_write_ply: cannot write ") + path);
+    const uint16_t probe = 1;
+    const bool little = *reinterpret_cast<const unsigned char*>(&probe) == 1;
+    std::fprintf(fp, "ply\nformat %s 1.0\nelement vertex %u\nproperty float x\nproperty float y\nproperty float z\n"
+                 "element face %u\nproperty list uchar uint vertex_indices\nend_header\n",
+                 little ? "binary_little_endian" : "binary_big_endian", n_vertices, n_faces);
+    bool ok = n_vertices == 0 || std::fwrite(vertices, sizeof(rmg_vec3), n_vertices, fp) == n_vertices;
+    for (uint32_t i = 0; ok && i < n_faces; ++i) {
+      const unsigned char c = 3;
+      ok = std::fwrite(&c, 1, 1, fp) == 1 && std::fwrite(&faces[i], sizeof(rmg_face), 1, fp) == 1;
+    }
+    ok = (std::fclose(fp) == 0) && ok;
+    return ok ? RMG_OK : rmg::fail(RMG_ERR_INVALID_ARG, "rmg_mesh_write_ply: write failed");
+  });
 }

@@ -343,58 +343,64 @@ int to_dev(const rmg_noise* noise, NoiseDev& p) {
 using namespace rmg;
 
 extern "C" int rmg_noise_apply(const rmg_noise* noise, float* ranges, uint64_t n, void* stream) {
-  NoiseDev p;
-  int s = to_dev(noise, p);
-  if (s != RMG_OK) return s;
-  if (n == 0) return RMG_OK;
-  if (!ranges) return fail(RMG_ERR_INVALID_ARG, "rmg_noise_apply: ranges is NULL");
-  const uint64_t groups = (n + 3) / 4;
-  uint64_t g0 = 0;
-  cudaStream_t st = as_stream(stream);
-  if (RMG_NOISE_TMA && (reinterpret_cast<uintptr_t>(ranges) & 15u) == 0) {
-    const uint64_t n_chunks = (n / 4) / kChunkF4;
-    if (n_chunks > 0) {
-      static thread_local int attr_device = -1;  // the ring may exceed the 48 KB default
-      int dev = 0;
-      RMG_CUDA_TRY(cudaGetDevice(&dev));
-      if (attr_device != dev) {
-        RMG_CUDA_TRY(cudaFuncSetAttribute(k_noise_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
-        attr_device = dev;
+  return guarded("rmg_noise_apply", [&]() -> int {
+    NoiseDev p;
+    int s = to_dev(noise, p);
+    if (s != RMG_OK) return s;
+    if (n == 0) return RMG_OK;
+    if (!ranges) return fail(RMG_ERR_INVALID_ARG, "rmg_noise_apply: ranges is NULL");
+    const uint64_t groups = (n + 3) / 4;
+    uint64_t g0 = 0;
+    cudaStream_t st = as_stream(stream);
+    if (RMG_NOISE_TMA && (reinterpret_cast<uintptr_t>(ranges) & 15u) == 0) {
+      const uint64_t n_chunks = (n / 4) / kChunkF4;
+      if (n_chunks > 0) {
+        static thread_local int attr_device = -1;  // the ring may exceed the 48 KB default
+        int dev = 0;
+        RMG_CUDA_TRY(cudaGetDevice(&dev));
+        if (attr_device != dev) {
+          RMG_CUDA_TRY(cudaFuncSetAttribute(k_noise_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRingBytes));
+          attr_device = dev;
+        }
+        const uint64_t cap = (uint64_t)RMG_NOISE_TMA_BLOCKS * (uint64_t)device_sm_count();  // resident CTAs
+        k_noise_tma<<<(unsigned)(n_chunks < cap ? n_chunks : cap), kTmaThreads, kRingBytes, st>>>(
+            reinterpret_cast<float4*>(ranges), n_chunks, p);
+        s = cuda_status(cudaGetLastError(), "k_noise_tma");
+        if (s != RMG_OK) return s;
+        g0 = n_chunks * kChunkF4;
       }
-      const uint64_t cap = (uint64_t)RMG_NOISE_TMA_BLOCKS * (uint64_t)device_sm_count();  // resident CTAs
-      k_noise_tma<<<(unsigned)(n_chunks < cap ? n_chunks : cap), kTmaThreads, kRingBytes, st>>>(
-          reinterpret_cast<float4*>(ranges), n_chunks, p);
-      s = cuda_status(cudaGetLastError(), "k_noise_tma");
-      if (s != RMG_OK) return s;
-      g0 = n_chunks * kChunkF4;
     }
-  }
-  if (g0 == groups) return RMG_OK;
-  const uint64_t want = (groups - g0 + 255) / 256;
-  const uint64_t cap = 8ull * (uint64_t)device_sm_count();  // grid-stride beyond this
-  const unsigned grid = (unsigned)(want < cap ? want : cap);
-  k_noise<<<grid, 256, 0, st>>>(ranges, n, g0, p);
-  return cuda_status(cudaGetLastError(), "k_noise");
+    if (g0 == groups) return RMG_OK;
+    const uint64_t want = (groups - g0 + 255) / 256;
+    const uint64_t cap = 8ull * (uint64_t)device_sm_count();  // grid-stride beyond this
+    const unsigned grid = (unsigned)(want < cap ? want : cap);
+    k_noise<<<grid, 256, 0, st>>>(ranges, n, g0, p);
+    return cuda_status(cudaGetLastError(), "k_noise");
+  });
 }
 
 extern "C" int rmg_noise_status(uint32_t* status, int clear) {
-  if (!status) return fail(RMG_ERR_INVALID_ARG, "rmg_noise_status: status is NULL");
-  unsigned v = 0;
-  RMG_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_noise_status, sizeof v));
-  *status = v;
-  if (clear) {
-    const unsigned zero = 0;
-    RMG_CUDA_TRY(cudaMemcpyToSymbol(g_noise_status, &zero, sizeof zero));
-  }
-  return RMG_OK;
+  return guarded("rmg_noise_status", [&]() -> int {
+    if (!status) return fail(RMG_ERR_INVALID_ARG, "rmg_noise_status: status is NULL");
+    unsigned v = 0;
+    RMG_CUDA_TRY(cudaMemcpyFromSymbol(&v, g_noise_status, sizeof v));
+    *status = v;
+    if (clear) {
+      const unsigned zero = 0;
+      RMG_CUDA_TRY(cudaMemcpyToSymbol(g_noise_status, &zero, sizeof zero));
+    }
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_noise_philox(const rmg_noise* noise, uint32_t* out, uint64_t n_blocks, void* stream) {
-  NoiseDev p;
-  int s = to_dev(noise, p);
-  if (s != RMG_OK) return s;
-  if (n_blocks == 0) return RMG_OK;
-  if (!out) return fail(RMG_ERR_INVALID_ARG, "rmg_noise_philox: out is NULL");
-  k_philox_raw<<<(unsigned)((n_blocks + 255) / 256), 256, 0, as_stream(stream)>>>(out, n_blocks, p);
-  return cuda_status(cudaGetLastError(), "k_philox_raw");
+  return guarded("rmg_noise_philox", [&]() -> int {
+    NoiseDev p;
+    int s = to_dev(noise, p);
+    if (s != RMG_OK) return s;
+    if (n_blocks == 0) return RMG_OK;
+    if (!out) return fail(RMG_ERR_INVALID_ARG, "rmg_noise_philox: out is NULL");
+    k_philox_raw<<<(unsigned)((n_blocks + 255) / 256), 256, 0, as_stream(stream)>>>(out, n_blocks, p);
+    return cuda_status(cudaGetLastError(), "k_philox_raw");
+  });
 }

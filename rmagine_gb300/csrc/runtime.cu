@@ -137,114 +137,126 @@ extern "C" const char* rmg_last_error(void) { return g_last_error.c_str(); }
 extern "C" int rmg_abi_version(void) { return RMG_ABI_VERSION; }
 
 extern "C" int rmg_device_info(int* sm_count, int* cc_major, int* cc_minor) {
-  int dev = 0;
-  RMG_CUDA_TRY(cudaGetDevice(&dev));
-  int sms = 0, ma = 0, mi = 0;
-  RMG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  RMG_CUDA_TRY(cudaDeviceGetAttribute(&ma, cudaDevAttrComputeCapabilityMajor, dev));
-  RMG_CUDA_TRY(cudaDeviceGetAttribute(&mi, cudaDevAttrComputeCapabilityMinor, dev));
-  if (sm_count) *sm_count = sms;
-  if (cc_major) *cc_major = ma;
-  if (cc_minor) *cc_minor = mi;
-  return RMG_OK;
+  return guarded("rmg_device_info", [&]() -> int {
+    int dev = 0;
+    RMG_CUDA_TRY(cudaGetDevice(&dev));
+    int sms = 0, ma = 0, mi = 0;
+    RMG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    RMG_CUDA_TRY(cudaDeviceGetAttribute(&ma, cudaDevAttrComputeCapabilityMajor, dev));
+    RMG_CUDA_TRY(cudaDeviceGetAttribute(&mi, cudaDevAttrComputeCapabilityMinor, dev));
+    if (sm_count) *sm_count = sms;
+    if (cc_major) *cc_major = ma;
+    if (cc_minor) *cc_minor = mi;
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_stream_wait(void* stream, uint32_t timeout_ms) {
-  cudaStream_t st = as_stream(stream);
-  const auto t0 = std::chrono::steady_clock::now();
-  for (;;) {
-    const cudaError_t e = cudaStreamQuery(st);
-    if (e == cudaSuccess) return RMG_OK;
-    if (e != cudaErrorNotReady) return cuda_status(e, "cudaStreamQuery");
-    const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(
-                        std::chrono::steady_clock::now() - t0).count();
-    if ((uint64_t)ms >= timeout_ms) return fail(RMG_ERR_TIMEOUT, "rmg_stream_wait: timed out");
-    std::this_thread::sleep_for(std::chrono::microseconds(100));
-  }
+  return guarded("rmg_stream_wait", [&]() -> int {
+    cudaStream_t st = as_stream(stream);
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+      const cudaError_t e = cudaStreamQuery(st);
+      if (e == cudaSuccess) return RMG_OK;
+      if (e != cudaErrorNotReady) return cuda_status(e, "cudaStreamQuery");
+      const auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(
+                          std::chrono::steady_clock::now() - t0).count();
+      if ((uint64_t)ms >= timeout_ms) return fail(RMG_ERR_TIMEOUT, "rmg_stream_wait: timed out");
+      std::this_thread::sleep_for(std::chrono::microseconds(100));
+    }
+  });
 }
 
 extern "C" int rmg_sensor_create(const rmg_model* model, void* stream, rmg_sensor** out) {
-  if (!out || !model) return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: NULL argument");
-  *out = nullptr;
-  uint32_t W = 0, H = 0;
-  switch (model->kind) {
-    case RMG_MODEL_SPHERICAL: W = model->theta.size; H = model->phi.size; break;
-    case RMG_MODEL_PINHOLE:
-      W = model->width; H = model->height;
-      if (!(model->f[0] != 0.0f) || !(model->f[1] != 0.0f))
-        return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: pinhole focal length is zero");
-      break;
-    case RMG_MODEL_O1DN:
-    case RMG_MODEL_ONDN:
-      W = model->width; H = model->height;
-      if (!model->dirs) return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: dirs is NULL");
-      if (model->kind == RMG_MODEL_ONDN && !model->origs)
-        return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: origs is NULL");
-      break;
-    default: return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: unknown model kind");
-  }
-  if (W == 0 || H == 0) return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: empty model");
-  if ((uint64_t)W * H > (1ull << 31)) return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: model too large");
-  if (!(model->range.max >= model->range.min))
-    return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: range.max < range.min");
-
-  cudaStream_t st = as_stream(stream);
-  rmg_sensor* s = new (std::nothrow) rmg_sensor;
-  if (!s) return fail(RMG_ERR_OOM, "rmg_sensor_create: host allocation");
-  std::memset(s, 0, sizeof(*s));
-  cudaGetDevice(&s->device);
-  s->model = *model;
-  s->model.dirs = nullptr;
-  s->model.origs = nullptr;
-  s->width = W;
-  s->height = H;
-  const size_t n = (size_t)W * H;
-  int r = dev_alloc(&s->d_dirs, 3 * n, "sensor dirs");
-  if (r == RMG_OK && model->kind == RMG_MODEL_ONDN) r = dev_alloc(&s->d_origs, 3 * n, "sensor origs");
-  if (r != RMG_OK) { free_sensor(s); return r; }
-  const unsigned grid = (unsigned)((n + 255) / 256);
-  switch (model->kind) {
-    case RMG_MODEL_SPHERICAL: {
-      std::vector<float> table;
-      dirs_spherical_host(model->phi, model->theta, table);
-      r = cuda_status(cudaMemcpyAsync(s->d_dirs, table.data(), 4 * table.size(), cudaMemcpyHostToDevice, st),
-                      "copy spherical dirs");
-      if (r == RMG_OK) r = cuda_status(cudaStreamSynchronize(st), "sensor sync");
-      break;
+  return guarded("rmg_sensor_create", [&]() -> int {
+    if (!out || !model) return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: NULL argument");
+    *out = nullptr;
+    uint32_t W = 0, H = 0;
+    switch (model->kind) {
+      case RMG_MODEL_SPHERICAL: W = model->theta.size; H = model->phi.size; break;
+      case RMG_MODEL_PINHOLE:
+        W = model->width; H = model->height;
+        if (!(model->f[0] != 0.0f) || !(model->f[1] != 0.0f))
+          return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: pinhole focal length is zero");
+        break;
+      case RMG_MODEL_O1DN:
+      case RMG_MODEL_ONDN:
+        W = model->width; H = model->height;
+        if (!model->dirs) return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: dirs is NULL");
+        if (model->kind == RMG_MODEL_ONDN && !model->origs)
+          return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: origs is NULL");
+        break;
+      default: return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: unknown model kind");
     }
-    case RMG_MODEL_PINHOLE:
-      k_dirs_pinhole<<<grid, 256, 0, st>>>(W, H, model->f[0], model->f[1], model->c[0], model->c[1],
-                                           s->d_dirs);
-      r = cuda_status(cudaGetLastError(), "k_dirs_pinhole");
-      break;
-    default:
-      r = cuda_status(cudaMemcpyAsync(s->d_dirs, model->dirs, 12 * n, cudaMemcpyHostToDevice, st),
-                      "copy dirs");
-      if (r == RMG_OK && model->kind == RMG_MODEL_ONDN)
-        r = cuda_status(cudaMemcpyAsync(s->d_origs, model->origs, 12 * n, cudaMemcpyHostToDevice, st),
-                        "copy origs");
-      break;
-  }
-  if (r == RMG_OK) r = cuda_status(cudaStreamSynchronize(st), "sensor sync");
-  if (r != RMG_OK) { free_sensor(s); return r; }
-  *out = s;
-  return RMG_OK;
+    if (W == 0 || H == 0) return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: empty model");
+    if ((uint64_t)W * H > (1ull << 31)) return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: model too large");
+    if (!(model->range.max >= model->range.min))
+      return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_create: range.max < range.min");
+  
+    cudaStream_t st = as_stream(stream);
+    rmg_sensor* s = new (std::nothrow) rmg_sensor;
+    if (!s) return fail(RMG_ERR_OOM, "rmg_sensor_create: host allocation");
+    std::memset(s, 0, sizeof(*s));
+    cudaGetDevice(&s->device);
+    s->model = *model;
+    s->model.dirs = nullptr;
+    s->model.origs = nullptr;
+    s->width = W;
+    s->height = H;
+    const size_t n = (size_t)W * H;
+    int r = dev_alloc(&s->d_dirs, 3 * n, "sensor dirs");
+    if (r == RMG_OK && model->kind == RMG_MODEL_ONDN) r = dev_alloc(&s->d_origs, 3 * n, "sensor origs");
+    if (r != RMG_OK) { free_sensor(s); return r; }
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    switch (model->kind) {
+      case RMG_MODEL_SPHERICAL: {
+        std::vector<float> table;
+        dirs_spherical_host(model->phi, model->theta, table);
+        r = cuda_status(cudaMemcpyAsync(s->d_dirs, table.data(), 4 * table.size(), cudaMemcpyHostToDevice, st),
+                        "copy spherical dirs");
+        if (r == RMG_OK) r = cuda_status(cudaStreamSynchronize(st), "sensor sync");
+        break;
+      }
+      case RMG_MODEL_PINHOLE:
+        k_dirs_pinhole<<<grid, 256, 0, st>>>(W, H, model->f[0], model->f[1], model->c[0], model->c[1],
+                                             s->d_dirs);
+        r = cuda_status(cudaGetLastError(), "k_dirs_pinhole");
+        break;
+      default:
+        r = cuda_status(cudaMemcpyAsync(s->d_dirs, model->dirs, 12 * n, cudaMemcpyHostToDevice, st),
+                        "copy dirs");
+        if (r == RMG_OK && model->kind == RMG_MODEL_ONDN)
+          r = cuda_status(cudaMemcpyAsync(s->d_origs, model->origs, 12 * n, cudaMemcpyHostToDevice, st),
+                          "copy origs");
+        break;
+    }
+    if (r == RMG_OK) r = cuda_status(cudaStreamSynchronize(st), "sensor sync");
+    if (r != RMG_OK) { free_sensor(s); return r; }
+    *out = s;
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_sensor_destroy(rmg_sensor* s) {
-  free_sensor(s);
-  return RMG_OK;
+  return guarded("rmg_sensor_destroy", [&]() -> int {
+    free_sensor(s);
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_sensor_directions(const rmg_sensor* s, rmg_vec3* host_out) {
-  if (!s || !host_out) return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_directions: NULL argument");
-  RMG_CUDA_TRY(cudaMemcpy(host_out, s->d_dirs, 12ull * s->width * s->height, cudaMemcpyDeviceToHost));
-  return RMG_OK;
+  return guarded("rmg_sensor_directions", [&]() -> int {
+    if (!s || !host_out) return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_directions: NULL argument");
+    RMG_CUDA_TRY(cudaMemcpy(host_out, s->d_dirs, 12ull * s->width * s->height, cudaMemcpyDeviceToHost));
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_sensor_size(const rmg_sensor* s, uint32_t* width, uint32_t* height) {
-  if (!s) return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_size: sensor is NULL");
-  if (width) *width = s->width;
-  if (height) *height = s->height;
-  return RMG_OK;
+  return guarded("rmg_sensor_size", [&]() -> int {
+    if (!s) return fail(RMG_ERR_INVALID_ARG, "rmg_sensor_size: sensor is NULL");
+    if (width) *width = s->width;
+    if (height) *height = s->height;
+    return RMG_OK;
+  });
 }

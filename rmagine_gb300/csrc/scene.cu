@@ -541,126 +541,136 @@ int build_top(rmg_scene* s, const rmg_instance_desc* inst, uint32_t n, bool rebu
 extern "C" int rmg_scene_create(const rmg_map* const* geometries, uint32_t n_geometries,
                                 const rmg_instance_desc* instances, uint32_t n_instances, void* stream,
                                 rmg_scene** out) {
-  if (!out) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_create: out is NULL");
-  *out = nullptr;
-  if (n_geometries > 0 && !geometries) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_create: geometries is NULL");
-  rmg_scene* s = new (std::nothrow) rmg_scene;
-  if (!s) return fail(RMG_ERR_OOM, "rmg_scene_create: host allocation");
-  cudaGetDevice(&s->device);
-  for (uint32_t g = 0; g < n_geometries; ++g) {
-    if (!geometries[g]) { delete s; return fail(RMG_ERR_INVALID_ARG, "rmg_scene_create: NULL geometry"); }
-    if (geometries[g]->n_faces > 0 && geometries[g]->depth > (unsigned)kFullStack) {
-      delete s;
-      return fail(RMG_ERR_UNSUPPORTED, "rmg_scene_create: a geometry's tree is deeper than 32 levels");
+  return guarded("rmg_scene_create", [&]() -> int {
+    if (!out) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_create: out is NULL");
+    *out = nullptr;
+    if (n_geometries > 0 && !geometries) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_create: geometries is NULL");
+    rmg_scene* s = new (std::nothrow) rmg_scene;
+    if (!s) return fail(RMG_ERR_OOM, "rmg_scene_create: host allocation");
+    cudaGetDevice(&s->device);
+    for (uint32_t g = 0; g < n_geometries; ++g) {
+      if (!geometries[g]) { delete s; return fail(RMG_ERR_INVALID_ARG, "rmg_scene_create: NULL geometry"); }
+      if (geometries[g]->n_faces > 0 && geometries[g]->depth > (unsigned)kFullStack) {
+        delete s;
+        return fail(RMG_ERR_UNSUPPORTED, "rmg_scene_create: a geometry's tree is deeper than 32 levels");
+      }
+      s->geoms.push_back(geometries[g]);
     }
-    s->geoms.push_back(geometries[g]);
-  }
-  int r = check_instances(s, instances, n_instances);
-  if (r != RMG_OK) { delete s; return r; }
-  cudaStream_t st = as_stream(stream);
-  r = dev_alloc(&s->d_status, 1, "scene status");
-  if (r == RMG_OK) r = cuda_status(cudaMemsetAsync(s->d_status, 0, 4, st), "memset");
-  if (r == RMG_OK && n_geometries > 0) {
-    std::vector<GeomDev> g(n_geometries);
-    for (uint32_t i = 0; i < n_geometries; ++i) {
-      const DeviceMap dm = device_view(geometries[i]);
-      g[i] = GeomDev{dm.nodes, dm.tris, dm.root, 2u * geometries[i]->n_nodes + 64u};
+    int r = check_instances(s, instances, n_instances);
+    if (r != RMG_OK) { delete s; return r; }
+    cudaStream_t st = as_stream(stream);
+    r = dev_alloc(&s->d_status, 1, "scene status");
+    if (r == RMG_OK) r = cuda_status(cudaMemsetAsync(s->d_status, 0, 4, st), "memset");
+    if (r == RMG_OK && n_geometries > 0) {
+      std::vector<GeomDev> g(n_geometries);
+      for (uint32_t i = 0; i < n_geometries; ++i) {
+        const DeviceMap dm = device_view(geometries[i]);
+        g[i] = GeomDev{dm.nodes, dm.tris, dm.root, 2u * geometries[i]->n_nodes + 64u};
+      }
+      r = dev_alloc(&s->d_geoms, n_geometries, "scene geometries");
+      if (r == RMG_OK)
+        r = cuda_status(cudaMemcpyAsync(s->d_geoms, g.data(), sizeof(GeomDev) * n_geometries, cudaMemcpyHostToDevice, st),
+                        "copy geometries");
     }
-    r = dev_alloc(&s->d_geoms, n_geometries, "scene geometries");
-    if (r == RMG_OK)
-      r = cuda_status(cudaMemcpyAsync(s->d_geoms, g.data(), sizeof(GeomDev) * n_geometries, cudaMemcpyHostToDevice, st),
-                      "copy geometries");
-  }
-  // Open the trees of large geometries into pieces (only those some instance places).
-  s->pieces.assign(n_geometries, {});
-  s->piece_base.assign(n_geometries, 0);
-  std::vector<bool> used(n_geometries, false);
-  for (uint32_t i = 0; i < n_instances; ++i) used[instances[i].geometry] = true;
-  std::vector<PieceReq> req;
-  for (uint32_t gi = 0; r == RMG_OK && gi < n_geometries; ++gi) {
-    if (!used[gi]) continue;
-    r = open_geometry(geometries[gi], st, s->pieces[gi]);
-    s->piece_base[gi] = (uint32_t)req.size();
-    for (const ScenePiece& p : s->pieces[gi]) req.push_back(PieceReq{geometries[gi]->d_nodes, p.parent, p.side});
-  }
-  // Bound the top tree: with more than 2^22 leaves from opened trees, open none.
-  uint64_t n_leaves = 0;
-  for (uint32_t i = 0; i < n_instances; ++i) n_leaves += std::max<size_t>(1, s->pieces[instances[i].geometry].size());
-  if (n_leaves > (1ull << 22)) {
-    for (auto& pc : s->pieces) pc.clear();
-    req.clear();
-  }
-  s->n_pieces = (uint32_t)req.size();
-  if (r == RMG_OK && !req.empty()) {
-    r = dev_alloc(&s->d_piece_req, req.size(), "scene pieces");
-    if (r == RMG_OK) r = dev_alloc(&s->d_piece_box, 6 * req.size(), "scene piece boxes");
-    if (r == RMG_OK)
-      r = cuda_status(cudaMemcpyAsync(s->d_piece_req, req.data(), sizeof(PieceReq) * req.size(), cudaMemcpyHostToDevice,
-                                      st), "copy pieces");
-  }
-  if (r == RMG_OK) r = build_top(s, instances, n_instances, true, st);
-  if (r != RMG_OK) { free_scene(s); return r; }
-  *out = s;
-  return RMG_OK;
+    // Open the trees of large geometries into pieces (only those some instance places).
+    s->pieces.assign(n_geometries, {});
+    s->piece_base.assign(n_geometries, 0);
+    std::vector<bool> used(n_geometries, false);
+    for (uint32_t i = 0; i < n_instances; ++i) used[instances[i].geometry] = true;
+    std::vector<PieceReq> req;
+    for (uint32_t gi = 0; r == RMG_OK && gi < n_geometries; ++gi) {
+      if (!used[gi]) continue;
+      r = open_geometry(geometries[gi], st, s->pieces[gi]);
+      s->piece_base[gi] = (uint32_t)req.size();
+      for (const ScenePiece& p : s->pieces[gi]) req.push_back(PieceReq{geometries[gi]->d_nodes, p.parent, p.side});
+    }
+    // Bound the top tree: with more than 2^22 leaves from opened trees, open none.
+    uint64_t n_leaves = 0;
+    for (uint32_t i = 0; i < n_instances; ++i) n_leaves += std::max<size_t>(1, s->pieces[instances[i].geometry].size());
+    if (n_leaves > (1ull << 22)) {
+      for (auto& pc : s->pieces) pc.clear();
+      req.clear();
+    }
+    s->n_pieces = (uint32_t)req.size();
+    if (r == RMG_OK && !req.empty()) {
+      r = dev_alloc(&s->d_piece_req, req.size(), "scene pieces");
+      if (r == RMG_OK) r = dev_alloc(&s->d_piece_box, 6 * req.size(), "scene piece boxes");
+      if (r == RMG_OK)
+        r = cuda_status(cudaMemcpyAsync(s->d_piece_req, req.data(), sizeof(PieceReq) * req.size(), cudaMemcpyHostToDevice,
+                                        st), "copy pieces");
+    }
+    if (r == RMG_OK) r = build_top(s, instances, n_instances, true, st);
+    if (r != RMG_OK) { free_scene(s); return r; }
+    *out = s;
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_scene_update(rmg_scene* s, const rmg_instance_desc* instances, uint32_t n_instances, int rebuild,
                                 void* stream) {
-  if (!s) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_update: scene is NULL");
-  if (n_instances != s->n_instances) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_update: instance count differs");
-  int r = check_instances(s, instances, n_instances);
-  if (r != RMG_OK) return r;
-  return build_top(s, instances, n_instances, rebuild != 0, as_stream(stream));
+  return guarded("rmg_scene_update", [&]() -> int {
+    if (!s) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_update: scene is NULL");
+    if (n_instances != s->n_instances) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_update: instance count differs");
+    int r = check_instances(s, instances, n_instances);
+    if (r != RMG_OK) return r;
+    return build_top(s, instances, n_instances, rebuild != 0, as_stream(stream));
+  });
 }
 
 extern "C" int rmg_scene_destroy(rmg_scene* s) {
-  if (!s) return RMG_OK;
-  free_scene(s);
-  return RMG_OK;
+  return guarded("rmg_scene_destroy", [&]() -> int {
+    if (!s) return RMG_OK;
+    free_scene(s);
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_scene_status(rmg_scene* s, int clear) {
-  if (!s) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_status: scene is NULL");
-  unsigned int word = 0;
-  RMG_CUDA_TRY(cudaMemcpy(&word, s->d_status, 4, cudaMemcpyDeviceToHost));
-  if (clear) RMG_CUDA_TRY(cudaMemset(s->d_status, 0, 4));
-  if (word != 0) {
-    set_error("a kernel recorded a device error on this scene");
-    return (int)word;
-  }
-  return RMG_OK;
+  return guarded("rmg_scene_status", [&]() -> int {
+    if (!s) return fail(RMG_ERR_INVALID_ARG, "rmg_scene_status: scene is NULL");
+    unsigned int word = 0;
+    RMG_CUDA_TRY(cudaMemcpy(&word, s->d_status, 4, cudaMemcpyDeviceToHost));
+    if (clear) RMG_CUDA_TRY(cudaMemset(s->d_status, 0, 4));
+    if (word != 0) {
+      set_error("a kernel recorded a device error on this scene");
+      return (int)word;
+    }
+    return RMG_OK;
+  });
 }
 
 extern "C" int rmg_simulate_scene(const rmg_scene* s, const rmg_sensor* sensor, const rmg_transform* Tsb,
                                   const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out, void* stream) {
-  if (!s || !sensor || !Tsb || !out)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene: NULL scene, sensor, Tsb or outputs");
-  if (n_poses == 0) return RMG_OK;
-  if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene: Tbm is NULL");
-  if (!out->hits && !out->ranges && !out->points && !out->normals && !out->face_ids && !out->geom_ids &&
-      !out->object_ids)
-    return RMG_OK;
-  rmg_launch_config cfg;
-  default_config(sensor, &cfg);
-  SceneParams S;
-  // the top-level tree's launch geometry; an empty scene uses a zero-face stand-in view
-  rmg_map empty;
-  std::memset(&empty, 0, sizeof(empty));
-  const rmg_map* top = s->tlas ? s->tlas : &empty;
-  make_trace_params(top, sensor, Tsb, Tbm, n_poses, out, cfg, S.T);
-  S.T.map.status = s->d_status;
-  S.inst = s->d_inst;
-  S.geoms = s->d_geoms;
-  S.leaves = s->d_leaves;
-  const uint64_t blocks = (S.T.n_tiles + cfg.block_warps - 1) / cfg.block_warps;
-  if (blocks > 0x7fffffffull) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene: too many rays for one launch");
-  const unsigned block = 32u * cfg.block_warps;
-  cudaStream_t st = as_stream(stream);
-  switch (sensor->model.kind) {
-    case RMG_MODEL_SPHERICAL:
-    case RMG_MODEL_PINHOLE: k_trace_scene<ORIGIN_POSE><<<(unsigned)blocks, block, 0, st>>>(S); break;
-    case RMG_MODEL_O1DN: k_trace_scene<ORIGIN_SINGLE><<<(unsigned)blocks, block, 0, st>>>(S); break;
-    default: k_trace_scene<ORIGIN_TABLE><<<(unsigned)blocks, block, 0, st>>>(S); break;
-  }
-  return cuda_status(cudaGetLastError(), "k_trace_scene");
+  return guarded("rmg_simulate_scene", [&]() -> int {
+    if (!s || !sensor || !Tsb || !out)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene: NULL scene, sensor, Tsb or outputs");
+    if (n_poses == 0) return RMG_OK;
+    if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene: Tbm is NULL");
+    if (!out->hits && !out->ranges && !out->points && !out->normals && !out->face_ids && !out->geom_ids &&
+        !out->object_ids)
+      return RMG_OK;
+    rmg_launch_config cfg;
+    default_config(sensor, &cfg);
+    SceneParams S;
+    // the top-level tree's launch geometry; an empty scene uses a zero-face stand-in view
+    rmg_map empty;
+    std::memset(&empty, 0, sizeof(empty));
+    const rmg_map* top = s->tlas ? s->tlas : &empty;
+    make_trace_params(top, sensor, Tsb, Tbm, n_poses, out, cfg, S.T);
+    S.T.map.status = s->d_status;
+    S.inst = s->d_inst;
+    S.geoms = s->d_geoms;
+    S.leaves = s->d_leaves;
+    const uint64_t blocks = (S.T.n_tiles + cfg.block_warps - 1) / cfg.block_warps;
+    if (blocks > 0x7fffffffull) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene: too many rays for one launch");
+    const unsigned block = 32u * cfg.block_warps;
+    cudaStream_t st = as_stream(stream);
+    switch (sensor->model.kind) {
+      case RMG_MODEL_SPHERICAL:
+      case RMG_MODEL_PINHOLE: k_trace_scene<ORIGIN_POSE><<<(unsigned)blocks, block, 0, st>>>(S); break;
+      case RMG_MODEL_O1DN: k_trace_scene<ORIGIN_SINGLE><<<(unsigned)blocks, block, 0, st>>>(S); break;
+      default: k_trace_scene<ORIGIN_TABLE><<<(unsigned)blocks, block, 0, st>>>(S); break;
+    }
+    return cuda_status(cudaGetLastError(), "k_trace_scene");
+  });
 }

@@ -146,34 +146,40 @@ using namespace rmg;
 
 extern "C" int rmg_default_launch_config(const rmg_map* map, const rmg_sensor* sensor,
                                          rmg_launch_config* cfg) {
-  (void)map;
-  if (!cfg) return fail(RMG_ERR_INVALID_ARG, "rmg_default_launch_config: cfg is NULL");
-  return default_config(sensor, cfg);
+  return guarded("rmg_default_launch_config", [&]() -> int {
+    (void)map;
+    if (!cfg) return fail(RMG_ERR_INVALID_ARG, "rmg_default_launch_config: cfg is NULL");
+    return default_config(sensor, cfg);
+  });
 }
 
 extern "C" int rmg_simulate_ex(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
                                const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
                                const rmg_launch_config* cfg_in, void* stream) {
-  if (!map || !sensor || !Tsb || !out)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_simulate: NULL map, sensor, Tsb or outputs");
-  if (n_poses == 0) return RMG_OK;
-  if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate: Tbm is NULL");
-  rmg_launch_config cfg;
-  if (cfg_in) cfg = *cfg_in; else default_config(sensor, &cfg);
-  int s = check_config(cfg);
-  if (s != RMG_OK) return s;
-  if (!out->hits && !out->ranges && !out->points && !out->normals && !out->face_ids &&
-      !out->geom_ids && !out->object_ids)
-    return RMG_OK;  // nothing requested: the reference writes nothing either
-  TraceParams P;
-  make_trace_params(map, sensor, Tsb, Tbm, n_poses, out, cfg, P);
-  return launch_plain(P, sensor, cfg, as_stream(stream));
+  return guarded("rmg_simulate_ex", [&]() -> int {
+    if (!map || !sensor || !Tsb || !out)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_simulate: NULL map, sensor, Tsb or outputs");
+    if (n_poses == 0) return RMG_OK;
+    if (!Tbm) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate: Tbm is NULL");
+    rmg_launch_config cfg;
+    if (cfg_in) cfg = *cfg_in; else default_config(sensor, &cfg);
+    int s = check_config(cfg);
+    if (s != RMG_OK) return s;
+    if (!out->hits && !out->ranges && !out->points && !out->normals && !out->face_ids &&
+        !out->geom_ids && !out->object_ids)
+      return RMG_OK;  // nothing requested: the reference writes nothing either
+    TraceParams P;
+    make_trace_params(map, sensor, Tsb, Tbm, n_poses, out, cfg, P);
+    return launch_plain(P, sensor, cfg, as_stream(stream));
+  });
 }
 
 extern "C" int rmg_simulate(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
                             const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
                             void* stream) {
-  return rmg_simulate_ex(map, sensor, Tsb, Tbm, n_poses, out, nullptr, stream);
+  return guarded("rmg_simulate", [&]() -> int {
+    return rmg_simulate_ex(map, sensor, Tsb, Tbm, n_poses, out, nullptr, stream);
+  });
 }
 
 // Launch autotuner for one (map, sensor, pose set): times a fixed list of
@@ -185,61 +191,63 @@ extern "C" int rmg_simulate(const rmg_map* map, const rmg_sensor* sensor, const 
 extern "C" int rmg_autotune_launch_config(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
                                           const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
                                           uint32_t reps, rmg_launch_config* best, void* stream) {
-  if (!map || !sensor || !Tsb || !Tbm || !out || !best || n_poses == 0)
-    return fail(RMG_ERR_INVALID_ARG, "rmg_autotune_launch_config: NULL argument or no poses");
-  reps = std::max(1u, std::min(reps, 50u));
-  cudaStream_t st = as_stream(stream);
-  rmg_launch_config base;
-  default_config(sensor, &base);
-  struct Walk { uint32_t bvh_width, packet; };
-  const Walk walks[4] = {{2, 0}, {2, 1}, {4, 0}, {8, 0}};
-  const uint32_t tiles[3][2] = {{8, 4}, {16, 2}, {4, 8}};
-  const uint32_t warps[2] = {4, 2};
-  cudaEvent_t e0, e1;
-  RMG_CUDA_TRY(cudaEventCreate(&e0));
-  RMG_CUDA_TRY(cudaEventCreate(&e1));
-  float best_ms = 1e30f;
-  int s = RMG_OK;
-  bool any = false;
-  for (const Walk& w : walks) {
-    for (const auto& t : tiles) {
-      for (uint32_t bw : warps) {
-        rmg_launch_config c = base;
-        c.bvh_width = w.bvh_width;
-        c.packet = w.packet;
-        c.tile_w = t[0];
-        c.tile_h = t[1];
-        c.block_warps = bw;
-        if (c.tile_w > sensor->width && c.tile_w != base.tile_w) continue;
-        if (check_config(c) != RMG_OK) continue;
-        TraceParams P;
-        make_trace_params(map, sensor, Tsb, Tbm, n_poses, out, c, P);
-        if ((w.bvh_width == 4 && !P.wide) || (w.bvh_width == 8 && !P.wide8) || (w.packet == 1 && !P.packet))
-          continue;  // not available here
-        s = launch_plain(P, sensor, c, st);
-        if (s != RMG_OK) break;
-        std::vector<float> ms;
-        for (uint32_t r = 0; r < reps && s == RMG_OK; ++r) {
-          s = cuda_status(cudaEventRecord(e0, st), "event");
-          if (s == RMG_OK) s = launch_plain(P, sensor, c, st);
-          if (s == RMG_OK) s = cuda_status(cudaEventRecord(e1, st), "event");
-          if (s == RMG_OK) s = cuda_status(cudaEventSynchronize(e1), "event sync");
-          float x = 0.f;
-          if (s == RMG_OK) s = cuda_status(cudaEventElapsedTime(&x, e0, e1), "event time");
-          ms.push_back(x);
+  return guarded("rmg_autotune_launch_config", [&]() -> int {
+    if (!map || !sensor || !Tsb || !Tbm || !out || !best || n_poses == 0)
+      return fail(RMG_ERR_INVALID_ARG, "rmg_autotune_launch_config: NULL argument or no poses");
+    reps = std::max(1u, std::min(reps, 50u));
+    cudaStream_t st = as_stream(stream);
+    rmg_launch_config base;
+    default_config(sensor, &base);
+    struct Walk { uint32_t bvh_width, packet; };
+    const Walk walks[4] = {{2, 0}, {2, 1}, {4, 0}, {8, 0}};
+    const uint32_t tiles[3][2] = {{8, 4}, {16, 2}, {4, 8}};
+    const uint32_t warps[2] = {4, 2};
+    cudaEvent_t e0, e1;
+    RMG_CUDA_TRY(cudaEventCreate(&e0));
+    RMG_CUDA_TRY(cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    int s = RMG_OK;
+    bool any = false;
+    for (const Walk& w : walks) {
+      for (const auto& t : tiles) {
+        for (uint32_t bw : warps) {
+          rmg_launch_config c = base;
+          c.bvh_width = w.bvh_width;
+          c.packet = w.packet;
+          c.tile_w = t[0];
+          c.tile_h = t[1];
+          c.block_warps = bw;
+          if (c.tile_w > sensor->width && c.tile_w != base.tile_w) continue;
+          if (check_config(c) != RMG_OK) continue;
+          TraceParams P;
+          make_trace_params(map, sensor, Tsb, Tbm, n_poses, out, c, P);
+          if ((w.bvh_width == 4 && !P.wide) || (w.bvh_width == 8 && !P.wide8) || (w.packet == 1 && !P.packet))
+            continue;  // not available here
+          s = launch_plain(P, sensor, c, st);
+          if (s != RMG_OK) break;
+          std::vector<float> ms;
+          for (uint32_t r = 0; r < reps && s == RMG_OK; ++r) {
+            s = cuda_status(cudaEventRecord(e0, st), "event");
+            if (s == RMG_OK) s = launch_plain(P, sensor, c, st);
+            if (s == RMG_OK) s = cuda_status(cudaEventRecord(e1, st), "event");
+            if (s == RMG_OK) s = cuda_status(cudaEventSynchronize(e1), "event sync");
+            float x = 0.f;
+            if (s == RMG_OK) s = cuda_status(cudaEventElapsedTime(&x, e0, e1), "event time");
+            ms.push_back(x);
+          }
+          if (s != RMG_OK) break;
+          std::sort(ms.begin(), ms.end());
+          const float med = ms[ms.size() / 2];
+          if (med < best_ms) { best_ms = med; *best = c; any = true; }
         }
         if (s != RMG_OK) break;
-        std::sort(ms.begin(), ms.end());
-        const float med = ms[ms.size() / 2];
-        if (med < best_ms) { best_ms = med; *best = c; any = true; }
       }
       if (s != RMG_OK) break;
     }
-    if (s != RMG_OK) break;
-  }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  if (s != RMG_OK) return s;
-  if (!any) *best = base;
-  return RMG_OK;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != RMG_OK) return s;
+    if (!any) *best = base;
+    return RMG_OK;
+  });
 }

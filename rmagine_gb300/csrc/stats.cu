@@ -465,8 +465,10 @@ extern "C" int rmg_statistics_p2p(const rmg_transform* pre_transforms, uint32_t 
                                   const uint8_t* model_mask, const uint32_t* model_ids,
                                   const rmg_umeyama_constraints* params, uint32_t n_batches, uint32_t n_per_batch,
                                   rmg_cross_stats* stats, rmg_transform* transforms, void* stream) {
-  return stats_entry(pre_transforms, pre_transform_stride, dataset_points, dataset_mask, dataset_ids, model_points,
-                     nullptr, model_mask, model_ids, params, n_batches, n_per_batch, stats, transforms, stream, false);
+  return guarded("rmg_statistics_p2p", [&]() -> int {
+    return stats_entry(pre_transforms, pre_transform_stride, dataset_points, dataset_mask, dataset_ids, model_points,
+                       nullptr, model_mask, model_ids, params, n_batches, n_per_batch, stats, transforms, stream, false);
+  });
 }
 
 extern "C" int rmg_statistics_p2l(const rmg_transform* pre_transforms, uint32_t pre_transform_stride,
@@ -476,9 +478,11 @@ extern "C" int rmg_statistics_p2l(const rmg_transform* pre_transforms, uint32_t 
                                   const uint32_t* model_ids, const rmg_umeyama_constraints* params,
                                   uint32_t n_batches, uint32_t n_per_batch, rmg_cross_stats* stats,
                                   rmg_transform* transforms, void* stream) {
-  return stats_entry(pre_transforms, pre_transform_stride, dataset_points, dataset_mask, dataset_ids, model_points,
-                     model_normals, model_mask, model_ids, params, n_batches, n_per_batch, stats, transforms, stream,
-                     true);
+  return guarded("rmg_statistics_p2l", [&]() -> int {
+    return stats_entry(pre_transforms, pre_transform_stride, dataset_points, dataset_mask, dataset_ids, model_points,
+                       model_normals, model_mask, model_ids, params, n_batches, n_per_batch, stats, transforms, stream,
+                       true);
+  });
 }
 
 // One 3x3 SVD per thread (binary64 inside, binary32 in and out; column-major
@@ -523,19 +527,23 @@ __global__ void k_svd3(const float* A, float* U, float* W, float* w, float* V, u
 
 extern "C" int rmg_svd3(const float* A, float* U, float* W, float* w, float* V, uint32_t n, int rotations,
                         void* stream) {
-  if (n == 0) return RMG_OK;
-  if (!A) return fail(RMG_ERR_INVALID_ARG, "rmg_svd3: A is NULL");
-  if (!U && !W && !w && !V) return RMG_OK;
-  const uint64_t grid = (n + 127ull) / 128ull;
-  k_svd3<<<(unsigned)grid, 128, 0, as_stream(stream)>>>(A, U, W, w, V, n, rotations);
-  return cuda_status(cudaGetLastError(), "k_svd3");
+  return guarded("rmg_svd3", [&]() -> int {
+    if (n == 0) return RMG_OK;
+    if (!A) return fail(RMG_ERR_INVALID_ARG, "rmg_svd3: A is NULL");
+    if (!U && !W && !w && !V) return RMG_OK;
+    const uint64_t grid = (n + 127ull) / 128ull;
+    k_svd3<<<(unsigned)grid, 128, 0, as_stream(stream)>>>(A, U, W, w, V, n, rotations);
+    return cuda_status(cudaGetLastError(), "k_svd3");
+  });
 }
 
 extern "C" int rmg_umeyama_transform(const rmg_cross_stats* stats, uint32_t n, rmg_transform* out, void* stream) {
-  if (n == 0) return RMG_OK;
-  if (!stats || !out) return fail(RMG_ERR_INVALID_ARG, "rmg_umeyama_transform: NULL argument");
-  k_umeyama_stats<<<(n + 127) / 128, 128, 0, as_stream(stream)>>>(stats, n, out);
-  return cuda_status(cudaGetLastError(), "k_umeyama_stats");
+  return guarded("rmg_umeyama_transform", [&]() -> int {
+    if (n == 0) return RMG_OK;
+    if (!stats || !out) return fail(RMG_ERR_INVALID_ARG, "rmg_umeyama_transform: NULL argument");
+    k_umeyama_stats<<<(n + 127) / 128, 128, 0, as_stream(stream)>>>(stats, n, out);
+    return cuda_status(cudaGetLastError(), "k_umeyama_stats");
+  });
 }
 
 extern "C" int rmg_umeyama_backward(const rmg_transform* pre_transforms, uint32_t pre_transform_stride,
@@ -545,25 +553,27 @@ extern "C" int rmg_umeyama_backward(const rmg_transform* pre_transforms, uint32_
                                     const rmg_umeyama_constraints* params, uint32_t n_batches, uint32_t n_per_batch,
                                     const rmg_cross_stats* stats, const float* grad_R, const float* grad_t,
                                     rmg_vec3* grad_dataset, rmg_vec3* grad_model, void* stream) {
-  if (n_batches == 0) return RMG_OK;
-  if (!stats) return fail(RMG_ERR_INVALID_ARG, "rmg_umeyama_backward: stats is NULL");
-  if (!grad_dataset && !grad_model) return RMG_OK;
-  BwdParams B;
-  int s = fill_params(pre_transforms, pre_transform_stride, dataset_points, dataset_mask, dataset_ids, model_points,
-                      nullptr, model_mask, model_ids, params, n_batches, n_per_batch, B.S);
-  if (s != RMG_OK) return s;
-  cudaStream_t st = as_stream(stream);
-  Coef* coef = nullptr;
-  RMG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&coef), sizeof(Coef) * (size_t)n_batches, st));
-  k_umeyama_bwd_coef<<<(n_batches + 127) / 128, 128, 0, st>>>(stats, grad_R, grad_t, n_batches, coef);
-  s = cuda_status(cudaGetLastError(), "k_umeyama_bwd_coef");
-  if (s == RMG_OK) {
-    B.coef = coef;
-    B.gd = reinterpret_cast<float*>(grad_dataset);
-    B.gm = reinterpret_cast<float*>(grad_model);
-    k_umeyama_bwd_stream<<<n_batches * B.S.chunks, kStatsThreads, 0, st>>>(B);
-    s = cuda_status(cudaGetLastError(), "k_umeyama_bwd_stream");
-  }
-  cudaFreeAsync(coef, st);
-  return s;
+  return guarded("rmg_umeyama_backward", [&]() -> int {
+    if (n_batches == 0) return RMG_OK;
+    if (!stats) return fail(RMG_ERR_INVALID_ARG, "rmg_umeyama_backward: stats is NULL");
+    if (!grad_dataset && !grad_model) return RMG_OK;
+    BwdParams B;
+    int s = fill_params(pre_transforms, pre_transform_stride, dataset_points, dataset_mask, dataset_ids, model_points,
+                        nullptr, model_mask, model_ids, params, n_batches, n_per_batch, B.S);
+    if (s != RMG_OK) return s;
+    cudaStream_t st = as_stream(stream);
+    Coef* coef = nullptr;
+    RMG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&coef), sizeof(Coef) * (size_t)n_batches, st));
+    k_umeyama_bwd_coef<<<(n_batches + 127) / 128, 128, 0, st>>>(stats, grad_R, grad_t, n_batches, coef);
+    s = cuda_status(cudaGetLastError(), "k_umeyama_bwd_coef");
+    if (s == RMG_OK) {
+      B.coef = coef;
+      B.gd = reinterpret_cast<float*>(grad_dataset);
+      B.gm = reinterpret_cast<float*>(grad_model);
+      k_umeyama_bwd_stream<<<n_batches * B.S.chunks, kStatsThreads, 0, st>>>(B);
+      s = cuda_status(cudaGetLastError(), "k_umeyama_bwd_stream");
+    }
+    cudaFreeAsync(coef, st);
+    return s;
+  });
 }
