@@ -71,16 +71,23 @@ TRAFFIC: dict = {
     "icp_stats_bwd": 16 * (403369216 + 357416960),
     # captured on 64 poses (4.19 M rays) and scaled by 64 to the 4,096-pose launch
     "pose_grad": 64 * (226699264 + 14085632),
+    # captured on 50 poses (15.4 M rays) / 100 poses (13.1 M rays) and scaled to the 1,000-pose launch
+    "terrain1m_pinhole": 20 * (87372800 + 503376896),
+    "terrain2m_spherical": 10 * (545676032 + 467888640),
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
-    "rcc_fused": 10 * (295375872 + 23611136),
+    "rcc_fused": 10 * (295333888 + 25030912),
     # full-size launch (131,072,000 ranges)
     "noise": 524465664 + 463988224,
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
-    "scene_terrain1m": 10 * (357533440 + 682603008),
+    "scene_terrain1m": 10 * (356430848 + 682092800),
+    # the whole 1,024-sensor launch (780,800 rays)
+    "batched_small": 208760064 + 28272896,
     # captured with every sensor cut to 16 poses (143,238,688 rays) and scaled by the ray count to the
     # full 64-sensor launch (9,025,081,856 rays)
     "batched": round(9025081856 / 143238688 * (2129916160 + 849543424)),
 }
+
+SRC_COUNTERS = "profiles/traversal_counters_by_workload.md (small cases)"
 
 # Warp instructions per unit (ray) of the dominant kernel, `smsp__inst_executed.sum` of one ncu
 # capture on the small case of the workload divided by its rays (profiles/), keyed by kernel walk.
@@ -89,6 +96,14 @@ ISSUE: dict = {
                                        "profiles/k_trace_terrain1m_spherical.md (100 poses, 13,107,200 rays)"},
     "pose_grad/k_range_grad": {"warp_inst_per_unit": 591522244 / 4194304, "source":
                                "profiles/k_range_grad_terrain2m_posegrad.md (64 poses, 4,194,304 rays)"},
+    "terrain1m_pinhole/packet": {"warp_inst_per_unit": 1218427530 / 15360000, "source": SRC_COUNTERS},
+    "terrain1m_pinhole/full_stack": {"warp_inst_per_unit": 1300374245 / 15360000, "source": SRC_COUNTERS},
+    "terrain2m_spherical/full_stack": {"warp_inst_per_unit": 1716707653 / 13107200, "source": SRC_COUNTERS},
+    "room_vlp16/packet": {"warp_inst_per_unit": 117898004 / 1440000, "source": SRC_COUNTERS},
+    "room_vlp16/full_stack": {"warp_inst_per_unit": 129417314 / 1440000, "source": SRC_COUNTERS},
+    "rcc_fused/k_trace_stats": {"warp_inst_per_unit": 1329978711 / 13107200, "source": SRC_COUNTERS},
+    "scene_terrain1m/k_trace_scene": {"warp_inst_per_unit": 2212654859 / 13107200, "source": SRC_COUNTERS},
+    "batched_small/k_trace_batched": {"warp_inst_per_unit": 189000011 / 780800, "source": SRC_COUNTERS},
     "batched/k_trace_batched": {"warp_inst_per_unit": 14537272107 / 143238688, "source":
                                 "profiles/k_trace_batched_mixed64.md (16 poses per sensor, 143,238,688 rays, "
                                 "autotuned launch options)"},
@@ -226,6 +241,18 @@ def issue_roofline(kernel, units_per_launch, launch_s, clocks, traffic, note):
     return out
 
 
+def traffic_roofline(traffic, launch_s, note):
+    """Measured DRAM bytes per launch (ncu) over the launch's CUDA-event time against the measured HBM
+    copy peak, where no instruction count is recorded; None without a capture."""
+    if not traffic:
+        return None
+    peak, kind = measured_hbm()
+    achieved = traffic / launch_s / 1e9
+    return {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": kind,
+            "note": note + "; bytes = the measured DRAM traffic of the dominant kernel"}
+
+
 def roofline(bytes_per_unit, units_per_launch, launch_s, note, traffic=None):
     peak, kind = measured_hbm()
     achieved = bytes_per_unit * units_per_launch / launch_s / 1e9
@@ -299,6 +326,10 @@ def raycast_config(desc, n_poses, rays, n_faces, world):
                    "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas{world}" if world > 1 else "single"})
     return config
+
+
+# --walk: a fixed traversal instead of the autotuned one (profiling cases)
+WALKS = {"full_stack": dict(packet=0, bvh_width=2), "packet": dict(packet=1), "wide4": dict(bvh_width=4, packet=0)}
 
 
 def walk_name(cfg, depth):
@@ -384,7 +415,10 @@ def gpu_raycast(args, world):
     sim = rm.make_simulator(model, m)
     Tbm = torch.from_numpy(poses).to(dev)
     bundle = rm.resize_memory_bundle(rm.Bundle(*attrs), W, H, n, device=dev)
-    if args.no_autotune:
+    if args.walk:
+        tuned = rm.launch_config(**WALKS[args.walk])
+        sim.launch_config = tuned
+    elif args.no_autotune:
         tuned = rm.launch_config()
         sim.launch_config = tuned
     else:
@@ -419,12 +453,9 @@ def gpu_raycast(args, world):
     rl = issue_roofline(f"{args.workload}/{walk}", rays, launch_s, clocks, TRAFFIC.get(args.workload),
                         f"{walk} walk of k_trace: issue-bound (ALU pipe, SIMD divergence, dependent node fetches); "
                         f"DRAM carries the outputs and tree re-reads")
-    if rl is None and wk:
-        rl = roofline(out_b + 64 * wk["nodes"] + 48 * wk["tris"], rays, launch_s,
-                      "algorithmic bytes per ray = outputs + 64 B per node visit + 48 B per triangle test, with the "
-                      "canonical LBVH's visit counts; node and triangle fetches are served mostly from L1/L2, so "
-                      "this exceeds the HBM roof (no instruction count is recorded for this walk)",
-                      TRAFFIC.get(args.workload))
+    if rl is None:
+        rl = traffic_roofline(TRAFFIC.get(args.workload), launch_s,
+                              f"no instruction count is recorded for the {walk} walk on this workload")
     if rl is not None and wk:
         rl["algorithmic_bytes_per_unit"] = round(out_b + 64 * wk["nodes"] + 48 * wk["tris"], 2)
     config = raycast_config(desc, n, rays, sc.n_faces, world)
@@ -498,11 +529,11 @@ def gpu_scene(args, world):
     e2e = rays / float(np.median(e2e_t)) / 1e6
     out_b = sum(OUT_BYTES[a] for a in SCENE_ATTRS)
     attrs_e2e = SCENE_ATTRS
-    wk = WORK_PER_RAY["terrain1m_spherical"]
-    rl = roofline(out_b + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
-                  "algorithmic bytes per ray of the same geometry as one mesh (canonical LBVH counts of the "
-                  "baked terrain): outputs 41 B + 64 B per node visit + 48 B per triangle test",
-                  TRAFFIC.get("scene_terrain1m"))
+    rl = issue_roofline("scene_terrain1m/k_trace_scene", rays, total_ms / args.steps / 1e3, clocks,
+                        TRAFFIC.get("scene_terrain1m"),
+                        "k_trace_scene (top-level walk with nested instance walks): issue-bound")
+    rl = rl or traffic_roofline(TRAFFIC.get("scene_terrain1m"), total_ms / args.steps / 1e3,
+                                "no instruction count is recorded for k_trace_scene")
     config = {"workload": "instanced scene: terrain 708x708 (999,698 tris) + 2,000 instances of one 12-triangle "
                           "unit box (scaled, placed), spherical 128x1024, 1000 poses, all seven attributes",
               "poses": int(n), "rays_per_step": int(rays), "instances": len(insts), "geometries": len(meshes),
@@ -806,14 +837,11 @@ def gpu_posegrad(args, world):
         l_.cpu()
         e2e_t.append(time.perf_counter() - t0)
     e2e = n_poses / float(np.median(e2e_t))
-    wk = WORK_PER_RAY["pose_grad"]
     rl = issue_roofline("pose_grad/k_range_grad", rays, total_ms / args.steps / 1e3, clocks, TRAFFIC.get("pose_grad"),
                         "k_range_grad (ray cast fused with the range adjoint and the per-pose reduction): "
                         "issue-bound like k_trace")
-    rl = rl or roofline(4 + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
-                  "per ray: observed range 4 B + 64 B per node visit + 48 B per triangle test (the adjoint re-reads "
-                  "the hit triangle from L1); node/triangle fetches are served mostly from L1/L2",
-                  TRAFFIC.get("pose_grad"))
+    rl = rl or traffic_roofline(TRAFFIC.get("pose_grad"), total_ms / args.steps / 1e3,
+                                "no instruction count is recorded for k_range_grad")
     config = {"workload": f"pose gradient: terrain 1024x1024 + 2000 boxes (2,117,058 tris), spherical 64x1024, "
                           f"{n_poses} poses perturbed N(0,0.1 m) / N(0,2 deg), Huber 0.2 m",
               "poses": n_poses, "rays_per_step": rays, "l2": "flushed between timed steps (256 MB write)",
@@ -922,11 +950,10 @@ def gpu_rcc(args, world):
         T.cpu()
         e2e_t.append(time.perf_counter() - t0)
     e2e = rays / float(np.median(e2e_t)) / 1e6
-    wk = WORK_PER_RAY["rcc_fused"]
-    rl = roofline(1 + wk["data_frac"] * 12 + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
-                  "per sensor ray: dataset mask 1 B + dataset point 12 B where valid + 64 B per node visit + 48 B per "
-                  "triangle test (rays without a valid dataset point are not cast); nothing is written per ray",
-                  TRAFFIC.get("rcc_fused"))
+    rl = issue_roofline("rcc_fused/k_trace_stats", rays, total_ms / args.steps / 1e3, clocks, TRAFFIC.get("rcc_fused"),
+                        "k_trace_stats (ray cast fused with statistics_p2l and the per-pose reduction): issue-bound")
+    rl = rl or traffic_roofline(TRAFFIC.get("rcc_fused"), total_ms / args.steps / 1e3,
+                                "no instruction count is recorded for k_trace_stats")
     config = {"workload": f"fused simulate -> statistics_p2l -> Umeyama: terrain 708x708 + 2000 boxes (1,023,698 "
                           f"tris), spherical 128x1024, {n_poses} pose estimates (perturbed N(0,0.1 m) / N(0,2 deg)) "
                           f"each against the scan at its true pose, max_dist 0.5 m",
@@ -1068,13 +1095,12 @@ def gpu_batched(args, world):
         e2e_step()
         e2e_t.append(time.perf_counter() - t0)
     e2e = rays / float(np.median(e2e_t)) / 1e6
-    wk = WORK_PER_RAY.get("terrain2m_spherical")
-    rl = None if small else issue_roofline(
-        "batched/k_trace_batched", rays, total_ms / args.steps / 1e3, clocks, TRAFFIC.get("batched"),
-        "k_trace_batched (persistent warps over all sensors' tiles, per-ray walk of k_trace): issue-bound")
-    rl = rl or roofline(5 + 64 * wk["nodes"] + 48 * wk["tris"], rays, total_ms / args.steps / 1e3,
-                  "per ray: Hits+Ranges 5 B + 64 B per node visit + 48 B per triangle test (work per ray of the "
-                  "2.1M-triangle terrain's spherical workload used as the estimate)", None if small else TRAFFIC.get("batched"))
+    key = "batched_small" if small else "batched"
+    rl = issue_roofline(f"{key}/k_trace_batched", rays, total_ms / args.steps / 1e3, clocks, TRAFFIC.get(key),
+                        "k_trace_batched (persistent warps over all sensors' tiles, per-ray walk of k_trace): "
+                        "issue-bound")
+    rl = rl or traffic_roofline(TRAFFIC.get(key), total_ms / args.steps / 1e3,
+                                "no instruction count is recorded for this batch")
     config = {"workload": ("batched small sensors: terrain 1024x1024 + 2000 boxes (2,117,058 tris), 1024 sensors "
                            "(O1Dn 256 dirs / pinhole 32x8, alternating), poses log-uniform [1,8], Hits+Ranges") if small
               else ("batched: terrain 1024x1024 + 2000 boxes (2,117,058 tris), 64 sensors from {VLP-16 16x900, "
@@ -1115,6 +1141,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="ray-cast workloads: the default launch configuration")
     ap.add_argument("--poses", type=int, default=0, help="use only the first N poses / batches (profiling case)")
+    ap.add_argument("--walk", choices=sorted(WALKS), default=None,
+                    help="ray-cast workloads: this traversal instead of the autotuned one (profiling cases)")
     ap.add_argument("--headline-only", action="store_true",
                     help="default workload: skip the batched and pose-gradient parts of the line")
     args = ap.parse_args()
