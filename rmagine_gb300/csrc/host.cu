@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cstring>
 #include <functional>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -244,6 +245,34 @@ struct Pipeline {
   }
 };
 
+// The streams and events of the simulate host forms, made once per host
+// thread and device and kept (creating them took a measurable share of a
+// small call): a call is synchronous, so the next call of the same thread
+// finds them idle; other threads have their own.
+int cached_pipeline(Pipeline** out) {
+  int dev = 0;
+  RMG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(RMG_ERR_UNSUPPORTED, "host forms: device ordinal out of range");
+  thread_local std::unique_ptr<Pipeline> cache[kMaxDevices];
+  if (!cache[dev]) {
+    std::unique_ptr<Pipeline> pl(new Pipeline);
+    for (int k = 0; k + 1 < kMaxCompute; ++k) {
+      RMG_CUDA_TRY(cudaStreamCreateWithFlags(&pl->side[k], cudaStreamNonBlocking));
+      RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl->side_done[k], cudaEventDisableTiming));
+    }
+    RMG_CUDA_TRY(cudaStreamCreateWithFlags(&pl->copy, cudaStreamNonBlocking));
+    for (int k = 0; k < kSlots; ++k) {
+      RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl->cast[k], cudaEventDisableTiming));
+      RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl->copied[k], cudaEventDisableTiming));
+    }
+    RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl->ready, cudaEventDisableTiming));
+    RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl->done, cudaEventDisableTiming));
+    cache[dev] = std::move(pl);
+  }
+  *out = cache[dev].get();
+  return RMG_OK;
+}
+
 // Chunk k is cast on compute stream k % nc into slot k % kSlots (nc compute
 // streams).  Chunks 0..nc-1 are launched first; then iteration k launches
 // chunk k+nc and issues chunk k's copies.  The launch of chunk j waits for the
@@ -274,18 +303,10 @@ int host_pipeline(const char* what, const rmg_sensor* sensor, const rmg_transfor
   cudaMemPool_t pool;
   int s = staging_pool(&pool);
   if (s != RMG_OK) return s;
-  Pipeline pl;
-  for (uint32_t k = 0; k + 1 < nc; ++k) {
-    RMG_CUDA_TRY(cudaStreamCreateWithFlags(&pl.side[k], cudaStreamNonBlocking));
-    RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.side_done[k], cudaEventDisableTiming));
-  }
-  RMG_CUDA_TRY(cudaStreamCreateWithFlags(&pl.copy, cudaStreamNonBlocking));
-  for (int k = 0; k < slots; ++k) {
-    RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.cast[k], cudaEventDisableTiming));
-    RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.copied[k], cudaEventDisableTiming));
-  }
-  RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.ready, cudaEventDisableTiming));
-  RMG_CUDA_TRY(cudaEventCreateWithFlags(&pl.done, cudaEventDisableTiming));
+  Pipeline* pp = nullptr;
+  s = cached_pipeline(&pp);
+  if (s != RMG_OK) return s;
+  Pipeline& pl = *pp;
   cudaStream_t compute[kMaxCompute] = {st};
   for (uint32_t k = 0; k + 1 < nc; ++k) compute[k + 1] = pl.side[k];
 
