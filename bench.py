@@ -347,28 +347,29 @@ def walk_name(cfg, depth):
 
 
 def cpu_raycast(sc, model, poses, attrs, target_s=15.0):
-    """The oracle's OpenMP restatement of rmagine's Embree path on all host cores over a bounded
-    pose sample (map build excluded, as in the reference's benchmark loop)."""
+    """rmagine's Embree path restated on all host cores (the oracle's simulation with its Embree-style
+    4-wide SIMD walk, outputs equal to the restatement's) over a bounded pose sample (map build
+    excluded, as in the reference's benchmark loop)."""
     import oracle
 
     ocs = oracle.Scene(sc.vertices, sc.faces)
     threads = oracle.lib().orc_max_threads()
     W, H = model_size(model)
     t0 = time.perf_counter()
-    ocs.simulate(model, IDENT, poses[:1], attrs=attrs, nthreads=threads)
+    ocs.simulate(model, IDENT, poses[:1], attrs=attrs, nthreads=threads, fast=True)
     per_pose = max(time.perf_counter() - t0, 1e-4)
     n = int(max(1, min(len(poses), target_s / per_pose)))
     t0 = time.perf_counter()
-    ocs.simulate(model, IDENT, poses[:n], attrs=attrs, nthreads=threads)
+    ocs.simulate(model, IDENT, poses[:n], attrs=attrs, nthreads=threads, fast=True)
     dt = time.perf_counter() - t0
     rays = n * W * H
     return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": int(threads), "kind": "port",
-            "sample": f"{n} of {len(poses)} poses ({rays} rays), all host threads, oracle SAH-BVH restatement "
-                      f"of the Embree path (Embree itself is not buildable here)", "seconds": dt}
+            "sample": f"{n} of {len(poses)} poses ({rays} rays), all host threads, Embree-style 4-wide SIMD single-ray walk over the oracle's binned-SAH tree "
+                      f"(Embree itself is not buildable here)", "seconds": dt}
 
 
 def cpu_batched(sc, spec, pose_seed=100, target_s=10.0):
-    """The oracle's OpenMP ray cast over every sensor of a batched set, each with its first k poses
+    """The oracle's OpenMP ray cast (4-wide walk) over every sensor of a batched set, each with its first k poses
     (k the same for all sensors, sized to about target_s): rays per second over the whole sample."""
     import oracle
     from rmagine_gb300 import scenes
@@ -382,7 +383,7 @@ def cpu_batched(sc, spec, pose_seed=100, target_s=10.0):
         t0 = time.perf_counter()
         for (mod, c), p in zip(spec, poses):
             kk = min(k, c)
-            ocs.simulate(mod, IDENT, p[:kk], attrs=("hits", "ranges"), nthreads=threads)
+            ocs.simulate(mod, IDENT, p[:kk], attrs=("hits", "ranges"), nthreads=threads, fast=True)
             W, H = model_size(mod)
             rays += kk * W * H
         return rays, time.perf_counter() - t0
@@ -392,7 +393,7 @@ def cpu_batched(sc, spec, pose_seed=100, target_s=10.0):
     rays, dt = run(k)
     return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": int(threads), "kind": "port",
             "sample": f"the first {k} poses of each of the {len(spec)} sensors ({rays} rays), all host threads, "
-                      f"oracle SAH-BVH restatement of the Embree path", "seconds": dt}
+                      f"Embree-style 4-wide SIMD single-ray walk over the oracle's binned-SAH tree", "seconds": dt}
 
 
 def gpu_raycast(args, world):
@@ -782,7 +783,7 @@ def cpu_posegrad(sc, model, true, est, obs_h, target_s=10.0):
     dirs = oracle.directions(model)
 
     def run(n):
-        sim = ocs.simulate(model, IDENT, est[:n], attrs=("ranges", "face_ids"), nthreads=threads)
+        sim = ocs.simulate(model, IDENT, est[:n], attrs=("ranges", "face_ids"), nthreads=threads, fast=True)
         obs = obs_h[:n * W * H]
         f, r = sim["face_ids"], sim["ranges"]
         valid = (f != 0xFFFFFFFF) & (r >= model.range.min) & (obs >= model.range.min) & (obs <= model.range.max)
@@ -799,7 +800,8 @@ def cpu_posegrad(sc, model, true, est, obs_h, target_s=10.0):
     run(n)
     dt = time.perf_counter() - t0
     return {"value": n / dt, "unit": "poses/s", "cores": int(threads), "kind": "port",
-            "sample": f"{n} of {len(est)} poses: oracle OpenMP ray cast + numpy binary64 adjoint", "seconds": dt}
+            "sample": f"{n} of {len(est)} poses: oracle OpenMP ray cast (4-wide SIMD walk) + numpy binary64 adjoint",
+            "seconds": dt}
 
 
 def gpu_posegrad(args, world):
@@ -882,7 +884,7 @@ def cpu_rcc(sc, model, true, est, data_h, target_s=10.0):
 
     def run(n):
         return ost.simulate_statistics(ocs, model, IDENT, est[:n], data_h["points"][:n * W * H],
-                                       dmask=data_h["hits"][:n * W * H], max_dist=0.5)
+                                       dmask=data_h["hits"][:n * W * H], max_dist=0.5, fast=True)
 
     t0 = time.perf_counter()
     run(1)
@@ -892,8 +894,8 @@ def cpu_rcc(sc, model, true, est, data_h, target_s=10.0):
     run(n)
     dt = time.perf_counter() - t0
     return {"value": n * W * H / dt / 1e6, "unit": "Mrays/s", "cores": int(threads), "kind": "port",
-            "sample": f"{n} of {len(est)} poses ({n * W * H} rays): oracle OpenMP ray cast + numpy binary64 "
-                      f"statistics_p2l + Umeyama", "seconds": dt}
+            "sample": f"{n} of {len(est)} poses ({n * W * H} rays): oracle OpenMP ray cast (4-wide SIMD walk) + "
+                      f"numpy binary64 statistics_p2l + Umeyama", "seconds": dt}
 
 
 def gpu_rcc(args, world):
@@ -1237,7 +1239,7 @@ def reference_arm(args, base):
         sc, model, true, est = posegrad_workload(16)
         import oracle
 
-        obs = oracle.Scene(sc.vertices, sc.faces).simulate(model, IDENT, true, attrs=("ranges",))["ranges"]
+        obs = oracle.Scene(sc.vertices, sc.faces).simulate(model, IDENT, true, attrs=("ranges",), fast=True)["ranges"]
         run = lambda: cpu_posegrad(sc, model, true, est, obs, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
         metric, unit, config = "pose-grad evals/s", "poses/s", {"workload": "pose gradient (CPU sample)"}
     elif args.workload == "scene_terrain1m":
@@ -1252,7 +1254,7 @@ def reference_arm(args, base):
         import oracle
 
         sc, model, true, est = rcc_workload(16)
-        data_h = oracle.Scene(sc.vertices, sc.faces).simulate(model, IDENT, true, attrs=("hits", "points"))
+        data_h = oracle.Scene(sc.vertices, sc.faces).simulate(model, IDENT, true, attrs=("hits", "points"), fast=True)
         run = lambda: cpu_rcc(sc, model, true, est, data_h, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
         metric, unit, config = "Mrays/s", "Mrays/s", {"workload": "fused simulate -> statistics_p2l (CPU sample)"}
     else:
@@ -1266,7 +1268,8 @@ def reference_arm(args, base):
         sc2 = scenes.terrain(grid=1024, n_boxes=2000, seed=0)
         extras["batched"] = cpu_batched(sc2, batched.mixed_sensor_set(64, seed=0), target_s=8.0)
         psc, pmodel, ptrue, pest = posegrad_workload(16)
-        pobs = oracle.Scene(psc.vertices, psc.faces).simulate(pmodel, IDENT, ptrue, attrs=("ranges",))["ranges"]
+        pobs = oracle.Scene(psc.vertices, psc.faces).simulate(pmodel, IDENT, ptrue, attrs=("ranges",),
+                                                              fast=True)["ranges"]
         extras["pose_grad"] = cpu_posegrad(psc, pmodel, ptrue, pest, pobs, target_s=8.0)
     vals, leg = [], None
     for _ in range(args.warmup + args.steps):

@@ -41,6 +41,10 @@ def lib() -> C.CDLL:
             "orc_bvh_num_nodes": (C.c_uint32, [_P]),
             "orc_simulate": (C.c_int, [_P, C.c_int, C.c_uint32, C.c_uint32, C.c_float, C.c_float, _P, _P, _P,
                                        _P, _P, C.c_uint32, _P, _P, _P, _P, _P, _P, _P, C.c_int, _P]),
+            "orc_bvh4_build": (_P, [_P]),
+            "orc_bvh4_free": (None, [_P]),
+            "orc_simulate4": (C.c_int, [_P, C.c_int, C.c_uint32, C.c_uint32, C.c_float, C.c_float, _P, _P, _P,
+                                        _P, _P, C.c_uint32, _P, _P, _P, _P, _P, _P, _P, C.c_int]),
             "orc_rays": (C.c_int, [C.c_int, C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P, _P, C.c_uint64, _P, _P]),
             "orc_intersect_f64": (C.c_int, [_P, _P, _P, C.c_uint32, _P, _P]),
             "orc_trace_rays": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_float, _P, _P, C.c_int]),
@@ -107,12 +111,22 @@ class Scene:
         self.h = lib().orc_bvh_build_ex(_p(self.v), self.v.shape[0], _p(self.f), self.f.shape[0], int(max_leaf))
 
     def __del__(self):
+        if getattr(self, "h4", None):
+            lib().orc_bvh4_free(self.h4)
+            self.h4 = None
         if getattr(self, "h", None):
             lib().orc_bvh_free(self.h)
             self.h = None
 
     def num_nodes(self) -> int:
         return int(lib().orc_bvh_num_nodes(self.h))
+
+    def _bvh4(self):
+        if getattr(self, "h4", None) is None:
+            self.h4 = lib().orc_bvh4_build(self.h)
+            if not self.h4:
+                raise ValueError("the SAH tree is too deep for the 4-wide walk's stack")
+        return self.h4
 
     def save_map(self, path) -> int:
         """Writes this tree (built with max_leaf=1) as a GPU map file (rmg_map_load reads it);
@@ -144,8 +158,10 @@ class Scene:
         return k, W, H, dirs, origs, orig
 
     def simulate(self, model, Tsb, Tbm, attrs=("hits", "ranges", "points", "normals", "face_ids", "geom_ids",
-                                                "object_ids"), nthreads: int = 0, count_tests: bool = False):
-        """Embree-path simulation of all (pose, row, col) rays; returns numpy arrays."""
+                                                "object_ids"), nthreads: int = 0, count_tests: bool = False,
+                 fast: bool = False):
+        """Embree-path simulation of all (pose, row, col) rays; returns numpy arrays.  fast: through
+        the Embree-class 4-wide SIMD walk (orc_simulate4; the same outputs, the timed CPU baseline)."""
         k, W, H, dirs, origs, orig = self._model_args(model)
         Tsb = np.ascontiguousarray(Tsb, np.float32).reshape(8)
         Tbm = np.ascontiguousarray(Tbm, np.float32).reshape(-1, 8)
@@ -157,6 +173,15 @@ class Scene:
         for a in attrs:
             shp, dt = shapes[a]
             out[a] = np.empty(shp, dt)
+        if fast:
+            if count_tests:
+                raise ValueError("the 4-wide walk does not count triangle tests")
+            lib().orc_simulate4(self._bvh4(), k, W, H, float(model.range.min), float(model.range.max), _p(dirs),
+                                _p(origs), _p(orig), _p(Tsb), _p(Tbm), Tbm.shape[0], _p(out.get("hits")),
+                                _p(out.get("ranges")), _p(out.get("points")), _p(out.get("normals")),
+                                _p(out.get("face_ids")), _p(out.get("geom_ids")), _p(out.get("object_ids")),
+                                int(nthreads))
+            return out
         tests = np.zeros(1, np.uint64)
         lib().orc_simulate(self.h, k, W, H, float(model.range.min), float(model.range.max), _p(dirs), _p(origs),
                            _p(orig), _p(Tsb), _p(Tbm), Tbm.shape[0], _p(out.get("hits")), _p(out.get("ranges")),

@@ -19,7 +19,7 @@ def build(force: bool = False) -> Path:
     if not force and OUT.exists() and OUT.stat().st_mtime >= src.stat().st_mtime:
         return OUT
     tmp = OUT.with_suffix(".so.tmp")
-    cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
+    cmd = ["g++", "-std=c++17", "-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC",
            "-shared", str(src), "-o", str(tmp)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -198,15 +198,16 @@ def loss_fd_gradients(dataset, model, gR, gt, pre=None, h=1e-6, **filt):
 
 
 def simulate_statistics(scene, model, Tsb, Tbm, dataset, dmask=None, dids=None, dataset_id=0, pre=None,
-                        max_dist=np.inf, point_to_plane=True):
+                        max_dist=np.inf, point_to_plane=True, fast=False):
     """The RCC / MICP-L inner step per pose (tests/embree/correction_rcc.cpp:139-160): simulate
     the model scan (Points, Normals, Hits) at Tbm[p] (oracle.Scene.simulate), pair it ray by ray
     with the dataset scan (one [W*H, 3] scan for all poses or [P, W*H, 3] per pose),
     statistics_p2l / _p2p (statistics.cpp:19-126) in binary64 and Umeyama (optimization.cpp:12-49).
-    Returns (stats dict, R, t, q, per-ray validity [P, W*H])."""
+    Returns (stats dict, R, t, q, per-ray validity [P, W*H]).  fast: the ray cast through the
+    4-wide walk (the same outputs)."""
     Tbm = np.asarray(Tbm, F32).reshape(-1, 8)
     P = Tbm.shape[0]
-    sim = scene.simulate(model, Tsb, Tbm, attrs=("hits", "points", "normals"))
+    sim = scene.simulate(model, Tsb, Tbm, attrs=("hits", "points", "normals"), fast=fast)
     N = sim["hits"].size // P
     ds = np.asarray(dataset, F32).reshape(-1, N, 3)
     ds = np.broadcast_to(ds, (P, N, 3)) if ds.shape[0] == 1 else ds
