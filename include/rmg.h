@@ -637,7 +637,7 @@ int rmg_transforms_compose(const rmg_transform* a, uint32_t a_stride, const rmg_
  * sort buffers, bounds) lives in a fixed 4 MiB device array inside the
  * library, which limits the mesh to RMG_NOALLOC_MAX_FACES faces (larger
  * meshes return RMG_ERR_INVALID_ARG).  The first call on a device looks up
- * that array's address; make it before any stream capture.  Calls share the
+ * that array's address.  Calls share the
  * array and it keeps the last call's contents (each call clears what must
  * start at zero): calls that overlap on the GPU race.  Synchronises with
  * `stream` once (face-index check).

@@ -853,7 +853,7 @@ extern "C" int rmg_map_debug_set_child(rmg_map* m, uint32_t node, uint32_t which
 //
 // The first call on a device resolves the array's device address with
 // cudaGetSymbolAddress (the host-side name is only a stand-in and must never
-// be handed to a kernel); make that first call before any stream capture.
+// be handed to a kernel).
 // All calls share the one array and it keeps the previous call's contents:
 // the words that must start at zero are cleared by each call, and calls whose
 // work overlaps on the GPU (different streams, no ordering between them) race
