@@ -633,20 +633,32 @@ def icp_data(B, N, dev, seed=0):
 
 
 def cpu_icp(src_h, tgt_h, target_s=10.0):
+    """statistics_p2p + Umeyama of a bounded batch sample on all host threads: the oracle's C++
+    OpenMP statistics (binary32 filter, binary64 two-pass means and covariance; equal to the numpy
+    restatement) and numpy's batched binary64 SVD for Umeyama."""
+    import oracle
     from oracle import stats as ost
 
     B = src_h.shape[0]
+    threads = oracle.lib().orc_max_threads()
+
+    def run(n):
+        return ost.umeyama(oracle.stats_batched(src_h[:n], tgt_h[:n], nthreads=threads))
+
     t0 = time.perf_counter()
-    ost.umeyama(ost.stats(*ost.correspondences(src_h[:1], tgt_h[:1])))
-    per = max(time.perf_counter() - t0, 1e-4)
+    run(min(B, 4))
+    per = max((time.perf_counter() - t0) / min(B, 4), 1e-5)
     n = int(max(1, min(B, target_s / per)))
+    reps = int(max(1, min(50, target_s / (per * n))))  # a small batch set is timed over repeated passes
     t0 = time.perf_counter()
-    ost.umeyama(ost.stats(*ost.correspondences(src_h[:n], tgt_h[:n])))
+    for _ in range(reps):
+        run(n)
     dt = time.perf_counter() - t0
-    corr = n * src_h.shape[1]
-    return {"value": corr / dt / 1e9, "unit": "Gcorr/s", "cores": 1, "kind": "port",
-            "sample": f"{n} of {B} batches ({corr} correspondences), forward statistics + Umeyama only, "
-                      f"numpy binary64 restatement (single thread)", "seconds": dt}
+    corr = reps * n * src_h.shape[1]
+    return {"value": corr / dt / 1e9, "unit": "Gcorr/s", "cores": int(threads), "kind": "port",
+            "sample": f"{n} of {B} batches x {reps} passes ({corr} correspondences), forward statistics + Umeyama "
+                      f"only: C++ OpenMP statistics_p2p in binary64 on all host threads + numpy binary64 Umeyama",
+            "seconds": dt}
 
 
 def gpu_icp(args, world):
@@ -774,24 +786,20 @@ def posegrad_workload(n_poses):
 
 
 def cpu_posegrad(sc, model, true, est, obs_h, target_s=10.0):
+    """Ray cast of the estimates (the oracle's 4-wide walk) + the analytic range adjoint (the oracle's
+    C++ OpenMP restatement in binary64, equal to oracle/grad.py's) on all host threads."""
     import oracle
-    from oracle import grad as og
 
     ocs = oracle.Scene(sc.vertices, sc.faces)
     threads = oracle.lib().orc_max_threads()
     W, H = model_size(model)
-    dirs = oracle.directions(model)
 
     def run(n):
         sim = ocs.simulate(model, IDENT, est[:n], attrs=("ranges", "face_ids"), nthreads=threads, fast=True)
-        obs = obs_h[:n * W * H]
-        f, r = sim["face_ids"], sim["ranges"]
-        valid = (f != 0xFFFFFFFF) & (r >= model.range.min) & (obs >= model.range.min) & (obs <= model.range.max)
-        gid = np.nonzero(valid)[0]
-        rset = og.RayFaceSet(sc.vertices, sc.faces, IDENT, est[:n], dirs[gid % (W * H)], np.zeros((gid.size, 3)),
-                             gid // (W * H), f[gid], obs[gid])
-        return rset.analytic(n, 0.2)
+        return oracle.pose_grad(ocs, model, IDENT, est[:n], sim["face_ids"], sim["ranges"], obs_h[:n * W * H], 0.2,
+                                nthreads=threads)
 
+    run(1)  # builds the 4-wide tree
     t0 = time.perf_counter()
     run(1)
     per = max(time.perf_counter() - t0, 1e-4)
@@ -800,8 +808,8 @@ def cpu_posegrad(sc, model, true, est, obs_h, target_s=10.0):
     run(n)
     dt = time.perf_counter() - t0
     return {"value": n / dt, "unit": "poses/s", "cores": int(threads), "kind": "port",
-            "sample": f"{n} of {len(est)} poses: oracle OpenMP ray cast (4-wide SIMD walk) + numpy binary64 adjoint",
-            "seconds": dt}
+            "sample": f"{n} of {len(est)} poses: oracle ray cast (4-wide SIMD walk) + C++ OpenMP binary64 adjoint, "
+                      f"all host threads", "seconds": dt}
 
 
 def gpu_posegrad(args, world):
@@ -873,8 +881,9 @@ def rcc_workload(n_poses=1000):
 
 
 def cpu_rcc(sc, model, true, est, data_h, target_s=10.0):
-    """The oracle's restatement of the step: OpenMP ray cast of the model scan + binary64 numpy
-    statistics_p2l + Umeyama, over a bounded pose sample."""
+    """The step on the host: ray cast of the model scan (the oracle's 4-wide walk), statistics_p2l in
+    binary64 (the oracle's C++ OpenMP statistics) and numpy binary64 Umeyama, all host threads; the
+    same results as oracle/stats.py's simulate_statistics."""
     import oracle
     from oracle import stats as ost
 
@@ -883,9 +892,13 @@ def cpu_rcc(sc, model, true, est, data_h, target_s=10.0):
     W, H = model_size(model)
 
     def run(n):
-        return ost.simulate_statistics(ocs, model, IDENT, est[:n], data_h["points"][:n * W * H],
-                                       dmask=data_h["hits"][:n * W * H], max_dist=0.5, fast=True)
+        sim = ocs.simulate(model, IDENT, est[:n], attrs=("hits", "points", "normals"), nthreads=threads, fast=True)
+        st = oracle.stats_batched(data_h["points"][:n * W * H].reshape(n, W * H, 3),
+                                  sim["points"].reshape(n, W * H, 3), normals=sim["normals"].reshape(n, W * H, 3),
+                                  dmask=data_h["hits"][:n * W * H], mmask=sim["hits"], max_dist=0.5, nthreads=threads)
+        return ost.umeyama(st)
 
+    run(1)  # builds the 4-wide tree
     t0 = time.perf_counter()
     run(1)
     per = max(time.perf_counter() - t0, 1e-4)
@@ -894,8 +907,8 @@ def cpu_rcc(sc, model, true, est, data_h, target_s=10.0):
     run(n)
     dt = time.perf_counter() - t0
     return {"value": n * W * H / dt / 1e6, "unit": "Mrays/s", "cores": int(threads), "kind": "port",
-            "sample": f"{n} of {len(est)} poses ({n * W * H} rays): oracle OpenMP ray cast (4-wide SIMD walk) + "
-                      f"numpy binary64 statistics_p2l + Umeyama", "seconds": dt}
+            "sample": f"{n} of {len(est)} poses ({n * W * H} rays): oracle ray cast (4-wide SIMD walk) + C++ OpenMP "
+                      f"binary64 statistics_p2l + numpy Umeyama, all host threads", "seconds": dt}
 
 
 def gpu_rcc(args, world):
@@ -1236,7 +1249,7 @@ def reference_arm(args, base):
         run = lambda: cpu_icp(src, tgt, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
         metric, unit, config = "Gcorr/s", "Gcorr/s", {"workload": "ICP statistics_p2p + Umeyama (CPU sample)"}
     elif args.workload == "pose_grad":
-        sc, model, true, est = posegrad_workload(16)
+        sc, model, true, est = posegrad_workload(64)
         import oracle
 
         obs = oracle.Scene(sc.vertices, sc.faces).simulate(model, IDENT, true, attrs=("ranges",), fast=True)["ranges"]
@@ -1253,7 +1266,7 @@ def reference_arm(args, base):
     elif args.workload == "rcc_fused":
         import oracle
 
-        sc, model, true, est = rcc_workload(16)
+        sc, model, true, est = rcc_workload(64)
         data_h = oracle.Scene(sc.vertices, sc.faces).simulate(model, IDENT, true, attrs=("hits", "points"), fast=True)
         run = lambda: cpu_rcc(sc, model, true, est, data_h, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
         metric, unit, config = "Mrays/s", "Mrays/s", {"workload": "fused simulate -> statistics_p2l (CPU sample)"}
@@ -1267,7 +1280,7 @@ def reference_arm(args, base):
 
         sc2 = scenes.terrain(grid=1024, n_boxes=2000, seed=0)
         extras["batched"] = cpu_batched(sc2, batched.mixed_sensor_set(64, seed=0), target_s=8.0)
-        psc, pmodel, ptrue, pest = posegrad_workload(16)
+        psc, pmodel, ptrue, pest = posegrad_workload(64)
         pobs = oracle.Scene(psc.vertices, psc.faces).simulate(pmodel, IDENT, ptrue, attrs=("ranges",),
                                                               fast=True)["ranges"]
         extras["pose_grad"] = cpu_posegrad(psc, pmodel, ptrue, pest, pobs, target_s=8.0)

@@ -45,6 +45,9 @@ def lib() -> C.CDLL:
             "orc_bvh4_free": (None, [_P]),
             "orc_simulate4": (C.c_int, [_P, C.c_int, C.c_uint32, C.c_uint32, C.c_float, C.c_float, _P, _P, _P,
                                         _P, _P, C.c_uint32, _P, _P, _P, _P, _P, _P, _P, C.c_int]),
+            "orc_stats_batched": (C.c_int, [_P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_float, C.c_int, _P]),
+            "orc_pose_grad": (C.c_int, [_P, C.c_int, C.c_uint32, C.c_uint32, C.c_float, C.c_float, _P, _P, _P, _P,
+                                        _P, C.c_uint32, _P, _P, _P, C.c_double, C.c_int, _P, _P]),
             "orc_rays": (C.c_int, [C.c_int, C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P, _P, C.c_uint64, _P, _P]),
             "orc_intersect_f64": (C.c_int, [_P, _P, _P, C.c_uint32, _P, _P]),
             "orc_trace_rays": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_float, _P, _P, C.c_int]),
@@ -217,6 +220,42 @@ class Scene:
         f = np.zeros(o.shape[0], np.uint32)
         lib().orc_trace_rays(self.h, _p(o), _p(d), o.shape[0], float(tfar), _p(t), _p(f), int(nthreads))
         return t, f
+
+
+def stats_batched(dataset, model, normals=None, dmask=None, mmask=None, max_dist=np.inf, nthreads: int = 0):
+    """stats.stats(*stats.correspondences(dataset, model, dmask=dmask, mmask=mmask, max_dist=max_dist,
+    normals=normals)) on all host threads in C++ (orc_stats_batched: the same binary32 filters, binary64
+    two-pass means and covariance).  dataset / model / normals: [B, N, 3]; masks [B, N]."""
+    D = np.ascontiguousarray(dataset, np.float32)
+    B, N = D.shape[0], D.shape[1]
+    M = np.ascontiguousarray(model, np.float32).reshape(B, N, 3)
+    Nn = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(B, N, 3)
+    dm = None if dmask is None else np.ascontiguousarray(np.asarray(dmask).reshape(B, N) > 0, np.uint8)
+    mm = None if mmask is None else np.ascontiguousarray(np.asarray(mmask).reshape(B, N) > 0, np.uint8)
+    out = np.zeros((B, 16), np.float64)
+    lib().orc_stats_batched(_p(D), _p(M), _p(Nn), _p(dm), _p(mm), B, N, float(max_dist), int(nthreads), _p(out))
+    return {"dataset_mean": out[:, 0:3].copy(), "model_mean": out[:, 3:6].copy(),
+            "covariance": out[:, 6:15].reshape(B, 3, 3).copy(), "n": out[:, 15].astype(np.int64)}
+
+
+def pose_grad(scene, model, Tsb, Tbm, face_ids, ranges, r_obs, delta: float, nthreads: int = 0):
+    """grad.RayFaceSet(...).analytic(P, delta) over every valid ray of the simulated scans (face set,
+    range >= range.min, range.min <= r_obs <= range.max) on all host threads in C++ (orc_pose_grad).
+    Returns (grad [P, 6], loss [P])."""
+    k, W, H, dirs, origs, orig = scene._model_args(model)
+    Tsb = np.ascontiguousarray(Tsb, np.float32).reshape(8)
+    Tbm = np.ascontiguousarray(Tbm, np.float32).reshape(-1, 8)
+    P = Tbm.shape[0]
+    f = np.ascontiguousarray(face_ids, np.uint32).reshape(-1)
+    r = np.ascontiguousarray(ranges, np.float32).reshape(-1)
+    o = np.ascontiguousarray(r_obs, np.float32).reshape(-1)
+    assert f.size == r.size == o.size == P * W * H
+    g = np.zeros((P, 6), np.float64)
+    L = np.zeros(P, np.float64)
+    lib().orc_pose_grad(scene.h, k, W, H, float(model.range.min), float(model.range.max), _p(dirs), _p(origs),
+                        _p(orig), _p(Tsb), _p(Tbm), P, _p(f), _p(r), _p(o), float(delta), int(nthreads), _p(g),
+                        _p(L))
+    return g, L
 
 
 class CanonicalLbvh:

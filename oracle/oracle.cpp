@@ -981,6 +981,134 @@ int orc_rays(int kind, uint32_t W, uint32_t H, const float* dirs, const float* o
   return 0;
 }
 
+// Batched correspondence statistics (statistics.cpp:19-126) on all host
+// threads, the CPU baseline of the statistics kernels: B batches of N
+// correspondences, filters in binary32 exactly as oracle/stats.py's
+// correspondences() (dmask / mmask > 0; point-to-point: |M - D|^2 < md^2;
+// point-to-plane when normals are given: |(M - D).n| < md, M := D + n sd), then
+// binary64 means and covariance in two passes.  out: 16 doubles per batch --
+// dataset mean, model mean, covariance row-major (row = model axis), count.
+int orc_stats_batched(const float* D, const float* M, const float* Nrm, const uint8_t* dmask, const uint8_t* mmask,
+                      uint32_t B, uint32_t N, float max_dist, int nthreads, double* out) {
+  const float md = max_dist, md2 = md * md;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads_or_default(nthreads))
+  for (int64_t b = 0; b < (int64_t)B; ++b) {
+    const size_t base = (size_t)b * N;
+    double sd[3] = {0, 0, 0}, sm[3] = {0, 0, 0}, n = 0;
+    auto pair = [&](size_t i, float* dd, float* mm) -> bool {
+      if (dmask && !(dmask[base + i] > 0)) return false;
+      if (mmask && !(mmask[base + i] > 0)) return false;
+      const float* d = D + 3 * (base + i);
+      const float* m = M + 3 * (base + i);
+      const float dx = m[0] - d[0], dy = m[1] - d[1], dz = m[2] - d[2];
+      if (Nrm) {
+        const float* nn = Nrm + 3 * (base + i);
+        const float s = (dx * nn[0] + dy * nn[1]) + dz * nn[2];
+        if (!(std::fabs(s) < md)) return false;
+        for (int k = 0; k < 3; ++k) { dd[k] = d[k]; mm[k] = d[k] + nn[k] * s; }
+      } else {
+        const float d2 = (dx * dx + dy * dy) + dz * dz;
+        if (!(d2 < md2)) return false;
+        for (int k = 0; k < 3; ++k) { dd[k] = d[k]; mm[k] = m[k]; }
+      }
+      return true;
+    };
+    float dd[3], mm[3];
+    for (uint32_t i = 0; i < N; ++i) {
+      if (!pair(i, dd, mm)) continue;
+      for (int k = 0; k < 3; ++k) { sd[k] += dd[k]; sm[k] += mm[k]; }
+      n += 1.0;
+    }
+    double* o = out + 16 * (size_t)b;
+    for (int k = 0; k < 16; ++k) o[k] = 0.0;
+    if (n == 0.0) continue;
+    double dm[3], mmean[3], C[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 3; ++k) { dm[k] = sd[k] / n; mmean[k] = sm[k] / n; }
+    for (uint32_t i = 0; i < N; ++i) {
+      if (!pair(i, dd, mm)) continue;
+      const double dc[3] = {dd[0] - dm[0], dd[1] - dm[1], dd[2] - dm[2]};
+      const double mc[3] = {mm[0] - mmean[0], mm[1] - mmean[1], mm[2] - mmean[2]};
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) C[3 * r + c] += mc[r] * dc[c];
+    }
+    for (int k = 0; k < 3; ++k) { o[k] = dm[k]; o[3 + k] = mmean[k]; }
+    for (int k = 0; k < 9; ++k) o[6 + k] = C[k] / n;
+    o[15] = n;
+  }
+  return 0;
+}
+
+// The range adjoint's analytic gradient on all host threads, the CPU baseline
+// of the pose-gradient kernel: the restatement of oracle/grad.py's
+// RayFaceSet.analytic in binary64 for every ray of n_poses x (W x H) whose
+// simulated hit (face, range) and observation are valid (face set, range >=
+// rmin, rmin <= r_obs <= rmax).  Per ray: r = n.(p0 - o)/(n.d) for the pose's
+// ray, psi = clamp(r - r_obs, -delta, delta), dr/drho = -n_b/(n_b.d_b), dr/domega
+// = -(p_b x n_b)/(n_b.d_b); grad (6 per pose) sums psi dr/dxi, loss the Huber terms.
+int orc_pose_grad(void* bvhp, int kind, uint32_t W, uint32_t H, float rmin, float rmax, const float* dirs,
+                  const float* origs, const float* orig, const float* Tsb, const float* Tbm, uint32_t n_poses,
+                  const uint32_t* face_ids, const float* ranges, const float* r_obs, double delta, int nthreads,
+                  double* grad, double* loss) {
+  const Mesh& mesh = static_cast<SahBvh*>(bvhp)->mesh;
+  auto rot = [](const float* q, double R[9]) {
+    const double x = q[0], y = q[1], z = q[2], w = q[3];
+    const double v[9] = {1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w),
+                         2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w),
+                         2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)};
+    for (int k = 0; k < 9; ++k) R[k] = v[k];
+  };
+  double Rsb[9];
+  rot(Tsb, Rsb);
+  const size_t WH = (size_t)W * H;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads_or_default(nthreads))
+  for (int64_t p = 0; p < (int64_t)n_poses; ++p) {
+    double Rbm[9];
+    rot(Tbm + 8 * (size_t)p, Rbm);
+    const double tbm[3] = {Tbm[8 * p + 4], Tbm[8 * p + 5], Tbm[8 * p + 6]};
+    double g[6] = {0, 0, 0, 0, 0, 0}, L = 0.0;
+    for (size_t loc = 0; loc < WH; ++loc) {
+      const size_t gid = (size_t)p * WH + loc;
+      const uint32_t f = face_ids[gid];
+      const double obs = r_obs[gid];
+      if (f == 0xffffffffu || !(ranges[gid] >= rmin) || !(obs >= rmin) || !(obs <= rmax)) continue;
+      const double ds[3] = {dirs[3 * loc], dirs[3 * loc + 1], dirs[3 * loc + 2]};
+      double os[3] = {0, 0, 0};
+      if (kind == 2) { os[0] = orig[0]; os[1] = orig[1]; os[2] = orig[2]; }
+      if (kind == 3) { os[0] = origs[3 * loc]; os[1] = origs[3 * loc + 1]; os[2] = origs[3 * loc + 2]; }
+      double db[3], ob[3];
+      for (int r = 0; r < 3; ++r) {
+        db[r] = Rsb[3 * r] * ds[0] + Rsb[3 * r + 1] * ds[1] + Rsb[3 * r + 2] * ds[2];
+        ob[r] = Tsb[4 + r] + (Rsb[3 * r] * os[0] + Rsb[3 * r + 1] * os[1] + Rsb[3 * r + 2] * os[2]);
+      }
+      double o[3], d[3];
+      for (int r = 0; r < 3; ++r) {
+        o[r] = Rbm[3 * r] * ob[0] + Rbm[3 * r + 1] * ob[1] + Rbm[3 * r + 2] * ob[2] + tbm[r];
+        d[r] = Rbm[3 * r] * db[0] + Rbm[3 * r + 1] * db[1] + Rbm[3 * r + 2] * db[2];
+      }
+      const V3 a = mesh.vert(f, 0), b1 = mesh.vert(f, 1), c = mesh.vert(f, 2);
+      const double p0[3] = {a.x, a.y, a.z};
+      const double e1[3] = {b1.x - p0[0], b1.y - p0[1], b1.z - p0[2]};
+      const double e2[3] = {c.x - p0[0], c.y - p0[1], c.z - p0[2]};
+      const double n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+      const double r = (n[0] * (p0[0] - o[0]) + n[1] * (p0[1] - o[1]) + n[2] * (p0[2] - o[2])) /
+                       (n[0] * d[0] + n[1] * d[1] + n[2] * d[2]);
+      const double e = r - obs;
+      const double psi = std::min(std::max(e, -delta), delta);
+      double nb[3];
+      for (int k = 0; k < 3; ++k) nb[k] = Rbm[k] * n[0] + Rbm[3 + k] * n[1] + Rbm[6 + k] * n[2];  // R_bm^T n
+      const double bb = nb[0] * db[0] + nb[1] * db[1] + nb[2] * db[2];
+      const double pb[3] = {ob[0] + r * db[0], ob[1] + r * db[1], ob[2] + r * db[2]};
+      const double cx[3] = {pb[1] * nb[2] - pb[2] * nb[1], pb[2] * nb[0] - pb[0] * nb[2], pb[0] * nb[1] - pb[1] * nb[0]};
+      for (int k = 0; k < 3; ++k) { g[k] += -nb[k] / bb * psi; g[3 + k] += -cx[k] / bb * psi; }
+      const double ae = std::fabs(e);
+      L += ae <= delta ? 0.5 * e * e : delta * (ae - 0.5 * delta);
+    }
+    for (int k = 0; k < 6; ++k) grad[6 * p + k] = g[k];
+    loss[p] = L;
+  }
+  return 0;
+}
+
 // Binary64 Moeller-Trumbore of one ray against one face.  Writes t and the
 // smallest barycentric coordinate (negative = outside).  Returns 1 when the
 // plane is hit in front of the origin (t > 0).
