@@ -593,17 +593,23 @@ def gpu_noise(args, world):
                     "h2d_bytes_per_step": 4 * (n // 8), "d2h_bytes_per_step": 4 * (n // 8)},
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
 
-    def cpu():
-        from oracle import noise as on
+    return line, cpu_noise, line["config"]
 
-        rr = np.random.default_rng(0).uniform(0, 100, 4_000_000).astype(np.float32)
-        t0 = time.perf_counter()
-        on.apply(0, rr, seed=42, call=0, stddev=0.02, max_range=130.0)
-        dt = time.perf_counter() - t0
-        return {"value": rr.size / dt / 1e9, "unit": "Granges/s", "cores": 1, "kind": "port",
-                "sample": "4,000,000 ranges, numpy restatement (binary64), one thread", "seconds": dt}
 
-    return line, cpu, line["config"]
+def cpu_noise(n=64_000_000):
+    """GaussianNoise(0, 0.02) on n ranges: the oracle's C++ OpenMP restatement (Philox4x32-10,
+    binary64 Box-Muller; equal to the numpy restatement) on all host threads."""
+    import oracle
+
+    threads = oracle.lib().orc_max_threads()
+    rr = np.random.default_rng(0).uniform(0, 100, n).astype(np.float32)
+    oracle.noise_apply(0, rr[:1_000_000], 42, 0, stddev=0.02, max_range=130.0, nthreads=threads)
+    t0 = time.perf_counter()
+    oracle.noise_apply(0, rr, 42, 0, stddev=0.02, max_range=130.0, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": rr.size / dt / 1e9, "unit": "Granges/s", "cores": int(threads), "kind": "port",
+            "sample": f"{n:,} ranges, C++ OpenMP restatement (Philox4x32-10, binary64 Box-Muller), all host threads",
+            "seconds": dt}
 
 
 # ---- ICP statistics + Umeyama (forward and backward) -----------------------------------------
@@ -1263,6 +1269,9 @@ def reference_arm(args, base):
         poses = scenes.terrain_poses(baked, 1000, seed=2)
         run = lambda: cpu_raycast(baked, model, poses, SCENE_ATTRS, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
         metric, unit, config = "Mrays/s", "Mrays/s", {"workload": "terrain 1M + 2000 boxes (CPU: the geometry as one mesh)"}
+    elif args.workload == "noise":
+        run = cpu_noise
+        metric, unit, config = "Granges/s", "Granges/s", {"workload": "GaussianNoise(0, 0.02) (CPU sample)"}
     elif args.workload == "rcc_fused":
         import oracle
 

@@ -48,6 +48,8 @@ def lib() -> C.CDLL:
             "orc_stats_batched": (C.c_int, [_P, _P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_float, C.c_int, _P]),
             "orc_pose_grad": (C.c_int, [_P, C.c_int, C.c_uint32, C.c_uint32, C.c_float, C.c_float, _P, _P, _P, _P,
                                         _P, C.c_uint32, _P, _P, _P, C.c_double, C.c_int, _P, _P]),
+            "orc_noise_apply": (C.c_int, [C.c_int, _P, _P, C.c_uint64, C.c_uint64, C.c_uint64, C.c_double,
+                                          C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, C.c_int]),
             "orc_rays": (C.c_int, [C.c_int, C.c_uint32, C.c_uint32, _P, _P, _P, _P, _P, _P, C.c_uint64, _P, _P]),
             "orc_intersect_f64": (C.c_int, [_P, _P, _P, C.c_uint32, _P, _P]),
             "orc_trace_rays": (C.c_int, [_P, _P, _P, C.c_uint64, C.c_float, _P, _P, C.c_int]),
@@ -256,6 +258,17 @@ def pose_grad(scene, model, Tsb, Tbm, face_ids, ranges, r_obs, delta: float, nth
                         _p(orig), _p(Tsb), _p(Tbm), P, _p(f), _p(r), _p(o), float(delta), int(nthreads), _p(g),
                         _p(L))
     return g, L
+
+
+def noise_apply(kind, ranges, seed, call, mean=0.0, stddev=0.0, range_exp=1.0, hit_p=0.0, ret_p=0.0,
+                max_range=10000.0, nthreads: int = 0):
+    """noise.apply(...)'s new ranges (binary64) on all host threads in C++ (orc_noise_apply)."""
+    r = np.ascontiguousarray(ranges, np.float32).reshape(-1)
+    out = np.empty(r.size, np.float64)
+    if lib().orc_noise_apply(int(kind), _p(r), _p(out), r.size, int(seed), int(call), float(mean), float(stddev),
+                             float(range_exp), float(hit_p), float(ret_p), float(max_range), int(nthreads)) != 0:
+        raise ValueError(f"noise kind {kind}")
+    return out
 
 
 class CanonicalLbvh:

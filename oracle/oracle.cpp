@@ -1109,6 +1109,71 @@ int orc_pose_grad(void* bvhp, int kind, uint32_t W, uint32_t H, float rmin, floa
   return 0;
 }
 
+}  // extern "C"
+
+// Range noise on all host threads, the CPU baseline of rmg_noise_apply: the
+// restatement of oracle/noise.py's apply() in C++ -- Philox4x32-10 (Salmon,
+// Moraes, Dror, Shaw, SC 2011; counter (i, call), key = seed), uniforms as odd
+// multiples of 2^-24, Box-Muller in binary64 -- for kind 0 (Gaussian), 1
+// (range-relative Gaussian) and 2 (uniform dust).  out: n binary64 ranges.
+namespace {
+struct Philox4 { uint32_t v[4]; };
+Philox4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1) {
+  uint32_t c[4] = {c0, c1, c2, c3};
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0], p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0, hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+  }
+  return Philox4{{c[0], c[1], c[2], c[3]}};
+}
+inline double uniform01(uint32_t x) { return (double)((x >> 8) | 1u) * 0x1p-24; }
+}  // namespace
+
+extern "C" int orc_noise_apply(int kind, const float* ranges, double* out, uint64_t n, uint64_t seed, uint64_t call,
+                               double mean, double stddev, double range_exp, double hit_p, double ret_p,
+                               double max_range, int nthreads) {
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32), c2 = (uint32_t)call, c3 = (uint32_t)(call >> 32);
+  const double two_pi = 2.0 * M_PI;
+  if (kind == 0 || kind == 1) {
+    const int64_t nb = (int64_t)((n + 3) / 4);
+#pragma omp parallel for schedule(static, 4096) num_threads(nthreads_or_default(nthreads))
+    for (int64_t i = 0; i < nb; ++i) {
+      const Philox4 b = philox4x32_10((uint32_t)i, (uint32_t)((uint64_t)i >> 32), c2, c3, k0, k1);
+      double u[4];
+      for (int k = 0; k < 4; ++k) u[k] = uniform01(b.v[k]);
+      const double r0 = std::sqrt(-2.0 * std::log(u[0])), r1 = std::sqrt(-2.0 * std::log(u[2]));
+      const double z[4] = {r0 * std::cos(two_pi * u[1]), r0 * std::sin(two_pi * u[1]),
+                           r1 * std::cos(two_pi * u[3]), r1 * std::sin(two_pi * u[3])};
+      for (int k = 0; k < 4; ++k) {
+        const uint64_t e = 4 * (uint64_t)i + k;
+        if (e >= n) break;
+        const double r = ranges[e];
+        const double sd = kind == 0 ? stddev : stddev * std::pow(std::max(r, 0.0), range_exp);
+        out[e] = r <= max_range ? r + (z[k] * sd + mean) : r;
+      }
+    }
+    return 0;
+  }
+  if (kind != 2) return 1;
+#pragma omp parallel for schedule(static, 4096) num_threads(nthreads_or_default(nthreads))
+  for (int64_t i = 0; i < (int64_t)n; ++i) {
+    const Philox4 b = philox4x32_10((uint32_t)i, (uint32_t)((uint64_t)i >> 32), c2, c3, k0, k1);
+    const double u0 = uniform01(b.v[0]), u1 = uniform01(b.v[1]), u2 = uniform01(b.v[2]);
+    const double r = ranges[i];
+    const double rr = std::min(r, max_range);
+    const double p_hit = 1.0 - std::pow(1.0 - hit_p, rr);
+    const double nr = (double)((float)u1 * (float)rr);
+    const double p_ret = std::pow(ret_p, nr);
+    out[i] = (u0 < p_hit && u2 < p_ret) ? nr : r;
+  }
+  return 0;
+}
+
+extern "C" {
+
 // Binary64 Moeller-Trumbore of one ray against one face.  Writes t and the
 // smallest barycentric coordinate (negative = outside).  Returns 1 when the
 // plane is hit in front of the origin (t > 0).

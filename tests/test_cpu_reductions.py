@@ -1,10 +1,11 @@
-"""The C++ OpenMP reductions of the timed CPU baselines equal the oracle's numpy restatements:
-batched statistics (point-to-point and point-to-plane, with masks and distance filters) and the
-range adjoint's analytic gradient."""
+"""The C++ OpenMP restatements of the timed CPU baselines equal the oracle's numpy restatements:
+batched statistics (point-to-point and point-to-plane, with masks and distance filters), the
+range adjoint's analytic gradient and the range noise."""
 import numpy as np
 
 import oracle
 from oracle import grad as og
+from oracle import noise as on
 from oracle import stats as ost
 from rmagine_gb300 import scenes, sensors
 
@@ -69,3 +70,17 @@ def test_rcc_step_equals_simulate_statistics():
     R2, t2, _ = ost.umeyama(got)
     np.testing.assert_allclose(R2, R, atol=1e-12)
     np.testing.assert_allclose(t2, t, atol=1e-9)
+
+
+def test_noise_equals_numpy_restatement():
+    rr = np.random.default_rng(1).uniform(0, 150, 200_003).astype(np.float32)
+    for kind, kw in ((0, dict(stddev=0.02, mean=0.01, max_range=130.0)),
+                     (1, dict(stddev=0.01, range_exp=1.3, max_range=130.0)),
+                     (2, dict(hit_p=0.01, ret_p=0.5, max_range=100.0))):
+        want = on.apply(kind, rr, seed=42, call=3, **kw)
+        want = want[0] if isinstance(want, tuple) else want
+        got = oracle.noise_apply(kind, rr, 42, 3, **kw)
+        if kind == 1:  # pow() of two libraries: the last bits may differ
+            np.testing.assert_allclose(got, want, rtol=1e-13, atol=1e-13)
+        else:
+            assert np.array_equal(got, want), kind
