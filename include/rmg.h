@@ -222,13 +222,22 @@ int rmg_map_debug_set_child(rmg_map* map, uint32_t node, uint32_t which, int32_t
  * directions (and OnDn origins) are materialised once in device memory:
  * SphericalModel::getDirection (sensor_models.h:169-174) and
  * PinholeModel::getDirection (:256-276) are evaluated on the GPU; O1Dn/OnDn
- * tables (:375-384, :460-468) are copied from the host arrays.
+ * tables (:375-384, :460-468) are copied from the host arrays.  An O1Dn/OnDn
+ * table whose directions are scattered (its neighbours far apart, as in a
+ * table of random directions) gets a visiting order sorted by elevation band
+ * and azimuth, so that the rays a warp walks together share their paths;
+ * outputs, observations and every other per-ray array keep the table's own
+ * order, and the results are the same.
  * ------------------------------------------------------------------------- */
 int rmg_sensor_create(const rmg_model* model, void* stream, rmg_sensor** out);
 int rmg_sensor_destroy(rmg_sensor* sensor);
 /* Copies the sensor-frame direction table (width*height) to host memory. */
 int rmg_sensor_directions(const rmg_sensor* sensor, rmg_vec3* host_out);
 int rmg_sensor_size(const rmg_sensor* sensor, uint32_t* width, uint32_t* height);
+/* *sorted = 1 when the sensor visits its rays in a sorted order (and, when
+ * host_out is not NULL, copies that order: width*height table indices),
+ * *sorted = 0 when it visits them in the table's order. */
+int rmg_sensor_visit_order(const rmg_sensor* sensor, uint32_t* host_out, int* sorted);
 
 /* ---------------------------------------------------------------------------
  * Simulate.

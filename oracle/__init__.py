@@ -211,6 +211,8 @@ class Scene:
     def intersect_f64(self, o, d, face: int):
         t = np.zeros(1, np.float64)
         b = np.zeros(1, np.float64)
+        if not 0 <= int(face) < self.f.shape[0]:
+            raise ValueError(f"intersect_f64: face {int(face)} is not a face of this mesh")
         hit = lib().orc_intersect_f64(self.h, _p(np.ascontiguousarray(o, np.float32)),
                                       _p(np.ascontiguousarray(d, np.float32)), int(face), _p(t), _p(b))
         return bool(hit), float(t[0]), float(b[0])
@@ -339,7 +341,9 @@ def certify(scene: Scene, model, Tsb, Tbm, got: dict, want: dict, band: float = 
     caller asserts report["unexcused"] == 0.
     """
     rmin, rmax = float(model.range.min), float(model.range.max)
-    f_got, f_want = got["face_ids"], want["face_ids"]
+    # face ids as unsigned 32-bit (a result held in int32 reads a miss as -1)
+    f_got = np.asarray(got["face_ids"]).astype(np.int64) & 0xFFFFFFFF
+    f_want = np.asarray(want["face_ids"]).astype(np.int64) & 0xFFFFFFFF
     r_got, r_want = got["ranges"], want["ranges"]
     h_got = got.get("hits")
     h_want = want.get("hits")

@@ -1176,10 +1176,12 @@ extern "C" {
 
 // Binary64 Moeller-Trumbore of one ray against one face.  Writes t and the
 // smallest barycentric coordinate (negative = outside).  Returns 1 when the
-// plane is hit in front of the origin (t > 0).
+// plane is hit in front of the origin (t > 0), -1 for a face index outside the
+// mesh.
 int orc_intersect_f64(void* bvhp, const float* o, const float* d, uint32_t face, double* t_out,
                       double* minbary_out) {
   const SahBvh& bvh = *static_cast<SahBvh*>(bvhp);
+  if ((size_t)face >= bvh.mesh.f.size() / 3) { *t_out = INFINITY; *minbary_out = -INFINITY; return -1; }
   const V3 a = bvh.mesh.vert(face, 0), b = bvh.mesh.vert(face, 1), c = bvh.mesh.vert(face, 2);
   const double p0[3] = {a.x, a.y, a.z}, p1[3] = {b.x, b.y, b.z}, p2[3] = {c.x, c.y, c.z};
   const double O[3] = {o[0], o[1], o[2]}, D[3] = {d[0], d[1], d[2]};

@@ -170,6 +170,7 @@ SIGNATURES: dict[str, tuple] = {
     "rmg_sensor_destroy": (C.c_int, [_P]),
     "rmg_sensor_directions": (C.c_int, [_P, _P]),
     "rmg_sensor_size": (C.c_int, [_P, C.POINTER(_U32), C.POINTER(_U32)]),
+    "rmg_sensor_visit_order": (C.c_int, [_P, _P, C.POINTER(C.c_int)]),
     "rmg_simulate": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(OutputsC), _P]),
     "rmg_simulate_ex": (C.c_int, [_P, _P, C.POINTER(TransformC), _P, _U32, C.POINTER(OutputsC),
                                   C.POINTER(LaunchConfigC), _P]),

@@ -60,7 +60,7 @@ __device__ __forceinline__ void batched_ray(const BatchParams& B, const JobDev& 
   const uint32_t hid = tx * tile_w + (lane & (tile_w - 1));
   const uint32_t W = J.sen.width, H = J.sen.height;
   if (vid >= H || hid >= W) return;
-  const uint32_t loc = vid * W + hid;
+  const uint32_t loc = visit_loc(J.sen, vid * W + hid);
   const uint64_t gid = (uint64_t)pose * W * H + loc;
   const Tf Tsm = tmul(load_tf(J.Tbm[pose]), J.Tsb);
   V dir_s, orig_s, o, d;

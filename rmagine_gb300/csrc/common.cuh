@@ -92,7 +92,15 @@ struct SensorDev {
   const float* dirs;    // 3*width*height floats (sensor frame)
   const float* origs;   // OnDn: 3*width*height floats, else NULL
   float3 orig;          // O1Dn origin
+  const uint32_t* order;  // visiting order of the table's rays (O1Dn / OnDn), NULL = the table's own
 };
+
+// The table entry (and output element) of launch slot i: a sensor whose table
+// of scattered directions was sorted for coherence visits its rays in that
+// order; every per-ray input and output stays at the table's own index.
+__device__ __forceinline__ uint32_t visit_loc(const SensorDev& sen, uint32_t i) {
+  return sen.order ? __ldg(sen.order + i) : i;
+}
 
 // ----------------------------------------------------------------------------
 // Exact-order small math (no contraction).

@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(256, RMG_FUSED_MIN_BLOCKS) k_trace_stats(const
     bool ok = false;
     V D{0.f, 0.f, 0.f}, M{0.f, 0.f, 0.f};
     if (vid < H && hid < W) {
-      const uint32_t loc = vid * W + hid;
+      const uint32_t loc = visit_loc(P.sen, vid * W + hid);
       const uint64_t di = dbase + loc;
       if ((!F.dmask || F.dmask[di] != 0) && (!F.dids || F.dids[di] == F.dataset_id)) {
         V dir_s, orig_s, o, d;

@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(256, RMG_GRAD_MIN_BLOCKS) k_range_grad(const G
     const uint32_t hid = tx * tile_w + (lane & (tile_w - 1));
     const uint32_t W = P.sen.width, H = P.sen.height;
     if (vid < H && hid < W) {
-      const uint32_t loc = vid * W + hid;
+      const uint32_t loc = visit_loc(P.sen, vid * W + hid);
       const uint64_t gid = (uint64_t)pose * W * H + loc;
       const Tf Tbm = load_tf(P.Tbm[pose]);
       const Tf Tsm = tmul(Tbm, P.Tsb);

@@ -46,6 +46,7 @@ struct rmg_sensor {
   uint32_t width, height;
   float* d_dirs;              // 3*width*height
   float* d_origs;             // 3*width*height (OnDn only)
+  uint32_t* d_order;          // width*height visiting order (O1Dn / OnDn tables sorted for coherence), or NULL
 };
 
 namespace rmg {

@@ -869,7 +869,7 @@ __global__ void __launch_bounds__(256, trace_min_blocks<TB>()) k_trace(const Tra
   const uint32_t W = P.sen.width, H = P.sen.height;
   const bool inside = vid < H && hid < W;
   if (TB != kPacketTB && !inside) return;  // the packet walk needs every lane
-  const uint32_t loc = inside ? vid * W + hid : 0;
+  const uint32_t loc = inside ? visit_loc(P.sen, vid * W + hid) : 0;
   const uint64_t gid = (uint64_t)pose * W * H + loc;
 
   const Tf Tsm = tmul(load_tf(P.Tbm[pose]), P.Tsb);
@@ -912,7 +912,7 @@ __device__ __forceinline__ bool ray_coords(const TraceParams& P, uint64_t ray, u
   const uint32_t hid = tx * tile_w + (slot & (tile_w - 1));
   const uint32_t W = P.sen.width, H = P.sen.height;
   if (vid >= H || hid >= W) return false;
-  loc = vid * W + hid;
+  loc = visit_loc(P.sen, vid * W + hid);
   gid = (uint64_t)pose * W * H + loc;
   return true;
 }

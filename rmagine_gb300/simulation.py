@@ -264,6 +264,17 @@ class Sensor:
         L.call("rmg_sensor_directions", self._h, out.ctypes.data_as(C.c_void_p))
         return out
 
+    def visit_order(self):
+        """The sorted order in which the kernels visit this sensor's rays (table indices), or None when
+        they visit them in the table's own order (O1Dn/OnDn tables of scattered directions get one)."""
+        sorted_ = C.c_int()
+        L.call("rmg_sensor_visit_order", self._h, None, C.byref(sorted_))
+        if not sorted_.value:
+            return None
+        out = np.zeros(self.width * self.height, np.uint32)
+        L.call("rmg_sensor_visit_order", self._h, out.ctypes.data_as(C.c_void_p), C.byref(sorted_))
+        return out
+
     def destroy(self) -> None:
         if self._h is not None:
             L.load().rmg_sensor_destroy(self._h)
