@@ -177,6 +177,9 @@ struct rmg_batch {
 };
 
 namespace rmg {
+
+void fit_tile(uint32_t W, uint32_t H, uint32_t& tw, uint32_t& th);
+
 namespace {
 
 void drop_graph(rmg_batch* b) {
@@ -207,9 +210,8 @@ int build_jobs(rmg_batch* b) {
     J.Tbm = e.Tbm;
     J.n_poses = e.n_poses;
     J.out = e.out;
-    // 1-row sensors (O1Dn/OnDn lists) use 32 x 1 tiles; 2-D sensors the configured shape
     uint32_t tw = b->cfg.tile_w, th = b->cfg.tile_h;
-    if (e.sensor->height < th) { tw = 32; th = 1; }
+    fit_tile(e.sensor->width, e.sensor->height, tw, th);
     uint32_t l = 0;
     while ((1u << l) < tw) ++l;
     J.tile_w_log2 = l;

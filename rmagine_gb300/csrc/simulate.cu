@@ -65,6 +65,16 @@ int log2u(uint32_t v) {
   return l;
 }
 
+// Tile shape for a sensor: a configured tile taller (wider) than the sensor is
+// halved in height (width) and doubled in the other direction while the
+// smaller size still covers the sensor, so a 1-row O1Dn table walks 32 x 1
+// tiles instead of leaving three rows of an 8 x 4 tile idle.  Results do not
+// depend on the tile shape.
+void fit_tile(uint32_t W, uint32_t H, uint32_t& tw, uint32_t& th) {
+  while (th > 1 && th / 2 >= H) { th /= 2; tw *= 2; }
+  while (tw > 1 && tw / 2 >= W) { tw /= 2; th *= 2; }
+}
+
 // Fills the parameter block of one sensor's launch; returns the tile count.
 int make_trace_params(const rmg_map* map, const rmg_sensor* sensor, const rmg_transform* Tsb,
                       const rmg_transform* Tbm, uint32_t n_poses, const rmg_outputs* out,
@@ -76,10 +86,12 @@ int make_trace_params(const rmg_map* map, const rmg_sensor* sensor, const rmg_tr
   P.Tbm = Tbm;
   P.n_poses = n_poses;
   P.out = *out;
-  P.tile_w_log2 = (uint32_t)log2u(cfg.tile_w);
-  P.tile_h = cfg.tile_h;
-  P.tiles_x = (sensor->width + cfg.tile_w - 1) / cfg.tile_w;
-  const uint32_t tiles_y = (sensor->height + cfg.tile_h - 1) / cfg.tile_h;
+  uint32_t tw = cfg.tile_w, th = cfg.tile_h;
+  fit_tile(sensor->width, sensor->height, tw, th);
+  P.tile_w_log2 = (uint32_t)log2u(tw);
+  P.tile_h = th;
+  P.tiles_x = (sensor->width + tw - 1) / tw;
+  const uint32_t tiles_y = (sensor->height + th - 1) / th;
   P.tiles_per_pose = P.tiles_x * tiles_y;
   P.n_tiles = (uint64_t)P.tiles_per_pose * n_poses;
   P.budget = 2u * map->n_nodes + 64u;

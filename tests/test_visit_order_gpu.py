@@ -100,3 +100,19 @@ def test_pose_gradient_over_a_sorted_table(terrain):
     (g0, l0), (g1, l1) = grads
     np.testing.assert_allclose(g0, g1, rtol=1e-4, atol=1e-4 * np.abs(g1).max())
     np.testing.assert_allclose(l0, l1, rtol=1e-5)
+
+
+def test_tiles_fit_one_row_and_one_column_tables(terrain):
+    sc, m, poses = terrain
+    dirs = sensors.sphere_directions(640, seed=28)
+    for W, H in ((640, 1), (1, 640), (2, 320)):
+        model = sensors.O1DnModel(width=W, height=H, range=sensors.Interval(0.3, 130.0), orig=(0.0, 0.0, 0.1),
+                                  dirs=dirs)
+        _, base = outputs(m, model, poses)
+        for cfg in (rm.launch_config(16, 4, 8, 4, bvh_width=2, packet=0), rm.launch_config(16, 4, 32, 1, packet=0),
+                    rm.launch_config(16, 4, 1, 32, packet=0), rm.launch_config(16, 4, 8, 4, packet=1)):
+            sim = rm.make_simulator(model, m)
+            sim.launch_config = cfg
+            res = sim.simulate(torch.from_numpy(poses).cuda(), attrs=rm.ATTRIBUTES)
+            for a in rm.ATTRIBUTES:
+                assert np.array_equal(getattr(res, a).cpu().numpy().view(np.uint8), base[a].view(np.uint8)), (W, H, a)
