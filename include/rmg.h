@@ -234,7 +234,8 @@ int rmg_sensor_destroy(rmg_sensor* sensor);
 /* Copies the sensor-frame direction table (width*height) to host memory. */
 int rmg_sensor_directions(const rmg_sensor* sensor, rmg_vec3* host_out);
 int rmg_sensor_size(const rmg_sensor* sensor, uint32_t* width, uint32_t* height);
-/* *sorted = 1 when the sensor visits its rays in a sorted order (and, when
+/* No counterpart in the reference (Embree casts each ray on its own).
+ * *sorted = 1 when the sensor visits its rays in a sorted order (and, when
  * host_out is not NULL, copies that order: width*height table indices),
  * *sorted = 0 when it visits them in the table's order. */
 int rmg_sensor_visit_order(const rmg_sensor* sensor, uint32_t* host_out, int* sorted);
