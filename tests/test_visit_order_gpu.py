@@ -116,3 +116,23 @@ def test_tiles_fit_one_row_and_one_column_tables(terrain):
             res = sim.simulate(torch.from_numpy(poses).cuda(), attrs=rm.ATTRIBUTES)
             for a in rm.ATTRIBUTES:
                 assert np.array_equal(getattr(res, a).cpu().numpy().view(np.uint8), base[a].view(np.uint8)), (W, H, a)
+
+
+def test_sorted_table_with_zero_and_nan_directions(terrain):
+    sc, m, poses = terrain
+    dirs = sensors.sphere_directions(1200, seed=29)
+    dirs[5::97] = 0.0
+    dirs[11::89] = np.nan
+    model = sensors.O1DnModel(width=1200, height=1, range=sensors.Interval(0.3, 130.0), orig=(0.0, 0.0, 0.1),
+                              dirs=dirs)
+    sim, got = outputs(m, model, poses)
+    order = sim.sensor.visit_order()
+    assert order is not None and np.array_equal(np.sort(order), np.arange(1200))
+    bad = np.nonzero(~np.isfinite(dirs).all(1) | (np.abs(dirs).sum(1) == 0))[0]
+    assert set(order[-bad.size:].tolist()) == set(bad.tolist())  # visited last
+    ocs = oracle.Scene(sc.vertices, sc.faces)
+    ref = ocs.simulate(model, IDENT, poses)
+    rep = oracle.certify(ocs, model, IDENT, poses, {a: got[a].reshape(ref[a].shape) for a in got}, ref)
+    assert rep["unexcused"] == 0, rep
+    P = poses.shape[0]
+    assert np.all(got["hits"].reshape(P, -1)[:, bad] == 0)
