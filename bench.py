@@ -81,10 +81,10 @@ TRAFFIC: dict = {
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
     "scene_terrain1m": 10 * (356430848 + 682092800),
     # the whole 1,024-sensor launch (780,800 rays)
-    "batched_small": 208760064 + 28272896,
+    "batched_small": 207004928 + 27197184,
     # captured with every sensor cut to 16 poses (143,238,688 rays) and scaled by the ray count to the
     # full 64-sensor launch (9,025,081,856 rays)
-    "batched": round(9025081856 / 143238688 * (2129916160 + 849543424)),
+    "batched": round(9025081856 / 143238688 * (2130438912 + 852212224)),
 }
 
 SRC_COUNTERS = "profiles/traversal_counters_by_workload.md (small cases)"
@@ -92,7 +92,7 @@ SRC_COUNTERS = "profiles/traversal_counters_by_workload.md (small cases)"
 # Warp instructions per unit (ray) of the dominant kernel, `smsp__inst_executed.sum` of one ncu
 # capture on the small case of the workload divided by its rays (profiles/), keyed by kernel walk.
 ISSUE: dict = {
-    "terrain1m_spherical/full_stack": {"warp_inst_per_unit": 1598561620 / 13107200, "source":
+    "terrain1m_spherical/full_stack": {"warp_inst_per_unit": 1601428820 / 13107200, "source":
                                        "profiles/k_trace_terrain1m_spherical.md (100 poses, 13,107,200 rays)"},
     "pose_grad/k_range_grad": {"warp_inst_per_unit": 591522244 / 4194304, "source":
                                "profiles/k_range_grad_terrain2m_posegrad.md (64 poses, 4,194,304 rays)"},
@@ -103,8 +103,8 @@ ISSUE: dict = {
     "room_vlp16/full_stack": {"warp_inst_per_unit": 129417314 / 1440000, "source": SRC_COUNTERS},
     "rcc_fused/k_trace_stats": {"warp_inst_per_unit": 1329978711 / 13107200, "source": SRC_COUNTERS},
     "scene_terrain1m/k_trace_scene": {"warp_inst_per_unit": 2212654859 / 13107200, "source": SRC_COUNTERS},
-    "batched_small/k_trace_batched": {"warp_inst_per_unit": 189000011 / 780800, "source": SRC_COUNTERS},
-    "batched/k_trace_batched": {"warp_inst_per_unit": 14537272107 / 143238688, "source":
+    "batched_small/k_trace_batched": {"warp_inst_per_unit": 164797836 / 780800, "source": SRC_COUNTERS},
+    "batched/k_trace_batched": {"warp_inst_per_unit": 14365424579 / 143238688, "source":
                                 "profiles/k_trace_batched_mixed64.md (16 poses per sensor, 143,238,688 rays, "
                                 "autotuned launch options)"},
 }
