@@ -22,6 +22,14 @@
 // under exactly one piece and the ray transform does not depend on the piece,
 // so the hits and the result are those of the unopened tree.
 //
+// Identity instances (rotation (0,0,0,1), no translation, unit scale) leave the
+// top tree: the geometry of the first such instance of each geometry (up to
+// kMaxDirect geometries) is walked by every ray directly, in the map frame,
+// before the top tree, which then holds only the other instances and starts
+// with the closest hit found so far as its far limit.  Identity instances
+// after the first of the same geometry are dropped: their hits coincide with
+// the first's in range and face and lose the tie to its smaller index.
+//
 // Traversal (k_trace_scene): the top tree is walked with a full stack; at an
 // instance leaf the ray is taken into the instance's mesh frame,
 //     o_l = s^-1 (.) R^T (o - t),   d_l = s^-1 (.) R^T d   (R^T as conj(q) sandwich),
@@ -60,11 +68,15 @@ struct GeomDev {
   unsigned budget;
 };
 
+constexpr uint32_t kMaxDirect = 4;
+
 struct SceneParams {
   TraceParams T;  // T.map: the top-level tree, status = the scene's word
   const InstDev* inst;
   const GeomDev* geoms;
   const uint2* leaves;  // top-level leaf -> (instance record, start node in its geometry's tree)
+  uint2 direct[kMaxDirect];  // (geometry, instance record) walked in the map frame before the top tree
+  uint32_t n_direct;
 };
 
 struct Best {
@@ -114,6 +126,36 @@ __device__ __forceinline__ void instance_hit(const SceneParams& S, int k, const 
   }
 }
 
+// The geometry of an identity instance, walked in the map frame (its mesh frame
+// is the map frame); the same tie rule as instance_hit.
+__device__ __forceinline__ void direct_hit(const SceneParams& S, uint2 entry, const V& o, const V& d, Best& best,
+                                           bool& over) {
+  const GeomDev* gp = S.geoms + entry.x;
+  DeviceMap bm;
+  bm.nodes = reinterpret_cast<const Node*>(__ldg(reinterpret_cast<const unsigned long long*>(&gp->nodes)));
+  bm.tris = reinterpret_cast<const Tri*>(__ldg(reinterpret_cast<const unsigned long long*>(&gp->tris)));
+  bm.root = __ldg(&gp->root);
+  bm.n_nodes = 0;
+  bm.n_tris = 0;
+  bm.status = S.T.map.status;
+  const unsigned budget = __ldg(&gp->budget);
+  RayTrav<kFullStack, 0> r;
+  ShortStack<kFullStack> stack;
+  if (!r.init(bm, o, d, best.t)) return;
+  while (!r.step(bm, budget, stack)) {
+  }
+  if (r.over) { over = true; return; }
+  if (r.h.tri < 0) return;
+  const uint32_t order = __ldg(&S.inst[entry.y].ids.w);
+  if (r.h.t < best.t || best.inst < 0 || order < best.order || (order == best.order && r.h.face < best.face)) {
+    best.t = r.h.t;
+    best.tri = r.h.tri;
+    best.face = r.h.face;
+    best.inst = (int)entry.y;
+    best.order = order;
+  }
+}
+
 // Top-level walk with a full stack (depth <= 32 checked at creation; the guard
 // below only fires on a corrupt tree).
 __device__ __forceinline__ void trace_scene(const SceneParams& S, const V& o, const V& d, float tfar, Best& best,
@@ -123,8 +165,17 @@ __device__ __forceinline__ void trace_scene(const SceneParams& S, const V& o, co
   best.face = 0xffffffffu;
   best.inst = -1;
   best.order = 0xffffffffu;
+  for (uint32_t i = 0; i < S.n_direct && !over; ++i) direct_hit(S, S.direct[i], o, d, best, over);
   const DeviceMap& tl = S.T.map;
-  if (tl.root < 0) return;
+  if (tl.root < 0 || over) {
+    if (over) {
+      best.tri = -1;
+      best.t = tfar;
+      best.face = 0xffffffffu;
+      best.inst = -1;
+    }
+    return;
+  }
   const RayBox rb = make_raybox(o, d);
   int stk_node[kFullStack];
   float stk_t[kFullStack];
@@ -301,7 +352,8 @@ struct rmg_scene {
   uint32_t n_instances = 0;
   std::vector<uint32_t> live;   // instance index of each live instance record
   uint32_t n_leaves = 0;        // top-level leaves: (instance, piece) pairs
-  rmg_map* tlas = nullptr;      // NULL when no instance is live
+  std::vector<uint2> direct;    // (geometry, instance record) of the geometries walked without the top tree
+  rmg_map* tlas = nullptr;      // NULL when no instance is in the top tree
   InstDev* d_inst = nullptr;
   uint2* d_leaves = nullptr;
   GeomDev* d_geoms = nullptr;
@@ -449,12 +501,14 @@ void world_box(const rmg_instance_desc& I, const float lo_m[3], const float hi_m
 // record of every live instance.
 int instance_leaves(const rmg_scene* s, const rmg_instance_desc* inst, uint32_t n, cudaStream_t st,
                     std::vector<uint32_t>& live, std::vector<rmg_vec3>& verts, std::vector<rmg_face>& faces,
-                    std::vector<InstDev>& rec, std::vector<uint2>& leaves) {
+                    std::vector<InstDev>& rec, std::vector<uint2>& leaves, std::vector<uint2>& direct) {
   live.clear();
   verts.clear();
   faces.clear();
   rec.clear();
   leaves.clear();
+  direct.clear();
+  std::vector<char> walked(s->geoms.size(), 0);  // geometry walked directly
   std::vector<float> pbox;
   if (s->n_pieces > 0) {
     const unsigned grid = (s->n_pieces + 127) / 128;
@@ -468,9 +522,16 @@ int instance_leaves(const rmg_scene* s, const rmg_instance_desc* inst, uint32_t 
     const rmg_instance_desc& I = inst[i];
     const rmg_map* g = s->geoms[I.geometry];
     if (g->n_faces == 0) continue;
+    const bool identity = I.T.R.x == 0.0f && I.T.R.y == 0.0f && I.T.R.z == 0.0f && I.T.R.w == 1.0f &&
+                          I.T.t.x == 0.0f && I.T.t.y == 0.0f && I.T.t.z == 0.0f && I.scale.x == 1.0f &&
+                          I.scale.y == 1.0f && I.scale.z == 1.0f;
+    if (identity && walked[I.geometry]) continue;  // never wins against the first identity instance
     const uint32_t slot = (uint32_t)rec.size();
     const std::vector<ScenePiece>& pc = s->pieces[I.geometry];
-    if (pc.empty()) {
+    if (identity && direct.size() < kMaxDirect) {
+      walked[I.geometry] = 1;
+      direct.push_back(make_uint2(I.geometry, slot));
+    } else if (pc.empty()) {
       world_box(I, g->lo, g->hi, verts, faces);
       leaves.push_back(make_uint2(slot, 0u));
     } else {
@@ -500,10 +561,11 @@ int upload_instances(rmg_scene* s, const std::vector<InstDev>& rec, const std::v
   s->d_leaves = nullptr;
   if (rec.empty()) return RMG_OK;
   int r = dev_alloc(&s->d_inst, rec.size(), "scene instances");
-  if (r == RMG_OK) r = dev_alloc(&s->d_leaves, leaves.size(), "scene leaves");
+  if (r == RMG_OK) r = dev_alloc(&s->d_leaves, std::max<size_t>(1, leaves.size()), "scene leaves");
   if (r != RMG_OK) return r;
   RMG_CUDA_TRY(cudaMemcpyAsync(s->d_inst, rec.data(), sizeof(InstDev) * rec.size(), cudaMemcpyHostToDevice, st));
-  RMG_CUDA_TRY(cudaMemcpyAsync(s->d_leaves, leaves.data(), sizeof(uint2) * leaves.size(), cudaMemcpyHostToDevice, st));
+  if (!leaves.empty())
+    RMG_CUDA_TRY(cudaMemcpyAsync(s->d_leaves, leaves.data(), sizeof(uint2) * leaves.size(), cudaMemcpyHostToDevice, st));
   return RMG_OK;
 }
 
@@ -513,14 +575,19 @@ int build_top(rmg_scene* s, const rmg_instance_desc* inst, uint32_t n, bool rebu
   std::vector<rmg_face> faces;
   std::vector<InstDev> rec;
   std::vector<uint2> leaves;
-  int r = instance_leaves(s, inst, n, st, live, verts, faces, rec, leaves);
+  std::vector<uint2> direct;
+  int r = instance_leaves(s, inst, n, st, live, verts, faces, rec, leaves, direct);
   if (r != RMG_OK) return r;
-  const bool same = s->tlas && live.size() == s->live.size() && leaves.size() == s->n_leaves && !live.empty();
+  bool same_direct = direct.size() == s->direct.size();
+  for (size_t i = 0; same_direct && i < direct.size(); ++i)
+    same_direct = direct[i].x == s->direct[i].x && direct[i].y == s->direct[i].y;
+  const bool same = s->tlas && same_direct && live.size() == s->live.size() && leaves.size() == s->n_leaves &&
+                    !leaves.empty();
   if (!rebuild && same) {
     r = rmg_map_refit(s->tlas, verts.data(), (uint32_t)verts.size(), st);
   } else {
     if (s->tlas) { rmg_map_destroy(s->tlas); s->tlas = nullptr; }
-    if (!live.empty()) {
+    if (!faces.empty()) {
       r = rmg_map_build(verts.data(), (uint32_t)verts.size(), faces.data(), (uint32_t)faces.size(), st, &s->tlas);
       if (r == RMG_OK && s->tlas->depth > (unsigned)kFullStack)
         r = fail(RMG_ERR_UNSUPPORTED, "scene: top-level tree deeper than 32 levels");
@@ -532,6 +599,7 @@ int build_top(rmg_scene* s, const rmg_instance_desc* inst, uint32_t n, bool rebu
   RMG_CUDA_TRY(cudaStreamSynchronize(st));
   s->live = live;
   s->n_leaves = (uint32_t)leaves.size();
+  s->direct = direct;
   s->n_instances = n;
   return RMG_OK;
 }
@@ -661,6 +729,8 @@ extern "C" int rmg_simulate_scene(const rmg_scene* s, const rmg_sensor* sensor, 
     S.inst = s->d_inst;
     S.geoms = s->d_geoms;
     S.leaves = s->d_leaves;
+    S.n_direct = (uint32_t)s->direct.size();
+    for (uint32_t i = 0; i < kMaxDirect; ++i) S.direct[i] = i < S.n_direct ? s->direct[i] : make_uint2(0u, 0u);
     const uint64_t blocks = (S.T.n_tiles + cfg.block_warps - 1) / cfg.block_warps;
     if (blocks > 0x7fffffffull) return fail(RMG_ERR_INVALID_ARG, "rmg_simulate_scene: too many rays for one launch");
     const unsigned block = 32u * cfg.block_warps;

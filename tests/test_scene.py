@@ -400,3 +400,85 @@ def test_opened_tree_follows_a_geometry_refit(built):
     assert got["hits"].mean() > 0.3
     _agree(got, {k: want[k] for k in got}, osc.certify(model, IDENT, poses, got, want))
     assert scene.status() == 0
+
+
+# ---- identity instances walked directly (outside the top tree) -----------------------------
+def _mixed_identity_instances():
+    """Identity instances of three geometries (one of them twice, the duplicate with a larger index
+    and other ids), between rotated and scaled instances."""
+    rest = random_instances(12, 3, seed=31)
+    ident = lambda g, oid: dict(geometry=g, T=IDENT.copy(), scale=np.ones(3, np.float32), geom_id=g, object_id=oid)
+    return rest[:4] + [ident(2, 1)] + rest[4:8] + [ident(0, 2), ident(2, 3), ident(1, 4)] + rest[8:]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["spherical", "o1dn"])
+def test_identity_instances_walked_directly_match_the_oracle(built, kind):
+    import torch
+
+    torch.cuda.set_device(0)
+    meshes = mesh_library()
+    insts = _mixed_identity_instances()
+    scene = _gpu_scene(meshes, insts)
+    model = _models()[kind]
+    poses = np.stack([pose(quat([0, 0, 1], a), [np.cos(a) * 1.5, np.sin(a) * 1.5, 1.0])
+                      for a in np.linspace(0, 2 * np.pi, 4, endpoint=False)])
+    got = _run(scene, model, poses)
+    osc = InstancedScene(meshes, insts)
+    want = osc.simulate(model, IDENT, poses)
+    assert np.any(got["object_ids"] == 1) and not np.any(got["object_ids"] == 3)  # the duplicate never wins
+    rep = osc.certify(model, IDENT, poses, got, want)
+    _agree(got, {k: want[k] for k in got}, rep)
+    assert scene.status() == 0
+
+
+@pytest.mark.gpu
+def test_instances_leaving_and_entering_the_identity_follow_the_oracle(built):
+    import torch
+
+    import rmagine_gb300 as rm
+
+    torch.cuda.set_device(0)
+    meshes = mesh_library()
+    insts = _mixed_identity_instances()
+    scene = _gpu_scene(meshes, insts)
+    model = sensors.vlp16_900()
+    poses = np.stack([pose(IDENT[:4], [0.3, 0.2, 1.0]), pose(quat([0, 0, 1], 2.0), [-1.0, 0.5, 1.2])])
+    steps = []
+    moved = [dict(i) for i in insts]
+    moved[4] = dict(moved[4], T=pose(quat([0, 0, 1], 0.3), [0.5, 0.0, 0.0]))  # the room leaves the identity
+    steps.append(moved)
+    back = [dict(i) for i in moved]
+    back[4] = dict(back[4], T=IDENT.copy())                                     # and comes back
+    back[9] = dict(back[9], T=pose(quat([1, 0, 0], 0.2), [0.0, 0.0, 0.2]))     # the cube leaves it
+    steps.append(back)
+    for step in steps:
+        for rebuild in (False, True):
+            scene.update([rm.Instance(i["geometry"], i["T"], i.get("scale", (1, 1, 1)), i.get("geom_id", 0),
+                                      i.get("object_id", 0)) for i in step], rebuild=rebuild)
+            got = _run(scene, model, poses)
+            osc = InstancedScene(meshes, step)
+            want = osc.simulate(model, IDENT, poses)
+            _agree(got, {k: want[k] for k in got}, osc.certify(model, IDENT, poses, got, want))
+    assert scene.status() == 0
+
+
+@pytest.mark.gpu
+def test_more_identity_geometries_than_walked_directly(built):
+    import torch
+
+    torch.cuda.set_device(0)
+    meshes = []
+    for k in range(6):  # six small rooms side by side: the first four walked directly, the rest in the tree
+        room = scenes.box_room(seed=40 + k, n_boxes=3, half=1.5, height=2.0)
+        meshes.append(((room.vertices + np.array([4.0 * k, 0, 0], np.float32)).astype(np.float32), room.faces))
+    insts = [dict(geometry=k, T=IDENT.copy(), scale=np.ones(3, np.float32), geom_id=k, object_id=k)
+             for k in range(6)]
+    scene = _gpu_scene(meshes, insts)
+    model = sensors.vlp16_900()
+    poses = np.stack([pose(IDENT[:4], [4.0 * k, 0.2, 1.0]) for k in range(6)])
+    got = _run(scene, model, poses)
+    osc = InstancedScene(meshes, insts)
+    want = osc.simulate(model, IDENT, poses)
+    assert len(np.unique(got["object_ids"][got["hits"] > 0])) == 6
+    _agree(got, {k: want[k] for k in got}, osc.certify(model, IDENT, poses, got, want))
