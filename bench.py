@@ -79,7 +79,7 @@ TRAFFIC: dict = {
     # full-size launch (131,072,000 ranges)
     "noise": 524465664 + 463988224,
     # captured on 100 poses (13.1 M rays) and scaled by the ray count to the 1,000-pose launch
-    "scene_terrain1m": 10 * (356430848 + 682092800),
+    "scene_terrain1m": 10 * (364896000 + 665387776),
     # the whole 1,024-sensor launch (780,800 rays)
     "batched_small": 207004928 + 27197184,
     # captured with every sensor cut to 16 poses (143,238,688 rays) and scaled by the ray count to the
@@ -102,7 +102,7 @@ ISSUE: dict = {
     "room_vlp16/packet": {"warp_inst_per_unit": 117898004 / 1440000, "source": SRC_COUNTERS},
     "room_vlp16/full_stack": {"warp_inst_per_unit": 129417314 / 1440000, "source": SRC_COUNTERS},
     "rcc_fused/k_trace_stats": {"warp_inst_per_unit": 1329978711 / 13107200, "source": SRC_COUNTERS},
-    "scene_terrain1m/k_trace_scene": {"warp_inst_per_unit": 2212654859 / 13107200, "source": SRC_COUNTERS},
+    "scene_terrain1m/k_trace_scene": {"warp_inst_per_unit": 2033824909 / 13107200, "source": SRC_COUNTERS},
     "batched_small/k_trace_batched": {"warp_inst_per_unit": 164797836 / 780800, "source": SRC_COUNTERS},
     "batched/k_trace_batched": {"warp_inst_per_unit": 14365424579 / 143238688, "source":
                                 "profiles/k_trace_batched_mixed64.md (16 poses per sensor, 143,238,688 rays, "
@@ -532,7 +532,7 @@ def gpu_scene(args, world):
     attrs_e2e = SCENE_ATTRS
     rl = issue_roofline("scene_terrain1m/k_trace_scene", rays, total_ms / args.steps / 1e3, clocks,
                         TRAFFIC.get("scene_terrain1m"),
-                        "k_trace_scene (top-level walk with nested instance walks): issue-bound")
+                        "k_trace_scene (identity geometry walked directly, then the top-level walk with nested instance walks): issue-bound")
     rl = rl or traffic_roofline(TRAFFIC.get("scene_terrain1m"), total_ms / args.steps / 1e3,
                                 "no instruction count is recorded for k_trace_scene")
     config = {"workload": "instanced scene: terrain 708x708 (999,698 tris) + 2,000 instances of one 12-triangle "
