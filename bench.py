@@ -869,7 +869,7 @@ def gpu_posegrad(args, world):
             "e2e": {"value": round(e2e, 1), "unit": "poses/s", "h2d_bytes_per_step": int(est.nbytes + 4 * rays),
                     "d2h_bytes_per_step": int(28 * n_poses)},
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
-    obs_h = obs[:8 * W * H].cpu().numpy()
+    obs_h = obs[:128 * W * H].cpu().numpy()  # the CPU leg times up to 128 poses
     return line, lambda: cpu_posegrad(sc, model, true, est, obs_h), config
 
 
@@ -989,7 +989,7 @@ def gpu_rcc(args, world):
             "e2e": {"value": round(e2e, 1), "unit": "Mrays/s", "h2d_bytes_per_step": int(est.nbytes + 13 * rays),
                     "d2h_bytes_per_step": int(96 * n_poses)},
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
-    data_h = {"points": dp[:8].reshape(-1, 3).cpu().numpy(), "hits": dm[:8].reshape(-1).cpu().numpy()}
+    data_h = {"points": dp[:64].reshape(-1, 3).cpu().numpy(), "hits": dm[:64].reshape(-1).cpu().numpy()}  # CPU leg: up to 64 poses
     return line, lambda: cpu_rcc(sc, model, true, est, data_h), config
 
 
