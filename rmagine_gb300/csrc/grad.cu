@@ -29,8 +29,8 @@ struct GradParams {
   TraceParams T;
   const float* r_obs;
   float delta;
-  float* partial;         // [n_poses][ctas_per_pose][8]
-  uint32_t ctas_per_pose;
+  float* partial;         // [n_poses][warps_per_pose][8]: one slot per warp (tile), written without a barrier
+  uint32_t warps_per_pose;
 };
 
 #ifndef RMG_GRAD_MIN_BLOCKS
@@ -100,23 +100,24 @@ __global__ void __launch_bounds__(256, RMG_GRAD_MIN_BLOCKS) k_range_grad(const G
 #pragma unroll
   for (int k = 0; k < 7; ++k)
     for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], off);
-  __shared__ float red[8][8];
-  if (lane == 0)
-    for (int k = 0; k < 7; ++k) red[wib][k] = acc[k];
-  __syncthreads();
-  if (threadIdx.x < 7) {
-    float s = 0.f;
-    for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
-    G.partial[8ull * ((uint64_t)pose * G.ctas_per_pose + blockIdx.x) + threadIdx.x] = s;
+  // Each warp stores its sums in its own slot (no barrier: a warp whose rays end
+  // early retires at once instead of waiting for the CTA's slowest warp).
+  if (lane == 0) {
+    float4* slot = reinterpret_cast<float4*>(
+        G.partial + 8ull * ((uint64_t)pose * G.warps_per_pose + (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib));
+    slot[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    slot[1] = make_float4(acc[4], acc[5], acc[6], 0.0f);
   }
 }
 
-__global__ void k_grad_final(const float* partial, uint32_t n_poses, uint32_t ctas, float* grad, float* loss) {
+// Per pose and component, the warps' sums in slot order in binary64 (a fixed
+// order: the result does not depend on scheduling).
+__global__ void k_grad_final(const float* partial, uint32_t n_poses, uint32_t warps, float* grad, float* loss) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 7u * n_poses) return;
   const uint32_t pose = i / 7, k = i - pose * 7;
   double s = 0.0;
-  for (uint32_t c = 0; c < ctas; ++c) s += partial[8ull * ((uint64_t)pose * ctas + c) + k];
+  for (uint32_t c = 0; c < warps; ++c) s += partial[8ull * ((uint64_t)pose * warps + c) + k];
   if (k < 6) {
     if (grad) grad[6ull * pose + k] = (float)s;
   } else if (loss) {
@@ -179,13 +180,14 @@ extern "C" int rmg_range_pose_grad(const rmg_map* map, const rmg_sensor* sensor,
     make_trace_params(map, sensor, Tsb, Tbm, n_poses, &out, cfg, G.T);
     G.r_obs = ranges_obs;
     G.delta = huber_delta;
-    G.ctas_per_pose = (G.T.tiles_per_pose + cfg.block_warps - 1) / cfg.block_warps;
+    const uint32_t ctas_per_pose = (G.T.tiles_per_pose + cfg.block_warps - 1) / cfg.block_warps;
+    G.warps_per_pose = ctas_per_pose * cfg.block_warps;
     cudaStream_t st = as_stream(stream);
     float* partial = nullptr;
     RMG_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&partial),
-                                 8 * sizeof(float) * (size_t)n_poses * G.ctas_per_pose, st));
+                                 8 * sizeof(float) * (size_t)n_poses * G.warps_per_pose, st));
     G.partial = partial;
-    const dim3 grid(G.ctas_per_pose, n_poses);
+    const dim3 grid(ctas_per_pose, n_poses);
     const unsigned block = 32u * cfg.block_warps;
     cudaError_t e;
     switch (sensor->model.kind) {
@@ -196,7 +198,7 @@ extern "C" int rmg_range_pose_grad(const rmg_map* map, const rmg_sensor* sensor,
     }
     int s = cuda_status(e, "k_range_grad");
     if (s == RMG_OK) {
-      k_grad_final<<<(7 * n_poses + 255) / 256, 256, 0, st>>>(partial, n_poses, G.ctas_per_pose, grad, loss);
+      k_grad_final<<<(7 * n_poses + 255) / 256, 256, 0, st>>>(partial, n_poses, G.warps_per_pose, grad, loss);
       s = cuda_status(cudaGetLastError(), "k_grad_final");
     }
     cudaFreeAsync(partial, st);
