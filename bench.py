@@ -70,7 +70,7 @@ TRAFFIC: dict = {
     "icp_stats_fwd": 16 * (402915328 + 3088384),
     "icp_stats_bwd": 16 * (403369216 + 357416960),
     # captured on 64 poses (4.19 M rays) and scaled by 64 to the 4,096-pose launch
-    "pose_grad": 64 * (226699264 + 14085632),
+    "pose_grad": 64 * (224337920 + 14536960),
     # captured on 50 poses (15.4 M rays) / 100 poses (13.1 M rays) and scaled to the 1,000-pose launch
     "terrain1m_pinhole": 20 * (87372800 + 503376896),
     "terrain2m_spherical": 10 * (545676032 + 467888640),
@@ -94,7 +94,7 @@ SRC_COUNTERS = "profiles/traversal_counters_by_workload.md (small cases)"
 ISSUE: dict = {
     "terrain1m_spherical/full_stack": {"warp_inst_per_unit": 1601428820 / 13107200, "source":
                                        "profiles/k_trace_terrain1m_spherical.md (100 poses, 13,107,200 rays)"},
-    "pose_grad/k_range_grad": {"warp_inst_per_unit": 591522244 / 4194304, "source":
+    "pose_grad/k_range_grad": {"warp_inst_per_unit": 591709423 / 4194304, "source":
                                "profiles/k_range_grad_terrain2m_posegrad.md (64 poses, 4,194,304 rays)"},
     "terrain1m_pinhole/packet": {"warp_inst_per_unit": 1218427530 / 15360000, "source": SRC_COUNTERS},
     "terrain1m_pinhole/full_stack": {"warp_inst_per_unit": 1300374245 / 15360000, "source": SRC_COUNTERS},
