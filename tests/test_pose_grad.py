@@ -202,3 +202,52 @@ def test_autograd_function_returns_kernel_gradient(rm_mod):
     loss.sum().backward()
     g, _ = rg.range_pose_grad(sim, Tbm, obs, DELTA)
     assert torch.equal(xi.grad, g.cpu())
+
+
+@gpu
+@pytest.mark.parametrize("kind", ["o1dn", "ondn"])
+def test_gpu_gradient_with_ray_origins_and_sensor_offset(rm_mod, kind):
+    """Sensors whose rays start off the sensor origin (O1Dn: one origin, OnDn: one per ray; random
+    direction tables, walked in their sorted visiting order) behind a rotated, offset Tsb: the
+    kernel's gradient against the binary64 reference with the same origins."""
+    import torch
+
+    from rmagine_gb300 import grad as rg
+
+    rm = rm_mod
+    sc = scenes.terrain(grid=96, n_boxes=60, seed=40, size=500.0)
+    true = scenes.terrain_poses(sc, 5, seed=41, size=500.0)
+    est = perturbed(true, 42)
+    rng = np.random.default_rng(43)
+    dirs = sensors.sphere_directions(3000, seed=44)
+    dirs[:, 2] = -np.abs(dirs[:, 2])  # looking down at the terrain
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    dirs = dirs.astype(np.float32)
+    if kind == "o1dn":
+        model = sensors.O1DnModel(width=3000, height=1, range=sensors.Interval(0.3, 130.0), orig=(0.2, -0.1, 0.3),
+                                  dirs=dirs)
+        origs = np.tile(np.array(model.orig, np.float64), (3000, 1))
+    else:
+        o = rng.uniform(-0.3, 0.3, (3000, 3)).astype(np.float32)
+        model = sensors.OnDnModel(width=60, height=50, range=sensors.Interval(0.3, 130.0), origs=o, dirs=dirs)
+        origs = o.astype(np.float64)
+    Tsb = np.array([0, 0, np.sin(0.1), np.cos(0.1), 0.1, 0.05, 0.4, 0], np.float32)
+    m = rm.Map(sc.vertices, sc.faces)
+    sim = rm.make_simulator(model, m)
+    sim.setTsb(Tsb)
+    assert sim.sensor.visit_order() is not None
+    obs = sim.simulate(torch.from_numpy(true).cuda(), attrs=("ranges",)).ranges
+    g, loss, rs, fs = rg.range_pose_grad(sim, torch.from_numpy(est).cuda(), obs, DELTA, want_sim=True)
+    torch.cuda.synchronize()
+    g, loss = g.cpu().numpy(), loss.cpu().numpy()
+    rs, fs, ob = rs.cpu().numpy(), fs.cpu().numpy().view(np.uint32), obs.cpu().numpy()
+    rmin, rmax = model.range.min, model.range.max
+    valid = (fs != 0xFFFFFFFF) & (rs >= rmin) & (ob >= rmin) & (ob <= rmax)
+    gid = np.nonzero(valid)[0]
+    assert gid.size > 0.3 * fs.size
+    rset = og.RayFaceSet(sc.vertices, sc.faces, Tsb, est, dirs[gid % 3000], origs[gid % 3000], gid // 3000,
+                         fs[gid], ob[gid])
+    an, an_loss = rset.analytic(est.shape[0], DELTA)
+    assert np.abs(g - an).max() / np.abs(an).max() < 1e-3
+    assert np.abs(loss - an_loss).max() / np.abs(an_loss).max() < 1e-3
+    assert m.status() == 0
