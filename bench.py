@@ -469,7 +469,7 @@ def gpu_raycast(args, world):
                     "step_ms": [round(1e3 * x, 3) for x in e2e_t]},
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms],
             "map": {k: m.info()[k] for k in ("n_faces", "n_nodes", "depth", "device_bytes")}}
-    return line, lambda: cpu_raycast(sc, model, poses, attrs), config
+    return line, lambda: cpu_raycast(sc, model, poses, attrs, target_s=getattr(args, "cpu_target_s", 15.0)), config
 
 
 # ---- instanced scene (two-level BVH) ----------------------------------------------------------
@@ -549,7 +549,7 @@ def gpu_scene(args, world):
                     "d2h_bytes_per_step": int(rays * host_link_bytes(attrs_e2e, rays)),
                     "step_ms": [round(1e3 * x, 3) for x in e2e_t]},
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
-    return line, lambda: cpu_raycast(baked, model, poses, SCENE_ATTRS), config
+    return line, lambda: cpu_raycast(baked, model, poses, SCENE_ATTRS, target_s=getattr(args, "cpu_target_s", 15.0)), config
 
 
 # ---- range noise ---------------------------------------------------------------------------------
@@ -777,7 +777,7 @@ def gpu_icp(args, world):
             "step_ms": [round(x, 3) for x in step_ms]}
     src_h = src[:min(B, 64)].cpu().numpy()
     tgt_h = tgt[:min(B, 64)].cpu().numpy()
-    return line, lambda: cpu_icp(src_h, tgt_h), config
+    return line, lambda: cpu_icp(src_h, tgt_h, target_s=getattr(args, "cpu_target_s", 10.0)), config
 
 
 # ---- pose gradient -----------------------------------------------------------------------------
@@ -870,7 +870,7 @@ def gpu_posegrad(args, world):
                     "d2h_bytes_per_step": int(28 * n_poses)},
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
     obs_h = obs[:128 * W * H].cpu().numpy()  # the CPU leg times up to 128 poses
-    return line, lambda: cpu_posegrad(sc, model, true, est, obs_h), config
+    return line, lambda: cpu_posegrad(sc, model, true, est, obs_h, target_s=getattr(args, "cpu_target_s", 10.0)), config
 
 
 # ---- fused simulate -> statistics (RCC / MICP-L inner step) ---------------------------------
@@ -990,7 +990,7 @@ def gpu_rcc(args, world):
                     "d2h_bytes_per_step": int(96 * n_poses)},
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
     data_h = {"points": dp[:64].reshape(-1, 3).cpu().numpy(), "hits": dm[:64].reshape(-1).cpu().numpy()}  # CPU leg: up to 64 poses
-    return line, lambda: cpu_rcc(sc, model, true, est, data_h), config
+    return line, lambda: cpu_rcc(sc, model, true, est, data_h, target_s=getattr(args, "cpu_target_s", 10.0)), config
 
 
 # ---- batched heterogeneous sensors ------------------------------------------------------------
@@ -1147,7 +1147,7 @@ def gpu_batched(args, world):
             "roofline": rl, "clocks": clocks, "step_ms": [round(x, 3) for x in step_ms]}
 
     def cpu():
-        return cpu_batched(sc, spec, target_s=10.0)
+        return cpu_batched(sc, spec, target_s=getattr(args, "cpu_target_s", 10.0))
 
     return line, cpu, config
 
@@ -1212,6 +1212,20 @@ def main():
             sline, scpu, _ = fn(sub_args, world)
             sline.update({"steps": steps, "warmup": sub_args.warmup})
             subs[key] = (sline, scpu)
+        # the other measured workloads, so that every figure of the measurement table has a record
+        # of this run; a failure there is reported in its own key and leaves the line intact
+        for key, fn in OTHER_SUBS:
+            torch.cuda.empty_cache()
+            sub_args = argparse.Namespace(**vars(args))
+            sub_args.workload, sub_args.steps, sub_args.warmup = key, min(args.steps, 5), 3
+            sub_args.cpu_target_s = 4.0
+            try:
+                sline, scpu, _ = fn(sub_args, world)
+                sline.update({"steps": sub_args.steps, "warmup": sub_args.warmup})
+                subs[key] = (sline, scpu)
+            except Exception as e:  # noqa: BLE001
+                subs[key] = ({"error": f"{type(e).__name__}: {e}"[:300]}, None)
+            torch.cuda.synchronize()
     if rank != 0:
         return
     out = dict(base)
@@ -1221,66 +1235,84 @@ def main():
 
         ob.build()
     for key, (sline, scpu) in subs.items():
-        if not args.no_cpu_baseline:
-            sline["cpu_baseline"] = rounded(scpu())
+        if not args.no_cpu_baseline and scpu is not None:
+            try:
+                sline["cpu_baseline"] = rounded(scpu())
+            except Exception as e:  # noqa: BLE001
+                sline["cpu_baseline"] = {"error": f"{type(e).__name__}: {e}"[:300]}
         out[key] = sline
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = rounded(cpu())
     print(json.dumps(out))
 
 
+# Sub-lines of the default line beside batched and pose_grad: (key = workload name, GPU arm).
+OTHER_SUBS = (("terrain1m_pinhole", lambda a, w: gpu_raycast(a, w)),
+              ("terrain2m_spherical", lambda a, w: gpu_raycast(a, w)),
+              ("room_vlp16", lambda a, w: gpu_raycast(a, w)),
+              ("scene_terrain1m", lambda a, w: gpu_scene(a, w)),
+              ("rcc_fused", lambda a, w: gpu_rcc(a, w)),
+              ("icp_stats", lambda a, w: gpu_icp(a, w)),
+              ("noise", lambda a, w: gpu_noise(a, w)))
+
+
 def rounded(c):
     return {k: (round(v, 4) if isinstance(v, float) else v) for k, v in c.items() if k != "seconds"}
 
 
-def reference_arm(args, base):
-    """CPU leg on the host cores for the same workload and metric (the reference's Embree path is not
-    buildable; the oracle's restatement of it stands in)."""
-    from oracle import build as ob
-
-    ob.build()
-    if args.workload in RAYCAST:
-        sc, model, poses, attrs, desc = raycast_workload(args.workload)
-        if args.poses:
+def cpu_leg(workload, args, target_s):
+    """The CPU leg of one workload on the host cores: (run, metric, unit, config), run() timing a
+    bounded sample of about target_s seconds (the reference's Embree path is not buildable; the
+    oracle's port of it stands in)."""
+    if workload in RAYCAST:
+        sc, model, poses, attrs, desc = raycast_workload(workload)
+        if args.poses and workload == args.workload:
             poses = poses[:args.poses]
-        run = lambda: cpu_raycast(sc, model, poses, attrs, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
+        run = lambda: cpu_raycast(sc, model, poses, attrs, target_s=target_s)  # noqa
         W, H = model_size(model)
-        metric, unit = "Mrays/s", "Mrays/s"
         config = raycast_config(desc, poses.shape[0], poses.shape[0] * W * H, sc.n_faces,
                                 int(os.environ.get("WORLD_SIZE", "1")))
-    elif args.workload == "icp_stats":
+        return run, "Mrays/s", "Mrays/s", config
+    if workload == "icp_stats":
         rng = np.random.default_rng(0)
         src = rng.uniform(-25, 25, (64, 32768, 3)).astype(np.float32)
         tgt = (src + rng.normal(0, 0.01, src.shape)).astype(np.float32)
-        run = lambda: cpu_icp(src, tgt, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
-        metric, unit, config = "Gcorr/s", "Gcorr/s", {"workload": "ICP statistics_p2p + Umeyama (CPU sample)"}
-    elif args.workload == "pose_grad":
+        return (lambda: cpu_icp(src, tgt, target_s=target_s), "Gcorr/s", "Gcorr/s",
+                {"workload": "ICP statistics_p2p + Umeyama (CPU sample)"})
+    if workload == "pose_grad":
         sc, model, true, est = posegrad_workload(64)
         import oracle
 
         obs = oracle.Scene(sc.vertices, sc.faces).simulate(model, IDENT, true, attrs=("ranges",), fast=True)["ranges"]
-        run = lambda: cpu_posegrad(sc, model, true, est, obs, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
-        metric, unit, config = "pose-grad evals/s", "poses/s", {"workload": "pose gradient (CPU sample)"}
-    elif args.workload == "scene_terrain1m":
+        return (lambda: cpu_posegrad(sc, model, true, est, obs, target_s=target_s), "pose-grad evals/s", "poses/s",
+                {"workload": "pose gradient (CPU sample)"})
+    if workload == "scene_terrain1m":
         from rmagine_gb300 import scenes, sensors
 
         _, _, baked = scenes.instanced_terrain(grid=708, n_boxes=2000, seed=0)
         model = sensors.ouster_like(128, 1024, 45.0, 0.5, 130.0)
         poses = scenes.terrain_poses(baked, 1000, seed=2)
-        run = lambda: cpu_raycast(baked, model, poses, SCENE_ATTRS, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
-        metric, unit, config = "Mrays/s", "Mrays/s", {"workload": "terrain 1M + 2000 boxes (CPU: the geometry as one mesh)"}
-    elif args.workload == "noise":
-        run = cpu_noise
-        metric, unit, config = "Granges/s", "Granges/s", {"workload": "GaussianNoise(0, 0.02) (CPU sample)"}
-    elif args.workload == "rcc_fused":
+        return (lambda: cpu_raycast(baked, model, poses, SCENE_ATTRS, target_s=target_s), "Mrays/s", "Mrays/s",
+                {"workload": "terrain 1M + 2000 boxes (CPU: the geometry as one mesh)"})
+    if workload == "noise":
+        return cpu_noise, "Granges/s", "Granges/s", {"workload": "GaussianNoise(0, 0.02) (CPU sample)"}
+    if workload == "rcc_fused":
         import oracle
 
         sc, model, true, est = rcc_workload(64)
         data_h = oracle.Scene(sc.vertices, sc.faces).simulate(model, IDENT, true, attrs=("hits", "points"), fast=True)
-        run = lambda: cpu_rcc(sc, model, true, est, data_h, target_s=max(2.0, 60.0 / (args.steps + args.warmup)))  # noqa
-        metric, unit, config = "Mrays/s", "Mrays/s", {"workload": "fused simulate -> statistics_p2l (CPU sample)"}
-    else:
-        raise SystemExit(f"unknown workload {args.workload}")
+        return (lambda: cpu_rcc(sc, model, true, est, data_h, target_s=target_s), "Mrays/s", "Mrays/s",
+                {"workload": "fused simulate -> statistics_p2l (CPU sample)"})
+    raise SystemExit(f"unknown workload {workload}")
+
+
+def reference_arm(args, base):
+    """CPU leg on the host cores for the same workload and metric (the reference's Embree path is not
+    buildable; the oracle's port of it stands in)."""
+    from oracle import build as ob
+
+    ob.build()
+    run, metric, unit, config = cpu_leg(args.workload, args, max(2.0, 60.0 / (args.steps + args.warmup)))
     extras = {}
     if args.workload == "terrain1m_spherical" and not args.headline_only and not args.poses:
         # the CPU legs of the line's batched and pose-gradient parts, one bounded sample each
@@ -1307,6 +1339,15 @@ def reference_arm(args, base):
     for key, leg2 in extras.items():
         out[key] = {"metric": "Mrays/s" if key == "batched" else "pose-grad evals/s", "unit": leg2["unit"],
                     "value": round(leg2["value"], 4), "cpu_baseline": rounded(leg2)}
+    if args.workload == "terrain1m_spherical" and not args.headline_only and not args.poses:
+        for key, _ in OTHER_SUBS:  # the CPU legs of the default line's other sub-lines
+            try:
+                run2, metric2, unit2, _ = cpu_leg(key, args, 4.0)
+                leg2 = run2()
+                out[key] = {"metric": metric2, "unit": unit2, "value": round(leg2["value"], 4),
+                            "cpu_baseline": rounded(leg2)}
+            except Exception as e:  # noqa: BLE001
+                out[key] = {"error": f"{type(e).__name__}: {e}"[:300]}
     return out
 
 
