@@ -291,6 +291,11 @@ class Timer:
         barrier(world)
         torch.cuda.synchronize(self.dev)
         with ClockSampler(self.dev.index) as clk:
+            # one more untimed step after the sampler's start-up pause: the GPU idles during the pause,
+            # and the first step after it would otherwise run while the clocks ramp back up
+            fn()
+            torch.cuda.synchronize(self.dev)
+            barrier(world)
             nvtx = nvtx_range("timed")  # lets a profiler select the timed launches (ncu --nvtx-include timed/)
             for s, e in self.ev:
                 self.flush.zero_()  # evict L2 between timed steps (outside the events)
