@@ -78,3 +78,9 @@ def test_invalid_arguments_fail_without_touching_the_gpu(built):
     assert st == _lib.RMG_ERR_UNSUPPORTED
     assert lib.rmg_host_set_pipeline(0, 9) == _lib.RMG_ERR_UNSUPPORTED
     assert lib.rmg_host_set_pipeline(0, 0) == _lib.RMG_OK
+    # the sensor queries reject a NULL sensor or output
+    flag = ctypes.c_int(7)
+    assert lib.rmg_sensor_visit_order(None, None, ctypes.byref(flag)) == _lib.RMG_ERR_INVALID_ARG
+    assert lib.rmg_sensor_visit_order(None, None, None) == _lib.RMG_ERR_INVALID_ARG
+    w, h = ctypes.c_uint32(), ctypes.c_uint32()
+    assert lib.rmg_sensor_size(None, ctypes.byref(w), ctypes.byref(h)) == _lib.RMG_ERR_INVALID_ARG
