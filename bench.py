@@ -1205,7 +1205,9 @@ def main():
     else:
         raise SystemExit(f"unknown workload {args.workload}")
     subs = {}
-    if args.workload == "terrain1m_spherical" and not args.headline_only and not args.poses:
+    if args.workload == "terrain1m_spherical" and not args.headline_only and not args.poses and world == 1:
+        # (at N = 1 only: the scaling run measures the headline; a sub-line failing on one rank would
+        # leave the others waiting at its barriers)
         # the other two parts of the headline metric ("plain vs batched", "pose-grad evals/s"), each
         # timed on its own workload with its own clocks, e2e, roofline and CPU baseline
         import torch
@@ -1318,8 +1320,9 @@ def reference_arm(args, base):
 
     ob.build()
     run, metric, unit, config = cpu_leg(args.workload, args, max(2.0, 60.0 / (args.steps + args.warmup)))
+    single = int(os.environ.get("WORLD_SIZE", "1")) == 1  # sub-line legs at N = 1 only, as in the GPU arm
     extras = {}
-    if args.workload == "terrain1m_spherical" and not args.headline_only and not args.poses:
+    if args.workload == "terrain1m_spherical" and not args.headline_only and not args.poses and single:
         # the CPU legs of the line's batched and pose-gradient parts, one bounded sample each
         import oracle
         from rmagine_gb300 import batched, scenes
@@ -1344,7 +1347,7 @@ def reference_arm(args, base):
     for key, leg2 in extras.items():
         out[key] = {"metric": "Mrays/s" if key == "batched" else "pose-grad evals/s", "unit": leg2["unit"],
                     "value": round(leg2["value"], 4), "cpu_baseline": rounded(leg2)}
-    if args.workload == "terrain1m_spherical" and not args.headline_only and not args.poses:
+    if args.workload == "terrain1m_spherical" and not args.headline_only and not args.poses and single:
         for key, _ in OTHER_SUBS:  # the CPU legs of the default line's other sub-lines
             try:
                 run2, metric2, unit2, _ = cpu_leg(key, args, 4.0)
