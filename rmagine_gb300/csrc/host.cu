@@ -752,7 +752,7 @@ extern "C" int rmg_range_pose_grad_host(const rmg_map* map, const rmg_sensor* se
     // device arrays of a chunk: Tbm, observed ranges (inputs); grad, loss, ranges, face ids (outputs)
     const std::vector<HostArray> arrays = {
         {Tbm, nullptr, sizeof(rmg_transform)}, {ranges_obs, nullptr, 4 * rays},
-        {nullptr, grad, grad ? 24 : 0}, {nullptr, loss, loss ? 4 : 0},
+        {nullptr, grad, grad ? size_t(24) : size_t(0)}, {nullptr, loss, loss ? size_t(4) : size_t(0)},
         {nullptr, ranges_sim, ranges_sim ? 4 * rays : 0}, {nullptr, face_ids, face_ids ? 4 * rays : 0}};
     return io_pipeline("rmg_range_pose_grad_host", n_poses, arrays, 65535,
                        [&](uint32_t, uint32_t np, char* const* d, cudaStream_t cs) {

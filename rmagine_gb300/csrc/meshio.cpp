@@ -74,16 +74,6 @@ PlyType ply_type(const std::string& t) {
   return P_BAD;
 }
 
-size_t ply_size(PlyType t) {
-  switch (t) {
-    case P_I8: case P_U8: return 1;
-    case P_I16: case P_U16: return 2;
-    case P_I32: case P_U32: case P_F32: return 4;
-    case P_F64: return 8;
-    default: return 0;
-  }
-}
-
 struct PlyProp {
   std::string name;
   bool list = false;

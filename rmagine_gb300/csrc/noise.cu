@@ -44,7 +44,9 @@ __host__ __device__ __forceinline__ void mulhilo(uint32_t a, uint32_t b, uint32_
 // Philox4x32 with 10 rounds (Salmon et al. 2011, section 3.3 constants).
 __host__ __device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1) {
   constexpr uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#ifdef __CUDA_ARCH__
 #pragma unroll
+#endif
   for (int r = 0; r < 10; ++r) {
     if (r > 0) { k0 += W0; k1 += W1; }
     uint32_t hi0, lo0, hi1, lo1;
